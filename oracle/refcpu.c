@@ -1,0 +1,974 @@
+/*
+ * refcpu.c -- CPU FP64 restatement of NekCEM's 3-D Maxwell DG time step.
+ *
+ * TEST INFRASTRUCTURE ONLY (the oracle).  Only the tests, the smoke check and
+ * the CPU-baseline leg of the benchmark load this file's library; the product
+ * library never does.
+ *
+ * Each function names the reference routine it restates (path:line inside the
+ * NekCEM source tree).  Layout is the reference's: a scalar field is
+ * u[i + n*j + n*n*k + n^3*e] (Fortran u(i,j,k,e)), a 3-vector field is three
+ * such arrays back to back (Fortran hn(npts,3)), face arrays are indexed by the
+ * face slot j + n^2*(f + 6*e) with f in the reference's "pff" face order.
+ * Summation orders follow the reference; build with -ffp-contract=off so no
+ * fused multiply-add changes the rounding on either x86 or Arm.
+ */
+#include "refcpu.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+static int g_threads = 1;
+void ref_set_threads(int nthreads) { g_threads = nthreads < 1 ? 1 : nthreads; }
+int ref_get_threads(void) { return g_threads; }
+
+struct ref_ctx {
+  int N, n, nelt, nel[3], bc[3];
+  long npts, nxzf, nxzfl, ncempec;
+  double lo[3], hi[3];
+  double *zgm1, *wxm1, *dxm1, *dxtm1, *w3m1;
+  double *xm1, *ym1, *zm1;
+  double *rxm1, *rym1, *rzm1, *sxm1, *sym1, *szm1, *txm1, *tym1, *tzm1, *jacm1, *bm1;
+  double *unx, *uny, *unz, *area;
+  int *cemface, *cbc, *cempec;
+  long long* glo_face;
+  int *gs_order, *gs_start, gs_ngroups;
+  double *permittivity, *permeability, *impede, *conduc, *zimpede, *yconduc;
+  double *Z_0, *Z_1, *Y_0, *Y_1, *ebm1, *hbm1;
+  double *hn, *en, *khn, *ken, *reshn, *resen, *fhn, *fen, *srflx;
+  double *src_w; /* bm1 * exp(-r^2/(2 sigma^2)) per node, or NULL */
+  double C0, src_amp, src_f0, src_t0;
+  double volvm1;
+};
+
+/* ------------------------------------------------------------------------ */
+/* Spectral library (src/nek5_speclib.F)                                     */
+/* ------------------------------------------------------------------------ */
+
+/* JACOBF (src/nek5_speclib.F:482-522): Jacobi polynomial of degree n at x,
+ * its derivative, and the degree n-1 / n-2 values. */
+static void jacobf(double* poly, double* pder, double* polym1, double* pderm1, double* polym2,
+                   double* pderm2, int n, double alp, double bet, double x) {
+  double apb = alp + bet;
+  double p = 1.0, pd = 0.0, pl, pdl, psave = 0.0, pdsave = 0.0;
+  *poly = p; *pder = pd;
+  if (n == 0) return;
+  pl = p; pdl = pd;
+  p = (alp - bet + (apb + 2.0) * x) / 2.0;
+  pd = (apb + 2.0) / 2.0;
+  if (n == 1) { *poly = p; *pder = pd; return; }
+  for (int k = 2; k <= n; ++k) {
+    double dk = (double)k;
+    double a1 = 2.0 * dk * (dk + apb) * (2.0 * dk + apb - 2.0);
+    double a2 = (2.0 * dk + apb - 1.0) * (alp * alp - bet * bet);
+    double b3 = (2.0 * dk + apb - 2.0);
+    double a3 = b3 * (b3 + 1.0) * (b3 + 2.0);
+    double a4 = 2.0 * (dk + alp - 1.0) * (dk + bet - 1.0) * (2.0 * dk + apb);
+    double polyn = ((a2 + a3 * x) * p - a4 * pl) / a1;
+    double pdern = ((a2 + a3 * x) * pd - a4 * pdl + a3 * p) / a1;
+    psave = pl; pdsave = pdl;
+    pl = p; p = polyn;
+    pdl = pd; pd = pdern;
+  }
+  *poly = p; *pder = pd;
+  *polym1 = pl; *pderm1 = pdl;
+  *polym2 = psave; *pderm2 = pdsave;
+}
+
+/* GAMMAF (src/nek5_speclib.F:373-394): table of the values the GLL code uses. */
+static double gammaf(double x) {
+  const double pi = 4.0 * atan(1.0);
+  double g = 1.0;
+  if (x == -0.5) g = -2.0 * sqrt(pi);
+  if (x == 0.5) g = sqrt(pi);
+  if (x == 1.0) g = 1.0;
+  if (x == 2.0) g = 1.0;
+  if (x == 1.5) g = sqrt(pi) / 2.0;
+  if (x == 2.5) g = 1.5 * sqrt(pi) / 2.0;
+  if (x == 3.5) g = 0.5 * (2.5 * (1.5 * sqrt(pi)));
+  if (x == 3.0) g = 2.0;
+  if (x == 4.0) g = 6.0;
+  if (x == 5.0) g = 24.0;
+  if (x == 6.0) g = 120.0;
+  return g;
+}
+
+/* PNORMJ (src/nek5_speclib.F:396-421) */
+static double pnormj(int n, double alpha, double beta) {
+  double dn = (double)n, cnst = alpha + beta + 1.0, prod;
+  if (n <= 1) {
+    prod = gammaf(dn + alpha) * gammaf(dn + beta);
+    prod = prod / (gammaf(dn) * gammaf(dn + alpha + beta));
+    return prod * pow(2.0, cnst) / (2.0 * dn + cnst);
+  }
+  prod = gammaf(alpha + 1.0) * gammaf(beta + 1.0);
+  prod = prod / (2.0 * (1.0 + cnst) * gammaf(cnst + 1.0));
+  prod = prod * (1.0 + alpha) * (2.0 + alpha);
+  prod = prod * (1.0 + beta) * (2.0 + beta);
+  for (int i = 3; i <= n; ++i) {
+    double di = (double)i;
+    double frac = (di + alpha) * (di + beta) / (di * (di + alpha + beta));
+    prod = prod * frac;
+  }
+  return prod * pow(2.0, cnst) / (2.0 * dn + cnst);
+}
+
+/* JACG (src/nek5_speclib.F:423-480): Gauss-Jacobi points by Newton with
+ * deflation, then sorted ascending. */
+static void jacg(double* xjac, int np, double alpha, double beta) {
+  const int kstop = 10;
+  const double eps = 1.0e-12;
+  int n = np - 1;
+  double dth = 4.0 * atan(1.0) / (2.0 * (double)n + 2.0);
+  double xlast = 0.0, p, pd, pm1, pdm1, pm2, pdm2;
+  for (int j = 1; j <= np; ++j) {
+    double x;
+    if (j == 1) {
+      x = cos((2.0 * ((double)j - 1.0) + 1.0) * dth);
+    } else {
+      double x1 = cos((2.0 * ((double)j - 1.0) + 1.0) * dth);
+      x = (x1 + xlast) / 2.0;
+    }
+    for (int k = 1; k <= kstop; ++k) {
+      jacobf(&p, &pd, &pm1, &pdm1, &pm2, &pdm2, np, alpha, beta, x);
+      double recsum = 0.0;
+      for (int i = 1; i <= j - 1; ++i) recsum = recsum + 1.0 / (x - xjac[np - i]);
+      double delx = -p / (pd - recsum * p);
+      x = x + delx;
+      if (fabs(delx) < eps) break;
+    }
+    xjac[np - j] = x;
+    xlast = x;
+  }
+  for (int i = 0; i < np; ++i) {
+    double xmin = 2.0;
+    int jmin = i;
+    for (int j = i; j < np; ++j)
+      if (xjac[j] < xmin) { xmin = xjac[j]; jmin = j; }
+    if (jmin != i) { double s = xjac[i]; xjac[i] = xjac[jmin]; xjac[jmin] = s; }
+  }
+}
+
+/* ZWGJD (src/nek5_speclib.F:156-205) */
+static void zwgjd(double* z, double* w, int np, double alpha, double beta) {
+  int n = np - 1;
+  double apb = alpha + beta, p, pd, pm1, pdm1, pm2, pdm2;
+  if (np == 1) {
+    z[0] = (beta - alpha) / (apb + 2.0);
+    w[0] = gammaf(alpha + 1.0) * gammaf(beta + 1.0) / gammaf(apb + 2.0) * pow(2.0, apb + 1.0);
+    return;
+  }
+  jacg(z, np, alpha, beta);
+  int np1 = n + 1, np2 = n + 2;
+  double dnp1 = (double)np1, dnp2 = (double)np2;
+  double fac1 = dnp1 + alpha + beta + 1.0;
+  double fac2 = fac1 + dnp1;
+  double fac3 = fac2 + 1.0;
+  double fnorm = pnormj(np1, alpha, beta);
+  double rcoef = (fnorm * fac2 * fac3) / (2.0 * fac1 * dnp2);
+  for (int i = 0; i < np; ++i) {
+    jacobf(&p, &pd, &pm1, &pdm1, &pm2, &pdm2, np2, alpha, beta, z[i]);
+    w[i] = -rcoef / (p * pdm1);
+  }
+}
+
+/* ENDW1 / ENDW2 (src/nek5_speclib.F:285-371) */
+static double endw(int which, int n, double alpha, double beta) {
+  double apb = alpha + beta, f1, f2, f3 = 0.0, fint1, fint2;
+  if (n == 0) return 0.0;
+  if (which == 1) {
+    f1 = gammaf(alpha + 2.0) * gammaf(beta + 1.0) / gammaf(apb + 3.0);
+  } else {
+    f1 = gammaf(alpha + 1.0) * gammaf(beta + 2.0) / gammaf(apb + 3.0);
+  }
+  f1 = f1 * (apb + 2.0) * pow(2.0, apb + 2.0) / 2.0;
+  if (n == 1) return f1;
+  if (which == 1) {
+    fint1 = gammaf(alpha + 2.0) * gammaf(beta + 1.0) / gammaf(apb + 3.0);
+  } else {
+    fint1 = gammaf(alpha + 1.0) * gammaf(beta + 2.0) / gammaf(apb + 3.0);
+  }
+  fint1 = fint1 * pow(2.0, apb + 2.0);
+  fint2 = gammaf(alpha + 2.0) * gammaf(beta + 2.0) / gammaf(apb + 4.0);
+  fint2 = fint2 * pow(2.0, apb + 3.0);
+  if (which == 1)
+    f2 = (-2.0 * (beta + 2.0) * fint1 + (apb + 4.0) * fint2) * (apb + 3.0) / 4.0;
+  else
+    f2 = (2.0 * (alpha + 2.0) * fint1 - (apb + 4.0) * fint2) * (apb + 3.0) / 4.0;
+  if (n == 2) return f2;
+  for (int i = 3; i <= n; ++i) {
+    double di = (double)(i - 1);
+    double abn = alpha + beta + di;
+    double abnn = abn + di;
+    double a1 = -(2.0 * (di + alpha) * (di + beta)) / (abn * abnn * (abnn + 1.0));
+    double a2 = (2.0 * (alpha - beta)) / (abnn * (abnn + 2.0));
+    double a3 = (2.0 * (abn + 1.0)) / ((abnn + 2.0) * (abnn + 1.0));
+    f3 = -(a2 * f2 + a1 * f1) / a3;
+    f1 = f2;
+    f2 = f3;
+  }
+  return f3;
+}
+
+/* ZWGLL -> ZWGLJ -> ZWGLJD (src/nek5_speclib.F:107-121, 208-283), alpha=beta=0 */
+void ref_zwgll(double* z, double* w, int np) {
+  const double alpha = 0.0, beta = 0.0;
+  int n = np - 1, nm1 = n - 1;
+  double p, pd, pm1, pdm1, pm2, pdm2;
+  if (nm1 > 0) zwgjd(z + 1, w + 1, nm1, alpha + 1.0, beta + 1.0);
+  z[0] = -1.0;
+  z[np - 1] = 1.0;
+  for (int i = 1; i < np - 1; ++i) w[i] = w[i] / (1.0 - z[i] * z[i]);
+  jacobf(&p, &pd, &pm1, &pdm1, &pm2, &pdm2, n, alpha, beta, z[0]);
+  w[0] = endw(1, n, alpha, beta) / (2.0 * pd);
+  jacobf(&p, &pd, &pm1, &pdm1, &pm2, &pdm2, n, alpha, beta, z[np - 1]);
+  w[np - 1] = endw(2, n, alpha, beta) / (2.0 * pd);
+}
+
+/* PNLEG (src/nek5_speclib.F:882-910) */
+double ref_pnleg(double z, int n) {
+  if (fabs(z) < 1.0e-25) z = 0.0;
+  double p1 = 1.0, p2, p3;
+  if (n == 0) return p1;
+  p2 = z;
+  p3 = p2;
+  for (int k = 1; k <= n - 1; ++k) {
+    double fk = (double)k;
+    p3 = ((2.0 * fk + 1.0) * z * p2 - fk * p1) / (fk + 1.0);
+    p1 = p2;
+    p2 = p3;
+  }
+  return p3;
+}
+
+/* DGLL (src/nek5_speclib.F:807-840) */
+void ref_dgll(double* d, double* dt, const double* z, int nz) {
+  int n = nz - 1;
+  if (nz == 1) { d[0] = 0.0; dt[0] = 0.0; return; }
+  double fn = (double)n;
+  double d0 = fn * (fn + 1.0) / 4.0;
+  for (int i = 0; i < nz; ++i)
+    for (int j = 0; j < nz; ++j) {
+      double v = 0.0;
+      if (i != j) v = ref_pnleg(z[i], n) / (ref_pnleg(z[j], n) * (z[i] - z[j]));
+      if (i == j && i == 0) v = -d0;
+      if (i == j && i == nz - 1) v = d0;
+      d[i + nz * j] = v;
+      dt[j + nz * i] = v;
+    }
+}
+
+/* ------------------------------------------------------------------------ */
+/* Tensor contractions (src/nek5_grad.F:2-19, src/nek5_mxm_std.F:173-191)    */
+/* ------------------------------------------------------------------------ */
+
+/* mxm with the mxf summation order: c(i,j) = sum_l a(i,l) b(l,j), l ascending */
+static void mxm(const double* a, int n1, const double* b, int n2, double* c, int n3) {
+  for (int j = 0; j < n3; ++j)
+    for (int i = 0; i < n1; ++i) {
+      double s = a[i] * b[(size_t)n2 * j];
+      for (int l = 1; l < n2; ++l) s = s + a[i + (size_t)n1 * l] * b[l + (size_t)n2 * j];
+      c[i + (size_t)n1 * j] = s;
+    }
+}
+
+/* local_grad3 (src/nek5_grad.F:2-19): ur = D u, us_k = u_k Dt, ut = u Dt */
+void ref_local_grad3(double* ur, double* us, double* ut, const double* u, int n, const double* D,
+                     const double* Dt) {
+  int m2 = n * n;
+  mxm(D, n, u, n, ur, m2);
+  for (int k = 0; k < n; ++k) mxm(u + (size_t)m2 * k, n, Dt, n, us + (size_t)m2 * k, n);
+  mxm(u, m2, Dt, n, ut, n);
+}
+
+/* ------------------------------------------------------------------------ */
+/* Mesh / geometry                                                           */
+/* ------------------------------------------------------------------------ */
+
+/* Face slot f (0..5, the reference's pff order) -> reference axis (0=r,1=s,2=t)
+ * and side; EFACE/SKPDAT (src/nek5_connect11.F:1067-1078, 1483-1530). */
+static const int slot_axis[6] = {1, 0, 1, 0, 2, 2};
+static const int slot_side[6] = {-1, +1, +1, -1, -1, +1};
+
+/* volume index (within element) of node (a,b) of slot f; a walks fastest
+ * (cem_set_fc_ptr, src/cem_common.F:214-257 with SKPDAT) */
+static int face_vol_index(int f, int a, int b, int n) {
+  int fixed = slot_side[f] < 0 ? 0 : n - 1;
+  switch (slot_axis[f]) {
+    case 0: return fixed + n * a + n * n * b;
+    case 1: return a + n * fixed + n * n * b;
+    default: return a + n * b + n * n * fixed;
+  }
+}
+
+static double* dalloc(long n) { return (double*)calloc((size_t)(n > 0 ? n : 1), sizeof(double)); }
+static int* ialloc(long n) { return (int*)calloc((size_t)(n > 0 ? n : 1), sizeof(int)); }
+
+static long long* g_sort_keys;
+static int cmp_by_key(const void* a, const void* b) {
+  long long ka = g_sort_keys[*(const int*)a], kb = g_sort_keys[*(const int*)b];
+  if (ka != kb) return ka < kb ? -1 : 1;
+  return *(const int*)a - *(const int*)b;
+}
+
+/* gs_setup semantics (src/jl/gs.h:17-60): group face slots by global id. */
+static void gs_setup_local(ref_ctx* c) {
+  long m = c->nxzfl;
+  c->gs_order = ialloc(m);
+  c->gs_start = ialloc(m + 1);
+  for (long i = 0; i < m; ++i) c->gs_order[i] = (int)i;
+  g_sort_keys = c->glo_face;
+  qsort(c->gs_order, (size_t)m, sizeof(int), cmp_by_key);
+  g_sort_keys = NULL;
+  int ng = 0;
+  for (long i = 0; i < m; ++i)
+    if (i == 0 || c->glo_face[c->gs_order[i]] != c->glo_face[c->gs_order[i - 1]])
+      c->gs_start[ng++] = (int)i;
+  c->gs_start[ng] = (int)m;
+  c->gs_ngroups = ng;
+}
+
+/* genxyz for an axis-aligned hex (src/nek5_genxyz.F:562-655): trilinear map
+ * of the 8 corners, accumulated in the reference's corner loop order. */
+static void genxyz_box(ref_ctx* c) {
+  int n = c->n;
+  for (int e = 0; e < c->nelt; ++e) {
+    int ex = e % c->nel[0], ey = (e / c->nel[0]) % c->nel[1], ez = e / (c->nel[0] * c->nel[1]);
+    int ec[3] = {ex, ey, ez};
+    double cb[3][2];
+    for (int d = 0; d < 3; ++d) {
+      double L = c->hi[d] - c->lo[d];
+      cb[d][0] = c->lo[d] + L * (double)ec[d] / (double)c->nel[d];
+      cb[d][1] = c->lo[d] + L * (double)(ec[d] + 1) / (double)c->nel[d];
+    }
+    double h[16][2];
+    for (int i = 0; i < n; ++i) {
+      h[i][0] = (1.0 - c->zgm1[i]) * 0.5;
+      h[i][1] = (1.0 + c->zgm1[i]) * 0.5;
+    }
+    for (int k = 0; k < n; ++k)
+      for (int j = 0; j < n; ++j)
+        for (int i = 0; i < n; ++i) {
+          long idx = i + (long)n * j + (long)n * n * k + (long)n * n * n * e;
+          c->xm1[idx] = c->ym1[idx] = c->zm1[idx] = 0.0;
+        }
+    for (int izt = 0; izt < 2; ++izt)
+      for (int iyt = 0; iyt < 2; ++iyt)
+        for (int ixt = 0; ixt < 2; ++ixt)
+          for (int k = 0; k < n; ++k)
+            for (int j = 0; j < n; ++j) {
+              double hh = h[j][iyt] * h[k][izt];
+              for (int i = 0; i < n; ++i) {
+                double hhh = h[i][ixt] * hh;
+                long idx = i + (long)n * j + (long)n * n * k + (long)n * n * n * e;
+                c->xm1[idx] = c->xm1[idx] + hhh * cb[0][ixt];
+                c->ym1[idx] = c->ym1[idx] + hhh * cb[1][iyt];
+                c->zm1[idx] = c->zm1[idx] + hhh * cb[2][izt];
+              }
+            }
+  }
+}
+
+ref_ctx* ref_create_box(int N, int nelx, int nely, int nelz, const double lo[3],
+                        const double hi[3], const int bc[3]) {
+  if (N < 1 || N > 15 || nelx < 1 || nely < 1 || nelz < 1) return NULL;
+  ref_ctx* c = (ref_ctx*)calloc(1, sizeof(ref_ctx));
+  int n = N + 1;
+  c->N = N; c->n = n;
+  c->nel[0] = nelx; c->nel[1] = nely; c->nel[2] = nelz;
+  c->nelt = nelx * nely * nelz;
+  for (int d = 0; d < 3; ++d) { c->lo[d] = lo[d]; c->hi[d] = hi[d]; c->bc[d] = bc[d]; }
+  long n3 = (long)n * n * n;
+  c->npts = n3 * c->nelt;
+  c->nxzf = (long)n * n;
+  c->nxzfl = 6 * c->nxzf * c->nelt;
+  long npts = c->npts, nxzfl = c->nxzfl;
+
+  /* GENWZ (src/nek5_coef.F:1-260) */
+  c->zgm1 = dalloc(n); c->wxm1 = dalloc(n);
+  c->dxm1 = dalloc(n * n); c->dxtm1 = dalloc(n * n);
+  c->w3m1 = dalloc(n3);
+  ref_zwgll(c->zgm1, c->wxm1, n);
+  ref_dgll(c->dxm1, c->dxtm1, c->zgm1, n);
+  for (int iz = 0; iz < n; ++iz)
+    for (int iy = 0; iy < n; ++iy)
+      for (int ix = 0; ix < n; ++ix)
+        c->w3m1[ix + n * iy + n * n * iz] = c->wxm1[ix] * c->wxm1[iy] * c->wxm1[iz];
+
+  c->xm1 = dalloc(npts); c->ym1 = dalloc(npts); c->zm1 = dalloc(npts);
+  genxyz_box(c);
+
+  /* XYZRST (src/nek5_coef.F:877-924) + GLMAPM1 (555-635) + GEODAT1 bm1 (758) */
+  double *xr = dalloc(npts), *yr = dalloc(npts), *zr = dalloc(npts);
+  double *xs = dalloc(npts), *ys = dalloc(npts), *zs = dalloc(npts);
+  double *xt = dalloc(npts), *yt = dalloc(npts), *zt = dalloc(npts);
+  for (int e = 0; e < c->nelt; ++e) {
+    long o = n3 * e;
+    ref_local_grad3(xr + o, xs + o, xt + o, c->xm1 + o, n, c->dxm1, c->dxtm1);
+    ref_local_grad3(yr + o, ys + o, yt + o, c->ym1 + o, n, c->dxm1, c->dxtm1);
+    ref_local_grad3(zr + o, zs + o, zt + o, c->zm1 + o, n, c->dxm1, c->dxtm1);
+  }
+  c->rxm1 = dalloc(npts); c->rym1 = dalloc(npts); c->rzm1 = dalloc(npts);
+  c->sxm1 = dalloc(npts); c->sym1 = dalloc(npts); c->szm1 = dalloc(npts);
+  c->txm1 = dalloc(npts); c->tym1 = dalloc(npts); c->tzm1 = dalloc(npts);
+  c->jacm1 = dalloc(npts); c->bm1 = dalloc(npts);
+  for (long i = 0; i < npts; ++i) {
+    double jac = 0.0;
+    jac = jac + xr[i] * ys[i] * zt[i];
+    jac = jac + xt[i] * yr[i] * zs[i];
+    jac = jac + xs[i] * yt[i] * zr[i];
+    jac = jac - xr[i] * yt[i] * zs[i];
+    jac = jac - xs[i] * yr[i] * zt[i];
+    jac = jac - xt[i] * ys[i] * zr[i];
+    c->jacm1[i] = jac;
+    c->rxm1[i] = ys[i] * zt[i] - yt[i] * zs[i];
+    c->rym1[i] = xt[i] * zs[i] - xs[i] * zt[i];
+    c->rzm1[i] = xs[i] * yt[i] - xt[i] * ys[i];
+    c->sxm1[i] = yt[i] * zr[i] - yr[i] * zt[i];
+    c->sym1[i] = xr[i] * zt[i] - xt[i] * zr[i];
+    c->szm1[i] = xt[i] * yr[i] - xr[i] * yt[i];
+    c->txm1[i] = yr[i] * zs[i] - ys[i] * zr[i];
+    c->tym1[i] = xs[i] * zr[i] - xr[i] * zs[i];
+    c->tzm1[i] = xr[i] * ys[i] - xs[i] * yr[i];
+  }
+  for (int e = 0; e < c->nelt; ++e)
+    for (long i = 0; i < n3; ++i) c->bm1[n3 * e + i] = c->jacm1[n3 * e + i] * c->w3m1[i];
+  c->volvm1 = 0.0;
+  for (long i = 0; i < npts; ++i) c->volvm1 += c->bm1[i];
+
+  /* AREA3 (src/nek5_coef.F:1150-1237): per-node cross products, then the
+   * face restriction; UNITVEC (src/nek5_mat1.F:2006) normalises. */
+  c->unx = dalloc(nxzfl); c->uny = dalloc(nxzfl); c->unz = dalloc(nxzfl); c->area = dalloc(nxzfl);
+  for (int e = 0; e < c->nelt; ++e)
+    for (int f = 0; f < 6; ++f) {
+      int ax = slot_axis[f], sd = slot_side[f];
+      for (int b = 0; b < n; ++b)
+        for (int a = 0; a < n; ++a) {
+          long v = n3 * e + face_vol_index(f, a, b, n);
+          double A, B, C, wgt;
+          if (ax == 0) { /* "R": xs x xt */
+            A = ys[v] * zt[v] - zs[v] * yt[v];
+            B = zs[v] * xt[v] - xs[v] * zt[v];
+            C = xs[v] * yt[v] - ys[v] * xt[v];
+          } else if (ax == 1) { /* "S": xr x xt */
+            A = yr[v] * zt[v] - zr[v] * yt[v];
+            B = zr[v] * xt[v] - xr[v] * zt[v];
+            C = xr[v] * yt[v] - yr[v] * xt[v];
+          } else { /* "T": xr x xs */
+            A = yr[v] * zs[v] - zr[v] * ys[v];
+            B = zr[v] * xs[v] - xr[v] * zs[v];
+            C = xr[v] * ys[v] - yr[v] * xs[v];
+          }
+          double dot = A * A + B * B + C * C;
+          wgt = c->wxm1[a] * c->wxm1[b];
+          /* sign: r: +A on r=+1, -A on r=-1; s: +A on s=-1, -A on s=+1;
+           * t: -A on t=-1, +A on t=+1 */
+          double sg;
+          if (ax == 0) sg = sd > 0 ? 1.0 : -1.0;
+          else if (ax == 1) sg = sd < 0 ? 1.0 : -1.0;
+          else sg = sd > 0 ? 1.0 : -1.0;
+          long j = a + (long)n * b + c->nxzf * (f + 6L * e);
+          c->area[j] = sqrt(dot) * wgt;
+          double nx = sg * A, ny = sg * B, nz = sg * C;
+          double len = sqrt(nx * nx + ny * ny + nz * nz);
+          if (len != 0.0) { nx = nx / len; ny = ny / len; nz = nz / len; }
+          c->unx[j] = nx; c->uny[j] = ny; c->unz[j] = nz;
+        }
+    }
+  free(xr); free(yr); free(zr); free(xs); free(ys); free(zs); free(xt); free(yt); free(zt);
+
+  /* cem_set_fc_ptr (src/cem_common.F:214-257); face global numbering with the
+   * semantics of setup_dgds2 (src/nek5_connect11.F:2179-2233): the two
+   * slots that share a face node carry the same positive id; a PEC face node
+   * is a singleton.  CBC codes: 0 = 'E  ' interior, 1 = 'PEC', 2 = 'P  '. */
+  c->cemface = ialloc(nxzfl);
+  c->glo_face = (long long*)calloc((size_t)nxzfl, sizeof(long long));
+  c->cbc = ialloc(6L * c->nelt);
+  long long nplanes_off[3];
+  nplanes_off[0] = 0;
+  nplanes_off[1] = (long long)(nelx + 1) * nely * nelz;
+  nplanes_off[2] = nplanes_off[1] + (long long)(nely + 1) * nelx * nelz;
+  /* physical axis of each reference axis for an axis-aligned box: r->x, s->y, t->z */
+  for (int e = 0; e < c->nelt; ++e) {
+    int ec[3] = {e % nelx, (e / nelx) % nely, e / (nelx * nely)};
+    for (int f = 0; f < 6; ++f) {
+      int ax = slot_axis[f], sd = slot_side[f];
+      int plane = ec[ax] + (sd > 0 ? 1 : 0);
+      int boundary = (plane == 0 || plane == c->nel[ax]);
+      if (boundary) c->cbc[6 * e + f] = (c->bc[ax] == REF_BC_PERIODIC) ? 2 : 1;
+      if (boundary && c->bc[ax] == REF_BC_PERIODIC) plane = plane % c->nel[ax];
+      long long fid;
+      if (ax == 0) fid = nplanes_off[0] + ((long long)plane * nely + ec[1]) * nelz + ec[2];
+      else if (ax == 1) fid = nplanes_off[1] + ((long long)plane * nelx + ec[0]) * nelz + ec[2];
+      else fid = nplanes_off[2] + ((long long)plane * nelx + ec[0]) * nely + ec[1];
+      for (int b = 0; b < n; ++b)
+        for (int a = 0; a < n; ++a) {
+          long j = a + (long)n * b + c->nxzf * (f + 6L * e);
+          c->cemface[j] = (int)(n3 * e + face_vol_index(f, a, b, n));
+          c->glo_face[j] = fid * (long long)(n * n) + a + (long long)n * b + 1;
+        }
+    }
+  }
+  gs_setup_local(c);
+
+  /* cem_maxwell_pec_init (src/cem_maxwell.F:1338-1366) */
+  c->cempec = ialloc(nxzfl);
+  long l = 0;
+  for (int e = 0; e < c->nelt; ++e)
+    for (int f = 0; f < 6; ++f)
+      if (c->cbc[6 * e + f] == 1)
+        for (long j = 0; j < c->nxzf; ++j) c->cempec[l++] = (int)(j + c->nxzf * (f + 6L * e));
+  c->ncempec = l;
+
+  /* state and work arrays (src/EMWAVE) */
+  c->hn = dalloc(3 * npts); c->en = dalloc(3 * npts);
+  c->khn = dalloc(3 * npts); c->ken = dalloc(3 * npts);
+  c->reshn = dalloc(3 * npts); c->resen = dalloc(3 * npts);
+  c->fhn = dalloc(3 * nxzfl); c->fen = dalloc(3 * nxzfl);
+  c->srflx = dalloc(6 * nxzfl);
+  c->permittivity = dalloc(npts); c->permeability = dalloc(npts);
+  c->impede = dalloc(npts); c->conduc = dalloc(npts);
+  c->zimpede = dalloc(nxzfl); c->yconduc = dalloc(nxzfl);
+  c->Z_0 = dalloc(nxzfl); c->Z_1 = dalloc(nxzfl); c->Y_0 = dalloc(nxzfl); c->Y_1 = dalloc(nxzfl);
+  c->ebm1 = dalloc(npts); c->hbm1 = dalloc(npts);
+  c->C0 = 1.0;
+  double* one = dalloc(npts);
+  for (long i = 0; i < npts; ++i) one[i] = 1.0;
+  ref_set_materials(c, one, one);
+  free(one);
+  return c;
+}
+
+void ref_destroy(ref_ctx* c) {
+  if (!c) return;
+  double* d[] = {c->zgm1, c->wxm1, c->dxm1, c->dxtm1, c->w3m1, c->xm1, c->ym1, c->zm1,
+                 c->rxm1, c->rym1, c->rzm1, c->sxm1, c->sym1, c->szm1, c->txm1, c->tym1,
+                 c->tzm1, c->jacm1, c->bm1, c->unx, c->uny, c->unz, c->area,
+                 c->permittivity, c->permeability, c->impede, c->conduc, c->zimpede,
+                 c->yconduc, c->Z_0, c->Z_1, c->Y_0, c->Y_1, c->ebm1, c->hbm1, c->hn, c->en,
+                 c->khn, c->ken, c->reshn, c->resen, c->fhn, c->fen, c->srflx, c->src_w};
+  for (size_t i = 0; i < sizeof(d) / sizeof(d[0]); ++i) free(d[i]);
+  free(c->cemface); free(c->cbc); free(c->cempec); free(c->glo_face);
+  free(c->gs_order); free(c->gs_start);
+  free(c);
+}
+
+double* ref_darray(ref_ctx* c, const char* name, long* len) {
+  struct { const char* nm; double* p; long n; } t[] = {
+      {"zgm1", c->zgm1, c->n}, {"wxm1", c->wxm1, c->n}, {"dxm1", c->dxm1, (long)c->n * c->n},
+      {"dxtm1", c->dxtm1, (long)c->n * c->n}, {"w3m1", c->w3m1, (long)c->n * c->n * c->n},
+      {"xm1", c->xm1, c->npts}, {"ym1", c->ym1, c->npts}, {"zm1", c->zm1, c->npts},
+      {"rxm1", c->rxm1, c->npts}, {"rym1", c->rym1, c->npts}, {"rzm1", c->rzm1, c->npts},
+      {"sxm1", c->sxm1, c->npts}, {"sym1", c->sym1, c->npts}, {"szm1", c->szm1, c->npts},
+      {"txm1", c->txm1, c->npts}, {"tym1", c->tym1, c->npts}, {"tzm1", c->tzm1, c->npts},
+      {"jacm1", c->jacm1, c->npts}, {"bm1", c->bm1, c->npts},
+      {"unx", c->unx, c->nxzfl}, {"uny", c->uny, c->nxzfl}, {"unz", c->unz, c->nxzfl},
+      {"area", c->area, c->nxzfl},
+      {"permittivity", c->permittivity, c->npts}, {"permeability", c->permeability, c->npts},
+      {"Z_0", c->Z_0, c->nxzfl}, {"Z_1", c->Z_1, c->nxzfl}, {"Y_0", c->Y_0, c->nxzfl},
+      {"Y_1", c->Y_1, c->nxzfl}, {"ebm1", c->ebm1, c->npts}, {"hbm1", c->hbm1, c->npts},
+      {"hn", c->hn, 3 * c->npts}, {"en", c->en, 3 * c->npts}, {"khn", c->khn, 3 * c->npts},
+      {"ken", c->ken, 3 * c->npts}, {"reshn", c->reshn, 3 * c->npts},
+      {"resen", c->resen, 3 * c->npts}, {"fhn", c->fhn, 3 * c->nxzfl},
+      {"fen", c->fen, 3 * c->nxzfl}, {"srflx", c->srflx, 6 * c->nxzfl},
+      {"src_w", c->src_w, c->src_w ? c->npts : 0},
+  };
+  for (size_t i = 0; i < sizeof(t) / sizeof(t[0]); ++i)
+    if (strcmp(t[i].nm, name) == 0) { if (len) *len = t[i].n; return t[i].p; }
+  if (len) *len = 0;
+  return NULL;
+}
+
+int* ref_iarray(ref_ctx* c, const char* name, long* len) {
+  if (strcmp(name, "cemface") == 0) { if (len) *len = c->nxzfl; return c->cemface; }
+  if (strcmp(name, "cbc") == 0) { if (len) *len = 6L * c->nelt; return c->cbc; }
+  if (strcmp(name, "cempec") == 0) { if (len) *len = c->ncempec; return c->cempec; }
+  if (len) *len = 0;
+  return NULL;
+}
+
+long long* ref_larray(ref_ctx* c, const char* name, long* len) {
+  if (strcmp(name, "glo_face") == 0) { if (len) *len = c->nxzfl; return c->glo_face; }
+  if (len) *len = 0;
+  return NULL;
+}
+
+long ref_size(const ref_ctx* c, const char* name) {
+  if (strcmp(name, "n") == 0) return c->n;
+  if (strcmp(name, "nelt") == 0) return c->nelt;
+  if (strcmp(name, "npts") == 0) return c->npts;
+  if (strcmp(name, "nxzf") == 0) return c->nxzf;
+  if (strcmp(name, "nxzfl") == 0) return c->nxzfl;
+  if (strcmp(name, "ncempec") == 0) return c->ncempec;
+  return -1;
+}
+
+double ref_volvm1(const ref_ctx* c) { return c->volvm1; }
+
+/* ------------------------------------------------------------------------ */
+/* Materials (src/cem_maxwell.F:262-325, 183-186)                            */
+/* ------------------------------------------------------------------------ */
+void ref_set_materials(ref_ctx* c, const double* permittivity, const double* permeability) {
+  long npts = c->npts, nxzfl = c->nxzfl;
+  memcpy(c->permittivity, permittivity, sizeof(double) * npts);
+  memcpy(c->permeability, permeability, sizeof(double) * npts);
+  for (long i = 0; i < npts; ++i) {
+    c->impede[i] = sqrt(c->permeability[i] / c->permittivity[i]);
+    c->conduc[i] = sqrt(c->permittivity[i] / c->permeability[i]);
+  }
+  for (long j = 0; j < nxzfl; ++j) {
+    int i = c->cemface[j];
+    c->zimpede[j] = c->impede[i];
+    c->yconduc[j] = c->conduc[i];
+  }
+  memcpy(c->Z_0, c->zimpede, sizeof(double) * nxzfl);
+  memcpy(c->Y_0, c->yconduc, sizeof(double) * nxzfl);
+  ref_gs_op_fields(c, c->Z_0, nxzfl, 1);
+  ref_gs_op_fields(c, c->Y_0, nxzfl, 1);
+  for (int e = 0; e < c->nelt; ++e)
+    for (int f = 0; f < 6; ++f)
+      if (c->cbc[6 * e + f] == 1)
+        for (long j = 0; j < c->nxzf; ++j) {
+          long i = j + c->nxzf * (f + 6L * e);
+          c->Y_0[i] = 2.0 * c->Y_0[i];
+          c->Z_0[i] = 2.0 * c->Z_0[i];
+        }
+  for (long j = 0; j < nxzfl; ++j) {
+    c->Z_1[j] = c->Z_0[j] - c->zimpede[j];
+    c->Y_1[j] = c->Y_0[j] - c->yconduc[j];
+  }
+  for (long j = 0; j < nxzfl; ++j) {
+    c->Z_0[j] = 0.5 * c->Z_0[j];
+    c->Y_0[j] = 0.5 * c->Y_0[j];
+  }
+  /* ebm1 = 1/(eps*bm1), hbm1 = 1/(mu*bm1): col3 then invcol1 */
+  for (long i = 0; i < npts; ++i) {
+    c->ebm1[i] = 1.0 / (c->permittivity[i] * c->bm1[i]);
+    c->hbm1[i] = 1.0 / (c->permeability[i] * c->bm1[i]);
+  }
+}
+
+void ref_set_flux(ref_ctx* c, double C0) { c->C0 = C0; }
+
+double ref_source_time(double t, double f0, double t0) {
+  const double pi = 4.0 * atan(1.0);
+  double a = pi * f0 * (t - t0);
+  double a2 = a * a;
+  return (1.0 - 2.0 * a2) * exp(-a2);
+}
+
+void ref_set_source(ref_ctx* c, int enabled, const double xc[3], double sigma, double amp,
+                    double f0, double t0) {
+  free(c->src_w);
+  c->src_w = NULL;
+  if (!enabled) return;
+  c->src_w = dalloc(c->npts);
+  double s2 = 2.0 * sigma * sigma;
+  for (long i = 0; i < c->npts; ++i) {
+    double dx = c->xm1[i] - xc[0], dy = c->ym1[i] - xc[1], dz = c->zm1[i] - xc[2];
+    c->src_w[i] = c->bm1[i] * exp(-(dx * dx + dy * dy + dz * dz) / s2);
+  }
+  c->src_amp = amp; c->src_f0 = f0; c->src_t0 = t0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* The stage operator                                                        */
+/* ------------------------------------------------------------------------ */
+
+/* maxwell_wght_curl (src/cem_maxwell.F:1428-1497) */
+void ref_wght_curl(ref_ctx* c, double* w1, double* w2, double* w3, const double* u1,
+                   const double* u2, const double* u3) {
+  int n = c->n;
+  long n3 = (long)n * n * n;
+#pragma omp parallel for schedule(static) num_threads(g_threads)
+  for (int e = 0; e < c->nelt; ++e) {
+    double buf[9 * 16 * 16 * 16];
+    double *u1r = buf, *u1s = buf + n3, *u1t = buf + 2 * n3;
+    double *u2r = buf + 3 * n3, *u2s = buf + 4 * n3, *u2t = buf + 5 * n3;
+    double *u3r = buf + 6 * n3, *u3s = buf + 7 * n3, *u3t = buf + 8 * n3;
+    long j = n3 * e;
+    ref_local_grad3(u1r, u1s, u1t, u1 + j, n, c->dxm1, c->dxtm1);
+    ref_local_grad3(u2r, u2s, u2t, u2 + j, n, c->dxm1, c->dxtm1);
+    ref_local_grad3(u3r, u3s, u3t, u3 + j, n, c->dxm1, c->dxtm1);
+    for (long i = 0; i < n3; ++i) {
+      long k = i + j;
+      double w = c->w3m1[i];
+      double u1rw = u1r[i] * w, u1sw = u1s[i] * w, u1tw = u1t[i] * w;
+      double u2rw = u2r[i] * w, u2sw = u2s[i] * w, u2tw = u2t[i] * w;
+      double u3rw = u3r[i] * w, u3sw = u3s[i] * w, u3tw = u3t[i] * w;
+      double rx = c->rxm1[k], sx = c->sxm1[k], tx = c->txm1[k];
+      double ry = c->rym1[k], sy = c->sym1[k], ty = c->tym1[k];
+      double rz = c->rzm1[k], sz = c->szm1[k], tz = c->tzm1[k];
+      w1[k] = u3rw * ry + u3sw * sy + u3tw * ty - u2rw * rz - u2sw * sz - u2tw * tz;
+      w2[k] = u1rw * rz + u1sw * sz + u1tw * tz - u3rw * rx - u3sw * sx - u3tw * tx;
+      w3[k] = u2rw * rx + u2sw * sx + u2tw * tx - u1rw * ry - u1sw * sy - u1tw * ty;
+    }
+  }
+}
+
+/* cem_maxwell 3-D branch (src/cem_maxwell.F:574-582) */
+void ref_cem_maxwell(ref_ctx* c) {
+  long np = c->npts;
+  ref_wght_curl(c, c->resen, c->resen + np, c->resen + 2 * np, c->hn, c->hn + np, c->hn + 2 * np);
+  ref_wght_curl(c, c->reshn, c->reshn + np, c->reshn + 2 * np, c->en, c->en + np, c->en + 2 * np);
+#pragma omp parallel for schedule(static) num_threads(g_threads)
+  for (long i = 0; i < 3 * np; ++i) c->reshn[i] = -c->reshn[i];
+}
+
+/* cem_maxwell_restrict_to_face (src/cem_maxwell.F:604-623) */
+void ref_restrict_to_face(ref_ctx* c) {
+  long np = c->npts, nf = c->nxzfl;
+#pragma omp parallel for schedule(static) num_threads(g_threads)
+  for (long j = 0; j < nf; ++j) {
+    long i = c->cemface[j];
+    for (int q = 0; q < 3; ++q) {
+      c->fhn[j + q * nf] = c->hn[i + q * np];
+      c->fen[j + q * nf] = c->en[i + q * np];
+    }
+  }
+}
+
+/* first loop of cem_maxwell_flux3d (src/cem_maxwell.F:944-955) */
+void ref_flux_pre(ref_ctx* c) {
+  long k = c->nxzfl;
+  double *s = c->srflx, *fe = c->fen, *fh = c->fhn;
+#pragma omp parallel for schedule(static) num_threads(g_threads)
+  for (long i = 0; i < k; ++i) {
+    double nx = c->unx[i], ny = c->uny[i], nz = c->unz[i];
+    s[0 * k + i] = -ny * fe[2 * k + i] + nz * fe[1 * k + i];
+    s[1 * k + i] = -nz * fe[0 * k + i] + nx * fe[2 * k + i];
+    s[2 * k + i] = -nx * fe[1 * k + i] + ny * fe[0 * k + i];
+    s[3 * k + i] = -ny * fh[2 * k + i] + nz * fh[1 * k + i];
+    s[4 * k + i] = -nz * fh[0 * k + i] + nx * fh[2 * k + i];
+    s[5 * k + i] = -nx * fh[1 * k + i] + ny * fh[0 * k + i];
+  }
+}
+
+/* gs_op_fields(gsh_face, u, stride, nfld, dom=1, op=add, transpose=0)
+ * (src/jl/gs.c:2074-2099): every entry is replaced by the sum over its id
+ * group; summed in increasing slot order. */
+void ref_gs_op_fields(ref_ctx* c, double* u, long stride, int nfld) {
+  for (int fld = 0; fld < nfld; ++fld) {
+    double* v = u + stride * fld;
+#pragma omp parallel for schedule(static) num_threads(g_threads)
+    for (int g = 0; g < c->gs_ngroups; ++g) {
+      int b = c->gs_start[g], e = c->gs_start[g + 1];
+      if (e - b < 2) continue;
+      double s = v[c->gs_order[b]];
+      for (int q = b + 1; q < e; ++q) s = s + v[c->gs_order[q]];
+      for (int q = b; q < e; ++q) v[c->gs_order[q]] = s;
+    }
+  }
+}
+
+/* cem_maxwell_flux_pec (src/cem_maxwell.F:1368-1426) */
+void ref_flux_pec(ref_ctx* c) {
+  long k = c->nxzfl;
+  double* s = c->srflx;
+  for (long j = 0; j < c->ncempec; ++j) {
+    long i = c->cempec[j];
+    s[0 * k + i] = 2.0 * s[0 * k + i];
+    s[1 * k + i] = 2.0 * s[1 * k + i];
+    s[2 * k + i] = 2.0 * s[2 * k + i];
+    s[3 * k + i] = 0.0;
+    s[4 * k + i] = 0.0;
+    s[5 * k + i] = 0.0;
+  }
+}
+
+/* upwind combination (src/cem_maxwell.F:969-997) */
+void ref_flux_upwind(ref_ctx* c) {
+  long k = c->nxzfl;
+  double* s = c->srflx;
+  double C0 = c->C0;
+#pragma omp parallel for schedule(static) num_threads(g_threads)
+  for (long i = 0; i < k; ++i) {
+    double Y0 = c->Y_0[i], Y1 = c->Y_1[i], Z0 = c->Z_0[i], Z1 = c->Z_1[i];
+    double Y02 = -0.5 / Y0 * Y1;
+    double Z02 = 0.5 / Z0 * Z1;
+    double C02Y = 0.5 / Y0 * C0;
+    double C02Z = 0.5 / Z0 * C0;
+    double nx = c->unx[i], ny = c->uny[i], nz = c->unz[i];
+    double fu1 = ny * s[5 * k + i] - nz * s[4 * k + i];
+    double fu2 = nz * s[3 * k + i] - nx * s[5 * k + i];
+    double fu3 = nx * s[4 * k + i] - ny * s[3 * k + i];
+    double fw1 = ny * s[2 * k + i] - nz * s[1 * k + i];
+    double fw2 = nz * s[0 * k + i] - nx * s[2 * k + i];
+    double fw3 = nx * s[1 * k + i] - ny * s[0 * k + i];
+    s[0 * k + i] = Y02 * s[0 * k + i] - C02Y * fu1;
+    s[1 * k + i] = Y02 * s[1 * k + i] - C02Y * fu2;
+    s[2 * k + i] = Y02 * s[2 * k + i] - C02Y * fu3;
+    s[3 * k + i] = Z02 * s[3 * k + i] - C02Z * fw1;
+    s[4 * k + i] = Z02 * s[4 * k + i] - C02Z * fw2;
+    s[5 * k + i] = Z02 * s[5 * k + i] - C02Z * fw3;
+  }
+}
+
+/* cem_maxwell_flux3d (src/cem_maxwell.F:922-1002); userfsrc is a no-op */
+void ref_flux3d(ref_ctx* c) {
+  ref_flux_pre(c);
+  ref_gs_op_fields(c, c->srflx, c->nxzfl, 6);
+  if (c->ncempec > 0) ref_flux_pec(c);
+  ref_flux_upwind(c);
+}
+
+/* cem_maxwell_add_flux_to_res, CPU branch (src/cem_maxwell.F:725-735).  The
+ * serial loop adds face slots in increasing order; the element-parallel loop
+ * below keeps that order because an element's slots are contiguous and only
+ * touch that element's nodes. */
+void ref_add_flux_to_res(ref_ctx* c) {
+  long k = c->nxzfl, np = c->npts, per = 6 * c->nxzf;
+  double* s = c->srflx;
+#pragma omp parallel for schedule(static) num_threads(g_threads)
+  for (int e = 0; e < c->nelt; ++e)
+    for (long j = per * e; j < per * (e + 1); ++j) {
+      long i = c->cemface[j];
+      double a = c->area[j];
+      c->reshn[i + 0 * np] = c->reshn[i + 0 * np] + a * s[0 * k + j];
+      c->reshn[i + 1 * np] = c->reshn[i + 1 * np] + a * s[1 * k + j];
+      c->reshn[i + 2 * np] = c->reshn[i + 2 * np] + a * s[2 * k + j];
+      c->resen[i + 0 * np] = c->resen[i + 0 * np] + a * s[3 * k + j];
+      c->resen[i + 1 * np] = c->resen[i + 1 * np] + a * s[4 * k + j];
+      c->resen[i + 2 * np] = c->resen[i + 2 * np] + a * s[5 * k + j];
+    }
+}
+
+/* usersrc (src/cem_maxwell.F:503): mass-weighted E_z source */
+void ref_usersrc(ref_ctx* c, double rktime) {
+  if (!c->src_w) return;
+  double ft = c->src_amp * ref_source_time(rktime, c->src_f0, c->src_t0);
+  double* rez = c->resen + 2 * c->npts;
+  for (long i = 0; i < c->npts; ++i) rez[i] = rez[i] + c->src_w[i] * ft;
+}
+
+/* cem_maxwell_invqmass, CPU branch (src/cem_maxwell.F:1878-1886) */
+void ref_invqmass(ref_ctx* c) {
+  long np = c->npts;
+#pragma omp parallel for schedule(static) num_threads(g_threads)
+  for (long i = 0; i < np; ++i) {
+    for (int q = 0; q < 3; ++q) {
+      c->reshn[i + q * np] = c->reshn[i + q * np] * c->hbm1[i];
+      c->resen[i + q * np] = c->resen[i + q * np] * c->ebm1[i];
+    }
+  }
+}
+
+/* cem_maxwell_op (src/cem_maxwell.F:484-508); userinc/userfsrc no-ops, no PML */
+void ref_maxwell_op(ref_ctx* c, double rktime) {
+  ref_cem_maxwell(c);
+  ref_restrict_to_face(c);
+  ref_flux3d(c);
+  ref_add_flux_to_res(c);
+  ref_usersrc(c, rktime);
+  ref_invqmass(c);
+}
+
+/* rk4_upd (src/cem_common.F:18-75): kh = ca*kh + dt*resh; h = h + cb*kh */
+void ref_rk4_upd(double* h, double* kh, const double* resh, double cb, double ca, double dt,
+                 long n) {
+#pragma omp parallel for schedule(static) num_threads(g_threads)
+  for (long i = 0; i < n; ++i) {
+    kh[i] = ca * kh[i] + dt * resh[i];
+    h[i] = h[i] + cb * kh[i];
+  }
+}
+
+/* rk_storage, RK45 branch (src/cem_common.F:78-104) */
+void ref_rk_coeffs(double a[5], double b[5], double c[6]) {
+  a[0] = 0.0;
+  a[1] = -567301805773.0 / 1357537059087.0;
+  a[2] = -2404267990393.0 / 2016746695238.0;
+  a[3] = -3550918686646.0 / 2091501179385.0;
+  a[4] = -1275806237668.0 / 842570457699.0;
+  b[0] = 1432997174477.0 / 9575080441755.0;
+  b[1] = 5161836677717.0 / 13612068292357.0;
+  b[2] = 1720146321549.0 / 2090206949498.0;
+  b[3] = 3134564353537.0 / 4481467310338.0;
+  b[4] = 2277821191437.0 / 14882151754819.0;
+  c[0] = 0.0;
+  c[1] = 1432997174477.0 / 9575080441755.0;
+  c[2] = 2526269341429.0 / 6820363962896.0;
+  c[3] = 2006345519317.0 / 3224310063776.0;
+  c[4] = 2802321613138.0 / 2924317926251.0;
+  c[5] = 1.0;
+}
+
+/* one stage: rk_c, cem_maxwell_op, rk_maxwell_ab (src/cem_maxwell.F:336-340,
+ * src/cem_common.F:2-15, src/cem_maxwell.F:1906-1940) */
+void ref_rk_stage(ref_ctx* c, int rkstep, double time, double dt) {
+  double a[5], b[5], cc[6];
+  ref_rk_coeffs(a, b, cc);
+  double rktime = time + dt * cc[rkstep - 1];
+  ref_maxwell_op(c, rktime);
+  long np = c->npts;
+  for (int q = 0; q < 3; ++q)
+    ref_rk4_upd(c->hn + q * np, c->khn + q * np, c->reshn + q * np, b[rkstep - 1], a[rkstep - 1],
+                dt, np);
+  for (int q = 0; q < 3; ++q)
+    ref_rk4_upd(c->en + q * np, c->ken + q * np, c->resen + q * np, b[rkstep - 1], a[rkstep - 1],
+                dt, np);
+}
+
+/* cem_maxwell_op_rk (src/cem_maxwell.F:327-345) */
+void ref_op_rk(ref_ctx* c, double time, double dt) {
+  for (int s = 1; s <= 5; ++s) ref_rk_stage(c, s, time, dt);
+}
+
+/* time loop body of time_advancing_pde (src/cem_drive.F:618-651) */
+void ref_run(ref_ctx* c, int nsteps, double* time, double dt) {
+  for (int s = 0; s < nsteps; ++s) {
+    ref_op_rk(c, *time, dt);
+    *time = *time + dt;
+  }
+}
+
+/* get_dxmin (src/nek5_courant.F:2-75) */
+double ref_get_dxmin(const ref_ctx* c) {
+  int n = c->n;
+  double d2m = 1.0e20;
+  const double *x = c->xm1, *y = c->ym1, *z = c->zm1;
+#define IDX(i, j, k, e) ((long)(i) + (long)n * (j) + (long)n * n * (k) + (long)n * n * n * (e))
+  for (int e = 0; e < c->nelt; ++e)
+    for (int k = 1; k < n - 1; ++k)
+      for (int j = 1; j < n - 1; ++j)
+        for (int i = 1; i < n - 1; ++i) {
+          double dx, dy, dz, d2;
+          dx = x[IDX(i + 1, j, k, e)] - x[IDX(i - 1, j, k, e)];
+          dy = y[IDX(i + 1, j, k, e)] - y[IDX(i - 1, j, k, e)];
+          dz = z[IDX(i + 1, j, k, e)] - z[IDX(i - 1, j, k, e)];
+          d2 = dx * dx + dy * dy + dz * dz;
+          d2m = d2 < d2m ? d2 : d2m;
+          dx = x[IDX(i, j + 1, k, e)] - x[IDX(i, j - 1, k, e)];
+          dy = y[IDX(i, j + 1, k, e)] - y[IDX(i, j - 1, k, e)];
+          dz = z[IDX(i, j + 1, k, e)] - z[IDX(i, j - 1, k, e)];
+          d2 = dx * dx + dy * dy + dz * dz;
+          d2m = d2 < d2m ? d2 : d2m;
+          dx = x[IDX(i, j, k + 1, e)] - x[IDX(i, j, k - 1, e)];
+          dy = y[IDX(i, j, k + 1, e)] - y[IDX(i, j, k - 1, e)];
+          dz = z[IDX(i, j, k + 1, e)] - z[IDX(i, j, k - 1, e)];
+          d2 = dx * dx + dy * dy + dz * dz;
+          d2m = d2 < d2m ? d2 : d2m;
+        }
+#undef IDX
+  return sqrt(d2m) / 2.0;
+}
+
+/* cem_error (src/cem_common.F:1335-1355): L2 = sqrt(sum e*bm1*e / volvm1) */
+void ref_cem_error(const ref_ctx* c, const double* u, const double* exact, long n, double* l2,
+                   double* linf) {
+  double s = 0.0, m = 0.0;
+  for (long i = 0; i < n; ++i) {
+    double err = exact[i] - u[i];
+    s = s + err * c->bm1[i] * err;
+    double a = fabs(err);
+    m = a > m ? a : m;
+  }
+  s = s / c->volvm1;
+  if (s > 0.0) s = sqrt(s);
+  *l2 = s;
+  *linf = m;
+}

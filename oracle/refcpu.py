@@ -1,0 +1,224 @@
+"""ctypes wrapper around the oracle library (refcpu.c).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, by ``__graft_entry__.smoke()``
+and by the CPU-baseline leg of ``bench.py``.  The product library never loads
+it.  ``build()`` compiles ``refcpu.c`` in place with gcc (no FMA contraction,
+so x86 and Arm give the same bits).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "librefcpu.so")
+BC_PEC, BC_PERIODIC = 0, 1
+
+
+def build(force: bool = False) -> str:
+    src = os.path.join(HERE, "refcpu.c")
+    if (not force and os.path.exists(LIB_PATH)
+            and os.path.getmtime(LIB_PATH) >= os.path.getmtime(src)
+            and os.path.getmtime(LIB_PATH) >= os.path.getmtime(os.path.join(HERE, "refcpu.h"))):
+        return LIB_PATH
+    cmd = ["gcc", "-O3", "-std=c99", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off",
+           "-o", LIB_PATH + ".tmp", src, "-lm"]
+    subprocess.run(cmd, check=True)
+    os.replace(LIB_PATH + ".tmp", LIB_PATH)
+    return LIB_PATH
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(LIB_PATH)
+        vp, ip, dp = C.c_void_p, C.c_int, C.POINTER(C.c_double)
+        L.ref_create_box.restype = vp
+        L.ref_create_box.argtypes = [ip, ip, ip, ip, dp, dp, C.POINTER(C.c_int)]
+        L.ref_destroy.argtypes = [vp]
+        L.ref_darray.restype = dp
+        L.ref_darray.argtypes = [vp, C.c_char_p, C.POINTER(C.c_long)]
+        L.ref_iarray.restype = C.POINTER(C.c_int)
+        L.ref_iarray.argtypes = [vp, C.c_char_p, C.POINTER(C.c_long)]
+        L.ref_larray.restype = C.POINTER(C.c_longlong)
+        L.ref_larray.argtypes = [vp, C.c_char_p, C.POINTER(C.c_long)]
+        L.ref_size.restype = C.c_long
+        L.ref_size.argtypes = [vp, C.c_char_p]
+        L.ref_volvm1.restype = C.c_double
+        L.ref_volvm1.argtypes = [vp]
+        L.ref_set_materials.argtypes = [vp, dp, dp]
+        L.ref_set_flux.argtypes = [vp, C.c_double]
+        L.ref_set_source.argtypes = [vp, ip, dp, C.c_double, C.c_double, C.c_double, C.c_double]
+        L.ref_source_time.restype = C.c_double
+        L.ref_source_time.argtypes = [C.c_double, C.c_double, C.c_double]
+        for nm in ("ref_cem_maxwell", "ref_restrict_to_face", "ref_flux3d", "ref_flux_pre",
+                   "ref_flux_pec", "ref_flux_upwind", "ref_add_flux_to_res", "ref_invqmass"):
+            getattr(L, nm).argtypes = [vp]
+        L.ref_usersrc.argtypes = [vp, C.c_double]
+        L.ref_maxwell_op.argtypes = [vp, C.c_double]
+        L.ref_gs_op_fields.argtypes = [vp, dp, C.c_long, ip]
+        L.ref_rk_stage.argtypes = [vp, ip, C.c_double, C.c_double]
+        L.ref_op_rk.argtypes = [vp, C.c_double, C.c_double]
+        L.ref_run.argtypes = [vp, ip, dp, C.c_double]
+        L.ref_get_dxmin.restype = C.c_double
+        L.ref_get_dxmin.argtypes = [vp]
+        L.ref_cem_error.argtypes = [vp, dp, dp, C.c_long, dp, dp]
+        L.ref_rk_coeffs.argtypes = [dp, dp, dp]
+        L.ref_zwgll.argtypes = [dp, dp, ip]
+        L.ref_dgll.argtypes = [dp, dp, dp, ip]
+        L.ref_set_threads.argtypes = [ip]
+        L.ref_get_threads.restype = ip
+        _lib = L
+    return _lib
+
+
+def _dp(a: np.ndarray):
+    assert a.dtype == np.float64 and a.flags.c_contiguous
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def zwgll(np_: int):
+    z = np.zeros(np_); w = np.zeros(np_)
+    lib().ref_zwgll(_dp(z), _dp(w), np_)
+    return z, w
+
+
+def dgll(z: np.ndarray):
+    n = len(z)
+    d = np.zeros(n * n); dt = np.zeros(n * n)
+    lib().ref_dgll(_dp(d), _dp(dt), _dp(np.ascontiguousarray(z, dtype=np.float64)), n)
+    return d.reshape(n, n).T.copy(), dt  # D[i, j]
+
+
+def rk_coeffs():
+    a = np.zeros(5); b = np.zeros(5); c = np.zeros(6)
+    lib().ref_rk_coeffs(_dp(a), _dp(b), _dp(c))
+    return a, b, c
+
+
+def set_threads(n: int):
+    lib().ref_set_threads(int(n))
+
+
+class RefBox:
+    """Oracle for one structured affine box mesh (reference COMMON arrays)."""
+
+    def __init__(self, N, nel, lo, hi, bc):
+        L = lib()
+        lo_a = (C.c_double * 3)(*lo); hi_a = (C.c_double * 3)(*hi)
+        bc_a = (C.c_int * 3)(*bc)
+        self._c = L.ref_create_box(int(N), int(nel[0]), int(nel[1]), int(nel[2]),
+                                   lo_a, hi_a, bc_a)
+        if not self._c:
+            raise ValueError("ref_create_box rejected the mesh")
+        self.N, self.nel, self.lo, self.hi, self.bc = N, tuple(nel), tuple(lo), tuple(hi), tuple(bc)
+        self.n = N + 1
+        self.nelt = int(L.ref_size(self._c, b"nelt"))
+        self.npts = int(L.ref_size(self._c, b"npts"))
+        self.nxzf = int(L.ref_size(self._c, b"nxzf"))
+        self.nxzfl = int(L.ref_size(self._c, b"nxzfl"))
+
+    def close(self):
+        if getattr(self, "_c", None):
+            lib().ref_destroy(self._c)
+            self._c = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # --- named COMMON arrays as numpy views (they alias the C memory) ---
+    def d(self, name: str) -> np.ndarray:
+        n = C.c_long(0)
+        p = lib().ref_darray(self._c, name.encode(), C.byref(n))
+        if not p or n.value == 0:
+            raise KeyError(name)
+        return np.ctypeslib.as_array(p, shape=(n.value,))
+
+    def i(self, name: str) -> np.ndarray:
+        n = C.c_long(0)
+        p = lib().ref_iarray(self._c, name.encode(), C.byref(n))
+        if not p:
+            raise KeyError(name)
+        if n.value == 0:
+            return np.zeros(0, dtype=np.int32)
+        return np.ctypeslib.as_array(p, shape=(n.value,))
+
+    def l(self, name: str) -> np.ndarray:
+        n = C.c_long(0)
+        p = lib().ref_larray(self._c, name.encode(), C.byref(n))
+        if not p:
+            raise KeyError(name)
+        return np.ctypeslib.as_array(p, shape=(n.value,))
+
+    @property
+    def volvm1(self) -> float:
+        return lib().ref_volvm1(self._c)
+
+    def set_materials(self, eps: np.ndarray, mu: np.ndarray):
+        eps = np.ascontiguousarray(eps, dtype=np.float64)
+        mu = np.ascontiguousarray(mu, dtype=np.float64)
+        assert eps.size == self.npts and mu.size == self.npts
+        lib().ref_set_materials(self._c, _dp(eps), _dp(mu))
+
+    def set_flux(self, C0: float):
+        lib().ref_set_flux(self._c, float(C0))
+
+    def set_source(self, xc, sigma, amp, f0, t0, enabled=True):
+        xa = (C.c_double * 3)(*xc)
+        lib().ref_set_source(self._c, 1 if enabled else 0, xa, sigma, amp, f0, t0)
+
+    # state (hn, en) as (3, npts) views
+    @property
+    def hn(self):
+        return self.d("hn").reshape(3, self.npts)
+
+    @property
+    def en(self):
+        return self.d("en").reshape(3, self.npts)
+
+    def set_state(self, H: np.ndarray, E: np.ndarray, zero_k: bool = True):
+        self.hn[...] = H
+        self.en[...] = E
+        if zero_k:
+            self.d("khn")[:] = 0.0
+            self.d("ken")[:] = 0.0
+
+    def dxmin(self) -> float:
+        return lib().ref_get_dxmin(self._c)
+
+    def stage(self, rkstep: int, time: float, dt: float):
+        lib().ref_rk_stage(self._c, int(rkstep), float(time), float(dt))
+
+    def op_rk(self, time: float, dt: float):
+        lib().ref_op_rk(self._c, float(time), float(dt))
+
+    def run(self, nsteps: int, time: float, dt: float) -> float:
+        t = C.c_double(time)
+        lib().ref_run(self._c, int(nsteps), C.byref(t), float(dt))
+        return t.value
+
+    def maxwell_op(self, rktime: float):
+        lib().ref_maxwell_op(self._c, float(rktime))
+
+    def call(self, name: str, *args):
+        return getattr(lib(), "ref_" + name)(self._c, *args)
+
+    def cem_error(self, u: np.ndarray, exact: np.ndarray):
+        u = np.ascontiguousarray(u, dtype=np.float64)
+        ex = np.ascontiguousarray(exact, dtype=np.float64)
+        l2 = C.c_double(); li = C.c_double()
+        lib().ref_cem_error(self._c, _dp(u), _dp(ex), u.size, C.byref(l2), C.byref(li))
+        return l2.value, li.value
+
+    def coords(self):
+        return self.d("xm1"), self.d("ym1"), self.d("zm1")
