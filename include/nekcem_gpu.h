@@ -1,0 +1,213 @@
+/*
+ * nekcem_gpu.h -- C ABI of the GB300 (sm_103a) Maxwell DG time-step library.
+ *
+ * Drop-in boundary for NekCEM's 3-D Maxwell time step, run as `mpirun -np 1`
+ * on one GPU.  The Fortran driver keeps its subroutines and its
+ * element-major COMMON arrays; under a NEKGPU build, cem_maxwell_op_rk
+ * (src/cem_maxwell.F:327-345) calls nekgpu_step / nekgpu_op_rk_host instead of
+ * its five CPU stages, after cem_maxwell_init (src/cem_maxwell.F:65-191) has
+ * handed the static arrays to nekgpu_init.  The Fortran binding
+ * (iso_c_binding interfaces) is shown in INTEGRATION.md.
+ *
+ * Conventions
+ *   - Plain C types only; all arrays are caller-owned host memory in the
+ *     reference's Fortran layout.  Index arrays are 1-based as in Fortran.
+ *   - A 3-vector field is `hn(ld,3)`: component q of node i at hn[i + ld*q].
+ *   - Face arrays are in face-slot order j + nx1^2*(f + 6*e), f in the
+ *     reference's face order (src/nek5_coef.F:1182-1235).
+ *   - Every call returns NEKGPU_OK (0) or a negative NEKGPU_ERR_* code;
+ *     nekgpu_error_string() gives a message.  The Fortran side maps any
+ *     non-zero status to exitt(1).
+ *   - One host thread per context.  The context owns one CUDA stream; calls
+ *     that return host data synchronise that stream, others may return before
+ *     the GPU work ends.
+ */
+#ifndef NEKCEM_GPU_H
+#define NEKCEM_GPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define NEKGPU_OK 0
+#define NEKGPU_ERR_ARG -1         /* null pointer, bad size or index */
+#define NEKGPU_ERR_MESH -2        /* mesh the chosen form cannot run */
+#define NEKGPU_ERR_CUDA -3        /* CUDA runtime error */
+#define NEKGPU_ERR_NOMEM -4       /* device allocation failed / over budget */
+#define NEKGPU_ERR_STATE -5       /* call out of order */
+#define NEKGPU_ERR_BLOWUP -6      /* non-finite or |u| > 1e20 (chk_blowup) */
+#define NEKGPU_ERR_TIMEOUT -7     /* a bounded device wait ran out */
+#define NEKGPU_ERR_UNSUPPORTED -8 /* feature not built for this case */
+
+/* Compute forms. */
+#define NEKGPU_PLAIN 0   /* unfused all-FP64 kernels, one per reference routine */
+#define NEKGPU_FUSED64 1 /* fused curl+flux+lift+mass+RK stage kernel, all FP64 */
+#define NEKGPU_MIXED 2   /* fused stage kernel: FP32 contractions/curl/flux,
+                            FP64 state, RK register, inverse mass and norms */
+
+/* Face boundary codes (CBC in src/cem_maxwell.F:289-300, 1338-1366). */
+#define NEKGPU_BC_PEC 0
+#define NEKGPU_BC_PERIODIC 1
+
+typedef struct nekgpu_ctx nekgpu_ctx;
+
+/*
+ * Static arrays after cem_maxwell_init (src/cem_maxwell.F:65-191), as the
+ * Fortran COMMON blocks hold them (src/EMWAVE, src/GEOM).  npts = nx1^3*nelt,
+ * nxzfl = 6*nx1^2*nelt.
+ */
+typedef struct nekgpu_mesh {
+  int nx1;                 /* N+1 GLL points per direction */
+  int nelt;                /* elements on this rank */
+  const double* dxm1;      /* nx1*nx1, D(i,j) column-major (src/nek5_speclib.F:807) */
+  const double* w3mn;      /* nx1^3 GLL tensor weights */
+  const double* rxmn;      /* npts each: cofactor metrics jac*dr/dx ... */
+  const double* rymn;      /*   (src/nek5_coef.F:616-624, src/cem_maxwell.F:135-162) */
+  const double* rzmn;
+  const double* sxmn;
+  const double* symn;
+  const double* szmn;
+  const double* txmn;
+  const double* tymn;
+  const double* tzmn;
+  const double* bmn;       /* npts mass jac*w3 (src/nek5_coef.F:758) */
+  const double* xmn;       /* npts coordinates (used by source terms); may be NULL */
+  const double* ymn;
+  const double* zmn;
+  const double* unxm;      /* nxzfl unit normals (src/nek5_coef.F:1150-1237) */
+  const double* unym;
+  const double* unzm;
+  const double* aream;     /* nxzfl face area weights */
+  const int* cemface;      /* nxzfl, 1-based volume index (src/cem_common.F:214-257) */
+  const long long* glo_face; /* nxzfl gs ids of gsh_face (src/nek5_connect11.F:2223) */
+  const int* cempec;       /* ncempec 1-based PEC face slots (src/cem_maxwell.F:1338) */
+  int ncempec;
+  const double* Z_0;       /* nxzfl face impedances (src/cem_maxwell.F:262-325) */
+  const double* Z_1;
+  const double* Y_0;
+  const double* Y_1;
+  const double* ebm1;      /* npts 1/(eps*bm1) (src/cem_maxwell.F:183-186) */
+  const double* hbm1;      /* npts 1/(mu*bm1) */
+  double C0;               /* 1 upwind, 0 central (src/cem_maxwell.F:939-940) */
+} nekgpu_mesh;
+
+/*
+ * Structured affine box: what genbox + usrdat2 + uservp produce for the
+ * reference's box test cases, built on the host without the Fortran side.
+ * Elements are numbered x fastest, then y, then z.
+ */
+typedef struct nekgpu_box {
+  int N;                   /* polynomial order (nx1 = N+1), 1..15 */
+  int nelx, nely, nelz;
+  double lo[3], hi[3];     /* domain [lo,hi] per axis */
+  int bc[3];               /* NEKGPU_BC_PEC or NEKGPU_BC_PERIODIC per axis */
+  const double* permittivity; /* npts per node, or NULL for 1 */
+  const double* permeability; /* npts per node, or NULL for 1 */
+  double C0;               /* 1 upwind, 0 central */
+} nekgpu_box;
+
+const char* nekgpu_error_string(int status);
+int nekgpu_version(void);
+
+/* Select and check the CUDA device (default 0).  Called implicitly by init. */
+int nekgpu_device_check(int device);
+
+/* ---- setup / teardown ----------------------------------------------------- */
+/* Replaces cem_maxwell_init's hand-off: uploads the static arrays once.
+ * The face pairing comes from glo_face exactly as gs_setup groups it
+ * (src/jl/gs.h:17-60); groups of more than two are rejected.  The fused forms
+ * need affine elements (per-element-constant metrics) with axis-aligned faces
+ * whose paired nodes share in-face order; otherwise NEKGPU_ERR_MESH and the
+ * caller may use NEKGPU_PLAIN, which takes any conforming hex mesh. */
+int nekgpu_init(nekgpu_ctx** ctx, const nekgpu_mesh* mesh, int form);
+/* Builds the box case on the host (GLL points, geometry, face pairing,
+ * materials) and uploads it. */
+int nekgpu_init_box(nekgpu_ctx** ctx, const nekgpu_box* box, int form);
+int nekgpu_finalize(nekgpu_ctx* ctx);
+
+/* Host-only (no GPU needed): the box builder's reference-layout arrays, for
+ * checking the host setup.  Double arrays: "dxm1" (nx1^2), "w3mn" (nx1^3),
+ * "bmn","xmn","ymn","zmn","rxmn","symn","tzmn","ebm1","hbm1" (npts),
+ * "unxm","unym","unzm","aream","Z_0","Z_1","Y_0","Y_1" (nxzfl).  Integer
+ * arrays: "cemface" (nxzfl, 1-based), "glo_face" (nxzfl), "cempec" (1-based,
+ * *count entries).  *count receives the number of entries written. */
+int nekgpu_box_export_d(const nekgpu_box* box, const char* name, double* out, long* count);
+int nekgpu_box_export_i(const nekgpu_box* box, const char* name, long long* out, long* count);
+
+/* sizes: npts, nxzfl, nelt, nx1 */
+int nekgpu_sizes(const nekgpu_ctx* ctx, long* npts, long* nxzfl, int* nelt, int* nx1);
+/* the box builder's arrays (reference layout), for users that need
+ * coordinates / mass without the Fortran side: name in
+ * {"xmn","ymn","zmn","bmn","ebm1","hbm1"}; out has npts doubles */
+int nekgpu_get_array(nekgpu_ctx* ctx, const char* name, double* out);
+double nekgpu_volume(const nekgpu_ctx* ctx);
+
+/* Gaussian-in-space, Ricker-in-time E_z volume source in mass-weighted form,
+ * added before the inverse mass like usersrc (src/cem_maxwell.F:503):
+ * resEz += bm1 * amp * exp(-|x-xc|^2/(2 sigma^2)) * ricker(t; f0, t0),
+ * ricker(t) = (1 - 2 a^2) exp(-a^2), a = pi f0 (t - t0).  enabled=0 clears. */
+int nekgpu_set_source(nekgpu_ctx* ctx, int enabled, const double xc[3], double sigma,
+                      double amp, double f0, double t0);
+
+/* ---- state --------------------------------------------------------------- */
+/* hn(ld,3), en(ld,3) host arrays, ld >= npts (lpts1 in the reference). */
+int nekgpu_set_state(nekgpu_ctx* ctx, const double* hn, const double* en, long ld);
+int nekgpu_get_state(nekgpu_ctx* ctx, double* hn, double* en, long ld);
+/* RK register khn/ken (src/EMWAVE); zero after set_state unless set here. */
+int nekgpu_set_rk_register(nekgpu_ctx* ctx, const double* khn, const double* ken, long ld);
+int nekgpu_get_rk_register(nekgpu_ctx* ctx, double* khn, double* ken, long ld);
+/* Pin caller host memory once (cudaHostRegister) so per-step copies are DMA. */
+int nekgpu_register_host(nekgpu_ctx* ctx, void* ptr, long bytes);
+int nekgpu_unregister_host(nekgpu_ctx* ctx, void* ptr);
+
+/* ---- time stepping --------------------------------------------------------- */
+/* One RK stage rkstep=1..5 at time `time` (rk_c + cem_maxwell_op +
+ * rk_maxwell_ab; src/cem_maxwell.F:336-340). */
+int nekgpu_stage(nekgpu_ctx* ctx, int rkstep, double time, double dt);
+/* nsteps full steps (cem_maxwell_op_rk each), device-resident state;
+ * *time += dt after each step as time_advancing_pde does (src/cem_drive.F:639). */
+int nekgpu_step(nekgpu_ctx* ctx, int nsteps, double* time, double dt);
+/* Drop-in for one cem_maxwell_op_rk call on host arrays: copies hn/en in,
+ * runs the 5 stages, copies hn/en back.  The RK register stays on the GPU. */
+int nekgpu_op_rk_host(nekgpu_ctx* ctx, double* hn, double* en, long ld, double time,
+                      double dt);
+
+/* ---- the reference routines one by one (NEKGPU_PLAIN only) ---------------- */
+int nekgpu_cem_maxwell(nekgpu_ctx* ctx);            /* src/cem_maxwell.F:574-582 */
+int nekgpu_restrict_to_face(nekgpu_ctx* ctx);       /* src/cem_maxwell.F:604-623 */
+int nekgpu_flux3d(nekgpu_ctx* ctx);                 /* src/cem_maxwell.F:922-1002 */
+int nekgpu_add_flux_to_res(nekgpu_ctx* ctx);        /* src/cem_maxwell.F:725-735 */
+int nekgpu_usersrc(nekgpu_ctx* ctx, double rktime); /* src/cem_maxwell.F:503 */
+int nekgpu_invqmass(nekgpu_ctx* ctx);               /* src/cem_maxwell.F:1878-1886 */
+int nekgpu_rk_maxwell_ab(nekgpu_ctx* ctx, int rkstep, double dt); /* src/cem_maxwell.F:1906 */
+/* gs_op_fields(gsh_face, u, nxzfl, nfld, 1, 1, 0) on host data u(nxzfl,nfld)
+ * (src/jl/gs.c:2074), through the device face exchange. */
+int nekgpu_gs_op_fields(nekgpu_ctx* ctx, double* u, int nfld);
+/* intermediate arrays of the plain form: "reshn","resen" (npts*3),
+ * "fhn","fen" (nxzfl*3), "srflx" (nxzfl*6) */
+int nekgpu_get_work(nekgpu_ctx* ctx, const char* name, double* out);
+
+/* ---- norms ----------------------------------------------------------------- */
+/* cem_error (src/cem_common.F:1335-1355) for the 6 components against host
+ * exact fields: l2[q] = sqrt(sum e*bm1*e / vol), linf[q] = max|e|, FP64. */
+int nekgpu_norms(nekgpu_ctx* ctx, const double* exact_h, const double* exact_e, long ld,
+                 double l2[6], double linf[6]);
+/* field energy 0.5*sum bm1*(eps|E|^2 + mu|H|^2), FP64 on device */
+int nekgpu_energy(nekgpu_ctx* ctx, double* energy);
+/* chk_blowup (src/cem_common.F:1150-1165): NEKGPU_ERR_BLOWUP if any state
+ * value is non-finite or above 1e20 in magnitude */
+int nekgpu_check_blowup(nekgpu_ctx* ctx);
+
+/* ---- timing ---------------------------------------------------------------- */
+/* Runs nsteps steps between CUDA events on the context stream and returns the
+ * elapsed device milliseconds (state advances; *time += nsteps*dt). */
+int nekgpu_time_steps(nekgpu_ctx* ctx, int nsteps, double* time, double dt, double* ms);
+/* kernel launches issued by the last nekgpu_step / nekgpu_time_steps call */
+long nekgpu_last_launches(const nekgpu_ctx* ctx);
+/* synchronise the context stream */
+int nekgpu_sync(nekgpu_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,1254 @@
+// Host runtime of the GB300 Maxwell DG library: the C ABI of nekcem_gpu.h.
+//
+// Responsibilities: validate and upload the reference's static arrays
+// (nekgpu_init) or build a structured box case (nekgpu_init_box), own the
+// device memory and the stream, and drive the stage kernels.  No arithmetic
+// of the time step runs here.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "nekgpu_internal.h"
+
+using namespace nekgpu;
+
+struct nekgpu_ctx : public Context {};
+
+namespace nekgpu {
+
+static thread_local std::string g_last_cuda;
+
+int check_cuda(cudaError_t e) {
+  if (e == cudaSuccess) return NEKGPU_OK;
+  g_last_cuda = cudaGetErrorString(e);
+  return NEKGPU_ERR_CUDA;
+}
+
+// rk_storage, RK45 branch (src/cem_common.F:78-104): Carpenter-Kennedy
+// 5-stage 4th-order low-storage coefficients.
+void rk_coeffs(double a[5], double b[5], double c[6]) {
+  a[0] = 0.0;
+  a[1] = -567301805773.0 / 1357537059087.0;
+  a[2] = -2404267990393.0 / 2016746695238.0;
+  a[3] = -3550918686646.0 / 2091501179385.0;
+  a[4] = -1275806237668.0 / 842570457699.0;
+  b[0] = 1432997174477.0 / 9575080441755.0;
+  b[1] = 5161836677717.0 / 13612068292357.0;
+  b[2] = 1720146321549.0 / 2090206949498.0;
+  b[3] = 3134564353537.0 / 4481467310338.0;
+  b[4] = 2277821191437.0 / 14882151754819.0;
+  c[0] = 0.0;
+  c[1] = 1432997174477.0 / 9575080441755.0;
+  c[2] = 2526269341429.0 / 6820363962896.0;
+  c[3] = 2006345519317.0 / 3224310063776.0;
+  c[4] = 2802321613138.0 / 2924317926251.0;
+  c[5] = 1.0;
+}
+
+}  // namespace nekgpu
+
+namespace {
+
+// face slot (reference order) -> axis (0=r,1=s,2=t), side, opposite slot
+const int kSlotAxis[6] = {1, 0, 1, 0, 2, 2};
+const int kSlotSide[6] = {-1, +1, +1, -1, -1, +1};
+const int kSlotOpp[6] = {2, 3, 0, 1, 5, 4};
+
+int face_vol(int f, int a, int b, int n) {
+  int fixed = kSlotSide[f] < 0 ? 0 : n - 1;
+  switch (kSlotAxis[f]) {
+    case 0: return fixed + n * a + n * n * b;
+    case 1: return a + n * fixed + n * n * b;
+    default: return a + n * b + n * n * fixed;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// GLL points, weights and derivative matrix for the box builder: interior
+// points are the roots of P_N' (Newton on the Legendre recurrence, started at
+// the Chebyshev-Gauss-Lobatto points), w_i = 2/(N(N+1) P_N(z_i)^2), and
+// D(i,j) = P_N(z_i)/(P_N(z_j)(z_i-z_j)), D(0,0) = -N(N+1)/4,
+// D(N,N) = N(N+1)/4 (the same D as DGLL, src/nek5_speclib.F:807-840).
+// ---------------------------------------------------------------------------
+void legendre(int N, double x, double* p, double* dp) {
+  double p0 = 1.0, p1 = x;
+  if (N == 0) { *p = 1.0; *dp = 0.0; return; }
+  for (int k = 1; k < N; ++k) {
+    double p2 = ((2.0 * k + 1.0) * x * p1 - k * p0) / (k + 1.0);
+    p0 = p1;
+    p1 = p2;
+  }
+  *p = p1;
+  // P_N'(x) = N (x P_N - P_{N-1}) / (x^2 - 1), valid inside (-1,1)
+  *dp = (std::fabs(x) < 1.0) ? N * (x * p1 - p0) / (x * x - 1.0) : 0.5 * N * (N + 1.0) * (x > 0 ? 1.0 : (N % 2 ? 1.0 : -1.0));
+}
+
+void gll(int N, std::vector<double>& z, std::vector<double>& w, std::vector<double>& D) {
+  const int n = N + 1;
+  const double pi = 4.0 * std::atan(1.0);
+  z.assign(n, 0.0);
+  w.assign(n, 0.0);
+  z[0] = -1.0;
+  z[N] = 1.0;
+  for (int i = 1; i < N; ++i) {
+    double x = -std::cos(pi * i / N);
+    for (int it = 0; it < 100; ++it) {
+      double p, dp;
+      legendre(N, x, &p, &dp);
+      // P_N'' from (1-x^2) P'' = 2x P' - N(N+1) P
+      double d2p = (2.0 * x * dp - N * (N + 1.0) * p) / (1.0 - x * x);
+      double dx = dp / d2p;
+      x -= dx;
+      if (std::fabs(dx) < 1e-16) break;
+    }
+    z[i] = x;
+  }
+  for (int i = 0; i < n / 2; ++i) {  // symmetrise
+    double s = 0.5 * (z[N - i] - z[i]);
+    z[i] = -s;
+    z[N - i] = s;
+  }
+  if (n % 2) z[N / 2] = 0.0;
+  for (int i = 0; i < n; ++i) {
+    double p, dp;
+    legendre(N, z[i], &p, &dp);
+    w[i] = 2.0 / (N * (N + 1.0) * p * p);
+  }
+  D.assign((size_t)n * n, 0.0);
+  std::vector<double> pn(n);
+  for (int i = 0; i < n; ++i) {
+    double dp;
+    legendre(N, z[i], &pn[i], &dp);
+  }
+  const double d0 = N * (N + 1.0) / 4.0;
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < n; ++j) {
+      double v = 0.0;
+      if (i != j) v = pn[i] / (pn[j] * (z[i] - z[j]));
+      if (i == j && i == 0) v = -d0;
+      if (i == j && i == N) v = d0;
+      D[i + (size_t)n * j] = v;
+    }
+}
+
+// impedance combination of cem_maxwell_materials (src/cem_maxwell.F:262-325)
+// for one face node: own (Zm, Ym), partner (Zp, Yp) or pec.
+void face_impedance(double Zm, double Ym, double Zp, double Yp, bool pec, double C0, double out[4]) {
+  double Z0 = pec ? 2.0 * Zm : Zm + Zp;
+  double Y0 = pec ? 2.0 * Ym : Ym + Yp;
+  double Z1 = Z0 - Zm, Y1 = Y0 - Ym;
+  Z0 = 0.5 * Z0;
+  Y0 = 0.5 * Y0;
+  out[0] = -0.5 / Y0 * Y1;  // Y02
+  out[1] = 0.5 / Y0 * C0;   // C02Y
+  out[2] = 0.5 / Z0 * Z1;   // Z02
+  out[3] = 0.5 / Z0 * C0;   // C02Z
+}
+
+struct DevAlloc {
+  Context* c;
+  size_t budget, used = 0;
+  explicit DevAlloc(Context* cc) : c(cc) {
+    const char* b = std::getenv("NEKGPU_MEM_BUDGET_MB");
+    budget = b ? (size_t)std::atoll(b) << 20 : (size_t)-1;
+  }
+  template <typename T>
+  int get(T** p, size_t count) {
+    size_t bytes = std::max<size_t>(count, 1) * sizeof(T);
+    if (used + bytes > budget) return NEKGPU_ERR_NOMEM;
+    void* q = nullptr;
+    cudaError_t e = cudaMalloc(&q, bytes);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      return NEKGPU_ERR_NOMEM;
+    }
+    used += bytes;
+    c->allocs.push_back(q);
+    *p = (T*)q;
+    return NEKGPU_OK;
+  }
+  template <typename T>
+  int put(T** p, const std::vector<T>& h) {
+    int st = get(p, h.size());
+    if (st) return st;
+    if (!h.empty())
+      return check_cuda(cudaMemcpy(*p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice));
+    return NEKGPU_OK;
+  }
+};
+
+void free_all(Context* c) {
+  for (void* p : c->allocs) cudaFree(p);
+  c->allocs.clear();
+  if (c->ev0) cudaEventDestroy(c->ev0);
+  if (c->ev1) cudaEventDestroy(c->ev1);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  c->ev0 = c->ev1 = nullptr;
+  c->stream = nullptr;
+}
+
+// ---------------------------------------------------------------------------
+// Plain-form arrays from the reference's arrays (any conforming hex mesh).
+// ---------------------------------------------------------------------------
+int pairs_from_ids(const long long* ids, long m, std::vector<int>& pairs, std::vector<int>& single) {
+  std::vector<long> ord(m);
+  for (long i = 0; i < m; ++i) ord[i] = i;
+  std::sort(ord.begin(), ord.end(), [&](long a, long b) {
+    return ids[a] != ids[b] ? ids[a] < ids[b] : a < b;
+  });
+  pairs.clear();
+  single.clear();
+  long i = 0;
+  while (i < m) {
+    long j = i + 1;
+    while (j < m && ids[ord[j]] == ids[ord[i]]) ++j;
+    if (ids[ord[i]] <= 0) return NEKGPU_ERR_MESH;  // gs ignores id 0, flagged ids unsupported
+    if (j - i == 2) {
+      pairs.push_back((int)ord[i]);
+      pairs.push_back((int)ord[i + 1]);
+    } else if (j - i == 1) {
+      single.push_back((int)ord[i]);
+    } else {
+      return NEKGPU_ERR_MESH;
+    }
+    i = j;
+  }
+  return NEKGPU_OK;
+}
+
+int build_plain(const nekgpu_mesh* m, PlainHost& p) {
+  const int n = m->nx1;
+  const long n3 = (long)n * n * n, npts = n3 * m->nelt, nxzfl = 6L * n * n * m->nelt;
+  auto cp = [](const double* src, long len, std::vector<double>& dst) {
+    dst.assign(src, src + len);
+  };
+  cp(m->dxm1, (long)n * n, p.dxm1);
+  p.dxtm1.resize((size_t)n * n);
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < n; ++j) p.dxtm1[j + (size_t)n * i] = m->dxm1[i + (size_t)n * j];
+  cp(m->w3mn, n3, p.w3);
+  p.metrics.resize(9 * (size_t)npts);
+  const double* mt[9] = {m->rxmn, m->rymn, m->rzmn, m->sxmn, m->symn, m->szmn, m->txmn, m->tymn, m->tzmn};
+  for (int q = 0; q < 9; ++q) std::copy(mt[q], mt[q] + npts, p.metrics.begin() + q * npts);
+  cp(m->unxm, nxzfl, p.unx); cp(m->unym, nxzfl, p.uny); cp(m->unzm, nxzfl, p.unz);
+  cp(m->aream, nxzfl, p.area);
+  cp(m->Z_0, nxzfl, p.Z0); cp(m->Z_1, nxzfl, p.Z1); cp(m->Y_0, nxzfl, p.Y0); cp(m->Y_1, nxzfl, p.Y1);
+  cp(m->ebm1, npts, p.ebm1); cp(m->hbm1, npts, p.hbm1); cp(m->bmn, npts, p.bm1);
+  p.cemface.resize(nxzfl);
+  for (long j = 0; j < nxzfl; ++j) {
+    int v = m->cemface[j] - 1;
+    if (v < 0 || v >= npts) return NEKGPU_ERR_ARG;
+    p.cemface[j] = v;
+  }
+  std::vector<int> single;
+  int st = pairs_from_ids(m->glo_face, nxzfl, p.pairs, single);
+  if (st) return st;
+  p.cempec.resize(m->ncempec);
+  for (int j = 0; j < m->ncempec; ++j) {
+    int s = m->cempec[j] - 1;
+    if (s < 0 || s >= nxzfl) return NEKGPU_ERR_ARG;
+    p.cempec[j] = s;
+  }
+  // CSR: volume node -> face slots, ascending slot order
+  p.lift_ptr.assign(npts + 1, 0);
+  for (long j = 0; j < nxzfl; ++j) p.lift_ptr[p.cemface[j] + 1]++;
+  for (long v = 0; v < npts; ++v) p.lift_ptr[v + 1] += p.lift_ptr[v];
+  p.lift_slot.assign(nxzfl, 0);
+  std::vector<int> fill(p.lift_ptr.begin(), p.lift_ptr.end() - 1);
+  for (long j = 0; j < nxzfl; ++j) p.lift_slot[fill[p.cemface[j]]++] = (int)j;
+  p.C0 = m->C0;
+  return NEKGPU_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Compact (fused-form) description from the reference's arrays: requires
+// affine elements whose r,s,t axes are +x,+y,+z, canonical cemface, and
+// face pairs that join opposite slots with the same in-face order.
+// ---------------------------------------------------------------------------
+int build_compact(const nekgpu_mesh* m, Compact& cp) {
+  const int n = m->nx1, nelt = m->nelt;
+  const long n2 = (long)n * n, n3 = n2 * n, npts = n3 * nelt, nxzfl = 6 * n2 * nelt;
+  const double tol = 1e-9;
+  cp.nx = n;
+  cp.nelt = nelt;
+  cp.D.assign(m->dxm1, m->dxm1 + n * n);
+  cp.w3.assign(m->w3mn, m->w3mn + n3);
+  cp.w.resize(n);
+  const double w0 = std::cbrt(m->w3mn[0]);
+  for (int i = 0; i < n; ++i) cp.w[i] = m->w3mn[i] / (w0 * w0);
+  for (long v = 0; v < n3; ++v) {  // w3 must be a tensor product
+    int i = v % n, j = (v / n) % n, k = v / n2;
+    double t = cp.w[i] * cp.w[j] * cp.w[k];
+    if (std::fabs(t - m->w3mn[v]) > 1e-12 * std::fabs(t)) return NEKGPU_ERR_MESH;
+  }
+  cp.egeom.assign(9 * (size_t)nelt, 0.0);
+  const double* mt[9] = {m->rxmn, m->rymn, m->rzmn, m->sxmn, m->symn, m->szmn, m->txmn, m->tymn, m->tzmn};
+  for (int e = 0; e < nelt; ++e) {
+    const long o = n3 * e;
+    double diag[3] = {0, 0, 0};
+    const int di[3] = {0, 4, 8};
+    for (int d = 0; d < 3; ++d) {
+      double s = 0;
+      for (long v = 0; v < n3; ++v) s += mt[di[d]][o + v];
+      diag[d] = s / n3;
+      if (!(diag[d] > 0)) return NEKGPU_ERR_MESH;
+    }
+    const double scale = std::max(diag[0], std::max(diag[1], diag[2]));
+    for (int q = 0; q < 9; ++q) {
+      const bool isdiag = (q == 0 || q == 4 || q == 8);
+      const double ref = isdiag ? diag[q / 4] : 0.0;
+      for (long v = 0; v < n3; ++v)
+        if (std::fabs(mt[q][o + v] - ref) > tol * scale) return NEKGPU_ERR_MESH;
+    }
+    cp.egeom[9 * e + 0] = diag[0];
+    cp.egeom[9 * e + 1] = diag[1];
+    cp.egeom[9 * e + 2] = diag[2];
+    for (int f = 0; f < 6; ++f) {
+      const int ax = kSlotAxis[f], sd = kSlotSide[f];
+      double s = 0;
+      for (int b = 0; b < n; ++b)
+        for (int a = 0; a < n; ++a) {
+          const long j = a + (long)n * b + n2 * (f + 6L * e);
+          if (m->cemface[j] - 1 != o + face_vol(f, a, b, n)) return NEKGPU_ERR_MESH;
+          const double nv[3] = {m->unxm[j], m->unym[j], m->unzm[j]};
+          for (int d = 0; d < 3; ++d) {
+            const double want = (d == ax) ? (double)sd : 0.0;
+            if (std::fabs(nv[d] - want) > tol) return NEKGPU_ERR_MESH;
+          }
+          s += m->aream[j] / (cp.w[a] * cp.w[b]);
+        }
+      s /= n2;
+      for (int b = 0; b < n; ++b)
+        for (int a = 0; a < n; ++a) {
+          const long j = a + (long)n * b + n2 * (f + 6L * e);
+          if (std::fabs(m->aream[j] / (cp.w[a] * cp.w[b]) - s) > tol * s) return NEKGPU_ERR_MESH;
+        }
+      cp.egeom[9 * e + 3 + f] = s;
+    }
+  }
+  // pairing
+  std::vector<int> pairs, single;
+  int st = pairs_from_ids(m->glo_face, nxzfl, pairs, single);
+  if (st) return st;
+  std::vector<char> is_pec(nxzfl, 0);
+  for (int j = 0; j < m->ncempec; ++j) {
+    int s = m->cempec[j] - 1;
+    if (s < 0 || s >= nxzfl) return NEKGPU_ERR_ARG;
+    is_pec[s] = 1;
+  }
+  cp.nbr.assign(6 * (size_t)nelt, -3);  // -3: unset
+  auto set_nbr = [&](int e, int f, int val) {
+    int& r = cp.nbr[6 * e + f];
+    if (r == -3) r = val;
+    return r == val;
+  };
+  for (size_t p = 0; p < pairs.size(); p += 2) {
+    const long j0 = pairs[p], j1 = pairs[p + 1];
+    const int e0 = (int)(j0 / (6 * n2)), f0 = (int)((j0 / n2) % 6), ab0 = (int)(j0 % n2);
+    const int e1 = (int)(j1 / (6 * n2)), f1 = (int)((j1 / n2) % 6), ab1 = (int)(j1 % n2);
+    if (f1 != kSlotOpp[f0] || ab0 != ab1) return NEKGPU_ERR_MESH;
+    if (is_pec[j0] || is_pec[j1]) return NEKGPU_ERR_MESH;
+    if (!set_nbr(e0, f0, e1) || !set_nbr(e1, f1, e0)) return NEKGPU_ERR_MESH;
+  }
+  for (int s : single) {
+    if (!is_pec[s]) return NEKGPU_ERR_MESH;  // open (non-PEC singleton) faces: plain form only
+    const int e = (int)(s / (6 * n2)), f = (int)((s / n2) % 6);
+    if (!set_nbr(e, f, -1)) return NEKGPU_ERR_MESH;
+  }
+  for (int v : cp.nbr)
+    if (v == -3) return NEKGPU_ERR_MESH;
+  cp.ebm1.assign(m->ebm1, m->ebm1 + npts);
+  cp.hbm1.assign(m->hbm1, m->hbm1 + npts);
+  cp.bm1.assign(m->bmn, m->bmn + npts);
+  cp.C0 = m->C0;
+  cp.fcoef.resize(4 * (size_t)nxzfl);
+  cp.uniform = true;
+  const double def[4] = {-0.5, 0.5 * m->C0, 0.5, 0.5 * m->C0};
+  for (long j = 0; j < nxzfl; ++j) {
+    const double Y0 = m->Y_0[j], Y1 = m->Y_1[j], Z0 = m->Z_0[j], Z1 = m->Z_1[j];
+    double* o = &cp.fcoef[4 * j];
+    o[0] = -0.5 / Y0 * Y1;
+    o[1] = 0.5 / Y0 * m->C0;
+    o[2] = 0.5 / Z0 * Z1;
+    o[3] = 0.5 / Z0 * m->C0;
+    for (int q = 0; q < 4; ++q)
+      if (o[q] != def[q]) cp.uniform = false;
+  }
+  return NEKGPU_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Box builder: the reference arrays of a structured affine box, produced on
+// the host (genbox + genxyz + geometry + materials of the reference setup).
+// ---------------------------------------------------------------------------
+struct BoxArrays {
+  std::vector<double> D, w3, metrics[9], bm1, x, y, z, unx, uny, unz, area, Z0, Z1, Y0, Y1, ebm1, hbm1;
+  std::vector<int> cemface, cempec;
+  std::vector<long long> glo;
+  nekgpu_mesh mesh{};
+};
+
+// partner element across slot f of element ec, or -1 on a PEC wall
+long box_partner(const nekgpu_box* bx, const int nel[3], const long ec[3], int f) {
+  const int ax = kSlotAxis[f], sd = kSlotSide[f];
+  const long plane = ec[ax] + (sd > 0 ? 1 : 0);
+  if ((plane == 0 || plane == nel[ax]) && bx->bc[ax] == NEKGPU_BC_PEC) return -1;
+  long pc[3] = {ec[0], ec[1], ec[2]};
+  pc[ax] = (pc[ax] + sd + nel[ax]) % nel[ax];
+  return pc[0] + (long)nel[0] * (pc[1] + (long)nel[1] * pc[2]);
+}
+
+// impede / conduc of cem_maxwell_materials (src/cem_maxwell.F:272-275)
+double node_Z(const nekgpu_box* bx, long g) {
+  const double eps = bx->permittivity ? bx->permittivity[g] : 1.0;
+  const double mu = bx->permeability ? bx->permeability[g] : 1.0;
+  return std::sqrt(mu / eps);
+}
+double node_Y(const nekgpu_box* bx, long g) {
+  const double eps = bx->permittivity ? bx->permittivity[g] : 1.0;
+  const double mu = bx->permeability ? bx->permeability[g] : 1.0;
+  return std::sqrt(eps / mu);
+}
+
+int build_box(const nekgpu_box* bx, BoxArrays& A, bool full) {
+  const int N = bx->N, n = N + 1;
+  if (N < 1 || N > 15 || bx->nelx < 1 || bx->nely < 1 || bx->nelz < 1) return NEKGPU_ERR_ARG;
+  const int nel[3] = {bx->nelx, bx->nely, bx->nelz};
+  const long nelt = (long)nel[0] * nel[1] * nel[2];
+  const long n2 = (long)n * n, n3 = n2 * n, npts = n3 * nelt, nxzfl = 6 * n2 * nelt;
+  if (npts > (1L << 31) - 1 || nxzfl > (1L << 31) - 1) return NEKGPU_ERR_ARG;
+  for (int d = 0; d < 3; ++d)
+    if (!(bx->hi[d] > bx->lo[d]) || (bx->bc[d] != NEKGPU_BC_PEC && bx->bc[d] != NEKGPU_BC_PERIODIC))
+      return NEKGPU_ERR_ARG;
+  std::vector<double> z, w;
+  gll(N, z, w, A.D);
+  A.w3.resize(n3);
+  for (long v = 0; v < n3; ++v) A.w3[v] = w[v % n] * w[(v / n) % n] * w[v / n2];
+  double h[3];
+  for (int d = 0; d < 3; ++d) h[d] = (bx->hi[d] - bx->lo[d]) / nel[d];
+  const double xr = 0.5 * h[0], ys = 0.5 * h[1], zt = 0.5 * h[2];
+  const double jac = xr * ys * zt;
+  const double rx = ys * zt, sy = xr * zt, tz = xr * ys;
+  A.bm1.resize(npts);
+  A.x.resize(npts); A.y.resize(npts); A.z.resize(npts);
+  for (long e = 0; e < nelt; ++e) {
+    const long ex = e % nel[0], ey = (e / nel[0]) % nel[1], ez = e / ((long)nel[0] * nel[1]);
+    for (long v = 0; v < n3; ++v) {
+      const int i = v % n, j = (v / n) % n, k = v / n2;
+      const long g = e * n3 + v;
+      A.bm1[g] = jac * A.w3[v];
+      A.x[g] = bx->lo[0] + h[0] * ex + 0.5 * (z[i] + 1.0) * h[0];
+      A.y[g] = bx->lo[1] + h[1] * ey + 0.5 * (z[j] + 1.0) * h[1];
+      A.z[g] = bx->lo[2] + h[2] * ez + 0.5 * (z[k] + 1.0) * h[2];
+    }
+  }
+  // materials per node
+  A.ebm1.resize(npts);
+  A.hbm1.resize(npts);
+  for (long g = 0; g < npts; ++g) {
+    const double eps = bx->permittivity ? bx->permittivity[g] : 1.0;
+    const double mu = bx->permeability ? bx->permeability[g] : 1.0;
+    if (!(eps > 0) || !(mu > 0)) return NEKGPU_ERR_ARG;
+    A.ebm1[g] = 1.0 / (eps * A.bm1[g]);
+    A.hbm1[g] = 1.0 / (mu * A.bm1[g]);
+  }
+  if (full) {
+    for (int q = 0; q < 9; ++q) A.metrics[q].assign(npts, 0.0);
+    std::fill(A.metrics[0].begin(), A.metrics[0].end(), rx);
+    std::fill(A.metrics[4].begin(), A.metrics[4].end(), sy);
+    std::fill(A.metrics[8].begin(), A.metrics[8].end(), tz);
+  }
+  // faces: normals, areas, cemface, gs ids, PEC list, impedances (the
+  // reference-layout arrays; the fused path builds its compact form instead)
+  if (full) {
+    A.unx.assign(nxzfl, 0.0); A.uny.assign(nxzfl, 0.0); A.unz.assign(nxzfl, 0.0);
+    A.area.resize(nxzfl);
+    A.cemface.resize(nxzfl);
+    A.glo.resize(nxzfl);
+    A.Z0.resize(nxzfl); A.Z1.resize(nxzfl); A.Y0.resize(nxzfl); A.Y1.resize(nxzfl);
+    A.cempec.clear();
+    const double ascale[3] = {ys * zt, xr * zt, xr * ys};  // r-, s-, t-faces
+    const long long off[3] = {0, (long long)(nel[0] + 1) * nel[1] * nel[2],
+                              (long long)(nel[0] + 1) * nel[1] * nel[2] + (long long)(nel[1] + 1) * nel[0] * nel[2]};
+    for (long e = 0; e < nelt; ++e) {
+      const long ec[3] = {e % nel[0], (e / nel[0]) % nel[1], e / ((long)nel[0] * nel[1])};
+      for (int f = 0; f < 6; ++f) {
+        const int ax = kSlotAxis[f], sd = kSlotSide[f];
+        long plane = ec[ax] + (sd > 0 ? 1 : 0);
+        const bool boundary = (plane == 0 || plane == nel[ax]);
+        const bool pec = boundary && bx->bc[ax] == NEKGPU_BC_PEC;
+        if (boundary && !pec) plane = plane % nel[ax];
+        long long fid;
+        if (ax == 0) fid = off[0] + (plane * nel[1] + ec[1]) * nel[2] + ec[2];
+        else if (ax == 1) fid = off[1] + (plane * nel[0] + ec[0]) * nel[2] + ec[2];
+        else fid = off[2] + (plane * nel[0] + ec[0]) * nel[1] + ec[1];
+        const long pe = box_partner(bx, nel, ec, f);
+        for (int b = 0; b < n; ++b)
+          for (int a = 0; a < n; ++a) {
+            const long j = a + (long)n * b + n2 * (f + 6 * e);
+            const long g = e * n3 + face_vol(f, a, b, n);
+            A.cemface[j] = (int)(g + 1);
+            A.glo[j] = fid * (long long)n2 + a + (long long)n * b + 1;
+            if (ax == 0) A.unx[j] = sd; else if (ax == 1) A.uny[j] = sd; else A.unz[j] = sd;
+            A.area[j] = ascale[ax] * w[a] * w[b];
+            if (pec) A.cempec.push_back((int)(j + 1));
+            const long gp = pec ? g : pe * n3 + face_vol(kSlotOpp[f], a, b, n);
+            const double Zm = node_Z(bx, g), Ym = node_Y(bx, g);
+            const double Zp = node_Z(bx, gp), Yp = node_Y(bx, gp);
+            const double Z0 = pec ? 2.0 * Zm : Zm + Zp, Y0 = pec ? 2.0 * Ym : Ym + Yp;
+            A.Z1[j] = Z0 - Zm;
+            A.Y1[j] = Y0 - Ym;
+            A.Z0[j] = 0.5 * Z0;
+            A.Y0[j] = 0.5 * Y0;
+          }
+      }
+    }
+  }
+  nekgpu_mesh& m = A.mesh;
+  m.nx1 = n;
+  m.nelt = (int)nelt;
+  m.dxm1 = A.D.data();
+  m.w3mn = A.w3.data();
+  std::vector<double>* mt = A.metrics;
+  if (!full) {  // compact path: per-node metric arrays are not needed
+    for (int q = 0; q < 9; ++q) mt[q].clear();
+  }
+  m.rxmn = full ? mt[0].data() : nullptr; m.rymn = full ? mt[1].data() : nullptr;
+  m.rzmn = full ? mt[2].data() : nullptr; m.sxmn = full ? mt[3].data() : nullptr;
+  m.symn = full ? mt[4].data() : nullptr; m.szmn = full ? mt[5].data() : nullptr;
+  m.txmn = full ? mt[6].data() : nullptr; m.tymn = full ? mt[7].data() : nullptr;
+  m.tzmn = full ? mt[8].data() : nullptr;
+  m.bmn = A.bm1.data();
+  m.xmn = A.x.data(); m.ymn = A.y.data(); m.zmn = A.z.data();
+  m.unxm = A.unx.data(); m.unym = A.uny.data(); m.unzm = A.unz.data(); m.aream = A.area.data();
+  m.cemface = A.cemface.data();
+  m.glo_face = A.glo.data();
+  m.cempec = A.cempec.data();
+  m.ncempec = (int)A.cempec.size();
+  m.Z_0 = A.Z0.data(); m.Z_1 = A.Z1.data(); m.Y_0 = A.Y0.data(); m.Y_1 = A.Y1.data();
+  m.ebm1 = A.ebm1.data(); m.hbm1 = A.hbm1.data();
+  m.C0 = bx->C0;
+  return NEKGPU_OK;
+}
+
+// Compact description straight from the box (no per-node or per-face-node
+// reference arrays).
+void compact_from_box(const nekgpu_box* bx, const BoxArrays& A, Compact& cp) {
+  const int n = bx->N + 1;
+  const int nel[3] = {bx->nelx, bx->nely, bx->nelz};
+  const long nelt = (long)nel[0] * nel[1] * nel[2];
+  const long n2 = (long)n * n, n3 = n2 * n, nxzfl = 6 * n2 * nelt;
+  cp.nx = n;
+  cp.nelt = (int)nelt;
+  cp.D = A.D;
+  cp.w3 = A.w3;
+  std::vector<double> z, w, D;
+  gll(bx->N, z, w, D);
+  cp.w = w;
+  double h[3];
+  for (int d = 0; d < 3; ++d) h[d] = (bx->hi[d] - bx->lo[d]) / nel[d];
+  const double xr = 0.5 * h[0], ys = 0.5 * h[1], zt = 0.5 * h[2];
+  const double ascale[3] = {ys * zt, xr * zt, xr * ys};
+  cp.egeom.resize(9 * (size_t)nelt);
+  cp.nbr.resize(6 * (size_t)nelt);
+  for (long e = 0; e < nelt; ++e) {
+    const long ec[3] = {e % nel[0], (e / nel[0]) % nel[1], e / ((long)nel[0] * nel[1])};
+    cp.egeom[9 * e + 0] = ys * zt;
+    cp.egeom[9 * e + 1] = xr * zt;
+    cp.egeom[9 * e + 2] = xr * ys;
+    for (int f = 0; f < 6; ++f) {
+      cp.egeom[9 * e + 3 + f] = ascale[kSlotAxis[f]];
+      cp.nbr[6 * e + f] = (int)box_partner(bx, nel, ec, f);
+    }
+  }
+  cp.ebm1 = A.ebm1;
+  cp.hbm1 = A.hbm1;
+  cp.bm1 = A.bm1;
+  cp.C0 = bx->C0;
+  cp.uniform = true;
+  const long npts = n3 * nelt;
+  if (bx->permittivity)
+    for (long g = 0; g < npts && cp.uniform; ++g) cp.uniform = bx->permittivity[g] == 1.0;
+  if (bx->permeability)
+    for (long g = 0; g < npts && cp.uniform; ++g) cp.uniform = bx->permeability[g] == 1.0;
+  cp.fcoef.clear();
+  if (!cp.uniform) {
+    cp.fcoef.resize(4 * (size_t)nxzfl);
+    for (long e = 0; e < nelt; ++e) {
+      for (int f = 0; f < 6; ++f) {
+        const int pe = cp.nbr[6 * e + f];
+        for (int b = 0; b < n; ++b)
+          for (int a = 0; a < n; ++a) {
+            const long j = a + (long)n * b + n2 * (f + 6 * e);
+            const long g = e * n3 + face_vol(f, a, b, n);
+            const long gp = pe < 0 ? g : (long)pe * n3 + face_vol(kSlotOpp[f], a, b, n);
+            face_impedance(node_Z(bx, g), node_Y(bx, g), node_Z(bx, gp), node_Y(bx, gp), pe < 0,
+                           bx->C0, &cp.fcoef[4 * j]);
+          }
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// device upload
+// ---------------------------------------------------------------------------
+int common_setup(Context* c, int form, int nx, int nelt) {
+  int st = nekgpu_device_check(0);
+  if (st) return st;
+  c->form = form;
+  c->nx = nx;
+  c->nelt = nelt;
+  c->npts = (long)nx * nx * nx * nelt;
+  c->nxzfl = 6L * nx * nx * nelt;
+  rk_coeffs(c->rk_a, c->rk_b, c->rk_c);
+  if (check_cuda(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking))) return NEKGPU_ERR_CUDA;
+  if (check_cuda(cudaEventCreate(&c->ev0)) || check_cuda(cudaEventCreate(&c->ev1))) return NEKGPU_ERR_CUDA;
+  return NEKGPU_OK;
+}
+
+int upload_common(Context* c, DevAlloc& A, const std::vector<double>& bm1,
+                  const std::vector<double>& ebm1, const std::vector<double>& hbm1) {
+  int st;
+  if ((st = A.get(&c->d_k, 6 * c->npts))) return st;
+  if ((st = A.put(&c->d_bm1, bm1))) return st;
+  if ((st = A.put(&c->d_ebm1, ebm1))) return st;
+  if ((st = A.put(&c->d_hbm1, hbm1))) return st;
+  if ((st = A.get(&c->d_red, 512 * 12))) return st;
+  if ((st = A.get(&c->d_status, 4))) return st;
+  if (check_cuda(cudaMemset(c->d_k, 0, 6 * c->npts * sizeof(double)))) return NEKGPU_ERR_CUDA;
+  if (check_cuda(cudaMemset(c->d_status, 0, 4 * sizeof(int)))) return NEKGPU_ERR_CUDA;
+  double vol = 0;
+  for (double b : bm1) vol += b;
+  c->volume = vol;
+  c->host_bm1 = bm1;
+  return NEKGPU_OK;
+}
+
+int upload_plain(Context* c, const PlainHost& p) {
+  DevAlloc A(c);
+  int st;
+  if ((st = A.get(&c->d_u[0], 6 * c->npts))) return st;
+  if ((st = upload_common(c, A, p.bm1, p.ebm1, p.hbm1))) return st;
+  PlainDev& a = c->pargs;
+  a = PlainDev{};
+  a.nx = c->nx; a.nelt = c->nelt; a.npts = c->npts; a.nxzfl = c->nxzfl;
+  double *d1, *d2, *d3, *d4;
+  if ((st = A.put(&d1, p.dxm1)) || (st = A.put(&d2, p.dxtm1)) || (st = A.put(&d3, p.w3)) ||
+      (st = A.put(&d4, p.metrics)))
+    return st;
+  a.dxm1 = d1; a.dxtm1 = d2; a.w3 = d3; a.metrics = d4;
+  const std::vector<double>* fa[8] = {&p.unx, &p.uny, &p.unz, &p.area, &p.Z0, &p.Z1, &p.Y0, &p.Y1};
+  const double** fd[8] = {&a.unx, &a.uny, &a.unz, &a.area, &a.Z0, &a.Z1, &a.Y0, &a.Y1};
+  for (int q = 0; q < 8; ++q) {
+    double* d;
+    if ((st = A.put(&d, *fa[q]))) return st;
+    *fd[q] = d;
+  }
+  a.ebm1 = c->d_ebm1;
+  a.hbm1 = c->d_hbm1;
+  int *i1, *i2, *i3, *i4, *i5;
+  if ((st = A.put(&i1, p.cemface)) || (st = A.put(&i2, p.pairs)) || (st = A.put(&i3, p.cempec)) ||
+      (st = A.put(&i4, p.lift_ptr)) || (st = A.put(&i5, p.lift_slot)))
+    return st;
+  a.cemface = i1; a.pairs = i2; a.npairs = (int)(p.pairs.size() / 2);
+  a.cempec = i3; a.ncempec = (int)p.cempec.size();
+  a.lift_ptr = i4; a.lift_slot = i5;
+  a.C0 = p.C0;
+  a.u = c->d_u[0];
+  a.k = c->d_k;
+  double *r, *ff, *sf;
+  if ((st = A.get(&r, 6 * c->npts)) || (st = A.get(&ff, 6 * c->nxzfl)) || (st = A.get(&sf, 6 * c->nxzfl)))
+    return st;
+  a.res = r; a.fface = ff; a.srflx = sf;
+  cudaMemset(r, 0, 6 * c->npts * sizeof(double));
+  cudaMemset(ff, 0, 6 * c->nxzfl * sizeof(double));
+  cudaMemset(sf, 0, 6 * c->nxzfl * sizeof(double));
+  a.src_w = nullptr;
+  return NEKGPU_OK;
+}
+
+int upload_fused(Context* c, const Compact& cp) {
+  DevAlloc A(c);
+  int st;
+  if ((st = A.get(&c->d_u[0], 6 * c->npts)) || (st = A.get(&c->d_u[1], 6 * c->npts))) return st;
+  if ((st = upload_common(c, A, cp.bm1, cp.ebm1, cp.hbm1))) return st;
+  if ((st = A.get(&c->d_coef, 2 * c->npts))) return st;
+  if ((st = A.put(&c->d_nbr, cp.nbr))) return st;
+  if ((st = A.put(&c->d_egeom, cp.egeom))) return st;
+  std::vector<float> gf(cp.egeom.begin(), cp.egeom.end());
+  if ((st = A.put(&c->d_egeomf, gf))) return st;
+  c->uniform = cp.uniform;
+  c->d_fcoef = nullptr;
+  if (!cp.uniform) {
+    if (c->form == NEKGPU_MIXED) {
+      std::vector<float> f(cp.fcoef.begin(), cp.fcoef.end());
+      float* d;
+      if ((st = A.put(&d, f))) return st;
+      c->d_fcoef = d;
+    } else {
+      double* d;
+      if ((st = A.put(&d, cp.fcoef))) return st;
+      c->d_fcoef = d;
+    }
+  }
+  if ((st = fused_setup(c))) return st;
+  FusedDev& a = c->fargs;
+  a = FusedDev{};
+  a.nelt = c->nelt;
+  a.npts = c->npts;
+  a.k = c->d_k;
+  a.coef = c->d_coef;
+  a.nbr = c->d_nbr;
+  a.egeom = c->d_egeom;
+  a.egeomf = c->d_egeomf;
+  a.fcoef = c->d_fcoef;
+  a.C0 = cp.C0;
+  a.C0f = (float)cp.C0;
+  a.status = c->d_status;
+  for (int i = 0; i < c->nx * c->nx; ++i) {
+    a.D[i] = cp.D[i];
+    a.Df[i] = (float)cp.D[i];
+  }
+  for (int i = 0; i < c->nx; ++i) {
+    a.w[i] = cp.w[i];
+    a.wf[i] = (float)cp.w[i];
+  }
+  c->coef_dt = std::nan("");
+  return NEKGPU_OK;
+}
+
+int finish_init(Context* c, int st) {
+  if (st) {
+    free_all(c);
+    return st;
+  }
+  return NEKGPU_OK;
+}
+
+bool valid_form(int form) {
+  return form == NEKGPU_PLAIN || form == NEKGPU_FUSED64 || form == NEKGPU_MIXED;
+}
+
+int sync_status(Context* c) {
+  if (check_cuda(cudaStreamSynchronize(c->stream))) return NEKGPU_ERR_CUDA;
+  int h = 0;
+  if (check_cuda(cudaMemcpy(&h, c->d_status, sizeof(int), cudaMemcpyDeviceToHost))) return NEKGPU_ERR_CUDA;
+  return h ? NEKGPU_ERR_TIMEOUT : NEKGPU_OK;
+}
+
+double* state(Context* c) { return c->d_u[c->cur]; }
+
+int copy_fields_in(Context* c, double* dst, const double* hn, const double* en, long ld) {
+  const size_t w = c->npts * sizeof(double), pitch = ld * sizeof(double);
+  if (check_cuda(cudaMemcpy2DAsync(dst, w, hn, pitch, w, 3, cudaMemcpyHostToDevice, c->stream)))
+    return NEKGPU_ERR_CUDA;
+  if (check_cuda(cudaMemcpy2DAsync(dst + 3 * c->npts, w, en, pitch, w, 3, cudaMemcpyHostToDevice,
+                                   c->stream)))
+    return NEKGPU_ERR_CUDA;
+  return NEKGPU_OK;
+}
+
+int copy_fields_out(Context* c, const double* src, double* hn, double* en, long ld) {
+  const size_t w = c->npts * sizeof(double), pitch = ld * sizeof(double);
+  if (check_cuda(cudaMemcpy2DAsync(hn, pitch, src, w, w, 3, cudaMemcpyDeviceToHost, c->stream)))
+    return NEKGPU_ERR_CUDA;
+  if (check_cuda(cudaMemcpy2DAsync(en, pitch, src + 3 * c->npts, w, w, 3, cudaMemcpyDeviceToHost,
+                                   c->stream)))
+    return NEKGPU_ERR_CUDA;
+  return NEKGPU_OK;
+}
+
+double ricker(const Source& s, double t) {
+  const double pi = 4.0 * std::atan(1.0);
+  const double a = pi * s.f0 * (t - s.t0);
+  return (1.0 - 2.0 * a * a) * std::exp(-a * a);
+}
+
+int plain_stage(Context* c, int rkstep, double time, double dt) {
+  int st;
+  const double rktime = time + dt * c->rk_c[rkstep - 1];
+  if ((st = plain_cem_maxwell(c))) return st;
+  if ((st = plain_restrict_to_face(c))) return st;
+  if ((st = plain_flux3d(c))) return st;
+  if ((st = plain_add_flux_to_res(c))) return st;
+  if (c->src.enabled && (st = plain_usersrc(c, c->src.amp * ricker(c->src, rktime)))) return st;
+  if ((st = plain_invqmass(c))) return st;
+  return plain_rk_update(c, c->rk_a[rkstep - 1], c->rk_b[rkstep - 1], dt);
+}
+
+int do_stage(Context* c, int rkstep, double time, double dt) {
+  if (rkstep < 1 || rkstep > 5) return NEKGPU_ERR_ARG;
+  if (c->form == NEKGPU_PLAIN) return plain_stage(c, rkstep, time, dt);
+  return fused_stage(c, rkstep, time, dt);
+}
+
+int do_steps(Context* c, int nsteps, double* time, double dt) {
+  for (int s = 0; s < nsteps; ++s) {
+    for (int r = 1; r <= 5; ++r) {
+      int st = do_stage(c, r, *time, dt);
+      if (st) return st;
+    }
+    *time = *time + dt;
+  }
+  return NEKGPU_OK;
+}
+
+}  // namespace
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+extern "C" {
+
+const char* nekgpu_error_string(int status) {
+  switch (status) {
+    case NEKGPU_OK: return "ok";
+    case NEKGPU_ERR_ARG: return "invalid argument";
+    case NEKGPU_ERR_MESH: return "mesh not supported by this form";
+    case NEKGPU_ERR_CUDA: return g_last_cuda.empty() ? "CUDA error" : g_last_cuda.c_str();
+    case NEKGPU_ERR_NOMEM: return "device memory allocation failed or over budget";
+    case NEKGPU_ERR_STATE: return "call out of order";
+    case NEKGPU_ERR_BLOWUP: return "state blew up (non-finite or |u| > 1e20)";
+    case NEKGPU_ERR_TIMEOUT: return "a bounded device wait ran out";
+    case NEKGPU_ERR_UNSUPPORTED: return "not supported for this case";
+    default: return "unknown status";
+  }
+}
+
+int nekgpu_version(void) { return 1; }
+
+int nekgpu_device_check(int device) {
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess || count <= device || device < 0) {
+    cudaGetLastError();
+    g_last_cuda = "no CUDA device available";
+    return NEKGPU_ERR_CUDA;
+  }
+  if (check_cuda(cudaSetDevice(device))) return NEKGPU_ERR_CUDA;
+  cudaDeviceProp p;
+  if (check_cuda(cudaGetDeviceProperties(&p, device))) return NEKGPU_ERR_CUDA;
+  if (p.major < 10) {
+    g_last_cuda = "device is not Blackwell (sm_10x)";
+    return NEKGPU_ERR_CUDA;
+  }
+  return NEKGPU_OK;
+}
+
+int nekgpu_init(nekgpu_ctx** ctx, const nekgpu_mesh* m, int form) {
+  if (!ctx || !m || !valid_form(form)) return NEKGPU_ERR_ARG;
+  *ctx = nullptr;
+  if (m->nx1 < 2 || m->nx1 > kMaxNx || m->nelt < 1 || !m->dxm1 || !m->w3mn || !m->bmn ||
+      !m->unxm || !m->unym || !m->unzm || !m->aream || !m->cemface || !m->glo_face ||
+      !m->Z_0 || !m->Z_1 || !m->Y_0 || !m->Y_1 || !m->ebm1 || !m->hbm1 || !m->rxmn ||
+      !m->rymn || !m->rzmn || !m->sxmn || !m->symn || !m->szmn || !m->txmn || !m->tymn ||
+      !m->tzmn || m->ncempec < 0 || (m->ncempec > 0 && !m->cempec))
+    return NEKGPU_ERR_ARG;
+  nekgpu_ctx* c = new (std::nothrow) nekgpu_ctx();
+  if (!c) return NEKGPU_ERR_NOMEM;
+  int st;
+  if (form == NEKGPU_PLAIN) {
+    PlainHost p;
+    st = build_plain(m, p);
+    if (!st) st = common_setup(c, form, m->nx1, m->nelt);
+    if (!st) st = upload_plain(c, p);
+  } else {
+    Compact cp;
+    st = build_compact(m, cp);
+    if (!st) st = common_setup(c, form, m->nx1, m->nelt);
+    if (!st) st = upload_fused(c, cp);
+  }
+  if (!st && m->xmn && m->ymn && m->zmn) {
+    c->host_x.assign(m->xmn, m->xmn + c->npts);
+    c->host_y.assign(m->ymn, m->ymn + c->npts);
+    c->host_z.assign(m->zmn, m->zmn + c->npts);
+  }
+  st = finish_init(c, st);
+  if (st) {
+    delete c;
+    return st;
+  }
+  *ctx = c;
+  return NEKGPU_OK;
+}
+
+int nekgpu_init_box(nekgpu_ctx** ctx, const nekgpu_box* bx, int form) {
+  if (!ctx || !bx || !valid_form(form)) return NEKGPU_ERR_ARG;
+  *ctx = nullptr;
+  BoxArrays A;
+  int st = build_box(bx, A, form == NEKGPU_PLAIN);
+  if (st) return st;
+  if (form == NEKGPU_PLAIN) return nekgpu_init(ctx, &A.mesh, form);
+  if (bx->N + 1 < 3 || bx->N + 1 > 9) return NEKGPU_ERR_UNSUPPORTED;
+  nekgpu_ctx* c = new (std::nothrow) nekgpu_ctx();
+  if (!c) return NEKGPU_ERR_NOMEM;
+  Compact cp;
+  compact_from_box(bx, A, cp);
+  st = common_setup(c, form, bx->N + 1, A.mesh.nelt);
+  if (!st) st = upload_fused(c, cp);
+  if (!st) {
+    c->host_x = std::move(A.x); c->host_y = std::move(A.y); c->host_z = std::move(A.z);
+  }
+  st = finish_init(c, st);
+  if (st) {
+    delete c;
+    return st;
+  }
+  *ctx = c;
+  return NEKGPU_OK;
+}
+
+int nekgpu_box_export_d(const nekgpu_box* bx, const char* name, double* out, long* count) {
+  if (!bx || !name || !count) return NEKGPU_ERR_ARG;
+  BoxArrays A;
+  int st = build_box(bx, A, true);
+  if (st) return st;
+  std::string nm(name);
+  const std::vector<double>* v = nullptr;
+  if (nm == "dxm1") v = &A.D;
+  else if (nm == "w3mn") v = &A.w3;
+  else if (nm == "bmn") v = &A.bm1;
+  else if (nm == "xmn") v = &A.x;
+  else if (nm == "ymn") v = &A.y;
+  else if (nm == "zmn") v = &A.z;
+  else if (nm == "rxmn") v = &A.metrics[0];
+  else if (nm == "symn") v = &A.metrics[4];
+  else if (nm == "tzmn") v = &A.metrics[8];
+  else if (nm == "ebm1") v = &A.ebm1;
+  else if (nm == "hbm1") v = &A.hbm1;
+  else if (nm == "unxm") v = &A.unx;
+  else if (nm == "unym") v = &A.uny;
+  else if (nm == "unzm") v = &A.unz;
+  else if (nm == "aream") v = &A.area;
+  else if (nm == "Z_0") v = &A.Z0;
+  else if (nm == "Z_1") v = &A.Z1;
+  else if (nm == "Y_0") v = &A.Y0;
+  else if (nm == "Y_1") v = &A.Y1;
+  if (!v) return NEKGPU_ERR_ARG;
+  *count = (long)v->size();
+  if (out) std::copy(v->begin(), v->end(), out);
+  return NEKGPU_OK;
+}
+
+int nekgpu_box_export_i(const nekgpu_box* bx, const char* name, long long* out, long* count) {
+  if (!bx || !name || !count) return NEKGPU_ERR_ARG;
+  BoxArrays A;
+  int st = build_box(bx, A, true);
+  if (st) return st;
+  std::string nm(name);
+  if (nm == "glo_face") {
+    *count = (long)A.glo.size();
+    if (out) std::copy(A.glo.begin(), A.glo.end(), out);
+  } else if (nm == "cemface") {
+    *count = (long)A.cemface.size();
+    if (out) std::copy(A.cemface.begin(), A.cemface.end(), out);
+  } else if (nm == "cempec") {
+    *count = (long)A.cempec.size();
+    if (out) std::copy(A.cempec.begin(), A.cempec.end(), out);
+  } else {
+    return NEKGPU_ERR_ARG;
+  }
+  return NEKGPU_OK;
+}
+
+int nekgpu_finalize(nekgpu_ctx* c) {
+  if (!c) return NEKGPU_ERR_ARG;
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  free_all(c);
+  delete c;
+  return NEKGPU_OK;
+}
+
+int nekgpu_sizes(const nekgpu_ctx* c, long* npts, long* nxzfl, int* nelt, int* nx1) {
+  if (!c) return NEKGPU_ERR_ARG;
+  if (npts) *npts = c->npts;
+  if (nxzfl) *nxzfl = c->nxzfl;
+  if (nelt) *nelt = c->nelt;
+  if (nx1) *nx1 = c->nx;
+  return NEKGPU_OK;
+}
+
+double nekgpu_volume(const nekgpu_ctx* c) { return c ? c->volume : 0.0; }
+
+int nekgpu_get_array(nekgpu_ctx* c, const char* name, double* out) {
+  if (!c || !name || !out) return NEKGPU_ERR_ARG;
+  const std::vector<double>* v = nullptr;
+  std::string nm(name);
+  if (nm == "xmn") v = &c->host_x;
+  else if (nm == "ymn") v = &c->host_y;
+  else if (nm == "zmn") v = &c->host_z;
+  else if (nm == "bmn") v = &c->host_bm1;
+  if (v) {
+    if ((long)v->size() != c->npts) return NEKGPU_ERR_STATE;
+    std::copy(v->begin(), v->end(), out);
+    return NEKGPU_OK;
+  }
+  const double* d = nullptr;
+  if (nm == "ebm1") d = c->d_ebm1;
+  else if (nm == "hbm1") d = c->d_hbm1;
+  if (!d) return NEKGPU_ERR_ARG;
+  return check_cuda(cudaMemcpy(out, d, c->npts * sizeof(double), cudaMemcpyDeviceToHost));
+}
+
+int nekgpu_set_source(nekgpu_ctx* c, int enabled, const double xc[3], double sigma, double amp,
+                      double f0, double t0) {
+  if (!c) return NEKGPU_ERR_ARG;
+  if (!enabled) {
+    c->src.enabled = false;
+    c->pargs.src_w = nullptr;
+    c->fargs.src_elem = nullptr;
+    c->fargs.src_w = nullptr;
+    return NEKGPU_OK;
+  }
+  if (!xc || !(sigma > 0)) return NEKGPU_ERR_ARG;
+  if ((long)c->host_x.size() != c->npts) return NEKGPU_ERR_STATE;  // needs coordinates
+  const double s2 = 2.0 * sigma * sigma;
+  std::vector<double> g(c->npts);
+  double gmax = 0;
+  for (long i = 0; i < c->npts; ++i) {
+    const double dx = c->host_x[i] - xc[0], dy = c->host_y[i] - xc[1], dz = c->host_z[i] - xc[2];
+    g[i] = c->host_bm1[i] * std::exp(-(dx * dx + dy * dy + dz * dz) / s2);
+    gmax = std::max(gmax, g[i]);
+  }
+  DevAlloc A(c);
+  int st;
+  if (c->form == NEKGPU_PLAIN) {
+    if (!c->d_src_w_plain && (st = A.get(&c->d_src_w_plain, c->npts))) return st;
+    if (check_cuda(cudaMemcpy(c->d_src_w_plain, g.data(), c->npts * sizeof(double),
+                              cudaMemcpyHostToDevice)))
+      return NEKGPU_ERR_CUDA;
+    c->pargs.src_w = c->d_src_w_plain;
+  } else {
+    // elements whose weights are all below 1e-30 of the peak carry no source
+    const long n3 = (long)c->nx * c->nx * c->nx;
+    std::vector<int> off(c->nelt, -1);
+    std::vector<double> wd;
+    int cnt = 0;
+    for (int e = 0; e < c->nelt; ++e) {
+      double m = 0;
+      for (long v = 0; v < n3; ++v) m = std::max(m, g[e * n3 + v]);
+      if (m > 1e-30 * gmax) {
+        off[e] = cnt++;
+        wd.insert(wd.end(), g.begin() + e * n3, g.begin() + (e + 1) * n3);
+      }
+    }
+    int* d_off;
+    if ((st = A.put(&d_off, off))) return st;
+    if (c->form == NEKGPU_MIXED) {
+      std::vector<float> wf(wd.begin(), wd.end());
+      float* d;
+      if ((st = A.put(&d, wf))) return st;
+      c->d_src_w = d;
+    } else {
+      double* d;
+      if ((st = A.put(&d, wd))) return st;
+      c->d_src_w = d;
+    }
+    c->d_src_elem = d_off;
+    c->fargs.src_elem = d_off;
+    c->fargs.src_w = c->d_src_w;
+  }
+  c->src.enabled = true;
+  c->src.xc[0] = xc[0]; c->src.xc[1] = xc[1]; c->src.xc[2] = xc[2];
+  c->src.sigma = sigma; c->src.amp = amp; c->src.f0 = f0; c->src.t0 = t0;
+  return NEKGPU_OK;
+}
+
+int nekgpu_set_state(nekgpu_ctx* c, const double* hn, const double* en, long ld) {
+  if (!c || !hn || !en || ld < c->npts) return NEKGPU_ERR_ARG;
+  int st = copy_fields_in(c, state(c), hn, en, ld);
+  if (st) return st;
+  if (check_cuda(cudaMemsetAsync(c->d_k, 0, 6 * c->npts * sizeof(double), c->stream)))
+    return NEKGPU_ERR_CUDA;
+  c->have_state = true;
+  return check_cuda(cudaStreamSynchronize(c->stream));
+}
+
+int nekgpu_get_state(nekgpu_ctx* c, double* hn, double* en, long ld) {
+  if (!c || !hn || !en || ld < c->npts) return NEKGPU_ERR_ARG;
+  int st = copy_fields_out(c, state(c), hn, en, ld);
+  if (st) return st;
+  return sync_status(c);
+}
+
+int nekgpu_set_rk_register(nekgpu_ctx* c, const double* khn, const double* ken, long ld) {
+  if (!c || !khn || !ken || ld < c->npts) return NEKGPU_ERR_ARG;
+  int st = copy_fields_in(c, c->d_k, khn, ken, ld);
+  if (st) return st;
+  return check_cuda(cudaStreamSynchronize(c->stream));
+}
+
+int nekgpu_get_rk_register(nekgpu_ctx* c, double* khn, double* ken, long ld) {
+  if (!c || !khn || !ken || ld < c->npts) return NEKGPU_ERR_ARG;
+  int st = copy_fields_out(c, c->d_k, khn, ken, ld);
+  if (st) return st;
+  return sync_status(c);
+}
+
+int nekgpu_register_host(nekgpu_ctx* c, void* ptr, long bytes) {
+  if (!c || !ptr || bytes <= 0) return NEKGPU_ERR_ARG;
+  return check_cuda(cudaHostRegister(ptr, (size_t)bytes, cudaHostRegisterDefault));
+}
+
+int nekgpu_unregister_host(nekgpu_ctx* c, void* ptr) {
+  if (!c || !ptr) return NEKGPU_ERR_ARG;
+  return check_cuda(cudaHostUnregister(ptr));
+}
+
+int nekgpu_stage(nekgpu_ctx* c, int rkstep, double time, double dt) {
+  if (!c) return NEKGPU_ERR_ARG;
+  if (!c->have_state) return NEKGPU_ERR_STATE;
+  c->last_launches = 0;
+  return do_stage(c, rkstep, time, dt);
+}
+
+int nekgpu_step(nekgpu_ctx* c, int nsteps, double* time, double dt) {
+  if (!c || !time || nsteps < 0) return NEKGPU_ERR_ARG;
+  if (!c->have_state) return NEKGPU_ERR_STATE;
+  c->last_launches = 0;
+  return do_steps(c, nsteps, time, dt);
+}
+
+int nekgpu_op_rk_host(nekgpu_ctx* c, double* hn, double* en, long ld, double time, double dt) {
+  if (!c || !hn || !en || ld < c->npts) return NEKGPU_ERR_ARG;
+  c->last_launches = 0;
+  int st = copy_fields_in(c, state(c), hn, en, ld);
+  if (st) return st;
+  c->have_state = true;
+  for (int r = 1; r <= 5 && !st; ++r) st = do_stage(c, r, time, dt);
+  if (st) return st;
+  st = copy_fields_out(c, state(c), hn, en, ld);
+  if (st) return st;
+  return sync_status(c);
+}
+
+static int plain_only(nekgpu_ctx* c) {
+  if (!c) return NEKGPU_ERR_ARG;
+  if (c->form != NEKGPU_PLAIN) return NEKGPU_ERR_UNSUPPORTED;
+  c->last_launches = 0;
+  return NEKGPU_OK;
+}
+
+int nekgpu_cem_maxwell(nekgpu_ctx* c) {
+  int st = plain_only(c);
+  return st ? st : plain_cem_maxwell(c);
+}
+int nekgpu_restrict_to_face(nekgpu_ctx* c) {
+  int st = plain_only(c);
+  return st ? st : plain_restrict_to_face(c);
+}
+int nekgpu_flux3d(nekgpu_ctx* c) {
+  int st = plain_only(c);
+  return st ? st : plain_flux3d(c);
+}
+int nekgpu_add_flux_to_res(nekgpu_ctx* c) {
+  int st = plain_only(c);
+  return st ? st : plain_add_flux_to_res(c);
+}
+int nekgpu_usersrc(nekgpu_ctx* c, double rktime) {
+  int st = plain_only(c);
+  if (st) return st;
+  if (!c->src.enabled) return NEKGPU_OK;
+  return plain_usersrc(c, c->src.amp * ricker(c->src, rktime));
+}
+int nekgpu_invqmass(nekgpu_ctx* c) {
+  int st = plain_only(c);
+  return st ? st : plain_invqmass(c);
+}
+int nekgpu_rk_maxwell_ab(nekgpu_ctx* c, int rkstep, double dt) {
+  int st = plain_only(c);
+  if (st) return st;
+  if (rkstep < 1 || rkstep > 5) return NEKGPU_ERR_ARG;
+  return plain_rk_update(c, c->rk_a[rkstep - 1], c->rk_b[rkstep - 1], dt);
+}
+
+int nekgpu_gs_op_fields(nekgpu_ctx* c, double* u, int nfld) {
+  int st = plain_only(c);
+  if (st) return st;
+  if (!u || nfld < 1 || nfld > 6) return NEKGPU_ERR_ARG;
+  double* d = c->pargs.srflx;  // scratch of 6*nxzfl
+  const size_t bytes = (size_t)nfld * c->nxzfl * sizeof(double);
+  if (check_cuda(cudaMemcpyAsync(d, u, bytes, cudaMemcpyHostToDevice, c->stream))) return NEKGPU_ERR_CUDA;
+  if ((st = plain_gs(c, d, nfld))) return st;
+  if (check_cuda(cudaMemcpyAsync(u, d, bytes, cudaMemcpyDeviceToHost, c->stream))) return NEKGPU_ERR_CUDA;
+  return check_cuda(cudaStreamSynchronize(c->stream));
+}
+
+int nekgpu_get_work(nekgpu_ctx* c, const char* name, double* out) {
+  int st = plain_only(c);
+  if (st) return st;
+  if (!name || !out) return NEKGPU_ERR_ARG;
+  std::string nm(name);
+  const double* src = nullptr;
+  size_t count = 0;
+  if (nm == "reshn") { src = c->pargs.res; count = 3 * c->npts; }
+  else if (nm == "resen") { src = c->pargs.res + 3 * c->npts; count = 3 * c->npts; }
+  else if (nm == "fhn") { src = c->pargs.fface; count = 3 * c->nxzfl; }
+  else if (nm == "fen") { src = c->pargs.fface + 3 * c->nxzfl; count = 3 * c->nxzfl; }
+  else if (nm == "srflx") { src = c->pargs.srflx; count = 6 * c->nxzfl; }
+  else return NEKGPU_ERR_ARG;
+  if (check_cuda(cudaMemcpyAsync(out, src, count * sizeof(double), cudaMemcpyDeviceToHost, c->stream)))
+    return NEKGPU_ERR_CUDA;
+  return check_cuda(cudaStreamSynchronize(c->stream));
+}
+
+int nekgpu_norms(nekgpu_ctx* c, const double* exact_h, const double* exact_e, long ld,
+                 double l2[6], double linf[6]) {
+  if (!c || !exact_h || !exact_e || !l2 || !linf || ld < c->npts) return NEKGPU_ERR_ARG;
+  double* d = nullptr;
+  if (check_cuda(cudaMallocAsync(&d, 6 * c->npts * sizeof(double), c->stream))) return NEKGPU_ERR_NOMEM;
+  int st = copy_fields_in(c, d, exact_h, exact_e, ld);
+  if (!st) st = util_norms(c, d, l2, linf);
+  cudaFreeAsync(d, c->stream);
+  cudaStreamSynchronize(c->stream);
+  return st;
+}
+
+int nekgpu_energy(nekgpu_ctx* c, double* energy) {
+  if (!c || !energy) return NEKGPU_ERR_ARG;
+  return util_energy(c, energy);
+}
+
+int nekgpu_check_blowup(nekgpu_ctx* c) {
+  if (!c) return NEKGPU_ERR_ARG;
+  int bad = 0;
+  int st = util_blowup(c, &bad);
+  if (st) return st;
+  return bad ? NEKGPU_ERR_BLOWUP : NEKGPU_OK;
+}
+
+int nekgpu_time_steps(nekgpu_ctx* c, int nsteps, double* time, double dt, double* ms) {
+  if (!c || !time || !ms || nsteps < 0) return NEKGPU_ERR_ARG;
+  if (!c->have_state) return NEKGPU_ERR_STATE;
+  c->last_launches = 0;
+  if (c->form != NEKGPU_PLAIN) {
+    int st = scale_coef(c, dt);  // keep the one-off rescale out of the timed region
+    if (st) return st;
+  }
+  if (check_cuda(cudaEventRecord(c->ev0, c->stream))) return NEKGPU_ERR_CUDA;
+  c->last_launches = 0;
+  int st = do_steps(c, nsteps, time, dt);
+  if (st) return st;
+  if (check_cuda(cudaEventRecord(c->ev1, c->stream))) return NEKGPU_ERR_CUDA;
+  if (check_cuda(cudaEventSynchronize(c->ev1))) return NEKGPU_ERR_CUDA;
+  float f = 0;
+  if (check_cuda(cudaEventElapsedTime(&f, c->ev0, c->ev1))) return NEKGPU_ERR_CUDA;
+  *ms = f;
+  return sync_status(c);
+}
+
+long nekgpu_last_launches(const nekgpu_ctx* c) { return c ? c->last_launches : -1; }
+
+int nekgpu_sync(nekgpu_ctx* c) {
+  if (!c) return NEKGPU_ERR_ARG;
+  return sync_status(c);
+}
+
+}  // extern "C"

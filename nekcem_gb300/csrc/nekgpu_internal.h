@@ -1,0 +1,169 @@
+// Internal context of the GB300 Maxwell DG library (not part of the C ABI).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "nekcem_gpu.h"
+
+namespace nekgpu {
+
+constexpr int kMaxNx = 16;  // nx1 limit of the plain kernels (N <= 15)
+
+// Compact description of an affine, axis-aligned hex mesh: what the fused
+// forms consume.  Built either by the box builder or by compressing the
+// reference's per-node arrays (nekgpu_init).
+struct Compact {
+  int nx = 0, nelt = 0;
+  std::vector<double> D;        // nx*nx, D[i + nx*j] = D(i,j)
+  std::vector<double> w;        // nx GLL weights (w3 = w_i w_j w_k)
+  std::vector<double> w3;       // nx^3 (as given by the caller)
+  std::vector<double> egeom;    // per element: rx, sy, tz, area scale per slot (6)
+  std::vector<int> nbr;         // 6*nelt: partner element, -1 PEC mirror
+  std::vector<double> ebm1, hbm1;   // npts
+  std::vector<double> bm1;          // npts
+  std::vector<double> fcoef;    // 4*nxzfl: Y02, C02Y, Z02, C02Z per face node
+  bool uniform = true;          // all face coefficients equal the eps=mu=1 values
+  double C0 = 1.0;
+};
+
+// Full reference arrays, for the plain form (one kernel per routine).
+struct PlainHost {
+  std::vector<double> dxm1, dxtm1, w3, metrics;  // metrics: 9*npts rx,ry,rz,sx,sy,sz,tx,ty,tz
+  std::vector<double> unx, uny, unz, area, Z0, Z1, Y0, Y1, ebm1, hbm1, bm1;
+  std::vector<int> cemface;      // 0-based
+  std::vector<int> pairs;        // gs pairs (j0, j1), j0 < j1
+  std::vector<int> cempec;       // 0-based
+  std::vector<int> lift_ptr, lift_slot;  // CSR volume node -> face slots (ascending)
+  double C0 = 1.0;
+};
+
+struct Source {
+  bool enabled = false;
+  double xc[3] = {0, 0, 0}, sigma = 0, amp = 0, f0 = 0, t0 = 0;
+};
+
+// Kernel argument blocks ----------------------------------------------------
+
+struct PlainDev {
+  int nx, nelt;
+  long npts, nxzfl;
+  const double* dxm1;
+  const double* dxtm1;
+  const double* w3;
+  const double* metrics;
+  const double *unx, *uny, *unz, *area, *Z0, *Z1, *Y0, *Y1, *ebm1, *hbm1;
+  const int* cemface;
+  const int* pairs;
+  int npairs;
+  const int* cempec;
+  int ncempec;
+  const int *lift_ptr, *lift_slot;
+  double C0;
+  double* u;      // 6*npts state, H then E
+  double* k;      // 6*npts RK register
+  double* res;    // 6*npts
+  double* fface;  // 6*nxzfl restricted fields: fhn then fen
+  double* srflx;  // 6*nxzfl
+  const double* src_w;  // npts or null
+};
+
+struct FusedDev {
+  int nelt;
+  long npts;
+  const double* u_in;
+  double* u_out;
+  double* k;
+  const double* coef;   // 2*npts: dt*hbm1 then dt*ebm1
+  const int* nbr;       // 6*nelt
+  const double* egeom;  // 9*nelt
+  const float* egeomf;  // 9*nelt, FP32 copy for the mixed form
+  const void* fcoef;    // 4 per face node (T), null when uniform
+  const int* src_elem;  // nelt: offset (in elements) into src_w or -1; null if no source
+  const void* src_w;    // T, nx^3 per source element
+  double src_ft;        // amp*ricker(rktime)
+  float src_ftf;
+  double a, b;          // rk4a(i), rk4b(i)
+  double C0;
+  float C0f;
+  int* status;
+  double D[kMaxNx * kMaxNx];  // D(i,j) at [i + nx*j]
+  double w[kMaxNx];
+  float Df[kMaxNx * kMaxNx];  // FP32 copies (no FP64->FP32 conversion in the kernel)
+  float wf[kMaxNx];
+};
+
+struct Context {
+  int form = NEKGPU_MIXED;
+  int device = 0;
+  int nx = 0, nelt = 0;
+  long npts = 0, nxzfl = 0;
+  double volume = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+
+  // device memory
+  double* d_u[2] = {nullptr, nullptr};  // state (plain uses d_u[0] only)
+  int cur = 0;
+  double* d_k = nullptr;
+  double* d_bm1 = nullptr;
+  double* d_eps_mu = nullptr;  // 2*npts: eps (=1/(ebm1*bm1)), mu
+  double* d_red = nullptr;     // reduction scratch
+  int* d_status = nullptr;
+  std::vector<void*> allocs;
+
+  // fused form
+  double* d_coef = nullptr;  // 2*npts
+  double* d_hbm1 = nullptr;
+  double* d_ebm1 = nullptr;
+  double coef_dt = 0.0;
+  int* d_nbr = nullptr;
+  double* d_egeom = nullptr;
+  float* d_egeomf = nullptr;
+  void* d_fcoef = nullptr;
+  int* d_src_elem = nullptr;
+  void* d_src_w = nullptr;
+  bool uniform = true;
+  int fused_grid = 0;
+  FusedDev fargs{};
+
+  // plain form
+  PlainDev pargs{};
+  double* d_src_w_plain = nullptr;
+
+  Source src;
+  std::vector<double> host_bm1, host_x, host_y, host_z;
+  double rk_a[5], rk_b[5], rk_c[6];
+  long last_launches = 0;
+  bool have_state = false;
+};
+
+// host helpers (nekgpu_host.cpp)
+int check_cuda(cudaError_t e);
+void rk_coeffs(double a[5], double b[5], double c[6]);
+
+// kernel launchers (nekgpu_plain.cu)
+int plain_cem_maxwell(Context* c);
+int plain_restrict_to_face(Context* c);
+int plain_flux3d(Context* c);
+int plain_add_flux_to_res(Context* c);
+int plain_usersrc(Context* c, double ft);
+int plain_invqmass(Context* c);
+int plain_rk_update(Context* c, double ca, double cb, double dt);
+int plain_gs(Context* c, double* d_u, int nfld);
+
+// kernel launchers (nekgpu_fused.cu)
+int fused_setup(Context* c);  // grid size / smem attributes
+int fused_stage(Context* c, int rkstep, double time, double dt);
+int scale_coef(Context* c, double dt);
+
+// reductions / utilities (nekgpu_util.cu)
+int util_norms(Context* c, const double* d_exact, double l2[6], double linf[6]);
+int util_energy(Context* c, double* energy);
+int util_blowup(Context* c, int* bad);
+int util_strided_copy(Context* c, double* dst, const double* src, long n, int ncomp,
+                      long dst_ld, long src_ld);
+
+}  // namespace nekgpu

@@ -1,0 +1,287 @@
+// Plain form: one all-FP64 kernel per reference routine of the Maxwell stage.
+//
+// This translation unit is compiled with --fmad=false: every product and sum
+// is rounded separately, in the reference's order, so that on the reference's
+// own arrays the results are bit-identical to an unfused CPU evaluation
+// (Fortran without FMA contraction).  It works on the reference's general
+// per-node metric / per-face-node arrays, i.e. any conforming hex mesh.
+#include <cuda_runtime.h>
+
+#include "nekgpu_internal.h"
+
+namespace nekgpu {
+
+namespace {
+
+constexpr int kThreads = 256;
+
+inline int blocks_for(long n, int t = kThreads) {
+  long b = (n + t - 1) / t;
+  return (int)(b < 1 ? 1 : b);
+}
+
+// maxwell_wght_curl (src/cem_maxwell.F:1428-1497) with local_grad3
+// (src/nek5_grad.F:2-19) and the mxf summation order (src/nek5_mxm_std.F:173-191),
+// applied to H (-> resE) and E (-> resH, negated as chsign does,
+// src/cem_maxwell.F:580-582).  One CTA per element; field blocks in smem.
+__global__ void k_curl(PlainDev a) {
+  extern __shared__ double sm[];
+  const int n = a.nx;
+  const int n2 = n * n, n3 = n2 * n;
+  double* su = sm;           // 3*n3
+  double* sD = sm + 3 * n3;  // n2  D(i,l) at [i + n*l]
+  double* sDt = sD + n2;     // n2  Dt(l,j) at [l + n*j]
+  const int e = blockIdx.x;
+  for (int t = threadIdx.x; t < n2; t += blockDim.x) {
+    sD[t] = a.dxm1[t];
+    sDt[t] = a.dxtm1[t];
+  }
+  for (int fld = 0; fld < 2; ++fld) {
+    // fld 0: u = H (comps 0..2) -> resE (3..5); fld 1: u = E -> resH (0..2), negated
+    const int uin = fld == 0 ? 0 : 3, wout = fld == 0 ? 3 : 0;
+    __syncthreads();
+    for (int t = threadIdx.x; t < 3 * n3; t += blockDim.x) {
+      int q = t / n3, v = t - q * n3;
+      su[t] = a.u[(long)(uin + q) * a.npts + (long)e * n3 + v];
+    }
+    __syncthreads();
+    for (int v = threadIdx.x; v < n3; v += blockDim.x) {
+      const int i = v % n, j = (v / n) % n, k = v / n2;
+      double g[3][3];  // g[q][0..2] = d u_q / d(r,s,t)
+      for (int q = 0; q < 3; ++q) {
+        const double* u = su + q * n3;
+        // ur(i,jk) = sum_l D(i,l) u(l,jk)
+        double s = sD[i] * u[j * n + k * n2];
+        for (int l = 1; l < n; ++l) s = s + sD[i + n * l] * u[l + j * n + k * n2];
+        g[q][0] = s;
+        // us(i,j,k) = sum_l u(i,l,k) Dt(l,j)
+        s = u[i + k * n2] * sDt[n * j];
+        for (int l = 1; l < n; ++l) s = s + u[i + n * l + k * n2] * sDt[l + n * j];
+        g[q][1] = s;
+        // ut(ij,k) = sum_l u(ij,l) Dt(l,k)
+        s = u[i + n * j] * sDt[n * k];
+        for (int l = 1; l < n; ++l) s = s + u[i + n * j + n2 * l] * sDt[l + n * k];
+        g[q][2] = s;
+      }
+      const long gk = (long)e * n3 + v;
+      const double w = a.w3[v];
+      const double u1rw = g[0][0] * w, u1sw = g[0][1] * w, u1tw = g[0][2] * w;
+      const double u2rw = g[1][0] * w, u2sw = g[1][1] * w, u2tw = g[1][2] * w;
+      const double u3rw = g[2][0] * w, u3sw = g[2][1] * w, u3tw = g[2][2] * w;
+      const double* M = a.metrics;
+      const long P = a.npts;
+      const double rx = M[0 * P + gk], ry = M[1 * P + gk], rz = M[2 * P + gk];
+      const double sx = M[3 * P + gk], sy = M[4 * P + gk], sz = M[5 * P + gk];
+      const double tx = M[6 * P + gk], ty = M[7 * P + gk], tz = M[8 * P + gk];
+      double w1 = u3rw * ry + u3sw * sy + u3tw * ty - u2rw * rz - u2sw * sz - u2tw * tz;
+      double w2 = u1rw * rz + u1sw * sz + u1tw * tz - u3rw * rx - u3sw * sx - u3tw * tx;
+      double w3 = u2rw * rx + u2sw * sx + u2tw * tx - u1rw * ry - u1sw * sy - u1tw * ty;
+      if (fld == 1) { w1 = -w1; w2 = -w2; w3 = -w3; }
+      a.res[(long)(wout + 0) * P + gk] = w1;
+      a.res[(long)(wout + 1) * P + gk] = w2;
+      a.res[(long)(wout + 2) * P + gk] = w3;
+    }
+  }
+}
+
+// cem_maxwell_restrict_to_face (src/cem_maxwell.F:604-623)
+__global__ void k_restrict(PlainDev a) {
+  long j = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (j >= a.nxzfl) return;
+  long i = a.cemface[j];
+  for (int q = 0; q < 6; ++q) a.fface[q * a.nxzfl + j] = a.u[q * a.npts + i];
+}
+
+// first loop of cem_maxwell_flux3d (src/cem_maxwell.F:944-955): -n x E, -n x H
+__global__ void k_flux_pre(PlainDev a) {
+  long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  const long k = a.nxzfl;
+  if (i >= k) return;
+  const double nx = a.unx[i], ny = a.uny[i], nz = a.unz[i];
+  const double* fh = a.fface;
+  const double* fe = a.fface + 3 * k;
+  double* s = a.srflx;
+  s[0 * k + i] = -ny * fe[2 * k + i] + nz * fe[1 * k + i];
+  s[1 * k + i] = -nz * fe[0 * k + i] + nx * fe[2 * k + i];
+  s[2 * k + i] = -nx * fe[1 * k + i] + ny * fe[0 * k + i];
+  s[3 * k + i] = -ny * fh[2 * k + i] + nz * fh[1 * k + i];
+  s[4 * k + i] = -nz * fh[0 * k + i] + nx * fh[2 * k + i];
+  s[5 * k + i] = -nx * fh[1 * k + i] + ny * fh[0 * k + i];
+}
+
+// gs_op_fields(gsh_face, u, stride, nfld, 1, add, 0) on single-rank face ids
+// (src/jl/gs.c:2074-2099): each id group is a pair (or a singleton, left
+// alone); both members receive the same sum.
+__global__ void k_gs_pairs(const int* pairs, int npairs, double* u, long stride, int nfld) {
+  int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= npairs) return;
+  const int j0 = pairs[2 * p], j1 = pairs[2 * p + 1];
+  for (int q = 0; q < nfld; ++q) {
+    double* v = u + q * stride;
+    const double s = v[j0] + v[j1];
+    v[j0] = s;
+    v[j1] = s;
+  }
+}
+
+// cem_maxwell_flux_pec (src/cem_maxwell.F:1368-1426)
+__global__ void k_flux_pec(PlainDev a) {
+  int jj = blockIdx.x * blockDim.x + threadIdx.x;
+  if (jj >= a.ncempec) return;
+  const long k = a.nxzfl, i = a.cempec[jj];
+  double* s = a.srflx;
+  s[0 * k + i] = 2.0 * s[0 * k + i];
+  s[1 * k + i] = 2.0 * s[1 * k + i];
+  s[2 * k + i] = 2.0 * s[2 * k + i];
+  s[3 * k + i] = 0.0;
+  s[4 * k + i] = 0.0;
+  s[5 * k + i] = 0.0;
+}
+
+// upwind combination (src/cem_maxwell.F:969-997)
+__global__ void k_flux_upwind(PlainDev a) {
+  long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  const long k = a.nxzfl;
+  if (i >= k) return;
+  double* s = a.srflx;
+  const double Y0 = a.Y0[i], Y1 = a.Y1[i], Z0 = a.Z0[i], Z1 = a.Z1[i];
+  const double Y02 = -0.5 / Y0 * Y1;
+  const double Z02 = 0.5 / Z0 * Z1;
+  const double C02Y = 0.5 / Y0 * a.C0;
+  const double C02Z = 0.5 / Z0 * a.C0;
+  const double nx = a.unx[i], ny = a.uny[i], nz = a.unz[i];
+  const double s0 = s[0 * k + i], s1 = s[1 * k + i], s2 = s[2 * k + i];
+  const double s3 = s[3 * k + i], s4 = s[4 * k + i], s5 = s[5 * k + i];
+  const double fu1 = ny * s5 - nz * s4;
+  const double fu2 = nz * s3 - nx * s5;
+  const double fu3 = nx * s4 - ny * s3;
+  const double fw1 = ny * s2 - nz * s1;
+  const double fw2 = nz * s0 - nx * s2;
+  const double fw3 = nx * s1 - ny * s0;
+  s[0 * k + i] = Y02 * s0 - C02Y * fu1;
+  s[1 * k + i] = Y02 * s1 - C02Y * fu2;
+  s[2 * k + i] = Y02 * s2 - C02Y * fu3;
+  s[3 * k + i] = Z02 * s3 - C02Z * fw1;
+  s[4 * k + i] = Z02 * s4 - C02Z * fw2;
+  s[5 * k + i] = Z02 * s5 - C02Z * fw3;
+}
+
+// cem_maxwell_add_flux_to_res (src/cem_maxwell.F:725-735).  The reference's
+// serial loop adds face slots in increasing order; here each volume node
+// gathers its slots (CSR, ascending) so the per-node order is the same and
+// no two threads write one node (the OpenACC variant's cemface_ptr idea,
+// src/cem_common.F:262-275).
+__global__ void k_lift(PlainDev a) {
+  long v = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (v >= a.npts) return;
+  const int b = a.lift_ptr[v], e = a.lift_ptr[v + 1];
+  if (b == e) return;
+  const long k = a.nxzfl, P = a.npts;
+  double r[6];
+  for (int q = 0; q < 6; ++q) r[q] = a.res[q * P + v];
+  for (int t = b; t < e; ++t) {
+    const long j = a.lift_slot[t];
+    const double ar = a.area[j];
+    for (int q = 0; q < 6; ++q) r[q] = r[q] + ar * a.srflx[q * k + j];
+  }
+  for (int q = 0; q < 6; ++q) a.res[q * P + v] = r[q];
+}
+
+// usersrc for the Gaussian E_z source (src/cem_maxwell.F:503)
+__global__ void k_usersrc(PlainDev a, double ft) {
+  long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (i >= a.npts) return;
+  double* rez = a.res + 5 * a.npts;
+  rez[i] = rez[i] + a.src_w[i] * ft;
+}
+
+// cem_maxwell_invqmass (src/cem_maxwell.F:1878-1886)
+__global__ void k_invqmass(PlainDev a) {
+  long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (i >= a.npts) return;
+  const long P = a.npts;
+  const double hb = a.hbm1[i], eb = a.ebm1[i];
+  for (int q = 0; q < 3; ++q) a.res[q * P + i] = a.res[q * P + i] * hb;
+  for (int q = 3; q < 6; ++q) a.res[q * P + i] = a.res[q * P + i] * eb;
+}
+
+// rk_maxwell_ab -> rk4_upd (src/cem_maxwell.F:1906-1940, src/cem_common.F:18-75)
+__global__ void k_rk(PlainDev a, double ca, double cb, double dt) {
+  long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (i >= 6 * a.npts) return;
+  const double kh = ca * a.k[i] + dt * a.res[i];
+  a.k[i] = kh;
+  a.u[i] = a.u[i] + cb * kh;
+}
+
+int last_error() { return check_cuda(cudaGetLastError()); }
+
+}  // namespace
+
+int plain_cem_maxwell(Context* c) {
+  const int n = c->nx, n3 = n * n * n;
+  size_t smem = (3 * (size_t)n3 + 2 * n * n) * sizeof(double);
+  static bool attr_set = false;
+  if (!attr_set) {
+    cudaFuncSetAttribute(k_curl, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    attr_set = true;
+  }
+  k_curl<<<c->nelt, kThreads, smem, c->stream>>>(c->pargs);
+  c->last_launches += 1;
+  return last_error();
+}
+
+int plain_restrict_to_face(Context* c) {
+  k_restrict<<<blocks_for(c->nxzfl), kThreads, 0, c->stream>>>(c->pargs);
+  c->last_launches += 1;
+  return last_error();
+}
+
+int plain_gs(Context* c, double* d_u, int nfld) {
+  if (c->pargs.npairs == 0) return NEKGPU_OK;
+  k_gs_pairs<<<blocks_for(c->pargs.npairs), kThreads, 0, c->stream>>>(
+      c->pargs.pairs, c->pargs.npairs, d_u, c->nxzfl, nfld);
+  c->last_launches += 1;
+  return last_error();
+}
+
+int plain_flux3d(Context* c) {
+  k_flux_pre<<<blocks_for(c->nxzfl), kThreads, 0, c->stream>>>(c->pargs);
+  int st = plain_gs(c, c->pargs.srflx, 6);
+  if (st) return st;
+  c->last_launches += 1;
+  if (c->pargs.ncempec > 0) {
+    k_flux_pec<<<blocks_for(c->pargs.ncempec), kThreads, 0, c->stream>>>(c->pargs);
+    c->last_launches += 1;
+  }
+  k_flux_upwind<<<blocks_for(c->nxzfl), kThreads, 0, c->stream>>>(c->pargs);
+  c->last_launches += 1;
+  return last_error();
+}
+
+int plain_add_flux_to_res(Context* c) {
+  k_lift<<<blocks_for(c->npts), kThreads, 0, c->stream>>>(c->pargs);
+  c->last_launches += 1;
+  return last_error();
+}
+
+int plain_usersrc(Context* c, double ft) {
+  if (!c->pargs.src_w) return NEKGPU_OK;
+  k_usersrc<<<blocks_for(c->npts), kThreads, 0, c->stream>>>(c->pargs, ft);
+  c->last_launches += 1;
+  return last_error();
+}
+
+int plain_invqmass(Context* c) {
+  k_invqmass<<<blocks_for(c->npts), kThreads, 0, c->stream>>>(c->pargs);
+  c->last_launches += 1;
+  return last_error();
+}
+
+int plain_rk_update(Context* c, double ca, double cb, double dt) {
+  k_rk<<<blocks_for(6 * c->npts), kThreads, 0, c->stream>>>(c->pargs, ca, cb, dt);
+  c->last_launches += 1;
+  return last_error();
+}
+
+}  // namespace nekgpu

@@ -1,0 +1,231 @@
+"""Host-side mirror of NekCEM's Maxwell time-step interface over the C ABI.
+
+``MaxwellGPU`` plays the part the Fortran driver plays in the reference
+(src/cem_drive.F, src/cem_maxwell.F): it hands the static arrays to the
+library once, sets the fields, advances them with ``op_rk`` /
+``time_advancing`` and evaluates ``cem_error``.  Method names follow the
+reference routines.  All arithmetic runs in the CUDA library; this module
+only moves numpy arrays across the ABI.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import Optional, Sequence
+
+import numpy as np
+
+from . import _lib as L
+
+
+def _dp(a: np.ndarray):
+    if a.dtype != np.float64 or not a.flags.c_contiguous:
+        raise TypeError("expected a C-contiguous float64 array")
+    return a.ctypes.data_as(L.dp)
+
+
+def _ip(a: np.ndarray):
+    if a.dtype != np.int32 or not a.flags.c_contiguous:
+        raise TypeError("expected a C-contiguous int32 array")
+    return a.ctypes.data_as(L.ip)
+
+
+class MaxwellGPU:
+    """One GPU context: mesh, materials, fields and the stage kernels."""
+
+    def __init__(self, handle: C.c_void_p, form: int, keep: list):
+        self._h = handle
+        self.form = form
+        self._keep = keep  # arrays the ABI structs point into (kept alive)
+        npts, nxzfl = C.c_long(), C.c_long()
+        nelt, nx1 = C.c_int(), C.c_int()
+        L.check(L.load().nekgpu_sizes(self._h, C.byref(npts), C.byref(nxzfl), C.byref(nelt),
+                                      C.byref(nx1)), "nekgpu_sizes")
+        self.npts, self.nxzfl, self.nelt, self.nx1 = npts.value, nxzfl.value, nelt.value, nx1.value
+
+    # ---- construction -------------------------------------------------------
+    @classmethod
+    def from_box(cls, N: int, nel: Sequence[int], lo: Sequence[float], hi: Sequence[float],
+                 bc: Sequence[int], form: str = "mixed", permittivity: Optional[np.ndarray] = None,
+                 permeability: Optional[np.ndarray] = None, C0: float = 1.0) -> "MaxwellGPU":
+        """Structured affine box (genbox + geometry + uservp of the reference)."""
+        lib = L.load()
+        b = L.NekgpuBox()
+        b.N = int(N)
+        b.nelx, b.nely, b.nelz = (int(v) for v in nel)
+        for d in range(3):
+            b.lo[d] = float(lo[d]); b.hi[d] = float(hi[d]); b.bc[d] = int(bc[d])
+        keep = []
+        for name, arr in (("permittivity", permittivity), ("permeability", permeability)):
+            if arr is not None:
+                a = np.ascontiguousarray(arr, dtype=np.float64)
+                keep.append(a)
+                setattr(b, name, _dp(a))
+        b.C0 = float(C0)
+        h = C.c_void_p()
+        L.check(lib.nekgpu_init_box(C.byref(h), C.byref(b), L.FORMS[form]), "nekgpu_init_box")
+        return cls(h, L.FORMS[form], keep)
+
+    @classmethod
+    def from_arrays(cls, arrays: dict, nx1: int, nelt: int, form: str = "plain",
+                    C0: float = 1.0) -> "MaxwellGPU":
+        """Drop-in init from the reference's arrays (as cem_maxwell_init leaves
+        them).  ``arrays`` holds the COMMON arrays by their Fortran names;
+        ``cemface``/``cempec`` are 0-based here and converted to Fortran's
+        1-based convention."""
+        lib = L.load()
+        m = L.NekgpuMesh()
+        m.nx1, m.nelt = int(nx1), int(nelt)
+        keep = []
+
+        def d(name):
+            a = np.ascontiguousarray(arrays[name], dtype=np.float64)
+            keep.append(a)
+            return _dp(a)
+
+        m.dxm1 = d("dxm1"); m.w3mn = d("w3mn")
+        for nm in ("rx", "ry", "rz", "sx", "sy", "sz", "tx", "ty", "tz"):
+            setattr(m, nm + "mn", d(nm + "mn"))
+        m.bmn = d("bmn")
+        for nm in ("xmn", "ymn", "zmn"):
+            if nm in arrays:
+                setattr(m, nm, d(nm))
+        m.unxm = d("unxm"); m.unym = d("unym"); m.unzm = d("unzm"); m.aream = d("aream")
+        cf = np.ascontiguousarray(np.asarray(arrays["cemface"]) + 1, dtype=np.int32)
+        keep.append(cf); m.cemface = _ip(cf)
+        gl = np.ascontiguousarray(arrays["glo_face"], dtype=np.int64)
+        keep.append(gl); m.glo_face = gl.ctypes.data_as(L.lp)
+        pec = np.ascontiguousarray(np.asarray(arrays["cempec"]) + 1, dtype=np.int32)
+        keep.append(pec); m.cempec = _ip(pec); m.ncempec = int(pec.size)
+        m.Z_0 = d("Z_0"); m.Z_1 = d("Z_1"); m.Y_0 = d("Y_0"); m.Y_1 = d("Y_1")
+        m.ebm1 = d("ebm1"); m.hbm1 = d("hbm1")
+        m.C0 = float(C0)
+        h = C.c_void_p()
+        L.check(lib.nekgpu_init(C.byref(h), C.byref(m), L.FORMS[form]), "nekgpu_init")
+        return cls(h, L.FORMS[form], keep)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            L.load().nekgpu_finalize(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # ---- arrays ------------------------------------------------------------
+    def array(self, name: str) -> np.ndarray:
+        out = np.empty(self.npts)
+        L.check(L.load().nekgpu_get_array(self._h, name.encode(), _dp(out)), "nekgpu_get_array")
+        return out
+
+    def coords(self):
+        return self.array("xmn"), self.array("ymn"), self.array("zmn")
+
+    @property
+    def volume(self) -> float:
+        return L.load().nekgpu_volume(self._h)
+
+    def set_source(self, xc, sigma, amp, f0, t0, enabled: bool = True):
+        x = (C.c_double * 3)(*xc)
+        L.check(L.load().nekgpu_set_source(self._h, 1 if enabled else 0, x, sigma, amp, f0, t0),
+                "nekgpu_set_source")
+
+    # ---- fields (Fortran hn(npts,3), en(npts,3) as (3, npts)) --------------
+    def set_state(self, H: np.ndarray, E: np.ndarray):
+        H = np.ascontiguousarray(H, dtype=np.float64).reshape(3, self.npts)
+        E = np.ascontiguousarray(E, dtype=np.float64).reshape(3, self.npts)
+        L.check(L.load().nekgpu_set_state(self._h, _dp(H), _dp(E), self.npts), "nekgpu_set_state")
+
+    def get_state(self):
+        H = np.empty((3, self.npts)); E = np.empty((3, self.npts))
+        L.check(L.load().nekgpu_get_state(self._h, _dp(H), _dp(E), self.npts), "nekgpu_get_state")
+        return H, E
+
+    def set_rk_register(self, kH: np.ndarray, kE: np.ndarray):
+        kH = np.ascontiguousarray(kH, dtype=np.float64).reshape(3, self.npts)
+        kE = np.ascontiguousarray(kE, dtype=np.float64).reshape(3, self.npts)
+        L.check(L.load().nekgpu_set_rk_register(self._h, _dp(kH), _dp(kE), self.npts),
+                "nekgpu_set_rk_register")
+
+    def get_rk_register(self):
+        kH = np.empty((3, self.npts)); kE = np.empty((3, self.npts))
+        L.check(L.load().nekgpu_get_rk_register(self._h, _dp(kH), _dp(kE), self.npts),
+                "nekgpu_get_rk_register")
+        return kH, kE
+
+    # ---- time stepping -------------------------------------------------------
+    def stage(self, rkstep: int, time: float, dt: float):
+        L.check(L.load().nekgpu_stage(self._h, int(rkstep), float(time), float(dt)), "nekgpu_stage")
+
+    def run(self, nsteps: int, time: float, dt: float) -> float:
+        """time_advancing_pde's loop: nsteps of cem_maxwell_op_rk, time += dt each."""
+        t = C.c_double(time)
+        L.check(L.load().nekgpu_step(self._h, int(nsteps), C.byref(t), float(dt)), "nekgpu_step")
+        return t.value
+
+    def op_rk_host(self, H: np.ndarray, E: np.ndarray, time: float, dt: float):
+        """One cem_maxwell_op_rk on host fields, updated in place."""
+        L.check(L.load().nekgpu_op_rk_host(self._h, _dp(H), _dp(E), self.npts, float(time),
+                                           float(dt)), "nekgpu_op_rk_host")
+
+    def time_steps(self, nsteps: int, time: float, dt: float):
+        t = C.c_double(time); ms = C.c_double()
+        L.check(L.load().nekgpu_time_steps(self._h, int(nsteps), C.byref(t), float(dt),
+                                           C.byref(ms)), "nekgpu_time_steps")
+        return t.value, ms.value
+
+    def last_launches(self) -> int:
+        return int(L.load().nekgpu_last_launches(self._h))
+
+    def sync(self):
+        L.check(L.load().nekgpu_sync(self._h), "nekgpu_sync")
+
+    def register_host(self, arr: np.ndarray):
+        L.check(L.load().nekgpu_register_host(self._h, arr.ctypes.data, arr.nbytes),
+                "nekgpu_register_host")
+
+    def unregister_host(self, arr: np.ndarray):
+        L.check(L.load().nekgpu_unregister_host(self._h, arr.ctypes.data), "nekgpu_unregister_host")
+
+    # ---- the reference routines one by one (plain form) -----------------------
+    def call(self, routine: str, *args):
+        fn = getattr(L.load(), "nekgpu_" + routine)
+        L.check(fn(self._h, *args), "nekgpu_" + routine)
+
+    def work(self, name: str) -> np.ndarray:
+        n = {"reshn": 3 * self.npts, "resen": 3 * self.npts, "fhn": 3 * self.nxzfl,
+             "fen": 3 * self.nxzfl, "srflx": 6 * self.nxzfl}[name]
+        out = np.empty(n)
+        L.check(L.load().nekgpu_get_work(self._h, name.encode(), _dp(out)), "nekgpu_get_work")
+        return out
+
+    def gs_op_fields(self, u: np.ndarray, nfld: int) -> np.ndarray:
+        u = np.ascontiguousarray(u, dtype=np.float64).copy()
+        L.check(L.load().nekgpu_gs_op_fields(self._h, _dp(u), int(nfld)), "nekgpu_gs_op_fields")
+        return u
+
+    # ---- norms -----------------------------------------------------------------
+    def cem_error(self, Hex: np.ndarray, Eex: np.ndarray):
+        """L2 and Linf of exact - numerical for the 6 components (cem_error)."""
+        Hex = np.ascontiguousarray(Hex, dtype=np.float64).reshape(3, self.npts)
+        Eex = np.ascontiguousarray(Eex, dtype=np.float64).reshape(3, self.npts)
+        l2 = np.zeros(6); li = np.zeros(6)
+        L.check(L.load().nekgpu_norms(self._h, _dp(Hex), _dp(Eex), self.npts, _dp(l2), _dp(li)),
+                "nekgpu_norms")
+        return l2, li
+
+    def energy(self) -> float:
+        e = C.c_double()
+        L.check(L.load().nekgpu_energy(self._h, C.byref(e)), "nekgpu_energy")
+        return e.value
+
+    def check_blowup(self):
+        L.check(L.load().nekgpu_check_blowup(self._h), "nekgpu_check_blowup")
