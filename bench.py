@@ -1,0 +1,341 @@
+"""Benchmark of the Maxwell DG time step (DOF-stage updates per second).
+
+Workload: the periodic plane-wave box, 16^3 affine hex elements, N=7
+(2,097,152 nodes x 6 field components), k=(1,1,1), dt = 0.5 x smallest GLL
+spacing.  One benchmark step is one RK5 time step (5 stages) of the whole
+mesh.  The headline form is the mixed-precision fused kernel; the all-FP64
+fused form, the plain per-routine FP64 form and the CPU oracle are measured
+beside it on the same workload.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line.  With --gpus N > 1 (under torchrun) every rank runs its
+own replica of the workload on its GPU ("replicas only": the time step does
+not shard inside one GPU's mesh), the timed region is bracketed by barriers
+and the slowest rank's time is used.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "DOF-stage updates/s FP64 vs mixed at fixed L2 error; adjoint/forward time ratio"
+UNIT = "DOF-stage updates/s"
+BYTES_PER_NODE_STAGE = 208  # u r/w 96 + k r/w 96 + inverse-mass coefficients 16
+CASE = "planewave"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=2000)
+    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--no-accuracy", action="store_true", help="skip the full-length L2 runs")
+    p.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline sample")
+    return p.parse_args()
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def ncu_traffic(kernel: str):
+    """Per-launch DRAM bytes of a kernel at this workload, from the committed
+    ncu summary (profiles/traffic.json), or None."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
+            return json.load(f).get(kernel)
+    except Exception:
+        return None
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_setup(n):
+    if n <= 1 or "RANK" not in os.environ:
+        return None, 0, 1
+    import torch
+    import torch.distributed as dist
+    rank = int(os.environ["RANK"])
+    world = int(os.environ["WORLD_SIZE"])
+    local = int(os.environ.get("LOCAL_RANK", rank))
+    torch.cuda.set_device(local)
+    dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    return dist, rank, world
+
+
+def reduce_max(dist, x: float) -> float:
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def build_gpu_case(form, device_note=None):
+    from nekcem_gb300 import MaxwellGPU, cases
+    c = cases.make(CASE)
+    g = MaxwellGPU.from_box(c.N, c.nel, c.lo, c.hi, c.bc, form=form)
+    x, y, z = g.coords()
+    dt = c.timestep(x, y, z)
+    H, E = c.init_fields(x, y, z)
+    return c, g, (x, y, z), dt, H, E
+
+
+def time_form(form, steps, warmup, dist=None, clocks=None):
+    c, g, xyz, dt, H, E = build_gpu_case(form)
+    g.set_state(H, E)
+    t = 0.0
+    if warmup:
+        t, _ = g.time_steps(warmup, t, dt)
+    barrier(dist)
+    g.sync()
+    if clocks is not None:
+        clocks.__enter__()
+        time.sleep(0.15)  # let the sampler start before the timed region
+    try:
+        t, ms = g.time_steps(steps, t, dt)
+    finally:
+        if clocks is not None:
+            clocks.__exit__(None, None, None)
+    launches = g.last_launches()
+    ms = reduce_max(dist, ms)
+    npts = g.npts
+    g.close()
+    return dict(ms=ms, steps=steps, npts=npts, launches=launches, dt=dt, case=c)
+
+
+def accuracy(form, nsteps=None):
+    c, g, (x, y, z), dt, H, E = build_gpu_case(form)
+    g.set_state(H, E)
+    n = nsteps or c.nsteps
+    t = g.run(n, 0.0, dt)
+    l2, li = g.cem_error(*c.exact(x, y, z, t))
+    g.close()
+    return float(np.sqrt(np.sum(l2 ** 2))), n
+
+
+def e2e(steps, warmup, dist=None):
+    """Through the C ABI with host buffers: every step copies the host fields
+    in (H2D), runs the 5 stages and copies them back (D2H) -- the drop-in for
+    one cem_maxwell_op_rk call (nekgpu_op_rk_host), pinned host memory."""
+    c, g, xyz, dt, H, E = build_gpu_case("mixed")
+    H = np.ascontiguousarray(H); E = np.ascontiguousarray(E)
+    g.register_host(H); g.register_host(E)
+    t = 0.0
+    for _ in range(warmup):
+        g.op_rk_host(H, E, t, dt); t += dt
+    barrier(dist)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        g.op_rk_host(H, E, t, dt); t += dt
+    sec = time.perf_counter() - t0
+    sec = reduce_max(dist, sec)
+    g.unregister_host(H); g.unregister_host(E)
+    bytes_io = 6 * g.npts * 8
+    npts = g.npts
+    g.close()
+    return dict(sec=sec, npts=npts, h2d=bytes_io, d2h=bytes_io)
+
+
+def cpu_sample(steps):
+    """The CPU oracle (FP64 restatement of the reference's routines, all host
+    threads) on the same mesh, `steps` RK steps."""
+    from nekcem_gb300 import cases
+    from oracle import refcpu as R
+    threads = os.cpu_count() or 1
+    R.set_threads(threads)
+    c = cases.make(CASE)
+    ref = R.RefBox(c.N, c.nel, c.lo, c.hi, c.bc)
+    x, y, z = ref.coords()
+    dt = c.timestep(x, y, z)
+    ref.set_state(*c.init_fields(x, y, z))
+    ref.run(1, 0.0, dt)  # warm caches / threads
+    t0 = time.perf_counter()
+    ref.run(steps, dt, dt)
+    sec = time.perf_counter() - t0
+    npts = ref.npts
+    ref.close()
+    return dict(value=6 * npts * 5 * steps / sec, sec=sec, threads=threads, npts=npts)
+
+
+def run_reference(args):
+    dist, rank, world = dist_setup(args.gpus)
+    if rank != 0:
+        return
+    steps = max(1, min(args.steps, 60))
+    warm = min(args.warmup, 2)
+    from nekcem_gb300 import cases
+    from oracle import refcpu as R
+    threads = os.cpu_count() or 1
+    R.set_threads(threads)
+    c = cases.make(CASE)
+    ref = R.RefBox(c.N, c.nel, c.lo, c.hi, c.bc)
+    x, y, z = ref.coords()
+    dt = c.timestep(x, y, z)
+    ref.set_state(*c.init_fields(x, y, z))
+    t = ref.run(warm, 0.0, dt)
+    t0 = time.perf_counter()
+    ref.run(steps, t, dt)
+    sec = time.perf_counter() - t0
+    value = 6 * ref.npts * 5 * steps / sec
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": steps, "warmup": warm, "ms_per_step": 1e3 * sec / steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "planewave 16^3 el N=7 periodic (2,097,152 nodes x 6), RK45",
+                   "elements": c.nelt, "N": c.N, "form": "CPU oracle (FP64 restatement of the "
+                   "reference's Fortran routines; the Fortran cannot be built here)"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{steps} RK steps of the full mesh after {warm} warm-up"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    import nekcem_gb300
+    nekcem_gb300.load()
+    dist, rank, world = dist_setup(args.gpus)
+    device = int(os.environ.get("LOCAL_RANK", 0))
+    peak, peak_kind = measured_peaks()
+
+    # headline: mixed form, device-resident inputs, CUDA-event timed
+    clk = ClockSampler(device)
+    mixed = time_form("mixed", args.steps, max(3, args.warmup), dist, clocks=clk)
+    clocks = clk.summary()
+    ms_step = mixed["ms"] / mixed["steps"]
+    npts = mixed["npts"]
+    dof_stage_per_step = 6 * npts * 5
+    value = world * dof_stage_per_step * mixed["steps"] / (mixed["ms"] * 1e-3)
+    launch_ms = mixed["ms"] / mixed["launches"]
+    achieved = BYTES_PER_NODE_STAGE * npts / (launch_ms * 1e-3) / 1e9
+
+    e = e2e(max(3, args.steps // 10), 2, dist)
+    e2e_value = world * dof_stage_per_step * max(3, args.steps // 10) / e["sec"]
+
+    if rank != 0:
+        return
+    fp64 = time_form("fused64", max(5, args.steps // 10), 3)
+    plain = time_form("plain", max(3, args.steps // 50), 2)
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": max(3, args.warmup), "ms_per_step": ms_step, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 contraction / f64 state+RK",
+        "data": "synthetic",
+        "config": {"workload": "planewave 16^3 el N=7 periodic (2,097,152 nodes x 6), RK45",
+                   "elements": 4096, "N": 7, "form": "mixed", "dt": mixed["dt"],
+                   "l2_policy": "inputs larger than L2: u in/out + k + inverse mass = 337 MB per stage",
+                   "parallelism": "replicas" if world > 1 else "1 GPU"},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": e["h2d"],
+                "d2h_bytes_per_step": e["d2h"], "path": "nekgpu_op_rk_host, pinned host fields"},
+        "gpu_launches": mixed["launches"],
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": ncu_traffic("k_fused_stage<8,float>"),
+                     "peak_kind": peak_kind,
+                     "algorithmic_bytes_per_launch": BYTES_PER_NODE_STAGE * npts},
+        "clocks": clocks,
+        "forms": {
+            "fused64": {"value": dof_stage_per_step * fp64["steps"] / (fp64["ms"] * 1e-3),
+                        "ms_per_step": fp64["ms"] / fp64["steps"]},
+            "plain64": {"value": dof_stage_per_step * plain["steps"] / (plain["ms"] * 1e-3),
+                        "ms_per_step": plain["ms"] / plain["steps"]},
+        },
+    }
+    out["forms"]["mixed_over_fused64"] = value / world / out["forms"]["fused64"]["value"]
+    out["forms"]["mixed_over_plain64"] = value / world / out["forms"]["plain64"]["value"]
+    if not args.no_accuracy and world == 1:
+        l2m, n = accuracy("mixed")
+        l2d, _ = accuracy("fused64")
+        out["l2_vs_analytic"] = {"steps": n, "mixed": l2m, "fused64": l2d, "ratio": l2m / l2d}
+    if not args.no_cpu and world == 1:
+        cpu = cpu_sample(max(2, min(20, args.steps // 10)))
+        out["cpu_baseline"] = {"value": cpu["value"], "unit": UNIT, "cores": cpu["threads"],
+                               "kind": "port", "sample": f"{max(2, min(20, args.steps // 10))} RK "
+                               f"steps of the full mesh, {cpu['sec']:.1f} s"}
+    print(json.dumps(out), flush=True)
+
+
+if __name__ == "__main__":
+    main()
