@@ -43,7 +43,12 @@ extern "C" {
 #define NEKGPU_PLAIN 0   /* unfused all-FP64 kernels, one per reference routine */
 #define NEKGPU_FUSED64 1 /* fused curl+flux+lift+mass+RK stage kernel, all FP64 */
 #define NEKGPU_MIXED 2   /* fused stage kernel: FP32 contractions/curl/flux,
-                            FP64 state, RK register, inverse mass and norms */
+                            FP64 state, RK register, inverse mass and norms;
+                            exact-hi compensated contractions on a normalised
+                            residual (accuracy of the FP64 forms) */
+#define NEKGPU_MIXED_NAIVE 3 /* the same fused kernel as FUSED64 computed in
+                            plain FP32; kept to measure what the compensation
+                            of NEKGPU_MIXED costs (its L2 error is far larger) */
 
 /* Face boundary codes (CBC in src/cem_maxwell.F:289-300, 1338-1366). */
 #define NEKGPU_BC_PEC 0

@@ -17,8 +17,8 @@ ERR = {
     -5: "NEKGPU_ERR_STATE", -6: "NEKGPU_ERR_BLOWUP", -7: "NEKGPU_ERR_TIMEOUT",
     -8: "NEKGPU_ERR_UNSUPPORTED",
 }
-PLAIN, FUSED64, MIXED = 0, 1, 2
-FORMS = {"plain": PLAIN, "fused64": FUSED64, "mixed": MIXED}
+PLAIN, FUSED64, MIXED, MIXED_NAIVE = 0, 1, 2, 3
+FORMS = {"plain": PLAIN, "fused64": FUSED64, "mixed": MIXED, "mixed_naive": MIXED_NAIVE}
 BC_PEC, BC_PERIODIC = 0, 1
 
 dp = C.POINTER(C.c_double)

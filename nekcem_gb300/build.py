@@ -21,9 +21,10 @@ LIB = os.path.join(PKG, "libnekcem_gb300.so")
 OBJDIR = os.path.join(PKG, "_build")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = {
-    "nekgpu_host.cpp": [],
+    "nekgpu_host.cpp": ["-Xcompiler", "-ffp-contract=off"],  # same rounding on x86 and Arm
     "nekgpu_plain.cu": ["--fmad=false"],
     "nekgpu_fused.cu": [],
+    "nekgpu_mixed.cu": [],
     "nekgpu_util.cu": [],
 }
 

@@ -78,6 +78,11 @@ __device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
 __device__ __forceinline__ void fence_mbar_init() {
   asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 }
+// orders the block's generic-proxy shared-memory accesses (after a barrier)
+// before later async-proxy (TMA) accesses
+__device__ __forceinline__ void fence_proxy_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
 __device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, unsigned bytes) {
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)),
                "r"(bytes)
@@ -402,7 +407,10 @@ __global__ void __launch_bounds__(Cfg<NX, T>::NT, Cfg<NX, T>::kMinBlocks)
     }
     __syncthreads();  // staged blocks consumed: the next element may land
     const int en = e + gridDim.x;
-    if (C::kTma && tid == 0 && en < a.nelt) issue_tma(en);
+    if (C::kTma && tid == 0 && en < a.nelt) {
+      fence_proxy_async_smem();
+      issue_tma(en);
+    }
     if (node) {
       const long g = (long)e * N3 + tid;
 #pragma unroll
@@ -414,13 +422,11 @@ __global__ void __launch_bounds__(Cfg<NX, T>::NT, Cfg<NX, T>::kMinBlocks)
   }
 }
 
-// dt-scaled inverse mass: coef = dt*hbm1 | dt*ebm1
-__global__ void k_scale_coef(double* coef, const double* hbm1, const double* ebm1, long n,
-                             double dt) {
+// dt-scaled inverse-mass coefficients: coef = dt * base (2*n entries)
+__global__ void k_scale_coef(double* coef, const double* base, long n2, double dt) {
   long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  coef[i] = dt * hbm1[i];
-  coef[n + i] = dt * ebm1[i];
+  if (i >= n2) return;
+  coef[i] = dt * base[i];
 }
 
 template <int NX, typename T>
@@ -466,9 +472,9 @@ int dispatch(Context* c, const FusedDev& a) {
 
 int scale_coef(Context* c, double dt) {
   if (c->coef_dt == dt) return NEKGPU_OK;
-  long n = c->npts;
-  k_scale_coef<<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(c->d_coef, c->d_hbm1,
-                                                                     c->d_ebm1, n, dt);
+  long n2 = 2 * c->npts;
+  k_scale_coef<<<(unsigned)((n2 + 255) / 256), 256, 0, c->stream>>>(c->d_coef, c->d_cbase, n2,
+                                                                      dt);
   c->last_launches += 1;
   c->coef_dt = dt;
   return check_cuda(cudaGetLastError());
@@ -494,7 +500,7 @@ int fused_stage(Context* c, int rkstep, double time, double dt) {
     a.src_ft = c->src.amp * (1.0 - 2.0 * x * x) * exp(-x * x);
     a.src_ftf = (float)a.src_ft;
   }
-  st = c->form == NEKGPU_MIXED ? dispatch<float>(c, a) : dispatch<double>(c, a);
+  st = c->form == NEKGPU_MIXED_NAIVE ? dispatch<float>(c, a) : dispatch<double>(c, a);
   if (st) return st;
   c->cur ^= 1;
   return NEKGPU_OK;

@@ -675,31 +675,100 @@ int upload_plain(Context* c, const PlainHost& p) {
   return NEKGPU_OK;
 }
 
+// D for the exact-hi contractions of the mixed form: per row i, Dh on the
+// 10-bit grid of that row's largest |D(i,l)|, Df = D rounded to FP32, and
+// the remainder D - Dh split into two FP32 pieces Dm + Dl (exact to ~2^-55)
+void split_D(const std::vector<double>& D, int n, float* Dh, float* Df, float* Dm, float* Dl) {
+  for (int i = 0; i < n; ++i) {
+    double rmax = 0;
+    for (int l = 0; l < n; ++l) rmax = std::max(rmax, std::fabs(D[i + (size_t)n * l]));
+    int ex = 0;
+    std::frexp(rmax, &ex);  // rmax < 2^ex
+    const double qd = std::ldexp(1.0, ex - 10);
+    for (int l = 0; l < n; ++l) {
+      const size_t k = i + (size_t)n * l;
+      const double h = std::nearbyint(D[k] / qd) * qd;  // at most 11 significant bits
+      Dh[k] = (float)h;
+      Df[k] = (float)D[k];
+      const double r = D[k] - h;
+      Dm[k] = (float)r;
+      Dl[k] = (float)(r - (double)Dm[k]);
+    }
+  }
+}
+
 int upload_fused(Context* c, const Compact& cp) {
   DevAlloc A(c);
   int st;
+  const long n3 = (long)c->nx * c->nx * c->nx;
   if ((st = A.get(&c->d_u[0], 6 * c->npts)) || (st = A.get(&c->d_u[1], 6 * c->npts))) return st;
   if ((st = upload_common(c, A, cp.bm1, cp.ebm1, cp.hbm1))) return st;
   if ((st = A.get(&c->d_coef, 2 * c->npts))) return st;
   if ((st = A.put(&c->d_nbr, cp.nbr))) return st;
-  if ((st = A.put(&c->d_egeom, cp.egeom))) return st;
-  std::vector<float> gf(cp.egeom.begin(), cp.egeom.end());
-  if ((st = A.put(&c->d_egeomf, gf))) return st;
+  c->host_w3 = cp.w3;
+  c->host_rx.resize(c->nelt);
+  for (int e = 0; e < c->nelt; ++e) c->host_rx[e] = cp.egeom[9 * (size_t)e];
+  // unscaled inverse-mass coefficients: hbm1|ebm1, or for the mixed form the
+  // normalised hbm1*w3*rx | ebm1*w3*rx (the residual is res/(bm1*2/hx))
+  {
+    std::vector<double> base(2 * c->npts);
+    for (long g = 0; g < c->npts; ++g) {
+      double f = 1.0;
+      if (c->form == NEKGPU_MIXED) f = cp.w3[g % n3] * cp.egeom[9 * (g / n3)];
+      base[g] = cp.hbm1[g] * f;
+      base[c->npts + g] = cp.ebm1[g] * f;
+    }
+    if ((st = A.put(&c->d_cbase, base))) return st;
+  }
   c->uniform = cp.uniform;
   c->d_fcoef = nullptr;
   if (!cp.uniform) {
-    if (c->form == NEKGPU_MIXED) {
+    if (c->form == NEKGPU_FUSED64) {
+      double* d;
+      if ((st = A.put(&d, cp.fcoef))) return st;
+      c->d_fcoef = d;
+    } else {
       std::vector<float> f(cp.fcoef.begin(), cp.fcoef.end());
       float* d;
       if ((st = A.put(&d, f))) return st;
       c->d_fcoef = d;
-    } else {
-      double* d;
-      if ((st = A.put(&d, cp.fcoef))) return st;
-      c->d_fcoef = d;
     }
   }
   if ((st = fused_setup(c))) return st;
+  c->coef_dt = std::nan("");
+  if (c->form == NEKGPU_MIXED) {
+    // per element: rho_y = sy/rx and rho_z = tz/rx as float pairs, the lift
+    // factor area/(bm1*2/hx) = A_f/(w_end*rx) per slot, and a cubic flag
+    const double wend = cp.w[0];
+    std::vector<float> egm(12 * (size_t)c->nelt, 0.0f);
+    for (int e = 0; e < c->nelt; ++e) {
+      const double* g = &cp.egeom[9 * (size_t)e];
+      const double ry = g[1] / g[0], rz = g[2] / g[0];
+      float* o = &egm[12 * (size_t)e];
+      o[0] = (float)ry; o[1] = (float)(ry - (double)o[0]);
+      o[2] = (float)rz; o[3] = (float)(rz - (double)o[2]);
+      for (int f = 0; f < 6; ++f) o[4 + f] = (float)(g[3 + f] / (wend * g[0]));
+      o[10] = (ry == 1.0 && rz == 1.0) ? 1.0f : 0.0f;
+    }
+    if ((st = A.put(&c->d_egm, egm))) return st;
+    MixedDev& m = c->margs;
+    m = MixedDev{};
+    m.nelt = c->nelt;
+    m.npts = c->npts;
+    m.k = c->d_k;
+    m.coef = c->d_coef;
+    m.nbr = c->d_nbr;
+    m.egm = c->d_egm;
+    m.fcoef = c->d_fcoef;
+    m.C0f = (float)cp.C0;
+    m.status = c->d_status;
+    if (c->nx > kMaxMixed) return NEKGPU_ERR_UNSUPPORTED;
+    split_D(cp.D, c->nx, m.Dh, m.Df, m.Dm, m.Dl);
+    return NEKGPU_OK;
+  }
+  if ((st = A.put(&c->d_egeom, cp.egeom))) return st;
+  std::vector<float> gf(cp.egeom.begin(), cp.egeom.end());
+  if ((st = A.put(&c->d_egeomf, gf))) return st;
   FusedDev& a = c->fargs;
   a = FusedDev{};
   a.nelt = c->nelt;
@@ -721,7 +790,6 @@ int upload_fused(Context* c, const Compact& cp) {
     a.w[i] = cp.w[i];
     a.wf[i] = (float)cp.w[i];
   }
-  c->coef_dt = std::nan("");
   return NEKGPU_OK;
 }
 
@@ -734,7 +802,8 @@ int finish_init(Context* c, int st) {
 }
 
 bool valid_form(int form) {
-  return form == NEKGPU_PLAIN || form == NEKGPU_FUSED64 || form == NEKGPU_MIXED;
+  return form == NEKGPU_PLAIN || form == NEKGPU_FUSED64 || form == NEKGPU_MIXED ||
+         form == NEKGPU_MIXED_NAIVE;
 }
 
 int sync_status(Context* c) {
@@ -787,6 +856,7 @@ int plain_stage(Context* c, int rkstep, double time, double dt) {
 int do_stage(Context* c, int rkstep, double time, double dt) {
   if (rkstep < 1 || rkstep > 5) return NEKGPU_ERR_ARG;
   if (c->form == NEKGPU_PLAIN) return plain_stage(c, rkstep, time, dt);
+  if (c->form == NEKGPU_MIXED) return mixed_stage(c, rkstep, time, dt);
   return fused_stage(c, rkstep, time, dt);
 }
 
@@ -1005,6 +1075,8 @@ int nekgpu_set_source(nekgpu_ctx* c, int enabled, const double xc[3], double sig
     c->pargs.src_w = nullptr;
     c->fargs.src_elem = nullptr;
     c->fargs.src_w = nullptr;
+    c->margs.src_elem = nullptr;
+    c->margs.src_w = nullptr;
     return NEKGPU_OK;
   }
   if (!xc || !(sigma > 0)) return NEKGPU_ERR_ARG;
@@ -1042,6 +1114,20 @@ int nekgpu_set_source(nekgpu_ctx* c, int enabled, const double xc[3], double sig
     int* d_off;
     if ((st = A.put(&d_off, off))) return st;
     if (c->form == NEKGPU_MIXED) {
+      // normalised like the residual: weight / (bm1 * 2/hx) = weight / (w3 * rx)
+      std::vector<float> wf(wd.size());
+      for (int e = 0, s0 = 0; e < c->nelt; ++e) {
+        if (off[e] < 0) continue;
+        for (long v = 0; v < n3; ++v)
+          wf[(size_t)s0 * n3 + v] = (float)(wd[(size_t)s0 * n3 + v] / (c->host_w3[v] * c->host_rx[e]));
+        ++s0;
+      }
+      float* d;
+      if ((st = A.put(&d, wf))) return st;
+      c->d_src_w = d;
+      c->margs.src_elem = d_off;
+      c->margs.src_w = d;
+    } else if (c->form == NEKGPU_MIXED_NAIVE) {
       std::vector<float> wf(wd.begin(), wd.end());
       float* d;
       if ((st = A.put(&d, wf))) return st;

@@ -10,7 +10,8 @@
 
 namespace nekgpu {
 
-constexpr int kMaxNx = 16;  // nx1 limit of the plain kernels (N <= 15)
+constexpr int kMaxNx = 16;     // nx1 limit of the plain kernels (N <= 15)
+constexpr int kMaxMixed = 10;  // nx1 limit of the parameter-resident D of the mixed form
 
 // Compact description of an affine, axis-aligned hex mesh: what the fused
 // forms consume.  Built either by the box builder or by compressing the
@@ -95,6 +96,33 @@ struct FusedDev {
   float wf[kMaxNx];
 };
 
+// Mixed form (nekgpu_mixed.cu): exact-hi FP32 contractions on a normalised
+// residual; see that file for the scheme.
+struct MixedDev {
+  int nelt;
+  long npts;
+  const double* u_in;
+  double* u_out;
+  double* k;
+  const double* coef;   // 2*npts: dt*hbm1*w3*rx | dt*ebm1*w3*rx (per element rx)
+  const int* nbr;       // 6*nelt
+  const float* egm;     // 12*nelt: rho_y (hi,lo), rho_z (hi,lo), lift factor per slot, cubic
+  const void* fcoef;    // float4 per face node, null when uniform
+  const int* src_elem;  // nelt or null
+  const float* src_w;   // normalised source weights, nx^3 per source element
+  float src_ftf;
+  double a, b;
+  float C0f;
+  int* status;
+  // D(i,j) at [i + nx*j] in four FP32 pieces: Dh on a 10-bit grid per row
+  // (exact products with the 10-bit uh), Df = D rounded, and the remainder
+  // D - Dh = Dm + Dl to ~2^-55.
+  float Dh[kMaxMixed * kMaxMixed];
+  float Df[kMaxMixed * kMaxMixed];
+  float Dm[kMaxMixed * kMaxMixed];
+  float Dl[kMaxMixed * kMaxMixed];
+};
+
 struct Context {
   int form = NEKGPU_MIXED;
   int device = 0;
@@ -115,7 +143,8 @@ struct Context {
   std::vector<void*> allocs;
 
   // fused form
-  double* d_coef = nullptr;  // 2*npts
+  double* d_coef = nullptr;   // 2*npts, dt-scaled
+  double* d_cbase = nullptr;  // 2*npts, the unscaled coefficients of the form
   double* d_hbm1 = nullptr;
   double* d_ebm1 = nullptr;
   double coef_dt = 0.0;
@@ -128,6 +157,8 @@ struct Context {
   bool uniform = true;
   int fused_grid = 0;
   FusedDev fargs{};
+  MixedDev margs{};
+  float* d_egm = nullptr;
 
   // plain form
   PlainDev pargs{};
@@ -135,6 +166,7 @@ struct Context {
 
   Source src;
   std::vector<double> host_bm1, host_x, host_y, host_z;
+  std::vector<double> host_w3, host_rx;  // for normalising source weights (mixed form)
   double rk_a[5], rk_b[5], rk_c[6];
   long last_launches = 0;
   bool have_state = false;
@@ -158,6 +190,9 @@ int plain_gs(Context* c, double* d_u, int nfld);
 int fused_setup(Context* c);  // grid size / smem attributes
 int fused_stage(Context* c, int rkstep, double time, double dt);
 int scale_coef(Context* c, double dt);
+
+// nekgpu_mixed.cu
+int mixed_stage(Context* c, int rkstep, double time, double dt);
 
 // reductions / utilities (nekgpu_util.cu)
 int util_norms(Context* c, const double* d_exact, double l2[6], double linf[6]);

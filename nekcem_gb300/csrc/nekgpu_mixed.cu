@@ -1,0 +1,589 @@
+// Mixed-precision Maxwell DG stage kernel for sm_103a (NEKGPU_MIXED).
+//
+// Same stage as nekgpu_fused.cu -- weighted curl from the GLL derivative
+// contractions (src/nek5_grad.F:2-19, src/cem_maxwell.F:1428-1497), upwind
+// face flux with the partner-face read that replaces gs_op_fields
+// (src/cem_maxwell.F:922-1002, 1368-1426), lift (src/cem_maxwell.F:725-735),
+// volume source, inverse mass (src/cem_maxwell.F:1878-1886) and the
+// low-storage RK update (src/cem_common.F:18-75) -- with the contractions, curl
+// and flux in FP32 and the state, RK register, inverse mass and update in
+// FP64.  FP32 is used so that it does not cost accuracy:
+//
+//  * Exact-hi contractions.  Per element and field component, u is split into
+//    uh = u rounded to a 10-bit grid q (q from the element's largest |u|) and
+//    ul = u - uh; each row of D is split the same way into Dh (10 bits) plus
+//    a remainder kept as two FP32 pieces Dm + Dl (so D itself is represented
+//    to ~2^-55: a rounded D would perturb the operator and drift the phase).
+//    Every product Dh*uh is an integer multiple of q*qD below 2^20 q*qD, so
+//    the FP32 sum over the <= 16 terms is exact.  The small remainder
+//    sum(D*ul + (Dm + Dl)*uh) is summed in FP32 beside it.  The FP32 rounding
+//    error is ~2^-34 of sum|D||u| instead of ~2^-24.
+//  * Thread per line.  Each thread contracts one GLL line at a time, so every
+//    D coefficient is a compile-time constant-bank operand of the FFMA.
+//  * Normalised residual.  For an affine axis-aligned element the mass
+//    cancels the GLL weights and metrics: res/(bm1*2/hx) = d_s Hz - d_t Hy
+//    (+ face terms flux*area/(bm1*2/hx)), etc.  All FP32 coefficients are then
+//    exact (1, or a float pair for non-cubic elements); the FP64 inverse-mass
+//    coefficient carries dt*(2/hx)/eps.
+//  * Pair residual.  The residual stays an unevaluated FP32 pair (hi, lo); it
+//    is multiplied by the FP64 coefficient as a float-float product, rounded
+//    to FP64 once (DADD) and enters the FP64 RK update (2 DFMA).
+//
+// FP64 <-> FP32 conversions use integer instructions only: every FP64-pipe
+// instruction on GB300 (including F2F) runs at 2 lanes/clock/SM.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "nekgpu_internal.h"
+
+namespace nekgpu {
+
+namespace {
+
+// ---------------------------------------------------------------------------
+// integer-only FP64 -> FP32 pieces
+// ---------------------------------------------------------------------------
+// top 24 bits of the mantissa (truncation); |d| < 2^-126 -> signed zero
+__device__ __forceinline__ float d2f_hi(double d) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(d);
+  const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
+  unsigned m = __funnelshift_l(lo, hi, 3) - 0xC0000000u;
+  m = (m & 0x7FFFFFFFu) | (hi & 0x80000000u);
+  return __uint_as_float((hi & 0x7FF00000u) >= 0x38100000u ? m : (hi & 0x80000000u));
+}
+// d - d2f_hi(d): the low 29 mantissa bits as a float (same sign as d);
+// zero when |d| < 2^-74 (where it is below 2^-97 in magnitude)
+__device__ __forceinline__ float d2f_lo(double d) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(d);
+  const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
+  const unsigned L = lo & 0x1FFFFFFFu;
+  const int ex = (int)((hi >> 20) & 0x7FFu);  // biased exponent
+  const float scale = __int_as_float((ex - 948) << 23);  // 2^(ex-1075)
+  float f = __uint2float_rn(L) * scale;
+  f = (ex >= 949) ? f : 0.0f;
+  return __uint_as_float(__float_as_uint(f) | (hi & 0x80000000u));
+}
+// exact FP32 -> FP64 (zero/subnormal -> signed zero)
+__device__ __forceinline__ double f2d(float f) {
+  const unsigned b = __float_as_uint(f);
+  const unsigned mag = b & 0x7FFFFFFFu;
+  unsigned hi = (b & 0x80000000u) | ((mag >> 3) + 0x38000000u);
+  unsigned lo = b << 29;
+  const bool tiny = (b & 0x7F800000u) == 0u;
+  hi = tiny ? (b & 0x80000000u) : hi;
+  lo = tiny ? 0u : lo;
+  return __longlong_as_double((long long)(((unsigned long long)hi << 32) | lo));
+}
+
+// Knuth two-sum: s + e == a + b exactly
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = a + b;
+  const float bb = s - a;
+  e = (a - (s - bb)) + (b - bb);
+}
+
+// ---------------------------------------------------------------------------
+// mbarrier + 1-D TMA bulk copy (PTX)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ unsigned smem_addr(const void* p) {
+  return (unsigned)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count)
+               : "memory");
+}
+__device__ __forceinline__ void fence_mbar_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+// orders this thread's (and, after a barrier, the block's) generic-proxy
+// shared-memory accesses before later async-proxy (TMA) accesses
+__device__ __forceinline__ void fence_proxy_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void tma_load_1d(void* dst, const void* src, unsigned bytes,
+                                            uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+          "r"(smem_addr(dst)),
+      "l"(src), "r"(bytes), "r"(smem_addr(bar))
+      : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_addr(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// gives up after ~2^22 polls (far beyond any copy time) and records it
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, unsigned parity, int* status) {
+  for (int it = 0; it < (1 << 22); ++it)
+    if (mbar_try_wait(bar, parity)) return true;
+  atomicExch(status, 1);
+  return false;
+}
+
+__host__ __device__ constexpr int slot_axis(int f) { return f == 1 || f == 3 ? 0 : (f < 4 ? 1 : 2); }
+__host__ __device__ constexpr int slot_side(int f) { return (f == 0 || f == 3 || f == 4) ? -1 : 1; }
+__host__ __device__ constexpr int slot_opp(int f) { return f < 4 ? (f + 2) & 3 : 9 - f; }
+
+template <int NX>
+__device__ __forceinline__ int face_vol(int f, int a, int b) {
+  const int fixed = slot_side(f) < 0 ? 0 : NX - 1;
+  const int ax = slot_axis(f);
+  return ax == 0 ? fixed + NX * a + NX * NX * b
+                 : (ax == 1 ? a + NX * fixed + NX * NX * b : a + NX * b + NX * NX * fixed);
+}
+
+constexpr int cmax(int a, int b) { return a > b ? a : b; }
+constexpr int round32(int a) { return (a + 31) / 32 * 32; }
+
+template <int NX>
+struct MCfg {
+  static constexpr int N2 = NX * NX, N3 = N2 * NX;
+  static constexpr int PAD = (N2 % 32 == 0) ? NX : 0;  // bank spread of s-lines
+  static constexpr int SZ = N2 + PAD;                  // k stride of the padded FP32 arrays
+  static constexpr int N3P = NX * SZ;
+  static constexpr int NF = 6 * N2;
+  static constexpr int NTASK = 4 * N2;  // line tasks per direction
+  static constexpr int NT = round32(cmax(NTASK, (N3 + 1) / 2));
+  static constexpr int NW = NT / 32;
+  static constexpr int NPT = (N3 + NT - 1) / NT;
+  static constexpr int FPT = (NF + NT - 1) / NT;
+  static constexpr int TPT = (NTASK + NT - 1) / NT;
+  static constexpr bool kTma = (N3 % 2) == 0;
+  static constexpr size_t off_u64 = 0;
+  static constexpr size_t off_uh = off_u64 + 6 * N3 * 8;
+  static constexpr size_t off_ul = off_uh + 6 * N3P * 4;
+  static constexpr size_t off_Rh = off_ul + 6 * N3P * 4;
+  static constexpr size_t off_Rl = off_Rh + 6 * N3P * 4;
+  static constexpr size_t off_nbh = off_Rl + 6 * N3P * 4;
+  static constexpr size_t off_nbl = off_nbh + 6 * NF * 4;
+  static constexpr size_t off_wmax = off_nbl + 6 * NF * 4;
+  static constexpr size_t off_E = off_wmax + NW * 6 * 4;
+  static constexpr size_t off_bar = (off_E + 8 * 4 + 15) / 16 * 16;
+  static constexpr size_t smem = off_bar + 16;
+};
+
+// components contracted in each direction, the residual they feed, the sign
+// and whether they start (init) or add to that residual.  Residual index
+// 0..2 = H1..H3 (-curl E), 3..5 = E1..E3 (curl H); field 0..2 = H, 3..5 = E.
+//   E1 = ds Hz - dt Hy   E2 = dt Hx - dr Hz   E3 = dr Hy - ds Hx
+//   H1 = dt Ey - ds Ez   H2 = dr Ez - dt Ex   H3 = ds Ex - dr Ey
+__constant__ const int kLineComp[3][4] = {{1, 2, 4, 5}, {0, 2, 3, 5}, {0, 1, 3, 4}};
+__constant__ const int kLineRes[3][4] = {{5, 4, 2, 1}, {5, 3, 2, 0}, {4, 3, 1, 0}};
+__constant__ const float kLineSign[3][4] = {{1, -1, -1, 1}, {-1, 1, 1, -1}, {1, -1, -1, 1}};
+__constant__ const int kLineInit[3][4] = {{1, 1, 1, 1}, {0, 1, 0, 1}, {0, 0, 0, 0}};
+
+template <int NX, int DIR>
+__device__ __forceinline__ int line_node(int a, int b, int l) {
+  constexpr int SZ = MCfg<NX>::SZ;
+  return DIR == 0 ? l + NX * a + SZ * b : (DIR == 1 ? a + NX * l + SZ * b : a + NX * b + SZ * l);
+}
+
+// One direction of the contraction: tasks (component, line) accumulate the
+// signed derivative pair into the residual pair arrays.
+template <int NX, int DIR>
+__device__ __forceinline__ void line_phase(const MixedDev& a, const float* s_uh, const float* s_ul,
+                                           float* s_Rh, float* s_Rl, const float* eg, int tid) {
+  using C = MCfg<NX>;
+  const bool cubic = eg[10] != 0.0f;
+  const float rh = DIR == 1 ? eg[0] : eg[2], rl = DIR == 1 ? eg[1] : eg[3];
+#pragma unroll
+  for (int q = 0; q < C::TPT; ++q) {
+    const int task = tid + q * C::NT;
+    if (task < C::NTASK) {
+      const int slot = task / C::N2, lam = task - slot * C::N2;
+      const int la = lam % NX, lb = lam / NX;
+      const int comp = kLineComp[DIR][slot], rt = kLineRes[DIR][slot];
+      const float sg = kLineSign[DIR][slot];
+      const bool init = kLineInit[DIR][slot] != 0;
+      float uh[NX], ul[NX];
+#pragma unroll
+      for (int l = 0; l < NX; ++l) {
+        const int pv = line_node<NX, DIR>(la, lb, l);
+        uh[l] = s_uh[comp * C::N3P + pv];
+        ul[l] = s_ul[comp * C::N3P + pv];
+      }
+#pragma unroll
+      for (int i = 0; i < NX; ++i) {
+        float hi = 0.0f, lo = 0.0f;
+#pragma unroll
+        for (int l = 0; l < NX; ++l) {
+          hi = fmaf(a.Dh[i + NX * l], uh[l], hi);  // exact
+          lo = fmaf(a.Df[i + NX * l], ul[l], lo);
+          lo = fmaf(a.Dm[i + NX * l], uh[l], lo);
+          lo = fmaf(a.Dl[i + NX * l], uh[l], lo);
+        }
+        if (DIR != 0 && !cubic) {  // times rho = g_dir/g_x as a float pair
+          const float p = rh * hi;
+          float e = fmaf(rh, hi, -p);
+          e = fmaf(rh, lo, e);
+          e = fmaf(rl, hi, e);
+          hi = p;
+          lo = e;
+        }
+        hi *= sg;
+        lo *= sg;
+        const int pv = line_node<NX, DIR>(la, lb, i);
+        float* Rh = s_Rh + rt * C::N3P + pv;
+        float* Rl = s_Rl + rt * C::N3P + pv;
+        if (init) {
+          *Rh = hi;
+          *Rl = lo;
+        } else {
+          float s, err;
+          two_sum(*Rh, hi, s, err);
+          *Rh = s;
+          *Rl = (*Rl + lo) + err;
+        }
+      }
+    }
+  }
+}
+
+template <int NX>
+__global__ void __launch_bounds__(MCfg<NX>::NT, 2) k_mixed_stage(const MixedDev a) {
+  using C = MCfg<NX>;
+  constexpr int N2 = C::N2, N3 = C::N3, NT = C::NT, NF = C::NF, N3P = C::N3P, SZ = C::SZ;
+  constexpr int NPT = C::NPT, FPT = C::FPT;
+  extern __shared__ __align__(16) unsigned char smem[];
+  double* s_u64 = reinterpret_cast<double*>(smem + C::off_u64);
+  float* s_uh = reinterpret_cast<float*>(smem + C::off_uh);
+  float* s_ul = reinterpret_cast<float*>(smem + C::off_ul);
+  float* s_Rh = reinterpret_cast<float*>(smem + C::off_Rh);
+  float* s_Rl = reinterpret_cast<float*>(smem + C::off_Rl);
+  float* s_nbh = reinterpret_cast<float*>(smem + C::off_nbh);  // partner hi; then the lifted flux
+  float* s_nbl = reinterpret_cast<float*>(smem + C::off_nbl);
+  unsigned* s_wmax = reinterpret_cast<unsigned*>(smem + C::off_wmax);
+  unsigned* s_E = reinterpret_cast<unsigned*>(smem + C::off_E);
+  uint64_t* bar = reinterpret_cast<uint64_t*>(smem + C::off_bar);
+  __shared__ int s_abort;
+
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const long P = a.npts;
+  const bool first_stage = (a.a == 0.0);  // rk4a(1) = 0: k restarts
+
+  if (tid == 0) {
+    s_abort = 0;
+    if (C::kTma) {
+      mbar_init(bar, 1);
+      fence_mbar_init();
+    }
+  }
+  __syncthreads();
+  auto issue_tma = [&](int e) {
+    const unsigned bytes = N3 * 8;
+    mbar_expect_tx(bar, 6u * bytes);
+    for (int c = 0; c < 6; ++c) tma_load_1d(s_u64 + c * N3, a.u_in + c * P + (long)e * N3, bytes, bar);
+  };
+  unsigned parity = 0;
+  if (C::kTma && tid == 0 && blockIdx.x < a.nelt) issue_tma(blockIdx.x);
+
+  for (int e = blockIdx.x; e < a.nelt; e += gridDim.x) {
+    const int* nbr = a.nbr + 6 * e;
+    const float* eg = a.egm + 12 * e;
+    // ---- early loads: partner face nodes, RK register and coefficients ----
+    double nbv[FPT][6];
+#pragma unroll
+    for (int q = 0; q < FPT; ++q) {
+      const int t = tid + q * NT;
+      if (t < NF) {
+        const int f = t / N2, ab = t - f * N2;
+        const int pe = nbr[f];
+        if (pe >= 0) {
+          const long pv = (long)pe * N3 + face_vol<NX>(slot_opp(f), ab % NX, ab / NX);
+#pragma unroll
+          for (int c = 0; c < 6; ++c) nbv[q][c] = __ldg(a.u_in + c * P + pv);
+        }
+      }
+    }
+    double kv[NPT][6], cv[NPT][2];
+#pragma unroll
+    for (int q = 0; q < NPT; ++q) {
+      const int v = tid + q * NT;
+      if (v < N3) {
+        const long g = (long)e * N3 + v;
+        if (!first_stage) {
+#pragma unroll
+          for (int c = 0; c < 6; ++c) kv[q][c] = a.k[c * P + g];
+        }
+        cv[q][0] = a.coef[g];
+        cv[q][1] = a.coef[P + g];
+      }
+    }
+    // ---- own element state ----------------------------------------------
+    if (C::kTma) {
+      if (!mbar_wait_bounded(bar, parity, a.status)) s_abort = 1;
+      parity ^= 1u;
+    } else {
+#pragma unroll
+      for (int q = 0; q < NPT; ++q) {
+        const int v = tid + q * NT;
+        if (v < N3)
+#pragma unroll
+          for (int c = 0; c < 6; ++c) s_u64[c * N3 + v] = a.u_in[c * P + (long)e * N3 + v];
+      }
+    }
+    __syncthreads();
+    if (s_abort) return;
+    // ---- per-component largest exponent of the element -> 10-bit grid ----
+    {
+      unsigned em[6] = {0, 0, 0, 0, 0, 0};
+#pragma unroll
+      for (int q = 0; q < NPT; ++q) {
+        const int v = tid + q * NT;
+        if (v < N3)
+#pragma unroll
+          for (int c = 0; c < 6; ++c) {
+            const unsigned hw = (unsigned)__double2hiint(s_u64[c * N3 + v]);
+            em[c] = max(em[c], (hw >> 20) & 0x7FFu);
+          }
+      }
+#pragma unroll
+      for (int c = 0; c < 6; ++c) em[c] = __reduce_max_sync(0xffffffffu, em[c]);
+      if (lane == 0)
+#pragma unroll
+        for (int c = 0; c < 6; ++c) s_wmax[warp * 6 + c] = em[c];
+    }
+    __syncthreads();
+    if (tid < 6) {
+      unsigned m = 0;
+      for (int w = 0; w < C::NW; ++w) m = max(m, s_wmax[w * 6 + tid]);
+      s_E[tid] = min(max(m, 906u), 1158u);
+    }
+    __syncthreads();
+    // ---- split: uh on the grid q = 2^(E-1032), ul = u - uh ----------------
+    {
+      const float M = 12582912.0f;  // 1.5 * 2^23: float rounding to integers
+#pragma unroll
+      for (int c = 0; c < 6; ++c) {
+        const int E = (int)s_E[c];
+        const float qv = __int_as_float((E - 905) << 23);    // 2^(E-1032)
+        const float qi = __int_as_float((1159 - E) << 23);   // 2^(1032-E)
+#pragma unroll
+        for (int q = 0; q < NPT; ++q) {
+          const int v = tid + q * NT;
+          if (v < N3) {
+            const int i = v % NX, j = (v / NX) % NX, k = v / N2;
+            const int pv = i + NX * j + SZ * k;
+            const double u = s_u64[c * N3 + v];
+            const float uf = d2f_hi(u), ulo = d2f_lo(u);
+            const float uh = (__fadd_rn(__fmaf_rn(uf, qi, M), -M)) * qv;
+            s_uh[c * N3P + pv] = uh;
+            s_ul[c * N3P + pv] = __fadd_rn(__fsub_rn(uf, uh), ulo);
+          }
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < FPT; ++q) {
+        const int t = tid + q * NT;
+        if (t < NF && nbr[t / N2] >= 0) {
+#pragma unroll
+          for (int c = 0; c < 6; ++c) {
+            s_nbh[c * NF + t] = d2f_hi(nbv[q][c]);
+            s_nbl[c * NF + t] = d2f_lo(nbv[q][c]);
+          }
+        }
+      }
+    }
+    __syncthreads();
+    // ---- contractions: r, s, t lines ----------------------------------------
+    line_phase<NX, 0>(a, s_uh, s_ul, s_Rh, s_Rl, eg, tid);
+    __syncthreads();
+    line_phase<NX, 1>(a, s_uh, s_ul, s_Rh, s_Rl, eg, tid);
+    __syncthreads();
+    line_phase<NX, 2>(a, s_uh, s_ul, s_Rh, s_Rl, eg, tid);
+    // ---- upwind flux per face node (same interval: reads uh/ul, writes nbh) -
+#pragma unroll
+    for (int q = 0; q < FPT; ++q) {
+      const int t = tid + q * NT;
+      if (t < NF) {
+        const int f = t / N2, ab = t - f * N2;
+        const int fa = ab % NX, fb = ab / NX;
+        const int v = face_vol<NX>(f, fa, fb);
+        const int pv = (v % NX) + NX * ((v / NX) % NX) + SZ * (v / N2);
+        const int pe = nbr[f];
+        float dH[3], dE[3];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          const float hh = s_uh[c * N3P + pv], hl = s_ul[c * N3P + pv];
+          const float eh = s_uh[(c + 3) * N3P + pv], el = s_ul[(c + 3) * N3P + pv];
+          if (pe >= 0) {  // jump = (partner_hi - own_hi) + (partner_lo - own_lo)
+            dH[c] = (s_nbh[c * NF + t] - hh) + (s_nbl[c * NF + t] - hl);
+            dE[c] = (s_nbh[(c + 3) * NF + t] - eh) + (s_nbl[(c + 3) * NF + t] - el);
+          } else {  // PEC mirror: H+ = H-, E+ = -E-
+            dH[c] = 0.0f;
+            dE[c] = -2.0f * (eh + el);
+          }
+        }
+        float Y02 = -0.5f, C02Y = 0.5f * a.C0f, Z02 = 0.5f, C02Z = 0.5f * a.C0f;
+        if (a.fcoef) {
+          const float4 fc = reinterpret_cast<const float4*>(a.fcoef)[(long)e * NF + t];
+          Y02 = fc.x; C02Y = fc.y; Z02 = fc.z; C02Z = fc.w;
+        }
+        const float sg = (float)slot_side(f);
+        const float lf = eg[4 + f];  // area / (bm1 * 2/hx) at this face
+        const float sY = sg * Y02, sZ = sg * Z02;
+        float fH[3], fE[3];
+        switch (slot_axis(f)) {
+          case 0:
+            fH[0] = 0.0f;
+            fH[1] = fmaf(-sY, dE[2], C02Y * dH[1]);
+            fH[2] = fmaf(sY, dE[1], C02Y * dH[2]);
+            fE[0] = 0.0f;
+            fE[1] = fmaf(-sZ, dH[2], C02Z * dE[1]);
+            fE[2] = fmaf(sZ, dH[1], C02Z * dE[2]);
+            break;
+          case 1:
+            fH[0] = fmaf(sY, dE[2], C02Y * dH[0]);
+            fH[1] = 0.0f;
+            fH[2] = fmaf(-sY, dE[0], C02Y * dH[2]);
+            fE[0] = fmaf(sZ, dH[2], C02Z * dE[0]);
+            fE[1] = 0.0f;
+            fE[2] = fmaf(-sZ, dH[0], C02Z * dE[2]);
+            break;
+          default:
+            fH[0] = fmaf(-sY, dE[1], C02Y * dH[0]);
+            fH[1] = fmaf(sY, dE[0], C02Y * dH[1]);
+            fH[2] = 0.0f;
+            fE[0] = fmaf(-sZ, dH[1], C02Z * dE[0]);
+            fE[1] = fmaf(sZ, dH[0], C02Z * dE[1]);
+            fE[2] = 0.0f;
+            break;
+        }
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          s_nbh[c * NF + t] = lf * fH[c];
+          s_nbh[(c + 3) * NF + t] = lf * fE[c];
+        }
+      }
+    }
+    __syncthreads();
+    // ---- lift, source, inverse mass, RK update --------------------------------
+    // Everything that reads the staged u is finished before the barrier that
+    // lets the next element's TMA overwrite it.
+    const int so = a.src_elem ? a.src_elem[e] : -1;
+    double kn[NPT][6], un[NPT][6];
+#pragma unroll
+    for (int q = 0; q < NPT; ++q) {
+      const int v = tid + q * NT;
+      if (v >= N3) continue;
+      const int i = v % NX, j = (v / NX) % NX, k = v / N2;
+      const int pv = i + NX * j + SZ * k;
+      float Rh[6], Rl[6];
+#pragma unroll
+      for (int c = 0; c < 6; ++c) {
+        Rh[c] = s_Rh[c * N3P + pv];
+        Rl[c] = s_Rl[c * N3P + pv];
+      }
+      auto add = [&](int f, int ab) {
+#pragma unroll
+        for (int c = 0; c < 6; ++c) Rl[c] += s_nbh[c * NF + f * N2 + ab];
+      };
+      if (j == 0) add(0, i + NX * k);
+      if (i == NX - 1) add(1, j + NX * k);
+      if (j == NX - 1) add(2, i + NX * k);
+      if (i == 0) add(3, j + NX * k);
+      if (k == 0) add(4, i + NX * j);
+      if (k == NX - 1) add(5, i + NX * j);
+      if (so >= 0) Rl[5] = fmaf(a.src_w[(long)so * N3 + v], a.src_ftf, Rl[5]);
+      const float chh = d2f_hi(cv[q][0]), chl = d2f_lo(cv[q][0]);
+      const float ceh = d2f_hi(cv[q][1]), cel = d2f_lo(cv[q][1]);
+#pragma unroll
+      for (int c = 0; c < 6; ++c) {
+        const float ch = c < 3 ? chh : ceh, cl = c < 3 ? chl : cel;
+        const float p = ch * Rh[c];
+        float ee = fmaf(ch, Rh[c], -p);
+        ee = fmaf(ch, Rl[c], ee);
+        ee = fmaf(cl, Rh[c], ee);
+        const double r = f2d(p) + f2d(ee);
+        kn[q][c] = first_stage ? r : fma(a.a, kv[q][c], r);
+        un[q][c] = fma(a.b, kn[q][c], s_u64[c * N3 + v]);
+      }
+    }
+    __syncthreads();  // staged u consumed: the next element may land
+    const int en = e + gridDim.x;
+    if (C::kTma && tid == 0 && en < a.nelt) {
+      fence_proxy_async_smem();
+      issue_tma(en);
+    }
+#pragma unroll
+    for (int q = 0; q < NPT; ++q) {
+      const int v = tid + q * NT;
+      if (v >= N3) continue;
+      const long g = (long)e * N3 + v;
+#pragma unroll
+      for (int c = 0; c < 6; ++c) {
+        a.k[c * P + g] = kn[q][c];
+        a.u_out[c * P + g] = un[q][c];
+      }
+    }
+  }
+}
+
+template <int NX>
+int launch_mixed(Context* c, const MixedDev& a) {
+  using C = MCfg<NX>;
+  auto kern = k_mixed_stage<NX>;
+  static bool ready = false;
+  static int grid = 0;
+  if (!ready) {
+    if (check_cuda(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)C::smem)))
+      return NEKGPU_ERR_CUDA;
+    int per_sm = 0, sms = 0;
+    if (check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, C::NT, C::smem)))
+      return NEKGPU_ERR_CUDA;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
+    if (per_sm < 1) return NEKGPU_ERR_UNSUPPORTED;
+    grid = per_sm * sms;
+    ready = true;
+  }
+  const int g = c->nelt < grid ? c->nelt : grid;
+  c->fused_grid = g;
+  kern<<<g, C::NT, C::smem, c->stream>>>(a);
+  c->last_launches += 1;
+  return check_cuda(cudaGetLastError());
+}
+
+}  // namespace
+
+int mixed_stage(Context* c, int rkstep, double time, double dt) {
+  int st = scale_coef(c, dt);
+  if (st) return st;
+  MixedDev a = c->margs;
+  a.u_in = c->d_u[c->cur];
+  a.u_out = c->d_u[c->cur ^ 1];
+  a.a = c->rk_a[rkstep - 1];
+  a.b = c->rk_b[rkstep - 1];
+  if (c->src.enabled) {
+    const double rktime = time + dt * c->rk_c[rkstep - 1];
+    const double pi = 4.0 * atan(1.0);
+    const double x = pi * c->src.f0 * (rktime - c->src.t0);
+    a.src_ftf = (float)(c->src.amp * (1.0 - 2.0 * x * x) * exp(-x * x));
+  }
+  switch (c->nx) {
+    case 3: st = launch_mixed<3>(c, a); break;
+    case 4: st = launch_mixed<4>(c, a); break;
+    case 5: st = launch_mixed<5>(c, a); break;
+    case 6: st = launch_mixed<6>(c, a); break;
+    case 7: st = launch_mixed<7>(c, a); break;
+    case 8: st = launch_mixed<8>(c, a); break;
+    case 9: st = launch_mixed<9>(c, a); break;
+    default: return NEKGPU_ERR_UNSUPPORTED;
+  }
+  if (st) return st;
+  c->cur ^= 1;
+  return NEKGPU_OK;
+}
+
+}  // namespace nekgpu

@@ -199,14 +199,9 @@ def test_reference_known_answer(name, form):
     g.set_state(H, E)
     t = g.run(c.nsteps, 0.0, c.dt)
     l2, linf = g.cem_error(*c.exact(x, y, z, t))
-    if form == "mixed":
-        # FP32 contractions: the reference's FP64 tolerance does not apply to
-        # 3dboxper (5e-10); the mixed form is held to 100x the FP64 bar there
-        scale = 1.0 if name == "3dboxpec" else 100.0
-    else:
-        scale = 1.0
-    assert np.all(l2 <= c.l2tol * scale), l2
-    assert np.all(linf <= c.linftol * scale), linf
+    # the reference's own tolerances, for the mixed form too
+    assert np.all(l2 <= c.l2tol), l2
+    assert np.all(linf <= c.linftol), linf
     g.close()
 
 
