@@ -763,7 +763,19 @@ int upload_fused(Context* c, const Compact& cp) {
     m.C0f = (float)cp.C0;
     m.status = c->d_status;
     if (c->nx > kMaxMixed) return NEKGPU_ERR_UNSUPPORTED;
-    split_D(cp.D, c->nx, m.Dh, m.Df, m.Dm, m.Dl);
+    // the mixed form uses the library's own GLL D of this order (exactly
+    // centro-antisymmetric, computed once per order); a caller's D must agree
+    std::vector<double> z, w, D;
+    gll(c->nx - 1, z, w, D);
+    double dmax = 0, diff = 0;
+    for (size_t k = 0; k < D.size(); ++k) {
+      dmax = std::max(dmax, std::fabs(D[k]));
+      diff = std::max(diff, std::fabs(D[k] - cp.D[k]));
+    }
+    if (diff > 1e-12 * dmax) return NEKGPU_ERR_MESH;
+    std::vector<float> Dh(D.size()), Df(D.size()), Dm(D.size()), Dl(D.size());
+    split_D(D, c->nx, Dh.data(), Df.data(), Dm.data(), Dl.data());
+    if ((st = mixed_upload_D(c->nx, Dh.data(), Df.data(), Dm.data(), Dl.data()))) return st;
     return NEKGPU_OK;
   }
   if ((st = A.put(&c->d_egeom, cp.egeom))) return st;

@@ -114,13 +114,6 @@ struct MixedDev {
   double a, b;
   float C0f;
   int* status;
-  // D(i,j) at [i + nx*j] in four FP32 pieces: Dh on a 10-bit grid per row
-  // (exact products with the 10-bit uh), Df = D rounded, and the remainder
-  // D - Dh = Dm + Dl to ~2^-55.
-  float Dh[kMaxMixed * kMaxMixed];
-  float Df[kMaxMixed * kMaxMixed];
-  float Dm[kMaxMixed * kMaxMixed];
-  float Dl[kMaxMixed * kMaxMixed];
 };
 
 struct Context {
@@ -193,6 +186,10 @@ int scale_coef(Context* c, double dt);
 
 // nekgpu_mixed.cu
 int mixed_stage(Context* c, int rkstep, double time, double dt);
+// D(i,j) at [i + nx*j] in four FP32 pieces: Dh on a 10-bit grid per row
+// (exact products with the 10-bit uh), Df = D rounded, and the remainder
+// D - Dh = Dm + Dl to ~2^-55; uploaded once per nx
+int mixed_upload_D(int nx, const float* Dh, const float* Df, const float* Dm, const float* Dl);
 
 // reductions / utilities (nekgpu_util.cu)
 int util_norms(Context* c, const double* d_exact, double l2[6], double linf[6]);

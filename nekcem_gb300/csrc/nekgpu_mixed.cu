@@ -143,6 +143,20 @@ __device__ __forceinline__ int face_vol(int f, int a, int b) {
                  : (ax == 1 ? a + NX * fixed + NX * NX * b : a + NX * b + NX * NX * fixed);
 }
 
+// D of order nx-1 in the four FP32 pieces of the exact-hi contraction,
+// indexed by nx so that every coefficient is a compile-time constant-bank
+// operand: [nx][piece: Dh, Df, Dm, Dl][i + nx*l].  D depends only on nx.
+__constant__ float c_mixD[kMaxMixed + 1][4][kMaxMixed * kMaxMixed];
+
+// A copy of the thread index the compiler cannot see through: index math
+// derived from it is recomputed in each phase instead of being hoisted out of
+// the element loop, where it would stay live in registers for every phase.
+__device__ __forceinline__ int opaque_tid() {
+  int t = threadIdx.x;
+  asm volatile("" : "+r"(t));
+  return t;
+}
+
 constexpr int cmax(int a, int b) { return a > b ? a : b; }
 constexpr int round32(int a) { return (a + 31) / 32 * 32; }
 
@@ -192,9 +206,10 @@ __device__ __forceinline__ int line_node(int a, int b, int l) {
 // One direction of the contraction: tasks (component, line) accumulate the
 // signed derivative pair into the residual pair arrays.
 template <int NX, int DIR>
-__device__ __forceinline__ void line_phase(const MixedDev& a, const float* s_uh, const float* s_ul,
-                                           float* s_Rh, float* s_Rl, const float* eg, int tid) {
+__device__ __forceinline__ void line_phase(const float* s_uh, const float* s_ul, float* s_Rh,
+                                           float* s_Rl, const float* eg) {
   using C = MCfg<NX>;
+  const int tid = opaque_tid();
   const bool cubic = eg[10] != 0.0f;
   const float rh = DIR == 1 ? eg[0] : eg[2], rl = DIR == 1 ? eg[1] : eg[3];
 #pragma unroll
@@ -206,44 +221,52 @@ __device__ __forceinline__ void line_phase(const MixedDev& a, const float* s_uh,
       const int comp = kLineComp[DIR][slot], rt = kLineRes[DIR][slot];
       const float sg = kLineSign[DIR][slot];
       const bool init = kLineInit[DIR][slot] != 0;
-      float uh[NX], ul[NX];
+      const float* ph = s_uh + comp * C::N3P;
+      const float* pl = s_ul + comp * C::N3P;
+      // all NX outputs of the line at once: compile-time coefficient indices,
+      // NX independent accumulator pairs
+      float hi[NX], lo[NX];
+#pragma unroll
+      for (int i = 0; i < NX; ++i) {
+        hi[i] = 0.0f;
+        lo[i] = 0.0f;
+      }
 #pragma unroll
       for (int l = 0; l < NX; ++l) {
         const int pv = line_node<NX, DIR>(la, lb, l);
-        uh[l] = s_uh[comp * C::N3P + pv];
-        ul[l] = s_ul[comp * C::N3P + pv];
+        const float h = ph[pv], r = pl[pv];
+#pragma unroll
+        for (int i = 0; i < NX; ++i) {
+          hi[i] = fmaf(c_mixD[NX][0][i + NX * l], h, hi[i]);  // exact
+          lo[i] = fmaf(c_mixD[NX][1][i + NX * l], r, lo[i]);
+          lo[i] = fmaf(c_mixD[NX][2][i + NX * l], h, lo[i]);
+          lo[i] = fmaf(c_mixD[NX][3][i + NX * l], h, lo[i]);
+        }
       }
+      float* Rh0 = s_Rh + rt * C::N3P;
+      float* Rl0 = s_Rl + rt * C::N3P;
 #pragma unroll
       for (int i = 0; i < NX; ++i) {
-        float hi = 0.0f, lo = 0.0f;
-#pragma unroll
-        for (int l = 0; l < NX; ++l) {
-          hi = fmaf(a.Dh[i + NX * l], uh[l], hi);  // exact
-          lo = fmaf(a.Df[i + NX * l], ul[l], lo);
-          lo = fmaf(a.Dm[i + NX * l], uh[l], lo);
-          lo = fmaf(a.Dl[i + NX * l], uh[l], lo);
-        }
+        float h = hi[i], r = lo[i];
         if (DIR != 0 && !cubic) {  // times rho = g_dir/g_x as a float pair
-          const float p = rh * hi;
-          float e = fmaf(rh, hi, -p);
-          e = fmaf(rh, lo, e);
-          e = fmaf(rl, hi, e);
-          hi = p;
-          lo = e;
+          const float p = rh * h;
+          float e = fmaf(rh, h, -p);
+          e = fmaf(rh, r, e);
+          e = fmaf(rl, h, e);
+          h = p;
+          r = e;
         }
-        hi *= sg;
-        lo *= sg;
+        h *= sg;
+        r *= sg;
         const int pv = line_node<NX, DIR>(la, lb, i);
-        float* Rh = s_Rh + rt * C::N3P + pv;
-        float* Rl = s_Rl + rt * C::N3P + pv;
         if (init) {
-          *Rh = hi;
-          *Rl = lo;
+          Rh0[pv] = h;
+          Rl0[pv] = r;
         } else {
-          float s, err;
-          two_sum(*Rh, hi, s, err);
-          *Rh = s;
-          *Rl = (*Rl + lo) + err;
+          float sum, err;
+          two_sum(Rh0[pv], h, sum, err);
+          Rh0[pv] = sum;
+          Rl0[pv] = (Rl0[pv] + r) + err;
         }
       }
     }
@@ -268,7 +291,8 @@ __global__ void __launch_bounds__(MCfg<NX>::NT, 2) k_mixed_stage(const MixedDev 
   uint64_t* bar = reinterpret_cast<uint64_t*>(smem + C::off_bar);
   __shared__ int s_abort;
 
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int tid = threadIdx.x;
   const long P = a.npts;
   const bool first_stage = (a.a == 0.0);  // rk4a(1) = 0: k restarts
 
@@ -289,6 +313,7 @@ __global__ void __launch_bounds__(MCfg<NX>::NT, 2) k_mixed_stage(const MixedDev 
   if (C::kTma && tid == 0 && blockIdx.x < a.nelt) issue_tma(blockIdx.x);
 
   for (int e = blockIdx.x; e < a.nelt; e += gridDim.x) {
+    int tid = opaque_tid();
     const int* nbr = a.nbr + 6 * e;
     const float* eg = a.egm + 12 * e;
     // ---- early loads: partner face nodes, RK register and coefficients ----
@@ -304,20 +329,6 @@ __global__ void __launch_bounds__(MCfg<NX>::NT, 2) k_mixed_stage(const MixedDev 
 #pragma unroll
           for (int c = 0; c < 6; ++c) nbv[q][c] = __ldg(a.u_in + c * P + pv);
         }
-      }
-    }
-    double kv[NPT][6], cv[NPT][2];
-#pragma unroll
-    for (int q = 0; q < NPT; ++q) {
-      const int v = tid + q * NT;
-      if (v < N3) {
-        const long g = (long)e * N3 + v;
-        if (!first_stage) {
-#pragma unroll
-          for (int c = 0; c < 6; ++c) kv[q][c] = a.k[c * P + g];
-        }
-        cv[q][0] = a.coef[g];
-        cv[q][1] = a.coef[P + g];
       }
     }
     // ---- own element state ----------------------------------------------
@@ -362,6 +373,7 @@ __global__ void __launch_bounds__(MCfg<NX>::NT, 2) k_mixed_stage(const MixedDev 
     }
     __syncthreads();
     // ---- split: uh on the grid q = 2^(E-1032), ul = u - uh ----------------
+    tid = opaque_tid();
     {
       const float M = 12582912.0f;  // 1.5 * 2^23: float rounding to integers
 #pragma unroll
@@ -397,12 +409,13 @@ __global__ void __launch_bounds__(MCfg<NX>::NT, 2) k_mixed_stage(const MixedDev 
     }
     __syncthreads();
     // ---- contractions: r, s, t lines ----------------------------------------
-    line_phase<NX, 0>(a, s_uh, s_ul, s_Rh, s_Rl, eg, tid);
+    line_phase<NX, 0>(s_uh, s_ul, s_Rh, s_Rl, eg);
     __syncthreads();
-    line_phase<NX, 1>(a, s_uh, s_ul, s_Rh, s_Rl, eg, tid);
+    line_phase<NX, 1>(s_uh, s_ul, s_Rh, s_Rl, eg);
     __syncthreads();
-    line_phase<NX, 2>(a, s_uh, s_ul, s_Rh, s_Rl, eg, tid);
+    line_phase<NX, 2>(s_uh, s_ul, s_Rh, s_Rl, eg);
     // ---- upwind flux per face node (same interval: reads uh/ul, writes nbh) -
+    tid = opaque_tid();
 #pragma unroll
     for (int q = 0; q < FPT; ++q) {
       const int t = tid + q * NT;
@@ -467,12 +480,27 @@ __global__ void __launch_bounds__(MCfg<NX>::NT, 2) k_mixed_stage(const MixedDev 
         }
       }
     }
+    // RK register and coefficients, loaded late to keep registers free above
+    tid = opaque_tid();
+    double kv[NPT][6], cv[NPT][2];
+#pragma unroll
+    for (int q = 0; q < NPT; ++q) {
+      const int v = tid + q * NT;
+      if (v < N3) {
+        const long g = (long)e * N3 + v;
+        if (!first_stage) {
+#pragma unroll
+          for (int c = 0; c < 6; ++c) kv[q][c] = a.k[c * P + g];
+        }
+        cv[q][0] = a.coef[g];
+        cv[q][1] = a.coef[P + g];
+      }
+    }
     __syncthreads();
     // ---- lift, source, inverse mass, RK update --------------------------------
-    // Everything that reads the staged u is finished before the barrier that
-    // lets the next element's TMA overwrite it.
+    // Every read of the staged u happens before the barrier that lets the
+    // next element's TMA overwrite it.
     const int so = a.src_elem ? a.src_elem[e] : -1;
-    double kn[NPT][6], un[NPT][6];
 #pragma unroll
     for (int q = 0; q < NPT; ++q) {
       const int v = tid + q * NT;
@@ -498,6 +526,7 @@ __global__ void __launch_bounds__(MCfg<NX>::NT, 2) k_mixed_stage(const MixedDev 
       if (so >= 0) Rl[5] = fmaf(a.src_w[(long)so * N3 + v], a.src_ftf, Rl[5]);
       const float chh = d2f_hi(cv[q][0]), chl = d2f_lo(cv[q][0]);
       const float ceh = d2f_hi(cv[q][1]), cel = d2f_lo(cv[q][1]);
+      const long g = (long)e * N3 + v;
 #pragma unroll
       for (int c = 0; c < 6; ++c) {
         const float ch = c < 3 ? chh : ceh, cl = c < 3 ? chl : cel;
@@ -506,8 +535,9 @@ __global__ void __launch_bounds__(MCfg<NX>::NT, 2) k_mixed_stage(const MixedDev 
         ee = fmaf(ch, Rl[c], ee);
         ee = fmaf(cl, Rh[c], ee);
         const double r = f2d(p) + f2d(ee);
-        kn[q][c] = first_stage ? r : fma(a.a, kv[q][c], r);
-        un[q][c] = fma(a.b, kn[q][c], s_u64[c * N3 + v]);
+        const double kn = first_stage ? r : fma(a.a, kv[q][c], r);
+        a.k[c * P + g] = kn;
+        a.u_out[c * P + g] = fma(a.b, kn, s_u64[c * N3 + v]);
       }
     }
     __syncthreads();  // staged u consumed: the next element may land
@@ -515,17 +545,6 @@ __global__ void __launch_bounds__(MCfg<NX>::NT, 2) k_mixed_stage(const MixedDev 
     if (C::kTma && tid == 0 && en < a.nelt) {
       fence_proxy_async_smem();
       issue_tma(en);
-    }
-#pragma unroll
-    for (int q = 0; q < NPT; ++q) {
-      const int v = tid + q * NT;
-      if (v >= N3) continue;
-      const long g = (long)e * N3 + v;
-#pragma unroll
-      for (int c = 0; c < 6; ++c) {
-        a.k[c * P + g] = kn[q][c];
-        a.u_out[c * P + g] = un[q][c];
-      }
     }
   }
 }
@@ -556,6 +575,20 @@ int launch_mixed(Context* c, const MixedDev& a) {
 }
 
 }  // namespace
+
+int mixed_upload_D(int nx, const float* Dh, const float* Df, const float* Dm, const float* Dl) {
+  static bool done[kMaxMixed + 1] = {false};
+  if (nx < 2 || nx > kMaxMixed) return NEKGPU_ERR_UNSUPPORTED;
+  if (done[nx]) return NEKGPU_OK;
+  float tab[4][kMaxMixed * kMaxMixed] = {};
+  for (int k = 0; k < nx * nx; ++k) {
+    tab[0][k] = Dh[k]; tab[1][k] = Df[k]; tab[2][k] = Dm[k]; tab[3][k] = Dl[k];
+  }
+  if (check_cuda(cudaMemcpyToSymbol(c_mixD, tab, sizeof(tab), sizeof(tab) * nx)))
+    return NEKGPU_ERR_CUDA;
+  done[nx] = true;
+  return NEKGPU_OK;
+}
 
 int mixed_stage(Context* c, int rkstep, double time, double dt) {
   int st = scale_coef(c, dt);
