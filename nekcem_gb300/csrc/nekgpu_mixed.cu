@@ -163,8 +163,10 @@ constexpr int round32(int a) { return (a + 31) / 32 * 32; }
 template <int NX>
 struct MCfg {
   static constexpr int N2 = NX * NX, N3 = N2 * NX;
-  static constexpr int PAD = (N2 % 32 == 0) ? NX : 0;  // bank spread of s-lines
-  static constexpr int SZ = N2 + PAD;                  // k stride of the padded FP32 arrays
+  // padded node layout i + RS*j + SZ*k: with NX=8 (RS=9, SZ=72) the warp's
+  // accesses along r- and s-lines hit 32 distinct banks
+  static constexpr int RS = NX + 1;
+  static constexpr int SZ = RS * NX;
   static constexpr int N3P = NX * SZ;
   static constexpr int NF = 6 * N2;
   static constexpr int NTASK = 4 * N2;  // line tasks per direction
@@ -175,13 +177,10 @@ struct MCfg {
   static constexpr int TPT = (NTASK + NT - 1) / NT;
   static constexpr bool kTma = (N3 % 2) == 0;
   static constexpr size_t off_u64 = 0;
-  static constexpr size_t off_uh = off_u64 + 6 * N3 * 8;
-  static constexpr size_t off_ul = off_uh + 6 * N3P * 4;
-  static constexpr size_t off_Rh = off_ul + 6 * N3P * 4;
-  static constexpr size_t off_Rl = off_Rh + 6 * N3P * 4;
-  static constexpr size_t off_nbh = off_Rl + 6 * N3P * 4;
-  static constexpr size_t off_nbl = off_nbh + 6 * NF * 4;
-  static constexpr size_t off_wmax = off_nbl + 6 * NF * 4;
+  static constexpr size_t off_u2 = off_u64 + 6 * N3 * 8;   // float2 (uh, ul)
+  static constexpr size_t off_R2 = off_u2 + 6 * N3P * 8;    // float2 residual (hi, lo)
+  static constexpr size_t off_nb2 = off_R2 + 6 * N3P * 8;   // float2 partner (hi, lo); then flux in .x
+  static constexpr size_t off_wmax = off_nb2 + 6 * NF * 8;
   static constexpr size_t off_E = off_wmax + NW * 6 * 4;
   static constexpr size_t off_bar = (off_E + 8 * 4 + 15) / 16 * 16;
   static constexpr size_t smem = off_bar + 16;
@@ -199,15 +198,18 @@ __constant__ const int kLineInit[3][4] = {{1, 1, 1, 1}, {0, 1, 0, 1}, {0, 0, 0, 
 
 template <int NX, int DIR>
 __device__ __forceinline__ int line_node(int a, int b, int l) {
-  constexpr int SZ = MCfg<NX>::SZ;
-  return DIR == 0 ? l + NX * a + SZ * b : (DIR == 1 ? a + NX * l + SZ * b : a + NX * b + SZ * l);
+  constexpr int RS = MCfg<NX>::RS, SZ = MCfg<NX>::SZ;
+  return DIR == 0 ? l + RS * a + SZ * b : (DIR == 1 ? a + RS * l + SZ * b : a + RS * b + SZ * l);
+}
+template <int NX>
+__device__ __forceinline__ int pnode(int v) {  // padded index of node v = i + NX*j + NX^2*k
+  return (v % NX) + MCfg<NX>::RS * ((v / NX) % NX) + MCfg<NX>::SZ * (v / (NX * NX));
 }
 
 // One direction of the contraction: tasks (component, line) accumulate the
 // signed derivative pair into the residual pair arrays.
 template <int NX, int DIR>
-__device__ __forceinline__ void line_phase(const float* s_uh, const float* s_ul, float* s_Rh,
-                                           float* s_Rl, const float* eg) {
+__device__ __forceinline__ void line_phase(const float2* s_u2, float2* s_R2, const float* eg) {
   using C = MCfg<NX>;
   const int tid = opaque_tid();
   const bool cubic = eg[10] != 0.0f;
@@ -221,8 +223,7 @@ __device__ __forceinline__ void line_phase(const float* s_uh, const float* s_ul,
       const int comp = kLineComp[DIR][slot], rt = kLineRes[DIR][slot];
       const float sg = kLineSign[DIR][slot];
       const bool init = kLineInit[DIR][slot] != 0;
-      const float* ph = s_uh + comp * C::N3P;
-      const float* pl = s_ul + comp * C::N3P;
+      const float2* pu = s_u2 + comp * C::N3P;
       // all NX outputs of the line at once: compile-time coefficient indices,
       // NX independent accumulator pairs
       float hi[NX], lo[NX];
@@ -233,8 +234,8 @@ __device__ __forceinline__ void line_phase(const float* s_uh, const float* s_ul,
       }
 #pragma unroll
       for (int l = 0; l < NX; ++l) {
-        const int pv = line_node<NX, DIR>(la, lb, l);
-        const float h = ph[pv], r = pl[pv];
+        const float2 hr = pu[line_node<NX, DIR>(la, lb, l)];
+        const float h = hr.x, r = hr.y;
 #pragma unroll
         for (int i = 0; i < NX; ++i) {
           hi[i] = fmaf(c_mixD[NX][0][i + NX * l], h, hi[i]);  // exact
@@ -243,8 +244,7 @@ __device__ __forceinline__ void line_phase(const float* s_uh, const float* s_ul,
           lo[i] = fmaf(c_mixD[NX][3][i + NX * l], h, lo[i]);
         }
       }
-      float* Rh0 = s_Rh + rt * C::N3P;
-      float* Rl0 = s_Rl + rt * C::N3P;
+      float2* R0 = s_R2 + rt * C::N3P;
 #pragma unroll
       for (int i = 0; i < NX; ++i) {
         float h = hi[i], r = lo[i];
@@ -258,15 +258,14 @@ __device__ __forceinline__ void line_phase(const float* s_uh, const float* s_ul,
         }
         h *= sg;
         r *= sg;
-        const int pv = line_node<NX, DIR>(la, lb, i);
+        float2* Rp = R0 + line_node<NX, DIR>(la, lb, i);
         if (init) {
-          Rh0[pv] = h;
-          Rl0[pv] = r;
+          *Rp = make_float2(h, r);
         } else {
+          const float2 old = *Rp;
           float sum, err;
-          two_sum(Rh0[pv], h, sum, err);
-          Rh0[pv] = sum;
-          Rl0[pv] = (Rl0[pv] + r) + err;
+          two_sum(old.x, h, sum, err);
+          *Rp = make_float2(sum, (old.y + r) + err);
         }
       }
     }
@@ -276,16 +275,13 @@ __device__ __forceinline__ void line_phase(const float* s_uh, const float* s_ul,
 template <int NX>
 __global__ void __launch_bounds__(MCfg<NX>::NT, 2) k_mixed_stage(const MixedDev a) {
   using C = MCfg<NX>;
-  constexpr int N2 = C::N2, N3 = C::N3, NT = C::NT, NF = C::NF, N3P = C::N3P, SZ = C::SZ;
+  constexpr int N2 = C::N2, N3 = C::N3, NT = C::NT, NF = C::NF, N3P = C::N3P;
   constexpr int NPT = C::NPT, FPT = C::FPT;
   extern __shared__ __align__(16) unsigned char smem[];
   double* s_u64 = reinterpret_cast<double*>(smem + C::off_u64);
-  float* s_uh = reinterpret_cast<float*>(smem + C::off_uh);
-  float* s_ul = reinterpret_cast<float*>(smem + C::off_ul);
-  float* s_Rh = reinterpret_cast<float*>(smem + C::off_Rh);
-  float* s_Rl = reinterpret_cast<float*>(smem + C::off_Rl);
-  float* s_nbh = reinterpret_cast<float*>(smem + C::off_nbh);  // partner hi; then the lifted flux
-  float* s_nbl = reinterpret_cast<float*>(smem + C::off_nbl);
+  float2* s_u2 = reinterpret_cast<float2*>(smem + C::off_u2);
+  float2* s_R2 = reinterpret_cast<float2*>(smem + C::off_R2);
+  float2* s_nb2 = reinterpret_cast<float2*>(smem + C::off_nb2);  // partner (hi, lo); then flux
   unsigned* s_wmax = reinterpret_cast<unsigned*>(smem + C::off_wmax);
   unsigned* s_E = reinterpret_cast<unsigned*>(smem + C::off_E);
   uint64_t* bar = reinterpret_cast<uint64_t*>(smem + C::off_bar);
@@ -385,13 +381,10 @@ __global__ void __launch_bounds__(MCfg<NX>::NT, 2) k_mixed_stage(const MixedDev 
         for (int q = 0; q < NPT; ++q) {
           const int v = tid + q * NT;
           if (v < N3) {
-            const int i = v % NX, j = (v / NX) % NX, k = v / N2;
-            const int pv = i + NX * j + SZ * k;
             const double u = s_u64[c * N3 + v];
             const float uf = d2f_hi(u), ulo = d2f_lo(u);
             const float uh = (__fadd_rn(__fmaf_rn(uf, qi, M), -M)) * qv;
-            s_uh[c * N3P + pv] = uh;
-            s_ul[c * N3P + pv] = __fadd_rn(__fsub_rn(uf, uh), ulo);
+            s_u2[c * N3P + pnode<NX>(v)] = make_float2(uh, __fadd_rn(__fsub_rn(uf, uh), ulo));
           }
         }
       }
@@ -400,20 +393,18 @@ __global__ void __launch_bounds__(MCfg<NX>::NT, 2) k_mixed_stage(const MixedDev 
         const int t = tid + q * NT;
         if (t < NF && nbr[t / N2] >= 0) {
 #pragma unroll
-          for (int c = 0; c < 6; ++c) {
-            s_nbh[c * NF + t] = d2f_hi(nbv[q][c]);
-            s_nbl[c * NF + t] = d2f_lo(nbv[q][c]);
-          }
+          for (int c = 0; c < 6; ++c)
+            s_nb2[c * NF + t] = make_float2(d2f_hi(nbv[q][c]), d2f_lo(nbv[q][c]));
         }
       }
     }
     __syncthreads();
     // ---- contractions: r, s, t lines ----------------------------------------
-    line_phase<NX, 0>(s_uh, s_ul, s_Rh, s_Rl, eg);
+    line_phase<NX, 0>(s_u2, s_R2, eg);
     __syncthreads();
-    line_phase<NX, 1>(s_uh, s_ul, s_Rh, s_Rl, eg);
+    line_phase<NX, 1>(s_u2, s_R2, eg);
     __syncthreads();
-    line_phase<NX, 2>(s_uh, s_ul, s_Rh, s_Rl, eg);
+    line_phase<NX, 2>(s_u2, s_R2, eg);
     // ---- upwind flux per face node (same interval: reads uh/ul, writes nbh) -
     tid = opaque_tid();
 #pragma unroll
@@ -422,20 +413,19 @@ __global__ void __launch_bounds__(MCfg<NX>::NT, 2) k_mixed_stage(const MixedDev 
       if (t < NF) {
         const int f = t / N2, ab = t - f * N2;
         const int fa = ab % NX, fb = ab / NX;
-        const int v = face_vol<NX>(f, fa, fb);
-        const int pv = (v % NX) + NX * ((v / NX) % NX) + SZ * (v / N2);
+        const int pv = pnode<NX>(face_vol<NX>(f, fa, fb));
         const int pe = nbr[f];
         float dH[3], dE[3];
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
-          const float hh = s_uh[c * N3P + pv], hl = s_ul[c * N3P + pv];
-          const float eh = s_uh[(c + 3) * N3P + pv], el = s_ul[(c + 3) * N3P + pv];
+          const float2 h = s_u2[c * N3P + pv], ev = s_u2[(c + 3) * N3P + pv];
           if (pe >= 0) {  // jump = (partner_hi - own_hi) + (partner_lo - own_lo)
-            dH[c] = (s_nbh[c * NF + t] - hh) + (s_nbl[c * NF + t] - hl);
-            dE[c] = (s_nbh[(c + 3) * NF + t] - eh) + (s_nbl[(c + 3) * NF + t] - el);
+            const float2 ph = s_nb2[c * NF + t], pE = s_nb2[(c + 3) * NF + t];
+            dH[c] = (ph.x - h.x) + (ph.y - h.y);
+            dE[c] = (pE.x - ev.x) + (pE.y - ev.y);
           } else {  // PEC mirror: H+ = H-, E+ = -E-
             dH[c] = 0.0f;
-            dE[c] = -2.0f * (eh + el);
+            dE[c] = -2.0f * (ev.x + ev.y);
           }
         }
         float Y02 = -0.5f, C02Y = 0.5f * a.C0f, Z02 = 0.5f, C02Z = 0.5f * a.C0f;
@@ -475,8 +465,8 @@ __global__ void __launch_bounds__(MCfg<NX>::NT, 2) k_mixed_stage(const MixedDev 
         }
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
-          s_nbh[c * NF + t] = lf * fH[c];
-          s_nbh[(c + 3) * NF + t] = lf * fE[c];
+          s_nb2[c * NF + t].x = lf * fH[c];
+          s_nb2[(c + 3) * NF + t].x = lf * fE[c];
         }
       }
     }
@@ -506,16 +496,17 @@ __global__ void __launch_bounds__(MCfg<NX>::NT, 2) k_mixed_stage(const MixedDev 
       const int v = tid + q * NT;
       if (v >= N3) continue;
       const int i = v % NX, j = (v / NX) % NX, k = v / N2;
-      const int pv = i + NX * j + SZ * k;
+      const int pv = pnode<NX>(v);
       float Rh[6], Rl[6];
 #pragma unroll
       for (int c = 0; c < 6; ++c) {
-        Rh[c] = s_Rh[c * N3P + pv];
-        Rl[c] = s_Rl[c * N3P + pv];
+        const float2 rr = s_R2[c * N3P + pv];
+        Rh[c] = rr.x;
+        Rl[c] = rr.y;
       }
       auto add = [&](int f, int ab) {
 #pragma unroll
-        for (int c = 0; c < 6; ++c) Rl[c] += s_nbh[c * NF + f * N2 + ab];
+        for (int c = 0; c < 6; ++c) Rl[c] += s_nb2[c * NF + f * N2 + ab].x;
       };
       if (j == 0) add(0, i + NX * k);
       if (i == NX - 1) add(1, j + NX * k);
