@@ -38,6 +38,7 @@ extern "C" {
 #define NEKGPU_ERR_BLOWUP -6      /* non-finite or |u| > 1e20 (chk_blowup) */
 #define NEKGPU_ERR_TIMEOUT -7     /* a bounded device wait ran out */
 #define NEKGPU_ERR_UNSUPPORTED -8 /* feature not built for this case */
+#define NEKGPU_ERR_TOO_LARGE -9   /* mesh larger than a fixed-size scratch allows */
 
 /* Compute forms. */
 #define NEKGPU_PLAIN 0   /* unfused all-FP64 kernels, one per reference routine */
@@ -197,6 +198,18 @@ int nekgpu_get_work(nekgpu_ctx* ctx, const char* name, double* out);
  * exact fields: l2[q] = sqrt(sum e*bm1*e / vol), linf[q] = max|e|, FP64. */
 int nekgpu_norms(nekgpu_ctx* ctx, const double* exact_h, const double* exact_e, long ld,
                  double l2[6], double linf[6]);
+/* No counterpart in the reference.  The same norms as nekgpu_norms for
+ * callers that cannot allocate device memory while time stepping (a driver
+ * that gave all free device memory to its own pool, or a loop that must not
+ * risk an allocation failure or cudaFree's synchronisation between steps).
+ * exact_dev: device array, 6*npts doubles, H then E, component after
+ * component.  Allocates nothing: the reduction's partial sums live in a fixed
+ * device array of the library (384 KB, held by every GPU that loads it until
+ * exit), so at most 8,388,608 nodes (else NEKGPU_ERR_TOO_LARGE).  Calls whose
+ * GPU work can overlap share that array and race.  The first call on a device
+ * looks the array up (cudaGetSymbolAddress); make it before any stream
+ * capture. */
+int nekgpu_norms_noalloc(nekgpu_ctx* ctx, const double* exact_dev, double l2[6], double linf[6]);
 /* field energy 0.5*sum bm1*(eps|E|^2 + mu|H|^2), FP64 on device */
 int nekgpu_energy(nekgpu_ctx* ctx, double* energy);
 /* chk_blowup (src/cem_common.F:1150-1165): NEKGPU_ERR_BLOWUP if any state

@@ -15,7 +15,7 @@ OK = 0
 ERR = {
     -1: "NEKGPU_ERR_ARG", -2: "NEKGPU_ERR_MESH", -3: "NEKGPU_ERR_CUDA", -4: "NEKGPU_ERR_NOMEM",
     -5: "NEKGPU_ERR_STATE", -6: "NEKGPU_ERR_BLOWUP", -7: "NEKGPU_ERR_TIMEOUT",
-    -8: "NEKGPU_ERR_UNSUPPORTED",
+    -8: "NEKGPU_ERR_UNSUPPORTED", -9: "NEKGPU_ERR_TOO_LARGE",
 }
 PLAIN, FUSED64, MIXED, MIXED_NAIVE = 0, 1, 2, 3
 FORMS = {"plain": PLAIN, "fused64": FUSED64, "mixed": MIXED, "mixed_naive": MIXED_NAIVE}
@@ -87,6 +87,7 @@ SIGNATURES = [
     ("nekgpu_gs_op_fields", C.c_int, [C.c_void_p, dp, C.c_int]),
     ("nekgpu_get_work", C.c_int, [C.c_void_p, C.c_char_p, dp]),
     ("nekgpu_norms", C.c_int, [C.c_void_p, dp, dp, C.c_long, dp, dp]),
+    ("nekgpu_norms_noalloc", C.c_int, [C.c_void_p, C.c_void_p, dp, dp]),
     ("nekgpu_energy", C.c_int, [C.c_void_p, dp]),
     ("nekgpu_check_blowup", C.c_int, [C.c_void_p]),
     ("nekgpu_time_steps", C.c_int, [C.c_void_p, C.c_int, dp, C.c_double, dp]),

@@ -26,6 +26,7 @@ SOURCES = {
     "nekgpu_fused.cu": [],
     "nekgpu_mixed.cu": [],
     "nekgpu_util.cu": [],
+    "nekgpu_noalloc.cu": [],
 }
 
 

@@ -901,6 +901,8 @@ const char* nekgpu_error_string(int status) {
     case NEKGPU_ERR_BLOWUP: return "state blew up (non-finite or |u| > 1e20)";
     case NEKGPU_ERR_TIMEOUT: return "a bounded device wait ran out";
     case NEKGPU_ERR_UNSUPPORTED: return "not supported for this case";
+    case NEKGPU_ERR_TOO_LARGE:
+      return "mesh larger than the fixed scratch of the no-allocation entry point (8,388,608 nodes)";
     default: return "unknown status";
   }
 }
@@ -1307,6 +1309,11 @@ int nekgpu_norms(nekgpu_ctx* c, const double* exact_h, const double* exact_e, lo
   cudaFreeAsync(d, c->stream);
   cudaStreamSynchronize(c->stream);
   return st;
+}
+
+int nekgpu_norms_noalloc(nekgpu_ctx* c, const double* exact_dev, double l2[6], double linf[6]) {
+  if (!c || !exact_dev || !l2 || !linf) return NEKGPU_ERR_ARG;
+  return norms_noalloc(c, exact_dev, l2, linf);
 }
 
 int nekgpu_energy(nekgpu_ctx* c, double* energy) {

@@ -191,6 +191,9 @@ int mixed_stage(Context* c, int rkstep, double time, double dt);
 // D - Dh = Dm + Dl to ~2^-55; uploaded once per nx
 int mixed_upload_D(int nx, const float* Dh, const float* Df, const float* Dm, const float* Dl);
 
+// nekgpu_noalloc.cu: cem_error norms with a fixed device scratch array
+int norms_noalloc(Context* c, const double* exact_dev, double l2[6], double linf[6]);
+
 // reductions / utilities (nekgpu_util.cu)
 int util_norms(Context* c, const double* d_exact, double l2[6], double linf[6]);
 int util_energy(Context* c, double* energy);

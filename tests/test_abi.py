@@ -38,7 +38,7 @@ def test_binding_covers_header():
 
 def test_error_strings():
     lib = L.load()
-    for code in range(0, -9, -1):
+    for code in range(0, -10, -1):
         s = lib.nekgpu_error_string(code).decode()
         assert s and s != "unknown status"
     assert lib.nekgpu_error_string(-99).decode() == "unknown status"
