@@ -216,6 +216,20 @@ int nekgpu_energy(nekgpu_ctx* ctx, double* energy);
  * value is non-finite or above 1e20 in magnitude */
 int nekgpu_check_blowup(nekgpu_ctx* ctx);
 
+/* ---- discrete adjoint (NEKGPU_FUSED64) --------------------------------------- */
+/* No routine of the reference computes gradients; this is the discrete
+ * adjoint of nsteps RK45 steps of the FP64 fused stage (cem_maxwell_op_rk,
+ * src/cem_maxwell.F:327-345) for J = sum_n jw[n] |E(n)|^2 at the final time.
+ * Starts from the context's current state and leaves it at the final state.
+ * The state is checkpointed every `stride` steps (0: ceil(sqrt(nsteps))); the
+ * reverse sweep recomputes one segment at a time and keeps its stage states
+ * and RK registers.  Returns J, dJ/deps at every node (npts, host array) and
+ * the device times of the forward pass and of the reverse sweep (recompute
+ * included), in ms.  jw: npts host weights (e.g. bm1 on a probe region). */
+int nekgpu_adjoint_gradient(nekgpu_ctx* ctx, int nsteps, double t0, double dt, const double* jw,
+                            double* J, double* dJdeps, int stride, double* fwd_ms,
+                            double* adj_ms);
+
 /* ---- timing ---------------------------------------------------------------- */
 /* Runs nsteps steps between CUDA events on the context stream and returns the
  * elapsed device milliseconds (state advances; *time += nsteps*dt). */

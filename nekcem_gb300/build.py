@@ -27,6 +27,8 @@ SOURCES = {
     "nekgpu_mixed.cu": [],
     "nekgpu_util.cu": [],
     "nekgpu_noalloc.cu": [],
+    "nekgpu_adjoint.cu": [],
+    "nekgpu_adjoint_host.cpp": ["-Xcompiler", "-ffp-contract=off"],
 }
 
 

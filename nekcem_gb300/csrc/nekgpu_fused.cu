@@ -415,7 +415,7 @@ __global__ void __launch_bounds__(Cfg<NX, T>::NT, Cfg<NX, T>::kMinBlocks)
       const long g = (long)e * N3 + tid;
 #pragma unroll
       for (int c = 0; c < 6; ++c) {
-        a.k[c * P + g] = kn[c];
+        a.k_out[c * P + g] = kn[c];
         a.u_out[c * P + g] = un[c];
       }
     }
@@ -480,6 +480,27 @@ int scale_coef(Context* c, double dt) {
   return check_cuda(cudaGetLastError());
 }
 
+int fused_stage_buffers(Context* c, int rkstep, double time, double dt, const double* u_in,
+                        double* u_out, double* k_in, double* k_out) {
+  int st = scale_coef(c, dt);
+  if (st) return st;
+  FusedDev a = c->fargs;
+  a.u_in = u_in;
+  a.u_out = u_out;
+  a.k = k_in;
+  a.k_out = k_out;
+  a.a = c->rk_a[rkstep - 1];
+  a.b = c->rk_b[rkstep - 1];
+  if (c->src.enabled) {
+    const double rktime = time + dt * c->rk_c[rkstep - 1];
+    const double pi = 4.0 * atan(1.0);
+    const double x = pi * c->src.f0 * (rktime - c->src.t0);
+    a.src_ft = c->src.amp * (1.0 - 2.0 * x * x) * exp(-x * x);
+    a.src_ftf = (float)a.src_ft;
+  }
+  return c->form == NEKGPU_MIXED_NAIVE ? dispatch<float>(c, a) : dispatch<double>(c, a);
+}
+
 int fused_setup(Context* c) {
   if (c->nx < 3 || c->nx > 9) return NEKGPU_ERR_UNSUPPORTED;
   return NEKGPU_OK;
@@ -491,6 +512,7 @@ int fused_stage(Context* c, int rkstep, double time, double dt) {
   FusedDev a = c->fargs;
   a.u_in = c->d_u[c->cur];
   a.u_out = c->d_u[c->cur ^ 1];
+  a.k_out = a.k;
   a.a = c->rk_a[rkstep - 1];
   a.b = c->rk_b[rkstep - 1];
   if (c->src.enabled) {

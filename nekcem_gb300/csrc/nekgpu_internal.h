@@ -76,7 +76,8 @@ struct FusedDev {
   long npts;
   const double* u_in;
   double* u_out;
-  double* k;
+  double* k;            // RK register read
+  double* k_out;        // RK register written (== k unless stage data is being kept)
   const double* coef;   // 2*npts: dt*hbm1 then dt*ebm1
   const int* nbr;       // 6*nelt
   const double* egeom;  // 9*nelt
@@ -116,6 +117,29 @@ struct MixedDev {
   int* status;
 };
 
+// Reverse of one FP64 stage (nekgpu_adjoint.cu)
+struct AdjointDev {
+  int nelt;
+  long npts;
+  const double* ub_in;   // adjoint of u_i
+  double* ub_out;        // adjoint of u_{i-1}
+  const double* w_in;    // dt M^-1 (adjoint of k_i + b_i ub_i): the stage-i weights
+  double* w_out;         // the same for stage i-1
+  const double* u_prev;  // forward u_{i-1}
+  const double* k_cur;   // forward k_i
+  const double* k_prev;  // forward k_{i-1} (unused when a == 0)
+  const double* coef;    // dt hbm1 (npts), dt ebm1 (npts)
+  const double* bm1;
+  double* deps;          // accumulated dJ/deps per node
+  const int* nbr;
+  const double* egeom;
+  const double* slot;    // [16][nxzfl] static face-slot coefficients
+  double a, b_next, inv_dt;
+  double Dw[kMaxNx * kMaxNx];  // D(m,i) w_m at [m + NX*i]
+  double w[kMaxNx];
+};
+
+
 struct Context {
   int form = NEKGPU_MIXED;
   int device = 0;
@@ -152,6 +176,8 @@ struct Context {
   FusedDev fargs{};
   MixedDev margs{};
   float* d_egm = nullptr;
+  // adjoint face-slot coefficients (built on first use, FP64 fused form)
+  double* d_adj_slot = nullptr;
 
   // plain form
   PlainDev pargs{};
@@ -182,6 +208,9 @@ int plain_gs(Context* c, double* d_u, int nfld);
 // kernel launchers (nekgpu_fused.cu)
 int fused_setup(Context* c);  // grid size / smem attributes
 int fused_stage(Context* c, int rkstep, double time, double dt);
+// one stage with explicit state / RK-register buffers (no ping-pong bookkeeping)
+int fused_stage_buffers(Context* c, int rkstep, double time, double dt, const double* u_in,
+                        double* u_out, double* k_in, double* k_out);
 int scale_coef(Context* c, double dt);
 
 // nekgpu_mixed.cu
@@ -190,6 +219,11 @@ int mixed_stage(Context* c, int rkstep, double time, double dt);
 // (exact products with the 10-bit uh), Df = D rounded, and the remainder
 // D - Dh = Dm + Dl to ~2^-55; uploaded once per nx
 int mixed_upload_D(int nx, const float* Dh, const float* Df, const float* Dm, const float* Dl);
+
+// nekgpu_adjoint.cu
+int adjoint_stage(Context* c, const AdjointDev& a);
+// w = b * coef * ub (the stage weights of the last stage of the last step)
+int adjoint_seed(Context* c, double* w, const double* ub, double b);
 
 // nekgpu_noalloc.cu: cem_error norms with a fixed device scratch array
 int norms_noalloc(Context* c, const double* exact_dev, double l2[6], double linf[6]);

@@ -229,3 +229,17 @@ class MaxwellGPU:
 
     def check_blowup(self):
         L.check(L.load().nekgpu_check_blowup(self._h), "nekgpu_check_blowup")
+
+    # ---- discrete adjoint (FP64 fused form) ------------------------------------
+    def adjoint_gradient(self, nsteps: int, t0: float, dt: float, jw: np.ndarray, stride: int = 0):
+        """J = sum_g jw[g] |E(g)|^2 after nsteps steps from the current state and
+        dJ/deps at every node, by the discrete adjoint with checkpoints every
+        ``stride`` steps (0: ceil(sqrt(nsteps))).  Leaves the final state in the
+        context.  Returns (J, dJdeps, forward_ms, adjoint_ms)."""
+        jw = np.ascontiguousarray(jw, dtype=np.float64).reshape(self.npts)
+        out = np.empty(self.npts)
+        J = C.c_double(); fms = C.c_double(); ams = C.c_double()
+        L.check(L.load().nekgpu_adjoint_gradient(self._h, int(nsteps), float(t0), float(dt), _dp(jw),
+                                                 C.byref(J), _dp(out), int(stride), C.byref(fms),
+                                                 C.byref(ams)), "nekgpu_adjoint_gradient")
+        return J.value, out, fms.value, ams.value

@@ -1,0 +1,173 @@
+"""Discrete adjoint dJ/deps of J = sum jw |E(T)|^2 (jw = bm1 on a probe box).
+
+CPU: the torch tape restatement (tests/tape_maxwell.py) matches the oracle's
+time steps, and its tape gradient matches central differences of the oracle.
+GPU: nekgpu_adjoint_gradient matches central differences of the library's
+own FP64 forward (h = 1e-6, 20 seeded directions, 1e-6 relative), the tape
+gradient node by node, and does not depend on the checkpoint stride.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+from helpers import make_ref  # noqa: E402
+from nekcem_gb300 import MaxwellGPU, cases  # noqa: E402
+from nekcem_gb300 import _lib as L  # noqa: E402
+from tape_maxwell import TapeMaxwell  # noqa: E402
+
+PEC, PER = 0, 1
+SOURCE = dict(xc=(0.3, 0.3, 0.3), sigma=0.1, amp=1.0, f0=2.0, t0=0.3)
+
+
+def problem_data(N, nel, bc, seed):
+    """Mesh on [0,1]^3, seeded random eps (smooth field + node noise), a
+    Gaussian E_z pulse plus the Gaussian/Ricker source, probe (0.5,1)^3."""
+    ref = make_ref(N, nel, (0, 0, 0), (1, 1, 1), bc)
+    x, y, z = (a.copy() for a in ref.coords())
+    rng = np.random.default_rng(seed)
+    eps = cases.eps_random(x, y, z, seed=seed, length=0.3) + 0.2 * rng.random(ref.npts)
+    ref.set_materials(eps, np.ones(ref.npts))
+    H0, E0 = cases.gaussian_pulse_ez((0.55, 0.5, 0.45), 0.15)(x, y, z)
+    bm1 = ref.d("bm1").copy()
+    inside = (x > 0.5) & (y > 0.5) & (z > 0.5)
+    jw = np.where(inside, bm1, 0.0)
+    dt = 0.5 * cases.CFL * cases.min_gll_spacing(x, y, z, ref.n, ref.nelt)
+    return ref, eps, H0, E0, jw, dt, (x, y, z)
+
+
+def oracle_J(ref, eps, H0, E0, jw, nsteps, dt):
+    ref.set_materials(eps, np.ones(ref.npts))
+    ref.set_source(**SOURCE)
+    ref.set_state(H0, E0)
+    ref.run(nsteps, 0.0, dt)
+    return float(np.sum(jw * ref.en ** 2))
+
+
+def tape_J(tm, eps_t, H0, E0, jw, nsteps, dt):
+    H, E = tm.run(torch.tensor(H0), torch.tensor(E0), eps_t, nsteps, 0.0, dt)
+    return torch.sum(torch.tensor(jw) * E * E)
+
+
+def make_tape(ref, xyz):
+    tm = TapeMaxwell(ref)
+    tm.set_source(*xyz, **SOURCE)
+    return tm
+
+
+# ---- CPU: the tape restatement against the oracle ------------------------------
+def test_tape_forward_matches_oracle():
+    ref, eps, H0, E0, jw, dt, xyz = problem_data(3, (2, 2, 2), (PEC, PER, PEC), seed=11)
+    nsteps = 6
+    tm = make_tape(ref, xyz)
+    H, E = tm.run(torch.tensor(H0), torch.tensor(E0), torch.tensor(eps), nsteps, 0.0, dt)
+    ref.set_source(**SOURCE)
+    ref.set_state(H0, E0)
+    ref.run(nsteps, 0.0, dt)
+    scale = max(np.abs(ref.hn).max(), np.abs(ref.en).max())
+    assert np.abs(H.numpy() - ref.hn).max() <= 1e-12 * scale
+    assert np.abs(E.numpy() - ref.en).max() <= 1e-12 * scale
+
+
+def test_tape_gradient_matches_oracle_central_differences():
+    ref, eps, H0, E0, jw, dt, xyz = problem_data(3, (2, 2, 2), (PEC, PEC, PER), seed=12)
+    nsteps = 6
+    tm = make_tape(ref, xyz)
+    eps_t = torch.tensor(eps, requires_grad=True)
+    tape_J(tm, eps_t, H0, E0, jw, nsteps, dt).backward()
+    grad = eps_t.grad.numpy()
+    rng = np.random.default_rng(5)
+    h = 1e-6
+    for _ in range(4):
+        d = rng.standard_normal(ref.npts)
+        fd = (oracle_J(ref, eps + h * d, H0, E0, jw, nsteps, dt)
+              - oracle_J(ref, eps - h * d, H0, E0, jw, nsteps, dt)) / (2 * h)
+        ad = float(grad @ d)
+        assert abs(fd - ad) <= 1e-6 * abs(ad), (fd, ad)
+
+
+# ---- GPU: the library's adjoint ------------------------------------------------------
+def gpu_problem(N, nel, bc, seed, nsteps, stride=0):
+    from adjoint_autograd import BoxProblem
+    ref, eps, H0, E0, jw, dt, xyz = problem_data(N, nel, bc, seed)
+    pb = BoxProblem(N, nel, (0, 0, 0), (1, 1, 1), bc, H0, E0, jw, nsteps, dt, source=SOURCE,
+                    stride=stride)
+    return pb, eps, ref, xyz
+
+
+MESHES = [
+    pytest.param(3, (2, 2, 2), (PEC, PEC, PEC), 30, id="N3-pec"),
+    pytest.param(4, (3, 2, 2), (PER, PEC, PER), 30, id="N4-mixed-bc"),
+    pytest.param(7, (2, 2, 2), (PEC, PER, PEC), 20, id="N7"),
+    pytest.param(6, (2, 2, 3), (PER, PER, PER), 20, id="N6-periodic"),
+]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("N,nel,bc,nsteps", MESHES)
+def test_adjoint_matches_central_differences(N, nel, bc, nsteps):
+    pb, eps, _, _ = gpu_problem(N, nel, bc, seed=21 + N, nsteps=nsteps)
+    J, grad = pb.gradient(eps)
+    assert J == pytest.approx(pb.objective(eps), rel=1e-14)
+    rng = np.random.default_rng(100 + N)
+    h = 1e-6
+    worst = 0.0
+    for _ in range(20):
+        d = rng.standard_normal(eps.size)
+        fd = (pb.objective(eps + h * d) - pb.objective(eps - h * d)) / (2 * h)
+        ad = float(grad @ d)
+        worst = max(worst, abs(fd - ad) / abs(ad))
+    assert worst <= 1e-6, worst
+
+
+@pytest.mark.gpu
+def test_adjoint_matches_tape_node_by_node():
+    N, nel, bc, nsteps = 3, (2, 2, 2), (PEC, PER, PEC), 12
+    pb, eps, ref, xyz = gpu_problem(N, nel, bc, seed=31, nsteps=nsteps)
+    J, grad = pb.gradient(eps)
+    tm = make_tape(ref, xyz)
+    eps_t = torch.tensor(eps, requires_grad=True)
+    Jt = tape_J(tm, eps_t, pb.H0, pb.E0, pb.jw, nsteps, pb.dt)
+    Jt.backward()
+    assert J == pytest.approx(Jt.item(), rel=1e-12)
+    gt = eps_t.grad.numpy()
+    assert np.abs(grad - gt).max() <= 1e-9 * np.abs(gt).max()
+
+
+@pytest.mark.gpu
+def test_adjoint_gradient_does_not_depend_on_the_checkpoint_stride():
+    pb, eps, _, _ = gpu_problem(4, (2, 2, 2), (PEC, PEC, PEC), seed=41, nsteps=17)
+    grads = []
+    for stride in (1, 4, 17, 0):
+        pb.stride = stride
+        grads.append(pb.gradient(eps)[1])
+    for g in grads[1:]:
+        np.testing.assert_array_equal(g, grads[0])
+
+
+@pytest.mark.gpu
+def test_autograd_function_backward_is_the_adjoint():
+    from adjoint_autograd import FieldEnergy
+    pb, eps, _, _ = gpu_problem(3, (2, 2, 2), (PEC, PEC, PEC), seed=51, nsteps=10)
+    eps_t = torch.tensor(eps, requires_grad=True)
+    J = FieldEnergy.apply(eps_t, pb)
+    (2.0 * J).backward()
+    _, grad = pb.gradient(eps)
+    np.testing.assert_array_equal(eps_t.grad.numpy(), 2.0 * grad)
+
+
+@pytest.mark.gpu
+def test_adjoint_rejects_other_forms_and_missing_state():
+    g = MaxwellGPU.from_box(3, (2, 2, 2), (0, 0, 0), (1, 1, 1), (PEC,) * 3, form="mixed")
+    g.set_state(np.zeros((3, g.npts)), np.zeros((3, g.npts)))
+    with pytest.raises(L.NekgpuError) as e:
+        g.adjoint_gradient(2, 0.0, 0.01, np.ones(g.npts))
+    assert e.value.status == -8
+    g.close()
+    g = MaxwellGPU.from_box(3, (2, 2, 2), (0, 0, 0), (1, 1, 1), (PEC,) * 3, form="fused64")
+    with pytest.raises(L.NekgpuError) as e:
+        g.adjoint_gradient(2, 0.0, 0.01, np.ones(g.npts))
+    assert e.value.status == -5
+    g.close()
