@@ -43,6 +43,7 @@ def parse():
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--no-accuracy", action="store_true", help="skip the full-length L2 runs")
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline sample")
+    p.add_argument("--no-adjoint", action="store_true", help="skip the adjoint/forward ratio run")
     return p.parse_args()
 
 
@@ -215,6 +216,41 @@ def e2e(steps, warmup, dist=None):
     return dict(sec=sec, npts=npts, h2d=bytes_io, d2h=bytes_io)
 
 
+def adjoint_ratio():
+    """Gradient time over forward time on the adjoint workload: unit PEC box,
+    8^3 elements, N=7, eps = 1 + 3 sigmoid(smooth random field, seed 4),
+    Gaussian E_z source, 2000 steps, J = sum bm1 |E|^2 over [0.7,0.9]^3.
+    Forward: nekgpu_time_steps of the FP64 fused form (CUDA events); gradient:
+    nekgpu_adjoint_gradient = forward pass with checkpoints + reverse sweep
+    (segment recompute included), its own CUDA-event times."""
+    from nekcem_gb300 import MaxwellGPU, cases
+    c = cases.make("adjoint")
+    g0 = MaxwellGPU.from_box(c.N, c.nel, c.lo, c.hi, c.bc, form="fused64")
+    x, y, z = g0.coords()
+    bm1 = g0.array("bmn")
+    g0.close()
+    g = MaxwellGPU.from_box(c.N, c.nel, c.lo, c.hi, c.bc, form="fused64",
+                            permittivity=c.eps(x, y, z))
+    g.set_source(**c.source)
+    H0, E0 = c.init_fields(x, y, z)
+    (p0, p1), (q0, q1), (r0, r1) = c.extra["probe"]
+    inside = (x > p0) & (x < p1) & (y > q0) & (y < q1) & (z > r0) & (z < r1)
+    jw = np.where(inside, bm1, 0.0)
+    dt = c.timestep(x, y, z)
+    g.set_state(H0, E0)
+    g.time_steps(3, 0.0, dt)  # warm-up
+    g.set_state(H0, E0)
+    _, fwd_ms = g.time_steps(c.nsteps, 0.0, dt)
+    g.set_state(H0, E0)
+    J, dJ, fwd_ckpt_ms, rev_ms = g.adjoint_gradient(c.nsteps, 0.0, dt, jw)
+    g.close()
+    return {"workload": "adjoint box 8^3 el N=7 PEC, random eps, E_z source, 2000 steps",
+            "steps": c.nsteps, "forward_ms": fwd_ms, "gradient_ms": fwd_ckpt_ms + rev_ms,
+            "forward_with_checkpoints_ms": fwd_ckpt_ms, "reverse_sweep_ms": rev_ms,
+            "ratio": (fwd_ckpt_ms + rev_ms) / fwd_ms, "J": J,
+            "grad_norm": float(np.linalg.norm(dJ))}
+
+
 def cpu_sample(steps):
     """The CPU oracle (FP64 restatement of the reference's routines, all host
     threads) on the same mesh, `steps` RK steps."""
@@ -312,7 +348,7 @@ def main():
                 "d2h_bytes_per_step": e["d2h"], "path": "nekgpu_op_rk_host, pinned host fields"},
         "gpu_launches": mixed["launches"],
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": ncu_traffic("k_fused_stage<8,float>"),
+                     "frac": achieved / peak, "traffic": ncu_traffic("k_mixed_stage<8>"),
                      "peak_kind": peak_kind,
                      "algorithmic_bytes_per_launch": BYTES_PER_NODE_STAGE * npts},
         "clocks": clocks,
@@ -329,6 +365,8 @@ def main():
         l2m, n = accuracy("mixed")
         l2d, _ = accuracy("fused64")
         out["l2_vs_analytic"] = {"steps": n, "mixed": l2m, "fused64": l2d, "ratio": l2m / l2d}
+    if not args.no_adjoint and world == 1:
+        out["adjoint"] = adjoint_ratio()
     if not args.no_cpu and world == 1:
         cpu = cpu_sample(max(2, min(20, args.steps // 10)))
         out["cpu_baseline"] = {"value": cpu["value"], "unit": UNIT, "cores": cpu["threads"],

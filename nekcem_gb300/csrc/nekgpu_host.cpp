@@ -678,7 +678,14 @@ int upload_plain(Context* c, const PlainHost& p) {
 // D for the exact-hi contractions of the mixed form: per row i, Dh on the
 // 10-bit grid of that row's largest |D(i,l)|, Df = D rounded to FP32, and
 // the remainder D - Dh split into two FP32 pieces Dm + Dl (exact to ~2^-55)
-void split_D(const std::vector<double>& D, int n, float* Dh, float* Df, float* Dm, float* Dl) {
+// D in the FP32 pieces of the mixed form's exact-hi contraction, as float
+// pairs [0][i + n*l] = (Dh, Df), [1][i + n*l] = (Dm, Dl) of D(i,l): Dh on a
+// 10-bit grid of row i (so every product Dh*uh with uh on a 10-bit grid has
+// at most 21 bits and the sum over <= 16 terms stays exact in FP32),
+// Df = RN32(D), Dm = RN32(D - Dh), Dl = RN32(D - Dh - Dm).
+void split_D(const std::vector<double>& D, int n, std::vector<float>& tab) {
+  const int M2 = kMaxMixed * kMaxMixed;
+  tab.assign(4 * (size_t)M2, 0.0f);
   for (int i = 0; i < n; ++i) {
     double rmax = 0;
     for (int l = 0; l < n; ++l) rmax = std::max(rmax, std::fabs(D[i + (size_t)n * l]));
@@ -688,11 +695,12 @@ void split_D(const std::vector<double>& D, int n, float* Dh, float* Df, float* D
     for (int l = 0; l < n; ++l) {
       const size_t k = i + (size_t)n * l;
       const double h = std::nearbyint(D[k] / qd) * qd;  // at most 11 significant bits
-      Dh[k] = (float)h;
-      Df[k] = (float)D[k];
       const double r = D[k] - h;
-      Dm[k] = (float)r;
-      Dl[k] = (float)(r - (double)Dm[k]);
+      const float m = (float)r;
+      tab[2 * k] = (float)h;
+      tab[2 * k + 1] = (float)D[k];
+      tab[2 * (M2 + k)] = m;
+      tab[2 * (M2 + k) + 1] = (float)(r - (double)m);
     }
   }
 }
@@ -773,9 +781,9 @@ int upload_fused(Context* c, const Compact& cp) {
       diff = std::max(diff, std::fabs(D[k] - cp.D[k]));
     }
     if (diff > 1e-12 * dmax) return NEKGPU_ERR_MESH;
-    std::vector<float> Dh(D.size()), Df(D.size()), Dm(D.size()), Dl(D.size());
-    split_D(D, c->nx, Dh.data(), Df.data(), Dm.data(), Dl.data());
-    if ((st = mixed_upload_D(c->nx, Dh.data(), Df.data(), Dm.data(), Dl.data()))) return st;
+    std::vector<float> tab;
+    split_D(D, c->nx, tab);
+    if ((st = mixed_upload_D(c->nx, tab.data(), tab.size()))) return st;
     return NEKGPU_OK;
   }
   if ((st = A.put(&c->d_egeom, cp.egeom))) return st;

@@ -218,7 +218,7 @@ int mixed_stage(Context* c, int rkstep, double time, double dt);
 // D(i,j) at [i + nx*j] in four FP32 pieces: Dh on a 10-bit grid per row
 // (exact products with the 10-bit uh), Df = D rounded, and the remainder
 // D - Dh = Dm + Dl to ~2^-55; uploaded once per nx
-int mixed_upload_D(int nx, const float* Dh, const float* Df, const float* Dm, const float* Dl);
+int mixed_upload_D(int nx, const float* tab, size_t count);  // even-odd D pieces
 
 // nekgpu_adjoint.cu
 int adjoint_stage(Context* c, const AdjointDev& a);

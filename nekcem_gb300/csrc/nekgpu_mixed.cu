@@ -19,7 +19,9 @@
 //    sum(D*ul + (Dm + Dl)*uh) is summed in FP32 beside it.  The FP32 rounding
 //    error is ~2^-34 of sum|D||u| instead of ~2^-24.
 //  * Thread per line.  Each thread contracts one GLL line at a time, so every
-//    D coefficient is a compile-time constant-bank operand of the FFMA.
+//    D coefficient is a compile-time constant-bank operand.  The four
+//    products of a term run as two packed FP32x2 FMAs (sm_100 family):
+//    (hi, lo) += (Dh, Df) * (uh, ul) and (m, l) += (Dm, Dl) * (uh, uh).
 //  * Normalised residual.  For an affine axis-aligned element the mass
 //    cancels the GLL weights and metrics: res/(bm1*2/hx) = d_s Hz - d_t Hy
 //    (+ face terms flux*area/(bm1*2/hx)), etc.  All FP32 coefficients are then
@@ -143,10 +145,12 @@ __device__ __forceinline__ int face_vol(int f, int a, int b) {
                  : (ax == 1 ? a + NX * fixed + NX * NX * b : a + NX * b + NX * NX * fixed);
 }
 
-// D of order nx-1 in the four FP32 pieces of the exact-hi contraction,
-// indexed by nx so that every coefficient is a compile-time constant-bank
-// operand: [nx][piece: Dh, Df, Dm, Dl][i + nx*l].  D depends only on nx.
-__constant__ float c_mixD[kMaxMixed + 1][4][kMaxMixed * kMaxMixed];
+// D of order nx-1 in the FP32 pieces of the exact-hi contraction, as float
+// pairs indexed by nx so that every coefficient is a compile-time
+// constant-bank operand: [nx][0][i + nx*l] = (Dh, Df), [nx][1][i + nx*l] =
+// (Dm, Dl) of D(i,l).  Dh is D on a 10-bit grid of its row, Df = RN32(D),
+// Dm = RN32(D - Dh), Dl = RN32(D - Dh - Dm).  D depends only on nx.
+__constant__ float2 c_mixD[kMaxMixed + 1][2][kMaxMixed * kMaxMixed];
 
 // A copy of the thread index the compiler cannot see through: index math
 // derived from it is recomputed in each phase instead of being hoisted out of
@@ -224,25 +228,32 @@ __device__ __forceinline__ void line_phase(const float2* s_u2, float2* s_R2, con
       const float sg = kLineSign[DIR][slot];
       const bool init = kLineInit[DIR][slot] != 0;
       const float2* pu = s_u2 + comp * C::N3P;
-      // all NX outputs of the line at once: compile-time coefficient indices,
-      // NX independent accumulator pairs
+      float2 u[NX];
+#pragma unroll
+      for (int l = 0; l < NX; ++l) u[l] = pu[line_node<NX, DIR>(la, lb, l)];
+      // all NX outputs of the line at once, packed in float pairs:
+      //   (hi, lo) += (Dh, Df) * (uh, ul)   hi exact
+      //   (m, l)   += (Dm, Dl) * (uh, uh)
+      float2 x[NX], y[NX];
+#pragma unroll
+      for (int i = 0; i < NX; ++i) {
+        x[i] = __fmul2_rn(c_mixD[NX][0][i], u[0]);
+        y[i] = __fmul2_rn(c_mixD[NX][1][i], make_float2(u[0].x, u[0].x));
+      }
+#pragma unroll
+      for (int l = 1; l < NX; ++l) {
+        const float2 uu = make_float2(u[l].x, u[l].x);
+#pragma unroll
+        for (int i = 0; i < NX; ++i) {
+          x[i] = __ffma2_rn(c_mixD[NX][0][i + NX * l], u[l], x[i]);
+          y[i] = __ffma2_rn(c_mixD[NX][1][i + NX * l], uu, y[i]);
+        }
+      }
       float hi[NX], lo[NX];
 #pragma unroll
       for (int i = 0; i < NX; ++i) {
-        hi[i] = 0.0f;
-        lo[i] = 0.0f;
-      }
-#pragma unroll
-      for (int l = 0; l < NX; ++l) {
-        const float2 hr = pu[line_node<NX, DIR>(la, lb, l)];
-        const float h = hr.x, r = hr.y;
-#pragma unroll
-        for (int i = 0; i < NX; ++i) {
-          hi[i] = fmaf(c_mixD[NX][0][i + NX * l], h, hi[i]);  // exact
-          lo[i] = fmaf(c_mixD[NX][1][i + NX * l], r, lo[i]);
-          lo[i] = fmaf(c_mixD[NX][2][i + NX * l], h, lo[i]);
-          lo[i] = fmaf(c_mixD[NX][3][i + NX * l], h, lo[i]);
-        }
+        hi[i] = x[i].x;
+        lo[i] = x[i].y + (y[i].x + y[i].y);
       }
       float2* R0 = s_R2 + rt * C::N3P;
 #pragma unroll
@@ -567,15 +578,12 @@ int launch_mixed(Context* c, const MixedDev& a) {
 
 }  // namespace
 
-int mixed_upload_D(int nx, const float* Dh, const float* Df, const float* Dm, const float* Dl) {
+int mixed_upload_D(int nx, const float* tab, size_t count) {
   static bool done[kMaxMixed + 1] = {false};
-  if (nx < 2 || nx > kMaxMixed) return NEKGPU_ERR_UNSUPPORTED;
+  constexpr size_t kCount = 2 * 2 * kMaxMixed * kMaxMixed;  // floats per nx
+  if (nx < 2 || nx > kMaxMixed || count != kCount) return NEKGPU_ERR_UNSUPPORTED;
   if (done[nx]) return NEKGPU_OK;
-  float tab[4][kMaxMixed * kMaxMixed] = {};
-  for (int k = 0; k < nx * nx; ++k) {
-    tab[0][k] = Dh[k]; tab[1][k] = Df[k]; tab[2][k] = Dm[k]; tab[3][k] = Dl[k];
-  }
-  if (check_cuda(cudaMemcpyToSymbol(c_mixD, tab, sizeof(tab), sizeof(tab) * nx)))
+  if (check_cuda(cudaMemcpyToSymbol(c_mixD, tab, sizeof(float) * kCount, sizeof(float) * kCount * nx)))
     return NEKGPU_ERR_CUDA;
   done[nx] = true;
   return NEKGPU_OK;
