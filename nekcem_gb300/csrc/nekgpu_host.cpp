@@ -764,7 +764,7 @@ int upload_fused(Context* c, const Compact& cp) {
     m.nelt = c->nelt;
     m.npts = c->npts;
     m.k = c->d_k;
-    m.coef = c->d_coef;
+    m.coef = reinterpret_cast<const float2*>(c->d_coef);
     m.nbr = c->d_nbr;
     m.egm = c->d_egm;
     m.fcoef = c->d_fcoef;
@@ -1342,7 +1342,8 @@ int nekgpu_time_steps(nekgpu_ctx* c, int nsteps, double* time, double dt, double
   if (!c->have_state) return NEKGPU_ERR_STATE;
   c->last_launches = 0;
   if (c->form != NEKGPU_PLAIN) {
-    int st = scale_coef(c, dt);  // keep the one-off rescale out of the timed region
+    // keep the one-off rescale out of the timed region
+    int st = c->form == NEKGPU_MIXED ? scale_coef_pairs(c, dt) : scale_coef(c, dt);
     if (st) return st;
   }
   if (check_cuda(cudaEventRecord(c->ev0, c->stream))) return NEKGPU_ERR_CUDA;

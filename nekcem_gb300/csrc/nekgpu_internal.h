@@ -105,7 +105,7 @@ struct MixedDev {
   const double* u_in;
   double* u_out;
   double* k;
-  const double* coef;   // 2*npts: dt*hbm1*w3*rx | dt*ebm1*w3*rx (per element rx)
+  const float2* coef;   // 2*npts (hi, lo) pairs of dt*hbm1*w3*rx | dt*ebm1*w3*rx
   const int* nbr;       // 6*nelt
   const float* egm;     // 12*nelt: rho_y (hi,lo), rho_z (hi,lo), lift factor per slot, cubic
   const void* fcoef;    // float4 per face node, null when uniform
@@ -215,6 +215,8 @@ int scale_coef(Context* c, double dt);
 
 // nekgpu_mixed.cu
 int mixed_stage(Context* c, int rkstep, double time, double dt);
+// the mixed form keeps dt-scaled coefficients as (hi, lo) float pairs in d_coef
+int scale_coef_pairs(Context* c, double dt);
 // D(i,j) at [i + nx*j] in four FP32 pieces: Dh on a 10-bit grid per row
 // (exact products with the 10-bit uh), Df = D rounded, and the remainder
 // D - Dh = Dm + Dl to ~2^-55; uploaded once per nx

@@ -180,10 +180,12 @@ struct MCfg {
   static constexpr int FPT = (NF + NT - 1) / NT;
   static constexpr int TPT = (NTASK + NT - 1) / NT;
   static constexpr bool kTma = (N3 % 2) == 0;
+  // the staged FP64 state is dead once split, so the residual pairs reuse
+  // its space: 74 KB at NX=8, three blocks per SM
   static constexpr size_t off_u64 = 0;
-  static constexpr size_t off_u2 = off_u64 + 6 * N3 * 8;   // float2 (uh, ul)
-  static constexpr size_t off_R2 = off_u2 + 6 * N3P * 8;    // float2 residual (hi, lo)
-  static constexpr size_t off_nb2 = off_R2 + 6 * N3P * 8;   // float2 partner (hi, lo); then flux in .x
+  static constexpr size_t off_R2 = 0;                       // float2 residual (hi, lo)
+  static constexpr size_t off_u2 = cmax(6 * N3 * 8, 6 * N3P * 8);  // float2 (uh, ul)
+  static constexpr size_t off_nb2 = off_u2 + 6 * N3P * 8;   // float2 partner (hi, lo); then flux in .x
   static constexpr size_t off_wmax = off_nb2 + 6 * NF * 8;
   static constexpr size_t off_E = off_wmax + NW * 6 * 4;
   static constexpr size_t off_bar = (off_E + 8 * 4 + 15) / 16 * 16;
@@ -284,7 +286,7 @@ __device__ __forceinline__ void line_phase(const float2* s_u2, float2* s_R2, con
 }
 
 template <int NX>
-__global__ void __launch_bounds__(MCfg<NX>::NT, 2) k_mixed_stage(const MixedDev a) {
+__global__ void __launch_bounds__(MCfg<NX>::NT, 3) k_mixed_stage(const MixedDev a) {
   using C = MCfg<NX>;
   constexpr int N2 = C::N2, N3 = C::N3, NT = C::NT, NF = C::NF, N3P = C::N3P;
   constexpr int NPT = C::NPT, FPT = C::FPT;
@@ -483,7 +485,8 @@ __global__ void __launch_bounds__(MCfg<NX>::NT, 2) k_mixed_stage(const MixedDev 
     }
     // RK register and coefficients, loaded late to keep registers free above
     tid = opaque_tid();
-    double kv[NPT][6], cv[NPT][2];
+    double kv[NPT][6];
+    float2 cv[NPT][2];
 #pragma unroll
     for (int q = 0; q < NPT; ++q) {
       const int v = tid + q * NT;
@@ -499,8 +502,10 @@ __global__ void __launch_bounds__(MCfg<NX>::NT, 2) k_mixed_stage(const MixedDev 
     }
     __syncthreads();
     // ---- lift, source, inverse mass, RK update --------------------------------
-    // Every read of the staged u happens before the barrier that lets the
-    // next element's TMA overwrite it.
+    // The state is read again from global memory (an L2 hit: this element's
+    // block was copied in at the start of its turn).  Every read of the
+    // residual pairs happens before the barrier that lets the next element's
+    // TMA overwrite them.
     const int so = a.src_elem ? a.src_elem[e] : -1;
 #pragma unroll
     for (int q = 0; q < NPT; ++q) {
@@ -526,8 +531,8 @@ __global__ void __launch_bounds__(MCfg<NX>::NT, 2) k_mixed_stage(const MixedDev 
       if (k == 0) add(4, i + NX * j);
       if (k == NX - 1) add(5, i + NX * j);
       if (so >= 0) Rl[5] = fmaf(a.src_w[(long)so * N3 + v], a.src_ftf, Rl[5]);
-      const float chh = d2f_hi(cv[q][0]), chl = d2f_lo(cv[q][0]);
-      const float ceh = d2f_hi(cv[q][1]), cel = d2f_lo(cv[q][1]);
+      const float chh = cv[q][0].x, chl = cv[q][0].y;
+      const float ceh = cv[q][1].x, cel = cv[q][1].y;
       const long g = (long)e * N3 + v;
 #pragma unroll
       for (int c = 0; c < 6; ++c) {
@@ -539,7 +544,7 @@ __global__ void __launch_bounds__(MCfg<NX>::NT, 2) k_mixed_stage(const MixedDev 
         const double r = f2d(p) + f2d(ee);
         const double kn = first_stage ? r : fma(a.a, kv[q][c], r);
         a.k[c * P + g] = kn;
-        a.u_out[c * P + g] = fma(a.b, kn, s_u64[c * N3 + v]);
+        a.u_out[c * P + g] = fma(a.b, kn, __ldg(a.u_in + c * P + g));
       }
     }
     __syncthreads();  // staged u consumed: the next element may land
@@ -549,6 +554,15 @@ __global__ void __launch_bounds__(MCfg<NX>::NT, 2) k_mixed_stage(const MixedDev 
       issue_tma(en);
     }
   }
+}
+
+// dt-scaled inverse-mass coefficients as float pairs: (hi, lo) of dt * base,
+// hi = the top 24 mantissa bits, lo = the rest (2*n entries)
+__global__ void k_scale_coef_pairs(float2* coef, const double* base, long n2, double dt) {
+  const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (i >= n2) return;
+  const double v = dt * base[i];
+  coef[i] = make_float2(d2f_hi(v), d2f_lo(v));
 }
 
 template <int NX>
@@ -589,8 +603,18 @@ int mixed_upload_D(int nx, const float* tab, size_t count) {
   return NEKGPU_OK;
 }
 
+int scale_coef_pairs(Context* c, double dt) {
+  if (c->coef_dt == dt) return NEKGPU_OK;
+  const long n2 = 2 * c->npts;
+  k_scale_coef_pairs<<<(unsigned)((n2 + 255) / 256), 256, 0, c->stream>>>(
+      reinterpret_cast<float2*>(c->d_coef), c->d_cbase, n2, dt);
+  c->last_launches += 1;
+  c->coef_dt = dt;
+  return check_cuda(cudaGetLastError());
+}
+
 int mixed_stage(Context* c, int rkstep, double time, double dt) {
-  int st = scale_coef(c, dt);
+  int st = scale_coef_pairs(c, dt);
   if (st) return st;
   MixedDev a = c->margs;
   a.u_in = c->d_u[c->cur];
