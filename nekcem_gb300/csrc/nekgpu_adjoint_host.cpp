@@ -165,6 +165,32 @@ int build_adjoint_data(Context* c) {
   return NEKGPU_OK;
 }
 
+// second stream and the events that hand buffer sets between the streams
+struct StreamPair {
+  cudaStream_t side = nullptr;
+  cudaEvent_t done_recompute[2] = {nullptr, nullptr}, done_reverse[2] = {nullptr, nullptr};
+  bool create() {
+    if (cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking) != cudaSuccess) return fail();
+    for (int b = 0; b < 2; ++b)
+      if (cudaEventCreateWithFlags(&done_recompute[b], cudaEventDisableTiming) != cudaSuccess ||
+          cudaEventCreateWithFlags(&done_reverse[b], cudaEventDisableTiming) != cudaSuccess)
+        return fail();
+    return true;
+  }
+  bool fail() {
+    cudaGetLastError();
+    return false;
+  }
+  ~StreamPair() {
+    if (side) cudaStreamSynchronize(side);
+    for (int b = 0; b < 2; ++b) {
+      if (done_recompute[b]) cudaEventDestroy(done_recompute[b]);
+      if (done_reverse[b]) cudaEventDestroy(done_reverse[b]);
+    }
+    if (side) cudaStreamDestroy(side);
+  }
+};
+
 int copy_state(Context* c, double* dst, const double* src) {
   return check_cuda(cudaMemcpyAsync(dst, src, 6 * c->npts * sizeof(double),
                                     cudaMemcpyDeviceToDevice, c->stream));
@@ -184,17 +210,29 @@ extern "C" int nekgpu_adjoint_gradient(nekgpu_ctx* c, int nsteps, double t0, dou
   const int S = stride > 0 ? stride : (int)std::ceil(std::sqrt((double)nsteps));
   const int nseg = (nsteps + S - 1) / S;
   Scratch mem;
-  std::vector<double*> ckpt(nseg), U(5 * S + 1), K(5 * S + 1);
+  std::vector<double*> ckpt(nseg);
   for (auto& p : ckpt)
-    if (!(p = mem.get(ns))) return NEKGPU_ERR_NOMEM;
-  for (auto& p : U)
-    if (!(p = mem.get(ns))) return NEKGPU_ERR_NOMEM;
-  for (auto& p : K)
     if (!(p = mem.get(ns))) return NEKGPU_ERR_NOMEM;
   double* ub[2] = {mem.get(ns), mem.get(ns)};
   double* wb[2] = {mem.get(ns), mem.get(ns)};
   double* deps = mem.get(npts);
   if (!ub[0] || !ub[1] || !wb[0] || !wb[1] || !deps) return NEKGPU_ERR_NOMEM;
+  // segment storage: stage states U and RK registers K of one segment; a
+  // second set (when it fits) lets the recompute of the next segment run on a
+  // second stream while the reverse stages of this one run
+  std::vector<double*> U[2], K[2];
+  int nsets = 0;
+  for (int b = 0; b < 2; ++b) {
+    U[b].resize(5 * S + 1);
+    K[b].resize(5 * S + 1);
+    bool ok = true;
+    for (int i = 0; i <= 5 * S && ok; ++i) ok = (U[b][i] = mem.get(ns)) && (K[b][i] = mem.get(ns));
+    if (!ok) break;
+    ++nsets;
+  }
+  if (nsets == 0) return NEKGPU_ERR_NOMEM;
+  StreamPair sp;
+  if (nsets == 2 && !sp.create()) nsets = 1;
   if ((st = scale_coef(c, dt))) return st;
 
   // ---- forward pass with checkpoints ------------------------------------------
@@ -246,16 +284,22 @@ extern "C" int nekgpu_adjoint_gradient(nekgpu_ctx* c, int nsteps, double t0, dou
     for (int m = 0; m < n; ++m) a.Dw[m + n * i] = c->fargs.D[m + n * i] * c->fargs.w[m];
   }
   int cu = 0;
-  if (check_cuda(cudaEventRecord(c->ev0, c->stream))) return NEKGPU_ERR_CUDA;
-  for (int seg = nseg - 1; seg >= 0; --seg) {
+  cudaStream_t main_stream = c->stream;
+  // recompute of segment seg into buffer set b, on stream `on`
+  auto recompute = [&](int seg, int b, cudaStream_t on) -> int {
     const int n0 = seg * S, nS = std::min(S, nsteps - n0);
-    if ((st = copy_state(c, U[0], ckpt[seg]))) return st;
-    for (int s = 0; s < nS; ++s)
-      for (int r = 1; r <= 5; ++r) {
-        const int i = 5 * s + r;
-        if ((st = fused_stage_buffers(c, r, tstep[n0 + s], dt, U[i - 1], U[i], K[i - 1], K[i])))
-          return st;
+    c->stream = on;
+    int r = copy_state(c, U[b][0], ckpt[seg]);
+    for (int s = 0; s < nS && !r; ++s)
+      for (int q = 1; q <= 5 && !r; ++q) {
+        const int i = 5 * s + q;
+        r = fused_stage_buffers(c, q, tstep[n0 + s], dt, U[b][i - 1], U[b][i], K[b][i - 1], K[b][i]);
       }
+    c->stream = main_stream;
+    return r;
+  };
+  auto reverse = [&](int seg, int b) -> int {
+    const int n0 = seg * S, nS = std::min(S, nsteps - n0);
     for (int s = nS - 1; s >= 0; --s)
       for (int r = 5; r >= 1; --r) {
         const int i = 5 * s + r;
@@ -263,14 +307,40 @@ extern "C" int nekgpu_adjoint_gradient(nekgpu_ctx* c, int nsteps, double t0, dou
         a.ub_out = ub[cu ^ 1];
         a.w_in = wb[cu];
         a.w_out = wb[cu ^ 1];
-        a.u_prev = U[i - 1];
-        a.k_cur = K[i];
-        a.k_prev = K[i - 1];
+        a.u_prev = U[b][i - 1];
+        a.k_cur = K[b][i];
+        a.k_prev = K[b][i - 1];
         a.a = c->rk_a[r - 1];
         a.b_next = c->rk_b[r == 1 ? 4 : r - 2];
-        if ((st = adjoint_stage(c, a))) return st;
+        int st2 = adjoint_stage(c, a);
+        if (st2) return st2;
         cu ^= 1;
       }
+    return NEKGPU_OK;
+  };
+  if (check_cuda(cudaEventRecord(c->ev0, c->stream))) return NEKGPU_ERR_CUDA;
+  if (nsets == 1) {
+    for (int seg = nseg - 1; seg >= 0; --seg)
+      if ((st = recompute(seg, 0, main_stream)) || (st = reverse(seg, 0))) return st;
+  } else {
+    // set b = seg & 1.  side stream: recompute(seg) after reverse(seg + 2)
+    // released set b; main stream: reverse(seg) after recompute(seg).
+    if (check_cuda(cudaStreamWaitEvent(sp.side, c->ev0, 0))) return NEKGPU_ERR_CUDA;
+    if ((st = recompute(nseg - 1, (nseg - 1) & 1, sp.side))) return st;
+    if (check_cuda(cudaEventRecord(sp.done_recompute[(nseg - 1) & 1], sp.side))) return NEKGPU_ERR_CUDA;
+    for (int seg = nseg - 1; seg >= 0; --seg) {
+      const int b = seg & 1;
+      if (seg > 0) {
+        const int bn = (seg - 1) & 1;
+        if (seg + 1 < nseg && check_cuda(cudaStreamWaitEvent(sp.side, sp.done_reverse[bn], 0)))
+          return NEKGPU_ERR_CUDA;
+        if ((st = recompute(seg - 1, bn, sp.side))) return st;
+        if (check_cuda(cudaEventRecord(sp.done_recompute[bn], sp.side))) return NEKGPU_ERR_CUDA;
+      }
+      if (check_cuda(cudaStreamWaitEvent(main_stream, sp.done_recompute[b], 0))) return NEKGPU_ERR_CUDA;
+      if ((st = reverse(seg, b))) return st;
+      if (check_cuda(cudaEventRecord(sp.done_reverse[b], main_stream))) return NEKGPU_ERR_CUDA;
+    }
   }
   if (check_cuda(cudaEventRecord(c->ev1, c->stream)) || check_cuda(cudaEventSynchronize(c->ev1)))
     return NEKGPU_ERR_CUDA;
