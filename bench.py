@@ -1,13 +1,21 @@
 """Benchmark of the Maxwell DG time step (DOF-stage updates per second).
 
-Workload: the periodic plane-wave box, 16^3 affine hex elements, N=7
+Default workload: the periodic plane-wave box, 16^3 affine hex elements, N=7
 (2,097,152 nodes x 6 field components), k=(1,1,1), dt = 0.5 x smallest GLL
 spacing.  One benchmark step is one RK5 time step (5 stages) of the whole
 mesh.  The headline form is the mixed-precision fused kernel; the all-FP64
 fused form, the plain per-routine FP64 form and the CPU oracle are measured
-beside it on the same workload.
+beside it on the same workload, and the adjoint workload (8^3 el, N=7, random
+eps, 2000 steps) gives the gradient/forward time ratio.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                  [--workload planewave|cavity|dielectric|large]
+
+--workload selects another configuration of the same contract: cavity (PEC
+4^3 el, N=7, TM110 mode), dielectric (PEC 32^3 el, N=5, eps=4 sphere,
+Gaussian E_z pulse; accuracy = L2 of mixed against the FP64 fused form) or
+large (PEC 64^3 el, N=7, random eps in [1,4], 134M nodes; accuracy over
+--accuracy-steps steps).
 
 Prints one JSON line.  With --gpus N > 1 (under torchrun) every rank runs its
 own replica of the workload on its GPU ("replicas only": the time step does
@@ -33,6 +41,13 @@ METRIC = "DOF-stage updates/s FP64 vs mixed at fixed L2 error; adjoint/forward t
 UNIT = "DOF-stage updates/s"
 BYTES_PER_NODE_STAGE = 208  # u r/w 96 + k r/w 96 + inverse-mass coefficients 16
 CASE = "planewave"
+WORKLOADS = {
+    "planewave": "planewave 16^3 el N=7 periodic (2,097,152 nodes x 6), RK45",
+    "cavity": "cavity 4^3 el N=7 PEC TM110 (32,768 nodes x 6), RK45",
+    "dielectric": "dielectric 32^3 el N=5 PEC eps=4 sphere (7,077,888 nodes x 6), RK45",
+    "large": "large 64^3 el N=7 PEC random eps (134,217,728 nodes x 6), RK45",
+}
+_EPS_CACHE = {}
 
 
 def parse():
@@ -44,6 +59,11 @@ def parse():
     p.add_argument("--no-accuracy", action="store_true", help="skip the full-length L2 runs")
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline sample")
     p.add_argument("--no-adjoint", action="store_true", help="skip the adjoint/forward ratio run")
+    p.add_argument("--workload", default="planewave", choices=sorted(WORKLOADS))
+    p.add_argument("--adjoint-steps", type=int, default=0,
+                   help="steps of the adjoint ratio run (default: the workload's 2000)")
+    p.add_argument("--accuracy-steps", type=int, default=0,
+                   help="steps of the accuracy runs (default: the configuration's own)")
     return p.parse_args()
 
 
@@ -150,10 +170,23 @@ def barrier(dist):
         dist.barrier()
 
 
+def case_eps(c):
+    """Per-node permittivity of the configuration (None when eps = 1)."""
+    if c.eps is None:
+        return None
+    if c.name not in _EPS_CACHE:
+        from nekcem_gb300 import MaxwellGPU
+        g = MaxwellGPU.from_box(c.N, c.nel, c.lo, c.hi, c.bc, form="fused64")
+        x, y, z = g.coords()
+        g.close()
+        _EPS_CACHE[c.name] = np.ascontiguousarray(c.eps(x, y, z), dtype=np.float64)
+    return _EPS_CACHE[c.name]
+
+
 def build_gpu_case(form, device_note=None):
     from nekcem_gb300 import MaxwellGPU, cases
     c = cases.make(CASE)
-    g = MaxwellGPU.from_box(c.N, c.nel, c.lo, c.hi, c.bc, form=form)
+    g = MaxwellGPU.from_box(c.N, c.nel, c.lo, c.hi, c.bc, form=form, permittivity=case_eps(c))
     x, y, z = g.coords()
     dt = c.timestep(x, y, z)
     H, E = c.init_fields(x, y, z)
@@ -184,13 +217,29 @@ def time_form(form, steps, warmup, dist=None, clocks=None):
 
 
 def accuracy(form, nsteps=None):
+    """L2 of the final state against the analytic solution, or (no analytic
+    solution) the final state itself for a comparison between forms."""
     c, g, (x, y, z), dt, H, E = build_gpu_case(form)
     g.set_state(H, E)
     n = nsteps or c.nsteps
     t = g.run(n, 0.0, dt)
-    l2, li = g.cem_error(*c.exact(x, y, z, t))
+    if c.exact is not None:
+        l2, li = g.cem_error(*c.exact(x, y, z, t))
+        g.close()
+        return float(np.sqrt(np.sum(l2 ** 2))), n, None
+    Hn, En = g.get_state()
+    bm1 = g.array("bmn")
     g.close()
-    return float(np.sqrt(np.sum(l2 ** 2))), n
+    return None, n, (Hn, En, bm1)
+
+
+def l2_between(a, b):
+    """sqrt(sum_c sum_n bm1 (a - b)^2) / sqrt(sum_c sum_n bm1 b^2): the
+    cem_error L2 of a against b, relative."""
+    (Ha, Ea, bm1), (Hb, Eb, _) = a, b
+    d = sum(float(np.sum(bm1 * (p - q) ** 2)) for p, q in ((Ha, Hb), (Ea, Eb)))
+    r = sum(float(np.sum(bm1 * q ** 2)) for q in (Hb, Eb))
+    return float(np.sqrt(d / r))
 
 
 def e2e(steps, warmup, dist=None):
@@ -216,7 +265,7 @@ def e2e(steps, warmup, dist=None):
     return dict(sec=sec, npts=npts, h2d=bytes_io, d2h=bytes_io)
 
 
-def adjoint_ratio():
+def adjoint_ratio(nsteps=0):
     """Gradient time over forward time on the adjoint workload: unit PEC box,
     8^3 elements, N=7, eps = 1 + 3 sigmoid(smooth random field, seed 4),
     Gaussian E_z source, 2000 steps, J = sum bm1 |E|^2 over [0.7,0.9]^3.
@@ -237,15 +286,16 @@ def adjoint_ratio():
     inside = (x > p0) & (x < p1) & (y > q0) & (y < q1) & (z > r0) & (z < r1)
     jw = np.where(inside, bm1, 0.0)
     dt = c.timestep(x, y, z)
+    n = nsteps or c.nsteps
     g.set_state(H0, E0)
     g.time_steps(3, 0.0, dt)  # warm-up
     g.set_state(H0, E0)
-    _, fwd_ms = g.time_steps(c.nsteps, 0.0, dt)
+    _, fwd_ms = g.time_steps(n, 0.0, dt)
     g.set_state(H0, E0)
-    J, dJ, fwd_ckpt_ms, rev_ms = g.adjoint_gradient(c.nsteps, 0.0, dt, jw)
+    J, dJ, fwd_ckpt_ms, rev_ms = g.adjoint_gradient(n, 0.0, dt, jw)
     g.close()
-    return {"workload": "adjoint box 8^3 el N=7 PEC, random eps, E_z source, 2000 steps",
-            "steps": c.nsteps, "forward_ms": fwd_ms, "gradient_ms": fwd_ckpt_ms + rev_ms,
+    return {"workload": "adjoint box 8^3 el N=7 PEC, random eps, E_z source",
+            "steps": n, "forward_ms": fwd_ms, "gradient_ms": fwd_ckpt_ms + rev_ms,
             "forward_with_checkpoints_ms": fwd_ckpt_ms, "reverse_sweep_ms": rev_ms,
             "ratio": (fwd_ckpt_ms + rev_ms) / fwd_ms, "J": J,
             "grad_norm": float(np.linalg.norm(dJ))}
@@ -261,6 +311,8 @@ def cpu_sample(steps):
     c = cases.make(CASE)
     ref = R.RefBox(c.N, c.nel, c.lo, c.hi, c.bc)
     x, y, z = ref.coords()
+    if c.eps is not None:
+        ref.set_materials(c.eps(x, y, z), np.ones(ref.npts))
     dt = c.timestep(x, y, z)
     ref.set_state(*c.init_fields(x, y, z))
     ref.run(1, 0.0, dt)  # warm caches / threads
@@ -285,6 +337,8 @@ def run_reference(args):
     c = cases.make(CASE)
     ref = R.RefBox(c.N, c.nel, c.lo, c.hi, c.bc)
     x, y, z = ref.coords()
+    if c.eps is not None:
+        ref.set_materials(c.eps(x, y, z), np.ones(ref.npts))
     dt = c.timestep(x, y, z)
     ref.set_state(*c.init_fields(x, y, z))
     t = ref.run(warm, 0.0, dt)
@@ -296,7 +350,7 @@ def run_reference(args):
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": steps, "warmup": warm, "ms_per_step": 1e3 * sec / steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": "planewave 16^3 el N=7 periodic (2,097,152 nodes x 6), RK45",
+        "config": {"workload": WORKLOADS[CASE],
                    "elements": c.nelt, "N": c.N, "form": "CPU oracle (FP64 restatement of the "
                    "reference's Fortran routines; the Fortran cannot be built here)"},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
@@ -307,7 +361,9 @@ def run_reference(args):
 
 
 def main():
+    global CASE
     args = parse()
+    CASE = args.workload
     if args.impl == "reference":
         run_reference(args)
         return
@@ -340,15 +396,19 @@ def main():
         "warmup": max(3, args.warmup), "ms_per_step": ms_step, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32 contraction / f64 state+RK",
         "data": "synthetic",
-        "config": {"workload": "planewave 16^3 el N=7 periodic (2,097,152 nodes x 6), RK45",
-                   "elements": 4096, "N": 7, "form": "mixed", "dt": mixed["dt"],
-                   "l2_policy": "inputs larger than L2: u in/out + k + inverse mass = 337 MB per stage",
+        "config": {"workload": WORKLOADS[CASE],
+                   "elements": mixed["case"].nelt, "N": mixed["case"].N, "form": "mixed",
+                   "dt": mixed["dt"],
+                   "l2_policy": f"inputs larger than L2: u in/out + k + inverse mass = "
+                                f"{(6 * 8 * 3 + 16) * npts / 1e6:.0f} MB per stage",
                    "parallelism": "replicas" if world > 1 else "1 GPU"},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": e["h2d"],
                 "d2h_bytes_per_step": e["d2h"], "path": "nekgpu_op_rk_host, pinned host fields"},
         "gpu_launches": mixed["launches"],
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": ncu_traffic("k_mixed_stage<8>"),
+                     "frac": achieved / peak,
+                     "traffic": ncu_traffic(f"k_mixed_stage<{mixed['case'].N + 1}>"
+                                            + ("" if CASE == "planewave" else f" {CASE}")),
                      "peak_kind": peak_kind,
                      "algorithmic_bytes_per_launch": BYTES_PER_NODE_STAGE * npts},
         "clocks": clocks,
@@ -362,12 +422,16 @@ def main():
     out["forms"]["mixed_over_fused64"] = value / world / out["forms"]["fused64"]["value"]
     out["forms"]["mixed_over_plain64"] = value / world / out["forms"]["plain64"]["value"]
     if not args.no_accuracy and world == 1:
-        l2m, n = accuracy("mixed")
-        l2d, _ = accuracy("fused64")
-        out["l2_vs_analytic"] = {"steps": n, "mixed": l2m, "fused64": l2d, "ratio": l2m / l2d}
-    if not args.no_adjoint and world == 1:
-        out["adjoint"] = adjoint_ratio()
-    if not args.no_cpu and world == 1:
+        nacc = args.accuracy_steps or (100 if CASE == "large" else None)
+        l2m, n, fin_m = accuracy("mixed", nacc)
+        l2d, _, fin_d = accuracy("fused64", nacc)
+        if l2m is not None:
+            out["l2_vs_analytic"] = {"steps": n, "mixed": l2m, "fused64": l2d, "ratio": l2m / l2d}
+        else:
+            out["l2_mixed_vs_fused64"] = {"steps": n, "relative_l2": l2_between(fin_m, fin_d)}
+    if not args.no_adjoint and world == 1 and CASE == "planewave":
+        out["adjoint"] = adjoint_ratio(args.adjoint_steps)
+    if not args.no_cpu and world == 1 and npts <= 10_000_000:
         cpu = cpu_sample(max(2, min(20, args.steps // 10)))
         out["cpu_baseline"] = {"value": cpu["value"], "unit": UNIT, "cores": cpu["threads"],
                                "kind": "port", "sample": f"{max(2, min(20, args.steps // 10))} RK "

@@ -158,16 +158,39 @@ def eps_sphere(x, y, z, center=(0.5, 0.5, 0.5), radius=0.25, inside=4.0):
 
 def gaussian_random_field(x, y, z, length: float, seed: int, nfeat: int = 512):
     """Zero-mean, unit-variance smooth random field from random Fourier
-    features: g = sqrt(2/F) sum_f cos(k_f . x + phi_f), k_f ~ N(0, 1/length^2)."""
+    features: g = sqrt(2/F) sum_f cos(k_f . x + phi_f), k_f ~ N(0, 1/length^2).
+    Evaluated in node blocks (bounded temporaries); on a CUDA device through
+    torch when one is present and the mesh is large."""
     rng = np.random.default_rng(seed)
     k = rng.normal(0.0, 1.0 / length, size=(nfeat, 3))
     ph = rng.uniform(0.0, TWO_PI, size=nfeat)
-    g = np.zeros_like(x)
-    chunk = 64
-    for s in range(0, nfeat, chunk):
-        arg = (np.outer(x, k[s:s + chunk, 0]) + np.outer(y, k[s:s + chunk, 1])
-               + np.outer(z, k[s:s + chunk, 2]) + ph[s:s + chunk])
-        g += np.cos(arg).sum(axis=1)
+    x = np.asarray(x, dtype=np.float64)
+    y = np.asarray(y, dtype=np.float64)
+    z = np.asarray(z, dtype=np.float64)
+    n = x.size
+    g = np.zeros(n)
+    if n > 4_000_000:
+        try:
+            import torch
+            if torch.cuda.is_available():
+                dev = torch.device("cuda")
+                kt = torch.tensor(k, device=dev)
+                pt = torch.tensor(ph, device=dev)
+                for s0 in range(0, n, 1 << 20):
+                    s1 = min(n, s0 + (1 << 20))
+                    xyz = torch.tensor(np.stack([x[s0:s1], y[s0:s1], z[s0:s1]], axis=1), device=dev)
+                    g[s0:s1] = torch.cos(xyz @ kt.T + pt).sum(dim=1).cpu().numpy()
+                return g * np.sqrt(2.0 / nfeat)
+        except ImportError:
+            pass
+    block, chunk = 1 << 16, 64
+    for s0 in range(0, n, block):
+        s1 = min(n, s0 + block)
+        for f0 in range(0, nfeat, chunk):
+            kk = k[f0:f0 + chunk]
+            arg = (np.outer(x[s0:s1], kk[:, 0]) + np.outer(y[s0:s1], kk[:, 1])
+                   + np.outer(z[s0:s1], kk[:, 2]) + ph[f0:f0 + chunk])
+            g[s0:s1] += np.cos(arg).sum(axis=1)
     return g * np.sqrt(2.0 / nfeat)
 
 
