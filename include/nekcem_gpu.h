@@ -229,6 +229,14 @@ int nekgpu_check_blowup(nekgpu_ctx* ctx);
 int nekgpu_adjoint_gradient(nekgpu_ctx* ctx, int nsteps, double t0, double dt, const double* jw,
                             double* J, double* dJdeps, int stride, double* fwd_ms,
                             double* adj_ms);
+/* The same split into the two calls of a driver that sets the objective once
+ * and evaluates it for several states or step counts: nekgpu_adjoint_init
+ * copies the weights jw (npts, host) and the checkpoint stride into the
+ * context (it allocates nothing on the device); nekgpu_adjoint_run runs
+ * nekgpu_adjoint_gradient with them.  NEKGPU_ERR_STATE if run comes first. */
+int nekgpu_adjoint_init(nekgpu_ctx* ctx, const double* jw, int stride);
+int nekgpu_adjoint_run(nekgpu_ctx* ctx, int nsteps, double t0, double dt, double* J,
+                       double* dJdeps);
 
 /* ---- timing ---------------------------------------------------------------- */
 /* Runs nsteps steps between CUDA events on the context stream and returns the

@@ -92,6 +92,8 @@ SIGNATURES = [
     ("nekgpu_check_blowup", C.c_int, [C.c_void_p]),
     ("nekgpu_adjoint_gradient", C.c_int, [C.c_void_p, C.c_int, C.c_double, C.c_double, dp, dp, dp,
                                          C.c_int, dp, dp]),
+    ("nekgpu_adjoint_init", C.c_int, [C.c_void_p, dp, C.c_int]),
+    ("nekgpu_adjoint_run", C.c_int, [C.c_void_p, C.c_int, C.c_double, C.c_double, dp, dp]),
     ("nekgpu_time_steps", C.c_int, [C.c_void_p, C.c_int, dp, C.c_double, dp]),
     ("nekgpu_last_launches", C.c_long, [C.c_void_p]),
     ("nekgpu_sync", C.c_int, [C.c_void_p]),

@@ -357,3 +357,19 @@ extern "C" int nekgpu_adjoint_gradient(nekgpu_ctx* c, int nsteps, double t0, dou
   if (adj_ms) *adj_ms = a_ms;
   return NEKGPU_OK;
 }
+
+extern "C" int nekgpu_adjoint_init(nekgpu_ctx* c, const double* jw, int stride) {
+  if (!c || !jw || stride < 0) return NEKGPU_ERR_ARG;
+  if (c->form != NEKGPU_FUSED64) return NEKGPU_ERR_UNSUPPORTED;
+  c->adj_jw.assign(jw, jw + c->npts);
+  c->adj_stride = stride;
+  return NEKGPU_OK;
+}
+
+extern "C" int nekgpu_adjoint_run(nekgpu_ctx* c, int nsteps, double t0, double dt, double* J,
+                                  double* dJdeps) {
+  if (!c || !J || !dJdeps) return NEKGPU_ERR_ARG;
+  if (c->adj_jw.empty()) return NEKGPU_ERR_STATE;
+  return nekgpu_adjoint_gradient(c, nsteps, t0, dt, c->adj_jw.data(), J, dJdeps, c->adj_stride,
+                                 nullptr, nullptr);
+}

@@ -178,6 +178,8 @@ struct Context {
   float* d_egm = nullptr;
   // adjoint face-slot coefficients (built on first use, FP64 fused form)
   double* d_adj_slot = nullptr;
+  std::vector<double> adj_jw;  // objective weights set by nekgpu_adjoint_init
+  int adj_stride = 0;
 
   // plain form
   PlainDev pargs{};

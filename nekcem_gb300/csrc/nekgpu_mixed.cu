@@ -65,16 +65,15 @@ __device__ __forceinline__ float d2f_lo(double d) {
   f = (ex >= 949) ? f : 0.0f;
   return __uint_as_float(__float_as_uint(f) | (hi & 0x80000000u));
 }
-// exact FP32 -> FP64 (zero/subnormal -> signed zero)
+// exact FP32 -> FP64 for normal floats and zeros (FP32 subnormals, below
+// 2^-126, come out as 2^-127 (1.m): their absolute error is below 2^-126).
+// The FP64 exponent is the FP32 one rebiased by 1023 - 127 = 896; it stays
+// below 2048, so the add never carries into the sign bit.
 __device__ __forceinline__ double f2d(float f) {
   const unsigned b = __float_as_uint(f);
   const unsigned mag = b & 0x7FFFFFFFu;
-  unsigned hi = (b & 0x80000000u) | ((mag >> 3) + 0x38000000u);
-  unsigned lo = b << 29;
-  const bool tiny = (b & 0x7F800000u) == 0u;
-  hi = tiny ? (b & 0x80000000u) : hi;
-  lo = tiny ? 0u : lo;
-  return __longlong_as_double((long long)(((unsigned long long)hi << 32) | lo));
+  const unsigned hi = ((mag >> 3) + 0x38000000u) | (b & 0x80000000u);
+  return __hiloint2double((int)(mag ? hi : b), (int)(b << 29));
 }
 
 // Knuth two-sum: s + e == a + b exactly
@@ -215,11 +214,10 @@ __device__ __forceinline__ int pnode(int v) {  // padded index of node v = i + N
 // One direction of the contraction: tasks (component, line) accumulate the
 // signed derivative pair into the residual pair arrays.
 template <int NX, int DIR>
-__device__ __forceinline__ void line_phase(const float2* s_u2, float2* s_R2, const float* eg) {
+__device__ __forceinline__ void line_phase(const float2* s_u2, float2* s_R2, bool cubic, float rh,
+                                           float rl) {
   using C = MCfg<NX>;
   const int tid = opaque_tid();
-  const bool cubic = eg[10] != 0.0f;
-  const float rh = DIR == 1 ? eg[0] : eg[2], rl = DIR == 1 ? eg[1] : eg[3];
 #pragma unroll
   for (int q = 0; q < C::TPT; ++q) {
     const int task = tid + q * C::NT;
@@ -413,11 +411,15 @@ __global__ void __launch_bounds__(MCfg<NX>::NT, 3) k_mixed_stage(const MixedDev 
     }
     __syncthreads();
     // ---- contractions: r, s, t lines ----------------------------------------
-    line_phase<NX, 0>(s_u2, s_R2, eg);
-    __syncthreads();
-    line_phase<NX, 1>(s_u2, s_R2, eg);
-    __syncthreads();
-    line_phase<NX, 2>(s_u2, s_R2, eg);
+    {
+      const bool cubic = eg[10] != 0.0f;
+      const float r1h = eg[0], r1l = eg[1], r2h = eg[2], r2l = eg[3];
+      line_phase<NX, 0>(s_u2, s_R2, cubic, 0.0f, 0.0f);
+      __syncthreads();
+      line_phase<NX, 1>(s_u2, s_R2, cubic, r1h, r1l);
+      __syncthreads();
+      line_phase<NX, 2>(s_u2, s_R2, cubic, r2h, r2l);
+    }
     // ---- upwind flux per face node (same interval: reads uh/ul, writes nbh) -
     tid = opaque_tid();
 #pragma unroll

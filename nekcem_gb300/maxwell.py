@@ -243,3 +243,16 @@ class MaxwellGPU:
                                                  C.byref(J), _dp(out), int(stride), C.byref(fms),
                                                  C.byref(ams)), "nekgpu_adjoint_gradient")
         return J.value, out, fms.value, ams.value
+
+    def adjoint_init(self, jw: np.ndarray, stride: int = 0):
+        """Set the objective weights and checkpoint stride for adjoint_run."""
+        jw = np.ascontiguousarray(jw, dtype=np.float64).reshape(self.npts)
+        L.check(L.load().nekgpu_adjoint_init(self._h, _dp(jw), int(stride)), "nekgpu_adjoint_init")
+
+    def adjoint_run(self, nsteps: int, t0: float, dt: float):
+        """(J, dJ/deps) with the weights of adjoint_init."""
+        out = np.empty(self.npts)
+        J = C.c_double()
+        L.check(L.load().nekgpu_adjoint_run(self._h, int(nsteps), float(t0), float(dt), C.byref(J),
+                                            _dp(out)), "nekgpu_adjoint_run")
+        return J.value, out

@@ -171,3 +171,18 @@ def test_adjoint_rejects_other_forms_and_missing_state():
         g.adjoint_gradient(2, 0.0, 0.01, np.ones(g.npts))
     assert e.value.status == -5
     g.close()
+
+
+@pytest.mark.gpu
+def test_adjoint_init_run_equals_gradient():
+    pb, eps, _, _ = gpu_problem(3, (2, 2, 2), (PEC, PER, PEC), seed=61, nsteps=9, stride=2)
+    J0, g0 = pb.gradient(eps)
+    g = pb.context(eps)
+    with pytest.raises(L.NekgpuError) as e:
+        g.adjoint_run(pb.nsteps, 0.0, pb.dt)
+    assert e.value.status == -5
+    g.adjoint_init(pb.jw, 2)
+    J1, g1 = g.adjoint_run(pb.nsteps, 0.0, pb.dt)
+    g.close()
+    assert J1 == J0
+    np.testing.assert_array_equal(g1, g0)
