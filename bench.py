@@ -265,40 +265,56 @@ def e2e(steps, warmup, dist=None):
     return dict(sec=sec, npts=npts, h2d=bytes_io, d2h=bytes_io)
 
 
-def adjoint_ratio(nsteps=0):
-    """Gradient time over forward time on the adjoint workload: unit PEC box,
-    8^3 elements, N=7, eps = 1 + 3 sigmoid(smooth random field, seed 4),
-    Gaussian E_z source, 2000 steps, J = sum bm1 |E|^2 over [0.7,0.9]^3.
-    Forward: nekgpu_time_steps of the FP64 fused form (CUDA events); gradient:
-    nekgpu_adjoint_gradient = forward pass with checkpoints + reverse sweep
-    (segment recompute included), its own CUDA-event times."""
+def adjoint_ratio(nsteps=0, case="adjoint", budget_mb=None):
+    """Gradient time over forward time.  Default: the adjoint workload (unit
+    PEC box, 8^3 elements, N=7, eps = 1 + 3 sigmoid(smooth random field, seed
+    4), Gaussian E_z source, 2000 steps, J = sum bm1 |E|^2 over [0.7,0.9]^3).
+    case="large": the 64^3-element N=7 box with its own eps, under a device
+    memory budget (NEKGPU_MEM_BUDGET_MB) that bounds the context and the
+    gradient together.  Forward: nekgpu_time_steps of the FP64 fused form
+    (CUDA events); gradient: nekgpu_adjoint_gradient, its own CUDA-event
+    times (forward part + reverse sweep, recomputation included)."""
     from nekcem_gb300 import MaxwellGPU, cases
-    c = cases.make("adjoint")
-    g0 = MaxwellGPU.from_box(c.N, c.nel, c.lo, c.hi, c.bc, form="fused64")
-    x, y, z = g0.coords()
-    bm1 = g0.array("bmn")
-    g0.close()
-    g = MaxwellGPU.from_box(c.N, c.nel, c.lo, c.hi, c.bc, form="fused64",
-                            permittivity=c.eps(x, y, z))
-    g.set_source(**c.source)
-    H0, E0 = c.init_fields(x, y, z)
-    (p0, p1), (q0, q1), (r0, r1) = c.extra["probe"]
-    inside = (x > p0) & (x < p1) & (y > q0) & (y < q1) & (z > r0) & (z < r1)
-    jw = np.where(inside, bm1, 0.0)
-    dt = c.timestep(x, y, z)
-    n = nsteps or c.nsteps
-    g.set_state(H0, E0)
-    g.time_steps(3, 0.0, dt)  # warm-up
-    g.set_state(H0, E0)
-    _, fwd_ms = g.time_steps(n, 0.0, dt)
-    g.set_state(H0, E0)
-    J, dJ, fwd_ckpt_ms, rev_ms = g.adjoint_gradient(n, 0.0, dt, jw)
-    g.close()
-    return {"workload": "adjoint box 8^3 el N=7 PEC, random eps, E_z source",
-            "steps": n, "forward_ms": fwd_ms, "gradient_ms": fwd_ckpt_ms + rev_ms,
-            "forward_with_checkpoints_ms": fwd_ckpt_ms, "reverse_sweep_ms": rev_ms,
-            "ratio": (fwd_ckpt_ms + rev_ms) / fwd_ms, "J": J,
-            "grad_norm": float(np.linalg.norm(dJ))}
+    c = cases.make(case)
+    old = os.environ.get("NEKGPU_MEM_BUDGET_MB")
+    if budget_mb:
+        os.environ["NEKGPU_MEM_BUDGET_MB"] = str(int(budget_mb))
+    try:
+        eps = case_eps(c)
+        g = MaxwellGPU.from_box(c.N, c.nel, c.lo, c.hi, c.bc, form="fused64", permittivity=eps)
+        x, y, z = g.coords()
+        bm1 = g.array("bmn")
+        if c.source:
+            g.set_source(**c.source)
+        H0, E0 = c.init_fields(x, y, z)
+        # probe box: the adjoint workload's; for the large box, around its pulse
+        probe = ((0.4, 0.6),) * 3 if case == "large" else cases.make("adjoint").extra["probe"]
+        (p0, p1), (q0, q1), (r0, r1) = probe
+        inside = (x > p0) & (x < p1) & (y > q0) & (y < q1) & (z > r0) & (z < r1)
+        jw = np.where(inside, bm1, 0.0)
+        dt = c.timestep(x, y, z)
+        n = nsteps or c.nsteps
+        g.set_state(H0, E0)
+        g.time_steps(3, 0.0, dt)  # warm-up
+        g.set_state(H0, E0)
+        _, fwd_ms = g.time_steps(n, 0.0, dt)
+        g.set_state(H0, E0)
+        J, dJ, fwd_part_ms, rev_ms = g.adjoint_gradient(n, 0.0, dt, jw)
+        g.close()
+    finally:
+        if budget_mb:
+            if old is None:
+                os.environ.pop("NEKGPU_MEM_BUDGET_MB", None)
+            else:
+                os.environ["NEKGPU_MEM_BUDGET_MB"] = old
+    out = {"workload": WORKLOADS.get(case, "adjoint box 8^3 el N=7 PEC, random eps, E_z source"),
+           "steps": n, "forward_ms": fwd_ms, "gradient_ms": fwd_part_ms + rev_ms,
+           "gradient_forward_part_ms": fwd_part_ms, "reverse_sweep_ms": rev_ms,
+           "ratio": (fwd_part_ms + rev_ms) / fwd_ms, "J": J,
+           "grad_norm": float(np.linalg.norm(dJ))}
+    if budget_mb:
+        out["device_memory_budget_bytes"] = int(budget_mb) << 20
+    return out
 
 
 def cpu_sample(steps):
@@ -431,6 +447,9 @@ def main():
             out["l2_mixed_vs_fused64"] = {"steps": n, "relative_l2": l2_between(fin_m, fin_d)}
     if not args.no_adjoint and world == 1 and CASE == "planewave":
         out["adjoint"] = adjoint_ratio(args.adjoint_steps)
+    if not args.no_adjoint and world == 1 and CASE == "large":
+        # 180 GB (171,661 MiB) for the context and the gradient together
+        out["adjoint"] = adjoint_ratio(args.adjoint_steps or 10, case="large", budget_mb=171661)
     if not args.no_cpu and world == 1 and npts <= 10_000_000:
         cpu = cpu_sample(max(2, min(20, args.steps // 10)))
         out["cpu_baseline"] = {"value": cpu["value"], "unit": UNIT, "cores": cpu["threads"],

@@ -221,11 +221,18 @@ int nekgpu_check_blowup(nekgpu_ctx* ctx);
  * adjoint of nsteps RK45 steps of the FP64 fused stage (cem_maxwell_op_rk,
  * src/cem_maxwell.F:327-345) for J = sum_n jw[n] |E(n)|^2 at the final time.
  * Starts from the context's current state and leaves it at the final state.
- * The state is checkpointed every `stride` steps (0: ceil(sqrt(nsteps))); the
- * reverse sweep recomputes one segment at a time and keeps its stage states
- * and RK registers.  Returns J, dJ/deps at every node (npts, host array) and
- * the device times of the forward pass and of the reverse sweep (recompute
- * included), in ms.  jw: npts host weights (e.g. bm1 on a probe region). */
+ * Schedules: stride > 0 checkpoints the state every `stride` steps and the
+ * reverse sweep recomputes one segment at a time, keeping its stage states
+ * and RK registers (ceil(nsteps/stride) + 4 x (5 stride + 1) + 4 states);
+ * stride = 0 does the same with stride = ceil(sqrt(nsteps)) when that fits in
+ * the device memory left (under NEKGPU_MEM_BUDGET_MB: the budget less the
+ * context's own memory), else falls back to the binomial schedule with the
+ * snapshots that fit; stride < 0 uses the binomial schedule with -stride
+ * snapshots (17 states + snapshots; forward steps recomputed more often).
+ * NEKGPU_ERR_NOMEM when the chosen schedule does not fit.  Returns J, dJ/deps
+ * at every node (npts, host array) and the device times up to J (forward)
+ * and of the rest (reverse sweep, recomputation included), in ms.
+ * jw: npts host weights (e.g. bm1 on a probe region). */
 int nekgpu_adjoint_gradient(nekgpu_ctx* ctx, int nsteps, double t0, double dt, const double* jw,
                             double* J, double* dJdeps, int stride, double* fwd_ms,
                             double* adj_ms);

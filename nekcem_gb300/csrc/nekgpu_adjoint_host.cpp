@@ -1,11 +1,18 @@
-// Driver of the discrete adjoint (nekgpu_adjoint_gradient): forward pass with
-// checkpoints every S steps, objective J = sum jw |E|^2, then a reverse sweep
-// that recomputes one segment at a time -- keeping every stage's state and RK
-// register of the segment -- and runs the reverse stages (nekgpu_adjoint.cu).
-// Memory: ceil(nsteps/S) checkpoints + 2*(5S+1) stage buffers + 5 states.
+// Driver of the discrete adjoint (nekgpu_adjoint_gradient).  J = sum jw |E|^2
+// at the final time; the reverse stages are in nekgpu_adjoint.cu.  Two
+// schedules, chosen by the device memory available:
+//  * sqrt(steps) checkpoints: the forward pass stores the state every S
+//    steps; the reverse sweep recomputes one segment at a time, keeping every
+//    stage's state and RK register of the segment, and runs its reverse
+//    stages (ceil(n/S) + 2 x 2 x (5S+1) + 4 states);
+//  * binomial snapshots when that does not fit: a revolve-type schedule over
+//    the snapshots that fit, with one step's stage storage (17 states +
+//    snapshots); more forward steps are recomputed.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <vector>
 
 #include "nekgpu_internal.h"
@@ -160,6 +167,7 @@ int build_adjoint_data(Context* c) {
     return NEKGPU_ERR_NOMEM;
   }
   c->allocs.push_back(pd);
+  c->dev_bytes += k.size() * 8;
   c->d_adj_slot = (double*)pd;
   if (check_cuda(cudaMemcpy(pd, k.data(), k.size() * 8, cudaMemcpyHostToDevice))) return NEKGPU_ERR_CUDA;
   return NEKGPU_OK;
@@ -198,168 +206,351 @@ int copy_state(Context* c, double* dst, const double* src) {
 
 }  // namespace
 
+namespace {
+
+// Device bytes a gradient evaluation may allocate: the free device memory
+// less a 1 GB margin, and under NEKGPU_MEM_BUDGET_MB what that budget leaves
+// after the context's own allocations.
+size_t adjoint_budget(const Context* c) {
+  size_t free_b = 0, total_b = 0;
+  if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) {
+    cudaGetLastError();
+    free_b = 0;
+  }
+  size_t avail = free_b > (size_t(1) << 30) ? free_b - (size_t(1) << 30) : 0;
+  if (const char* b = std::getenv("NEKGPU_MEM_BUDGET_MB")) {
+    const size_t budget = (size_t)std::atoll(b) << 20;
+    avail = std::min(avail, budget > c->dev_bytes ? budget - c->dev_bytes : size_t(0));
+  }
+  return avail;
+}
+
+// beta(s, t) = C(s + t, s): steps a binomial schedule with s free snapshots
+// reverses with at most t recomputations of each step
+double beta(int s, int t) {
+  double r = 1.0;
+  for (int i = 1; i <= s; ++i) r = r * (t + i) / i;
+  return r;
+}
+
+// State shared by the reverse sweeps of one gradient evaluation.
+struct Sweep {
+  Context* c;
+  int nsteps;
+  double dt;
+  const double* jw;
+  std::vector<double> tstep;  // time at the start of each step (time += dt, as nekgpu_step)
+  double* ub[2];
+  double* wb[2];
+  double* deps;
+  int cu = 0;
+  AdjointDev a{};
+  double J = 0.0;
+  bool seeded = false;
+
+  // J and the adjoint seed from the final state: ub = (0, 2 jw E), w = b_5 dt M^-1 ub
+  int seed(const double* u_final) {
+    const long npts = c->npts, ns = 6 * npts;
+    std::vector<double> uf(ns), ubf(ns, 0.0);
+    if (check_cuda(cudaMemcpyAsync(uf.data(), u_final, ns * 8, cudaMemcpyDeviceToHost, c->stream)) ||
+        check_cuda(cudaStreamSynchronize(c->stream)))
+      return NEKGPU_ERR_CUDA;
+    double Jv = 0.0;
+    for (int q = 3; q < 6; ++q)
+      for (long g = 0; g < npts; ++g) {
+        const double e = uf[q * npts + g];
+        Jv += jw[g] * e * e;
+        ubf[q * npts + g] = 2.0 * jw[g] * e;
+      }
+    J = Jv;
+    if (check_cuda(cudaMemcpyAsync(ub[0], ubf.data(), ns * 8, cudaMemcpyHostToDevice, c->stream)) ||
+        check_cuda(cudaMemsetAsync(deps, 0, npts * 8, c->stream)) ||
+        check_cuda(cudaStreamSynchronize(c->stream)))
+      return NEKGPU_ERR_CUDA;
+    cu = 0;
+    seeded = true;
+    return adjoint_seed(c, wb[0], ub[0], c->rk_b[4]);
+  }
+
+  // the five reverse stages of step j from its stage states (U[0..4]) and
+  // RK registers (K[1..5])
+  int reverse_step(double* const* U, double* const* K) {
+    for (int r = 5; r >= 1; --r) {
+      a.ub_in = ub[cu];
+      a.ub_out = ub[cu ^ 1];
+      a.w_in = wb[cu];
+      a.w_out = wb[cu ^ 1];
+      a.u_prev = U[r - 1];
+      a.k_cur = K[r];
+      a.k_prev = K[r - 1];
+      a.a = c->rk_a[r - 1];
+      a.b_next = c->rk_b[r == 1 ? 4 : r - 2];
+      int st = adjoint_stage(c, a);
+      if (st) return st;
+      cu ^= 1;
+    }
+    return NEKGPU_OK;
+  }
+
+  void init_args() {
+    a.nelt = c->nelt;
+    a.npts = c->npts;
+    a.coef = c->d_coef;
+    a.bm1 = c->d_bm1;
+    a.deps = deps;
+    a.nbr = c->d_nbr;
+    a.egeom = c->d_egeom;
+    a.slot = c->d_adj_slot;
+    a.inv_dt = 1.0 / dt;
+    const int n = c->nx;
+    for (int i = 0; i < n; ++i) {
+      a.w[i] = c->fargs.w[i];
+      for (int m = 0; m < n; ++m) a.Dw[m + n * i] = c->fargs.D[m + n * i] * c->fargs.w[m];
+    }
+  }
+};
+
+// Binomial (revolve-type) schedule for meshes whose sqrt(steps) segment
+// storage does not fit: snapshots of the state at chosen steps, one step's
+// stage storage, and the forward steps between snapshots recomputed.
+struct Binomial {
+  Sweep& w;
+  std::vector<double*> free_slots;
+  double* SU[6];  // stage states of one step: SU[0] is the step's start state, SU[5] its end
+  double* SK[6];  // RK registers: SK[0] is read (never used) by stage 1
+  double* scratch;      // a recomputed step start when no snapshot is free
+  double* final_state;  // u(T), put back in the context at the end
+  cudaEvent_t ev_seed = nullptr;
+
+  int advance(const double* src, int j0, int k, double* dst) {
+    Context* c = w.c;
+    int st = copy_state(c, c->d_u[c->cur], src);
+    for (int j = j0; j < j0 + k && !st; ++j)
+      for (int r = 1; r <= 5 && !st; ++r) st = fused_stage(c, r, w.tstep[j], w.dt);
+    if (!st) st = copy_state(c, dst, c->d_u[c->cur]);
+    return st;
+  }
+
+  int step(int j, double* src) {
+    Context* c = w.c;
+    SU[0] = src;
+    int st = NEKGPU_OK;
+    for (int r = 1; r <= 5 && !st; ++r)
+      st = fused_stage_buffers(c, r, w.tstep[j], w.dt, SU[r - 1], SU[r], SK[r - 1], SK[r]);
+    if (st) return st;
+    if (!w.seeded) {  // the first step reversed is the last one: its output is u(T)
+      if ((st = copy_state(c, final_state, SU[5])) || (st = w.seed(SU[5]))) return st;
+      if (check_cuda(cudaEventRecord(ev_seed, c->stream))) return NEKGPU_ERR_CUDA;
+    }
+    return w.reverse_step(SU, SK);
+  }
+
+  // reverse steps b-1 .. a; the state at step a is in `sa`; s free snapshots
+  int rev(int a, int b, double* sa, int s) {
+    const int n = b - a;
+    if (n == 1) return step(a, sa);
+    if (s == 0 || free_slots.empty()) {
+      for (int j = b - 1; j >= a; --j) {
+        int st = j > a ? advance(sa, a, j - a, scratch) : NEKGPU_OK;
+        if (!st) st = step(j, j > a ? scratch : sa);
+        if (st) return st;
+      }
+      return NEKGPU_OK;
+    }
+    int t = 1;
+    while (beta(s, t) < n) ++t;
+    const int right = (int)std::min<double>(beta(s - 1, t), (double)(n - 1));
+    const int m = b - right;
+    double* sm = free_slots.back();
+    free_slots.pop_back();
+    int st = advance(sa, a, m - a, sm);
+    if (!st) st = rev(m, b, sm, s - 1);
+    free_slots.push_back(sm);
+    if (!st) st = rev(a, m, sa, s);
+    return st;
+  }
+};
+
+}  // namespace
+
 extern "C" int nekgpu_adjoint_gradient(nekgpu_ctx* c, int nsteps, double t0, double dt,
                                        const double* jw, double* J, double* dJdeps, int stride,
                                        double* fwd_ms, double* adj_ms) {
-  if (!c || !jw || !J || !dJdeps || nsteps < 1 || stride < 0) return NEKGPU_ERR_ARG;
+  if (!c || !jw || !J || !dJdeps || nsteps < 1) return NEKGPU_ERR_ARG;
   if (c->form != NEKGPU_FUSED64) return NEKGPU_ERR_UNSUPPORTED;
   if (!c->have_state) return NEKGPU_ERR_STATE;
   int st = build_adjoint_data(c);
   if (st) return st;
   const long npts = c->npts, ns = 6 * npts;
+  const double state_b = (double)ns * 8;
+
+  // ---- memory plan ----------------------------------------------------------------
+  // sqrt scheme: ceil(n/S) checkpoints + sets x 2 x (5S+1) segment states +
+  // 4 adjoint states; binomial scheme: 4 adjoint + 11 stage + 2 states +
+  // snapshots.  Both also hold dJ/deps (npts doubles).
+  // stride > 0: segments of `stride` steps; 0: sqrt(steps) segments if they
+  // fit, else the binomial schedule with the snapshots that fit; < 0: the
+  // binomial schedule with -stride snapshots.
+  const double avail = (double)adjoint_budget(c) - (double)npts * 8;
   const int S = stride > 0 ? stride : (int)std::ceil(std::sqrt((double)nsteps));
   const int nseg = (nsteps + S - 1) / S;
-  Scratch mem;
-  std::vector<double*> ckpt(nseg);
-  for (auto& p : ckpt)
-    if (!(p = mem.get(ns))) return NEKGPU_ERR_NOMEM;
-  double* ub[2] = {mem.get(ns), mem.get(ns)};
-  double* wb[2] = {mem.get(ns), mem.get(ns)};
-  double* deps = mem.get(npts);
-  if (!ub[0] || !ub[1] || !wb[0] || !wb[1] || !deps) return NEKGPU_ERR_NOMEM;
-  // segment storage: stage states U and RK registers K of one segment; a
-  // second set (when it fits) lets the recompute of the next segment run on a
-  // second stream while the reverse stages of this one run
-  std::vector<double*> U[2], K[2];
+  auto sqrt_states = [&](int sets) { return (double)nseg + 4.0 + sets * 2.0 * (5.0 * S + 1.0); };
   int nsets = 0;
-  for (int b = 0; b < 2; ++b) {
-    U[b].resize(5 * S + 1);
-    K[b].resize(5 * S + 1);
-    bool ok = true;
-    for (int i = 0; i <= 5 * S && ok; ++i) ok = (U[b][i] = mem.get(ns)) && (K[b][i] = mem.get(ns));
-    if (!ok) break;
-    ++nsets;
+  if (stride >= 0) {
+    if (sqrt_states(2) * state_b <= avail) nsets = 2;
+    else if (sqrt_states(1) * state_b <= avail) nsets = 1;
+    else if (stride > 0) return NEKGPU_ERR_NOMEM;  // the caller fixed the stride
   }
-  if (nsets == 0) return NEKGPU_ERR_NOMEM;
-  StreamPair sp;
-  if (nsets == 2 && !sp.create()) nsets = 1;
+  int nslots = 0;
+  if (nsets == 0) {
+    const double fit = std::floor(avail / state_b - 17.0);
+    nslots = (int)std::min<double>(stride < 0 ? -(double)stride : fit, (double)nsteps);
+    if (nslots < 1 || nslots > fit) return NEKGPU_ERR_NOMEM;
+  }
+
+  Scratch mem;
+  Sweep w{c, nsteps, dt, jw};
+  w.tstep.resize(nsteps);
+  {
+    double t = t0;
+    for (int n = 0; n < nsteps; ++n) {
+      w.tstep[n] = t;
+      t = t + dt;
+    }
+  }
+  w.ub[0] = mem.get(ns);
+  w.ub[1] = mem.get(ns);
+  w.wb[0] = mem.get(ns);
+  w.wb[1] = mem.get(ns);
+  w.deps = mem.get(npts);
+  if (!w.ub[0] || !w.ub[1] || !w.wb[0] || !w.wb[1] || !w.deps) return NEKGPU_ERR_NOMEM;
+  w.init_args();
   if ((st = scale_coef(c, dt))) return st;
+  float f_ms = 0, a_ms = 0;
 
-  // ---- forward pass with checkpoints ------------------------------------------
-  std::vector<double> tstep(nsteps);
-  double t = t0;
-  if (check_cuda(cudaEventRecord(c->ev0, c->stream))) return NEKGPU_ERR_CUDA;
-  for (int n = 0; n < nsteps; ++n) {
-    if (n % S == 0 && (st = copy_state(c, ckpt[n / S], c->d_u[c->cur]))) return st;
-    tstep[n] = t;
+  if (nsets == 0) {
+    // ---- binomial schedule -------------------------------------------------------
+    Binomial bs{w};
     for (int r = 1; r <= 5; ++r)
-      if ((st = fused_stage(c, r, t, dt))) return st;
-    t = t + dt;
-  }
-  if (check_cuda(cudaEventRecord(c->ev1, c->stream)) || check_cuda(cudaEventSynchronize(c->ev1)))
-    return NEKGPU_ERR_CUDA;
-  float f_ms = 0;
-  cudaEventElapsedTime(&f_ms, c->ev0, c->ev1);
-
-  // ---- objective and its gradient with respect to the final state -----------
-  std::vector<double> uf(ns), ubf(ns, 0.0);
-  if (check_cuda(cudaMemcpy(uf.data(), c->d_u[c->cur], ns * 8, cudaMemcpyDeviceToHost)))
-    return NEKGPU_ERR_CUDA;
-  double Jv = 0.0;
-  for (int q = 3; q < 6; ++q)
-    for (long g = 0; g < npts; ++g) {
-      const double e = uf[q * npts + g];
-      Jv += jw[g] * e * e;
-      ubf[q * npts + g] = 2.0 * jw[g] * e;
-    }
-  if (check_cuda(cudaMemcpyAsync(ub[0], ubf.data(), ns * 8, cudaMemcpyHostToDevice, c->stream)) ||
-      check_cuda(cudaMemsetAsync(deps, 0, npts * 8, c->stream)))
-    return NEKGPU_ERR_CUDA;
-  if ((st = adjoint_seed(c, wb[0], ub[0], c->rk_b[4]))) return st;
-
-  // ---- reverse sweep ------------------------------------------------------------
-  AdjointDev a{};
-  a.nelt = c->nelt;
-  a.npts = npts;
-  a.coef = c->d_coef;
-  a.bm1 = c->d_bm1;
-  a.deps = deps;
-  a.nbr = c->d_nbr;
-  a.egeom = c->d_egeom;
-  a.slot = c->d_adj_slot;
-  a.inv_dt = 1.0 / dt;
-  const int n = c->nx;
-  for (int i = 0; i < n; ++i) {
-    a.w[i] = c->fargs.w[i];
-    for (int m = 0; m < n; ++m) a.Dw[m + n * i] = c->fargs.D[m + n * i] * c->fargs.w[m];
-  }
-  int cu = 0;
-  cudaStream_t main_stream = c->stream;
-  // recompute of segment seg into buffer set b, on stream `on`
-  auto recompute = [&](int seg, int b, cudaStream_t on) -> int {
-    const int n0 = seg * S, nS = std::min(S, nsteps - n0);
-    c->stream = on;
-    int r = copy_state(c, U[b][0], ckpt[seg]);
-    for (int s = 0; s < nS && !r; ++s)
-      for (int q = 1; q <= 5 && !r; ++q) {
-        const int i = 5 * s + q;
-        r = fused_stage_buffers(c, q, tstep[n0 + s], dt, U[b][i - 1], U[b][i], K[b][i - 1], K[b][i]);
-      }
-    c->stream = main_stream;
-    return r;
-  };
-  auto reverse = [&](int seg, int b) -> int {
-    const int n0 = seg * S, nS = std::min(S, nsteps - n0);
-    for (int s = nS - 1; s >= 0; --s)
-      for (int r = 5; r >= 1; --r) {
-        const int i = 5 * s + r;
-        a.ub_in = ub[cu];
-        a.ub_out = ub[cu ^ 1];
-        a.w_in = wb[cu];
-        a.w_out = wb[cu ^ 1];
-        a.u_prev = U[b][i - 1];
-        a.k_cur = K[b][i];
-        a.k_prev = K[b][i - 1];
-        a.a = c->rk_a[r - 1];
-        a.b_next = c->rk_b[r == 1 ? 4 : r - 2];
-        int st2 = adjoint_stage(c, a);
-        if (st2) return st2;
-        cu ^= 1;
-      }
-    return NEKGPU_OK;
-  };
-  if (check_cuda(cudaEventRecord(c->ev0, c->stream))) return NEKGPU_ERR_CUDA;
-  if (nsets == 1) {
-    for (int seg = nseg - 1; seg >= 0; --seg)
-      if ((st = recompute(seg, 0, main_stream)) || (st = reverse(seg, 0))) return st;
+      if (!(bs.SU[r] = mem.get(ns))) return NEKGPU_ERR_NOMEM;
+    for (int r = 0; r <= 5; ++r)
+      if (!(bs.SK[r] = mem.get(ns))) return NEKGPU_ERR_NOMEM;
+    if (!(bs.scratch = mem.get(ns)) || !(bs.final_state = mem.get(ns))) return NEKGPU_ERR_NOMEM;
+    std::vector<double*> slots(nslots);
+    for (auto& p : slots)
+      if (!(p = mem.get(ns))) return NEKGPU_ERR_NOMEM;
+    bs.free_slots.assign(slots.begin() + 1, slots.end());
+    if (check_cuda(cudaEventCreate(&bs.ev_seed))) return NEKGPU_ERR_CUDA;
+    struct EvGuard {
+      cudaEvent_t e;
+      ~EvGuard() { cudaEventDestroy(e); }
+    } guard{bs.ev_seed};
+    if (check_cuda(cudaEventRecord(c->ev0, c->stream))) return NEKGPU_ERR_CUDA;
+    if ((st = copy_state(c, slots[0], c->d_u[c->cur]))) return st;
+    if ((st = bs.rev(0, nsteps, slots[0], nslots - 1))) return st;
+    if ((st = copy_state(c, c->d_u[c->cur], bs.final_state))) return st;
+    if (check_cuda(cudaEventRecord(c->ev1, c->stream)) || check_cuda(cudaEventSynchronize(c->ev1)))
+      return NEKGPU_ERR_CUDA;
+    cudaEventElapsedTime(&f_ms, c->ev0, bs.ev_seed);
+    cudaEventElapsedTime(&a_ms, bs.ev_seed, c->ev1);
   } else {
-    // set b = seg & 1.  side stream: recompute(seg) after reverse(seg + 2)
-    // released set b; main stream: reverse(seg) after recompute(seg).
-    if (check_cuda(cudaStreamWaitEvent(sp.side, c->ev0, 0))) return NEKGPU_ERR_CUDA;
-    if ((st = recompute(nseg - 1, (nseg - 1) & 1, sp.side))) return st;
-    if (check_cuda(cudaEventRecord(sp.done_recompute[(nseg - 1) & 1], sp.side))) return NEKGPU_ERR_CUDA;
-    for (int seg = nseg - 1; seg >= 0; --seg) {
-      const int b = seg & 1;
-      if (seg > 0) {
-        const int bn = (seg - 1) & 1;
-        if (seg + 1 < nseg && check_cuda(cudaStreamWaitEvent(sp.side, sp.done_reverse[bn], 0)))
-          return NEKGPU_ERR_CUDA;
-        if ((st = recompute(seg - 1, bn, sp.side))) return st;
-        if (check_cuda(cudaEventRecord(sp.done_recompute[bn], sp.side))) return NEKGPU_ERR_CUDA;
-      }
-      if (check_cuda(cudaStreamWaitEvent(main_stream, sp.done_recompute[b], 0))) return NEKGPU_ERR_CUDA;
-      if ((st = reverse(seg, b))) return st;
-      if (check_cuda(cudaEventRecord(sp.done_reverse[b], main_stream))) return NEKGPU_ERR_CUDA;
+    // ---- sqrt(steps) checkpoints with segment storage ---------------------------
+    std::vector<double*> ckpt(nseg);
+    for (auto& p : ckpt)
+      if (!(p = mem.get(ns))) return NEKGPU_ERR_NOMEM;
+    // segment storage: stage states U and RK registers K of one segment; the
+    // second set lets the recompute of the next segment run on a second
+    // stream while the reverse stages of this one run
+    std::vector<double*> U[2], K[2];
+    for (int b = 0; b < nsets; ++b) {
+      U[b].resize(5 * S + 1);
+      K[b].resize(5 * S + 1);
+      for (int i = 0; i <= 5 * S; ++i)
+        if (!(U[b][i] = mem.get(ns)) || !(K[b][i] = mem.get(ns))) return NEKGPU_ERR_NOMEM;
     }
+    StreamPair sp;
+    if (nsets == 2 && !sp.create()) nsets = 1;
+
+    // forward pass with checkpoints
+    if (check_cuda(cudaEventRecord(c->ev0, c->stream))) return NEKGPU_ERR_CUDA;
+    for (int n = 0; n < nsteps; ++n) {
+      if (n % S == 0 && (st = copy_state(c, ckpt[n / S], c->d_u[c->cur]))) return st;
+      for (int r = 1; r <= 5; ++r)
+        if ((st = fused_stage(c, r, w.tstep[n], dt))) return st;
+    }
+    if (check_cuda(cudaEventRecord(c->ev1, c->stream)) || check_cuda(cudaEventSynchronize(c->ev1)))
+      return NEKGPU_ERR_CUDA;
+    cudaEventElapsedTime(&f_ms, c->ev0, c->ev1);
+    if ((st = w.seed(c->d_u[c->cur]))) return st;
+
+    cudaStream_t main_stream = c->stream;
+    // recompute of segment seg into buffer set b, on stream `on`
+    auto recompute = [&](int seg, int b, cudaStream_t on) -> int {
+      const int n0 = seg * S, nS = std::min(S, nsteps - n0);
+      c->stream = on;
+      int r = copy_state(c, U[b][0], ckpt[seg]);
+      for (int s2 = 0; s2 < nS && !r; ++s2)
+        for (int q = 1; q <= 5 && !r; ++q) {
+          const int i = 5 * s2 + q;
+          r = fused_stage_buffers(c, q, w.tstep[n0 + s2], dt, U[b][i - 1], U[b][i], K[b][i - 1],
+                                  K[b][i]);
+        }
+      c->stream = main_stream;
+      return r;
+    };
+    auto reverse = [&](int seg, int b) -> int {
+      const int n0 = seg * S, nS = std::min(S, nsteps - n0);
+      for (int s2 = nS - 1; s2 >= 0; --s2) {
+        const int st2 = w.reverse_step(&U[b][5 * s2], &K[b][5 * s2]);
+        if (st2) return st2;
+      }
+      return NEKGPU_OK;
+    };
+    if (check_cuda(cudaEventRecord(c->ev0, c->stream))) return NEKGPU_ERR_CUDA;
+    if (nsets == 1) {
+      for (int seg = nseg - 1; seg >= 0; --seg)
+        if ((st = recompute(seg, 0, main_stream)) || (st = reverse(seg, 0))) return st;
+    } else {
+      // set b = seg & 1.  side stream: recompute(seg) after reverse(seg + 2)
+      // released set b; main stream: reverse(seg) after recompute(seg).
+      if (check_cuda(cudaStreamWaitEvent(sp.side, c->ev0, 0))) return NEKGPU_ERR_CUDA;
+      if ((st = recompute(nseg - 1, (nseg - 1) & 1, sp.side))) return st;
+      if (check_cuda(cudaEventRecord(sp.done_recompute[(nseg - 1) & 1], sp.side)))
+        return NEKGPU_ERR_CUDA;
+      for (int seg = nseg - 1; seg >= 0; --seg) {
+        const int b = seg & 1;
+        if (seg > 0) {
+          const int bn = (seg - 1) & 1;
+          if (seg + 1 < nseg && check_cuda(cudaStreamWaitEvent(sp.side, sp.done_reverse[bn], 0)))
+            return NEKGPU_ERR_CUDA;
+          if ((st = recompute(seg - 1, bn, sp.side))) return st;
+          if (check_cuda(cudaEventRecord(sp.done_recompute[bn], sp.side))) return NEKGPU_ERR_CUDA;
+        }
+        if (check_cuda(cudaStreamWaitEvent(main_stream, sp.done_recompute[b], 0)))
+          return NEKGPU_ERR_CUDA;
+        if ((st = reverse(seg, b))) return st;
+        if (check_cuda(cudaEventRecord(sp.done_reverse[b], main_stream))) return NEKGPU_ERR_CUDA;
+      }
+    }
+    if (check_cuda(cudaEventRecord(c->ev1, c->stream)) || check_cuda(cudaEventSynchronize(c->ev1)))
+      return NEKGPU_ERR_CUDA;
+    cudaEventElapsedTime(&a_ms, c->ev0, c->ev1);
   }
-  if (check_cuda(cudaEventRecord(c->ev1, c->stream)) || check_cuda(cudaEventSynchronize(c->ev1)))
-    return NEKGPU_ERR_CUDA;
-  float a_ms = 0;
-  cudaEventElapsedTime(&a_ms, c->ev0, c->ev1);
-  if (check_cuda(cudaMemcpyAsync(dJdeps, deps, npts * 8, cudaMemcpyDeviceToHost, c->stream)) ||
+
+  if (check_cuda(cudaMemcpyAsync(dJdeps, w.deps, npts * 8, cudaMemcpyDeviceToHost, c->stream)) ||
       check_cuda(cudaStreamSynchronize(c->stream)))
     return NEKGPU_ERR_CUDA;
   int h = 0;
   if (check_cuda(cudaMemcpy(&h, c->d_status, sizeof(int), cudaMemcpyDeviceToHost))) return NEKGPU_ERR_CUDA;
   if (h) return NEKGPU_ERR_TIMEOUT;
-  *J = Jv;
+  *J = w.J;
   if (fwd_ms) *fwd_ms = f_ms;
   if (adj_ms) *adj_ms = a_ms;
   return NEKGPU_OK;
 }
 
 extern "C" int nekgpu_adjoint_init(nekgpu_ctx* c, const double* jw, int stride) {
-  if (!c || !jw || stride < 0) return NEKGPU_ERR_ARG;
+  if (!c || !jw) return NEKGPU_ERR_ARG;
   if (c->form != NEKGPU_FUSED64) return NEKGPU_ERR_UNSUPPORTED;
   c->adj_jw.assign(jw, jw + c->npts);
   c->adj_stride = stride;

@@ -170,6 +170,7 @@ struct DevAlloc {
       return NEKGPU_ERR_NOMEM;
     }
     used += bytes;
+    c->dev_bytes += bytes;
     c->allocs.push_back(q);
     *p = (T*)q;
     return NEKGPU_OK;

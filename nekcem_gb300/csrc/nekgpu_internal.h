@@ -158,6 +158,7 @@ struct Context {
   double* d_red = nullptr;     // reduction scratch
   int* d_status = nullptr;
   std::vector<void*> allocs;
+  size_t dev_bytes = 0;  // device bytes held in allocs
 
   // fused form
   double* d_coef = nullptr;   // 2*npts, dt-scaled

@@ -233,9 +233,11 @@ class MaxwellGPU:
     # ---- discrete adjoint (FP64 fused form) ------------------------------------
     def adjoint_gradient(self, nsteps: int, t0: float, dt: float, jw: np.ndarray, stride: int = 0):
         """J = sum_g jw[g] |E(g)|^2 after nsteps steps from the current state and
-        dJ/deps at every node, by the discrete adjoint with checkpoints every
-        ``stride`` steps (0: ceil(sqrt(nsteps))).  Leaves the final state in the
-        context.  Returns (J, dJdeps, forward_ms, adjoint_ms)."""
+        dJ/deps at every node, by the discrete adjoint.  ``stride`` > 0:
+        checkpoints every stride steps; 0: every ceil(sqrt(nsteps)) steps when
+        that fits in device memory, else the binomial schedule; < 0: the
+        binomial schedule with -stride snapshots.  Leaves the final state in
+        the context.  Returns (J, dJdeps, forward_ms, adjoint_ms)."""
         jw = np.ascontiguousarray(jw, dtype=np.float64).reshape(self.npts)
         out = np.empty(self.npts)
         J = C.c_double(); fms = C.c_double(); ams = C.c_double()

@@ -186,3 +186,34 @@ def test_adjoint_init_run_equals_gradient():
     g.close()
     assert J1 == J0
     np.testing.assert_array_equal(g1, g0)
+
+
+@pytest.mark.gpu
+def test_binomial_schedule_gives_the_same_gradient():
+    """Snapshot schedules (1, 2, 3 and 8 snapshots) against sqrt(steps)
+    segments: the same forward states and reverse stages in the same order,
+    so bit-identical gradients."""
+    pb, eps, _, _ = gpu_problem(4, (2, 2, 2), (PEC, PER, PEC), seed=71, nsteps=13)
+    J0, g0 = pb.gradient(eps)
+    for snaps in (1, 2, 3, 8):
+        pb.stride = -snaps
+        J1, g1 = pb.gradient(eps)
+        assert J1 == J0
+        np.testing.assert_array_equal(g1, g0, err_msg=f"{snaps} snapshots")
+
+
+@pytest.mark.gpu
+def test_memory_budget_selects_the_binomial_schedule(monkeypatch):
+    """Under a device-memory budget too small for the sqrt(steps) segment
+    storage the automatic schedule falls back to snapshots and gives the same
+    gradient; a forced stride that does not fit is refused."""
+    pb, eps, _, _ = gpu_problem(7, (4, 4, 4), (PEC, PEC, PEC), seed=81, nsteps=64)
+    J0, g0 = pb.gradient(eps)  # no budget: sqrt(64) = 8-step segments
+    monkeypatch.setenv("NEKGPU_MEM_BUDGET_MB", "120")  # segments need ~150-280 MB
+    J1, g1 = pb.gradient(eps)
+    assert J1 == J0
+    np.testing.assert_array_equal(g1, g0)
+    pb.stride = 8
+    with pytest.raises(L.NekgpuError) as e:
+        pb.gradient(eps)
+    assert e.value.status == -4
