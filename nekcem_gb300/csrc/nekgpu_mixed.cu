@@ -114,6 +114,11 @@ __device__ __forceinline__ void tma_load_1d(void* dst, const void* src, unsigned
       "l"(src), "r"(bytes), "r"(smem_addr(bar))
       : "memory");
 }
+// bulk prefetch of a global range into L2 (a hint: no completion to wait for);
+// address and size multiples of 16 bytes
+__device__ __forceinline__ void prefetch_l2(const void* src, unsigned bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(src), "r"(bytes) : "memory");
+}
 __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
   unsigned ok;
   asm volatile(
@@ -315,6 +320,11 @@ __global__ void __launch_bounds__(MCfg<NX>::NT, 3) k_mixed_stage(const MixedDev 
     const unsigned bytes = N3 * 8;
     mbar_expect_tx(bar, 6u * bytes);
     for (int c = 0; c < 6; ++c) tma_load_1d(s_u64 + c * N3, a.u_in + c * P + (long)e * N3, bytes, bar);
+    // the RK register and the coefficients are read at the end of the
+    // element's turn: start bringing them into L2 now
+    if (!first_stage)
+      for (int c = 0; c < 6; ++c) prefetch_l2(a.k + c * P + (long)e * N3, bytes);
+    for (int c = 0; c < 2; ++c) prefetch_l2(a.coef + c * P + (long)e * N3, N3 * 8u);
   };
   unsigned parity = 0;
   if (C::kTma && tid == 0 && blockIdx.x < a.nelt) issue_tma(blockIdx.x);
