@@ -54,6 +54,7 @@ extern "C" {
 /* Face boundary codes (CBC in src/cem_maxwell.F:289-300, 1338-1366). */
 #define NEKGPU_BC_PEC 0
 #define NEKGPU_BC_PERIODIC 1
+#define NEKGPU_BC_PML 2      /* 'PML' faces: a PEC wall behind perfectly matched layers */
 
 typedef struct nekgpu_ctx nekgpu_ctx;
 
@@ -95,6 +96,12 @@ typedef struct nekgpu_mesh {
   const double* ebm1;      /* npts 1/(eps*bm1) (src/cem_maxwell.F:183-186) */
   const double* hbm1;      /* npts 1/(mu*bm1) */
   double C0;               /* 1 upwind, 0 central (src/cem_maxwell.F:939-940) */
+  /* PML (src/cem_maxwell_pml.F; NULL / 0 without PML): */
+  const double* pmlsigma;  /* 3*npts sigma x, y, z of pml_calc_sigma (:433-506) */
+  const int* pmlptr;       /* npml 1-based PML elements (pmlptr of pml_calc_sigma) */
+  int npml;
+  const double* permittivity; /* npts per node (needed with PML) */
+  const double* permeability;
 } nekgpu_mesh;
 
 /*
@@ -106,10 +113,15 @@ typedef struct nekgpu_box {
   int N;                   /* polynomial order (nx1 = N+1), 1..15 */
   int nelx, nely, nelz;
   double lo[3], hi[3];     /* domain [lo,hi] per axis */
-  int bc[3];               /* NEKGPU_BC_PEC or NEKGPU_BC_PERIODIC per axis */
+  int bc[3];               /* NEKGPU_BC_PEC, _PERIODIC or _PML per axis */
   const double* permittivity; /* npts per node, or NULL for 1 */
   const double* permeability; /* npts per node, or NULL for 1 */
   double C0;               /* 1 upwind, 0 central */
+  /* PML layers behind NEKGPU_BC_PML faces (params 77-79 of the .rea file,
+   * src/cem_param.F:84-86): thickness in element layers (1..10), polynomial
+   * order of the sigma grading, reflection error */
+  int pml_thick;
+  double pml_order, pml_referr;
 } nekgpu_box;
 
 const char* nekgpu_error_string(int status);
@@ -134,9 +146,10 @@ int nekgpu_finalize(nekgpu_ctx* ctx);
 /* Host-only (no GPU needed): the box builder's reference-layout arrays, for
  * checking the host setup.  Double arrays: "dxm1" (nx1^2), "w3mn" (nx1^3),
  * "bmn","xmn","ymn","zmn","rxmn","symn","tzmn","ebm1","hbm1" (npts),
- * "unxm","unym","unzm","aream","Z_0","Z_1","Y_0","Y_1" (nxzfl).  Integer
- * arrays: "cemface" (nxzfl, 1-based), "glo_face" (nxzfl), "cempec" (1-based,
- * *count entries).  *count receives the number of entries written. */
+ * "unxm","unym","unzm","aream","Z_0","Z_1","Y_0","Y_1" (nxzfl), "pmlsigma"
+ * (3*npts with PML, else empty).  Integer arrays: "cemface" (nxzfl, 1-based),
+ * "glo_face" (nxzfl), "cempec" (1-based, *count entries), "pmlptr" (1-based
+ * PML elements).  *count receives the number of entries written. */
 int nekgpu_box_export_d(const nekgpu_box* box, const char* name, double* out, long* count);
 int nekgpu_box_export_i(const nekgpu_box* box, const char* name, long long* out, long* count);
 
@@ -144,10 +157,15 @@ int nekgpu_box_export_i(const nekgpu_box* box, const char* name, long long* out,
 int nekgpu_sizes(const nekgpu_ctx* ctx, long* npts, long* nxzfl, int* nelt, int* nx1);
 /* the box builder's arrays (reference layout), for users that need
  * coordinates / mass without the Fortran side: name in
- * {"xmn","ymn","zmn","bmn","ebm1","hbm1"}; out has npts doubles */
+ * {"xmn","ymn","zmn","bmn","ebm1","hbm1"}; out has npts doubles.  With PML:
+ * "pmlbn", "pmldn" (the auxiliary fields, 3*npts, zero outside the PML) and
+ * "pmlsigma" (3*npts). */
 int nekgpu_get_array(nekgpu_ctx* ctx, const char* name, double* out);
 double nekgpu_volume(const nekgpu_ctx* ctx);
 
+/* Time function of the source: 0 = Ricker (default), 1 = amp * sin(f0 * t)
+ * (the Gaussian dipole of tests/3dboxpml/3dboxpml.usr:28-85, omega = f0). */
+int nekgpu_set_source_kind(nekgpu_ctx* ctx, int kind);
 /* Gaussian-in-space, Ricker-in-time E_z volume source in mass-weighted form,
  * added before the inverse mass like usersrc (src/cem_maxwell.F:503):
  * resEz += bm1 * amp * exp(-|x-xc|^2/(2 sigma^2)) * ricker(t; f0, t0),

@@ -37,6 +37,8 @@ class NekgpuMesh(C.Structure):
         ("cemface", ip), ("glo_face", lp), ("cempec", ip), ("ncempec", C.c_int),
         ("Z_0", dp), ("Z_1", dp), ("Y_0", dp), ("Y_1", dp),
         ("ebm1", dp), ("hbm1", dp), ("C0", C.c_double),
+        ("pmlsigma", dp), ("pmlptr", ip), ("npml", C.c_int),
+        ("permittivity", dp), ("permeability", dp),
     ]
 
 
@@ -45,6 +47,7 @@ class NekgpuBox(C.Structure):
         ("N", C.c_int), ("nelx", C.c_int), ("nely", C.c_int), ("nelz", C.c_int),
         ("lo", C.c_double * 3), ("hi", C.c_double * 3), ("bc", C.c_int * 3),
         ("permittivity", dp), ("permeability", dp), ("C0", C.c_double),
+        ("pml_thick", C.c_int), ("pml_order", C.c_double), ("pml_referr", C.c_double),
     ]
 
 
@@ -67,6 +70,7 @@ SIGNATURES = [
     ("nekgpu_sizes", C.c_int, [C.c_void_p, C.POINTER(C.c_long), C.POINTER(C.c_long), ip, ip]),
     ("nekgpu_get_array", C.c_int, [C.c_void_p, C.c_char_p, dp]),
     ("nekgpu_volume", C.c_double, [C.c_void_p]),
+    ("nekgpu_set_source_kind", C.c_int, [C.c_void_p, C.c_int]),
     ("nekgpu_set_source", C.c_int, [C.c_void_p, C.c_int, dp, C.c_double, C.c_double, C.c_double, C.c_double]),
     ("nekgpu_set_state", C.c_int, [C.c_void_p, dp, dp, C.c_long]),
     ("nekgpu_get_state", C.c_int, [C.c_void_p, dp, dp, C.c_long]),

@@ -169,7 +169,7 @@ struct Cfg {
   static constexpr int kMinBlocks = kMixed ? (NT <= 256 ? 4 : (NT <= 512 ? 2 : 1)) : 1;
 };
 
-template <int NX, typename T>
+template <int NX, typename T, bool PML>
 __global__ void __launch_bounds__(Cfg<NX, T>::NT, Cfg<NX, T>::kMinBlocks)
     k_fused_stage(const FusedDev a) {
   using C = Cfg<NX, T>;
@@ -387,6 +387,50 @@ __global__ void __launch_bounds__(Cfg<NX, T>::NT, Cfg<NX, T>::kMinBlocks)
       if (vi == 0) add(3, vj + NX * vk);
       if (vk == 0) add(4, vi + NX * vj);
       if (vk == NX - 1) add(5, vi + NX * vj);
+      // ---- PML (pml_step, src/cem_maxwell_pml.F:508-590), FP64 form only:
+      // auxiliary residuals from the residual so far, their RK update
+      // (src/cem_maxwell.F:1942-1955), and their contribution to res
+      if (PML && !C::kMixed) {
+        const int l = a.pml.slot[e];
+        if (l >= 0) {
+          const long nn = a.pml.n, q = (long)l * N3 + tid;
+          const double* pd = a.pml.data;
+          const double sxp = pd[q], syp = pd[nn + q], szp = pd[2 * nn + q];
+          const double sigx = pd[3 * nn + q], sigy = pd[4 * nn + q], sigz = pd[5 * nn + q];
+          const double mu = pd[6 * nn + q], bm1 = pd[7 * nn + q], bm1inv = pd[8 * nn + q];
+          double* aux = a.pml.aux;
+          double* kx = a.pml.k;
+          const double bn[3] = {aux[q], aux[nn + q], aux[2 * nn + q]};
+          const double dn[3] = {aux[3 * nn + q], aux[4 * nn + q], aux[5 * nn + q]};
+          const double* hn = s_u64;
+          const double* en = s_u64 + 3 * N3;
+          double rp[6];
+          rp[0] = (double)res[0] * bm1inv - syp * bn[0];
+          rp[1] = (double)res[1] * bm1inv - szp * bn[1];
+          rp[2] = (double)res[2] * bm1inv - sxp * bn[2];
+          rp[3] = (double)res[3] * bm1inv - syp * dn[0];
+          rp[4] = (double)res[4] * bm1inv - szp * dn[1];
+          rp[5] = (double)res[5] * bm1inv - sxp * dn[2];
+          const double rh0 = -syp * bn[0] + sxp * bn[0] - szp * mu * hn[tid];
+          const double rh1 = -szp * bn[1] + syp * bn[1] - sxp * mu * hn[N3 + tid];
+          const double rh2 = -sxp * bn[2] + szp * bn[2] - syp * mu * hn[2 * N3 + tid];
+          const double re0 = -syp * dn[0] + sxp * dn[0] - sigz * en[tid];
+          const double re1 = -szp * dn[1] + syp * dn[1] - sigx * en[N3 + tid];
+          const double re2 = -sxp * dn[2] + szp * dn[2] - sigy * en[2 * N3 + tid];
+          res[0] = (T)((double)res[0] + rh0 * bm1);
+          res[1] = (T)((double)res[1] + rh1 * bm1);
+          res[2] = (T)((double)res[2] + rh2 * bm1);
+          res[3] = (T)((double)res[3] + re0 * bm1);
+          res[4] = (T)((double)res[4] + re1 * bm1);
+          res[5] = (T)((double)res[5] + re2 * bm1);
+#pragma unroll
+          for (int cc = 0; cc < 6; ++cc) {
+            const double kv = first_stage ? a.dt * rp[cc] : fma(a.a, kx[cc * nn + q], a.dt * rp[cc]);
+            kx[cc * nn + q] = kv;
+            aux[cc * nn + q] = fma(a.b, kv, cc < 3 ? bn[cc] : dn[cc - 3]);
+          }
+        }
+      }
       // ---- volume source (usersrc), mass-weighted -------------------------
       if (a.src_elem) {
         const int so = a.src_elem[e];
@@ -429,10 +473,12 @@ __global__ void k_scale_coef(double* coef, const double* base, long n2, double d
   coef[i] = dt * base[i];
 }
 
-template <int NX, typename T>
+// PML: the variant with the PML branch (a separate instantiation, so that
+// meshes without PML keep the kernel's register budget)
+template <int NX, typename T, bool PML>
 int launch(Context* c, const FusedDev& a) {
   using C = Cfg<NX, T>;
-  auto kern = k_fused_stage<NX, T>;
+  auto kern = k_fused_stage<NX, T, PML>;
   static bool ready = false;
   static int grid = 0;
   if (!ready) {
@@ -454,18 +500,23 @@ int launch(Context* c, const FusedDev& a) {
   return check_cuda(cudaGetLastError());
 }
 
-template <typename T>
-int dispatch(Context* c, const FusedDev& a) {
+template <typename T, bool PML>
+int dispatch_nx(Context* c, const FusedDev& a) {
   switch (c->nx) {
-    case 3: return launch<3, T>(c, a);
-    case 4: return launch<4, T>(c, a);
-    case 5: return launch<5, T>(c, a);
-    case 6: return launch<6, T>(c, a);
-    case 7: return launch<7, T>(c, a);
-    case 8: return launch<8, T>(c, a);
-    case 9: return launch<9, T>(c, a);
+    case 3: return launch<3, T, PML>(c, a);
+    case 4: return launch<4, T, PML>(c, a);
+    case 5: return launch<5, T, PML>(c, a);
+    case 6: return launch<6, T, PML>(c, a);
+    case 7: return launch<7, T, PML>(c, a);
+    case 8: return launch<8, T, PML>(c, a);
+    case 9: return launch<9, T, PML>(c, a);
     default: return NEKGPU_ERR_UNSUPPORTED;
   }
+}
+
+template <typename T>
+int dispatch(Context* c, const FusedDev& a) {
+  return a.pml.slot ? dispatch_nx<T, true>(c, a) : dispatch_nx<T, false>(c, a);
 }
 
 }  // namespace
@@ -491,11 +542,9 @@ int fused_stage_buffers(Context* c, int rkstep, double time, double dt, const do
   a.k_out = k_out;
   a.a = c->rk_a[rkstep - 1];
   a.b = c->rk_b[rkstep - 1];
+  a.dt = dt;
   if (c->src.enabled) {
-    const double rktime = time + dt * c->rk_c[rkstep - 1];
-    const double pi = 4.0 * atan(1.0);
-    const double x = pi * c->src.f0 * (rktime - c->src.t0);
-    a.src_ft = c->src.amp * (1.0 - 2.0 * x * x) * exp(-x * x);
+    a.src_ft = source_ft(c->src, time + dt * c->rk_c[rkstep - 1]);
     a.src_ftf = (float)a.src_ft;
   }
   return c->form == NEKGPU_MIXED_NAIVE ? dispatch<float>(c, a) : dispatch<double>(c, a);
@@ -515,11 +564,9 @@ int fused_stage(Context* c, int rkstep, double time, double dt) {
   a.k_out = a.k;
   a.a = c->rk_a[rkstep - 1];
   a.b = c->rk_b[rkstep - 1];
+  a.dt = dt;
   if (c->src.enabled) {
-    const double rktime = time + dt * c->rk_c[rkstep - 1];
-    const double pi = 4.0 * atan(1.0);
-    const double x = pi * c->src.f0 * (rktime - c->src.t0);
-    a.src_ft = c->src.amp * (1.0 - 2.0 * x * x) * exp(-x * x);
+    a.src_ft = source_ft(c->src, time + dt * c->rk_c[rkstep - 1]);
     a.src_ftf = (float)a.src_ft;
   }
   st = c->form == NEKGPU_MIXED_NAIVE ? dispatch<float>(c, a) : dispatch<double>(c, a);

@@ -139,10 +139,12 @@ void gll(int N, std::vector<double>& z, std::vector<double>& w, std::vector<doub
 }
 
 // impedance combination of cem_maxwell_materials (src/cem_maxwell.F:262-325)
-// for one face node: own (Zm, Ym), partner (Zp, Yp) or pec.
-void face_impedance(double Zm, double Ym, double Zp, double Yp, bool pec, double C0, double out[4]) {
-  double Z0 = pec ? 2.0 * Zm : Zm + Zp;
-  double Y0 = pec ? 2.0 * Ym : Ym + Yp;
+// for one face node: own (Zm, Ym) and partner (Zp, Yp); wall = 1 on a 'PEC'
+// face (Z_0 = 2 Z-), 2 on a 'PML' face (a singleton of the gs sum, no
+// doubling: Z_0 = Z-, so Z_1 = 0).
+void face_impedance(double Zm, double Ym, double Zp, double Yp, int wall, double C0, double out[4]) {
+  double Z0 = wall == 1 ? 2.0 * Zm : (wall == 2 ? Zm : Zm + Zp);
+  double Y0 = wall == 1 ? 2.0 * Ym : (wall == 2 ? Ym : Ym + Yp);
   double Z1 = Z0 - Zm, Y1 = Y0 - Ym;
   Z0 = 0.5 * Z0;
   Y0 = 0.5 * Y0;
@@ -224,6 +226,8 @@ int pairs_from_ids(const long long* ids, long m, std::vector<int>& pairs, std::v
   return NEKGPU_OK;
 }
 
+int pml_from_mesh(const nekgpu_mesh* m, PmlHost& p);
+
 int build_plain(const nekgpu_mesh* m, PlainHost& p) {
   const int n = m->nx1;
   const long n3 = (long)n * n * n, npts = n3 * m->nelt, nxzfl = 6L * n * n * m->nelt;
@@ -265,7 +269,7 @@ int build_plain(const nekgpu_mesh* m, PlainHost& p) {
   std::vector<int> fill(p.lift_ptr.begin(), p.lift_ptr.end() - 1);
   for (long j = 0; j < nxzfl; ++j) p.lift_slot[fill[p.cemface[j]]++] = (int)j;
   p.C0 = m->C0;
-  return NEKGPU_OK;
+  return pml_from_mesh(m, p.pml);
 }
 
 // ---------------------------------------------------------------------------
@@ -382,7 +386,7 @@ int build_compact(const nekgpu_mesh* m, Compact& cp) {
     for (int q = 0; q < 4; ++q)
       if (o[q] != def[q]) cp.uniform = false;
   }
-  return NEKGPU_OK;
+  return pml_from_mesh(m, cp.pml);
 }
 
 // ---------------------------------------------------------------------------
@@ -393,6 +397,8 @@ struct BoxArrays {
   std::vector<double> D, w3, metrics[9], bm1, x, y, z, unx, uny, unz, area, Z0, Z1, Y0, Y1, ebm1, hbm1;
   std::vector<int> cemface, cempec;
   std::vector<long long> glo;
+  PmlHost pml;
+  std::vector<int> pmlptr1;  // 1-based, for the mesh hand-off
   nekgpu_mesh mesh{};
 };
 
@@ -400,7 +406,7 @@ struct BoxArrays {
 long box_partner(const nekgpu_box* bx, const int nel[3], const long ec[3], int f) {
   const int ax = kSlotAxis[f], sd = kSlotSide[f];
   const long plane = ec[ax] + (sd > 0 ? 1 : 0);
-  if ((plane == 0 || plane == nel[ax]) && bx->bc[ax] == NEKGPU_BC_PEC) return -1;
+  if ((plane == 0 || plane == nel[ax]) && bx->bc[ax] != NEKGPU_BC_PERIODIC) return -1;
   long pc[3] = {ec[0], ec[1], ec[2]};
   pc[ax] = (pc[ax] + sd + nel[ax]) % nel[ax];
   return pc[0] + (long)nel[0] * (pc[1] + (long)nel[1] * pc[2]);
@@ -418,6 +424,99 @@ double node_Y(const nekgpu_box* bx, long g) {
   return std::sqrt(eps / mu);
 }
 
+// PML of a box (src/cem_maxwell_pml.F): for an axis-aligned box the marching
+// of pml_fill_faceary/march_faces (:85-190) tags exactly the elements within
+// pml_thick layers of a 'PML' face, on that face's side of that axis; the
+// extents inner/outer come from the tagged elements' node coordinates as in
+// pml_extent_and_tags (:261-431), and sigma as in pml_calc_sigma (:433-506).
+int pml_from_box(const nekgpu_box* bx, const BoxArrays& A, PmlHost& p) {
+  p = PmlHost();
+  bool any = false;
+  for (int d = 0; d < 3; ++d) any = any || bx->bc[d] == NEKGPU_BC_PML;
+  if (!any) return NEKGPU_OK;
+  const int thick = bx->pml_thick;
+  const double order = bx->pml_order, referr = bx->pml_referr;
+  // pml_errchk (:2-30); referr = 0 would make sigma infinite
+  if (thick < 1 || thick > 10 || !(order >= 1 && order <= 10) || !(referr > 0 && referr <= 1))
+    return NEKGPU_ERR_ARG;
+  const int n = bx->N + 1;
+  const int nel[3] = {bx->nelx, bx->nely, bx->nelz};
+  for (int d = 0; d < 3; ++d)
+    if (bx->bc[d] == NEKGPU_BC_PML && 2 * thick > nel[d]) return NEKGPU_ERR_ARG;  // colliding layers
+  const long nelt = (long)nel[0] * nel[1] * nel[2], n3 = (long)n * n * n, npts = n3 * nelt;
+  const double* coord[3] = {A.x.data(), A.y.data(), A.z.data()};
+  std::vector<int> tag(nelt, 0);
+  double inner[6], outer[6];
+  for (int d = 0; d < 3; ++d) {
+    outer[2 * d] = 1e20; inner[2 * d] = -1e20;
+    inner[2 * d + 1] = 1e20; outer[2 * d + 1] = -1e20;
+  }
+  for (long e = 0; e < nelt; ++e) {
+    const long ec[3] = {e % nel[0], (e / nel[0]) % nel[1], e / ((long)nel[0] * nel[1])};
+    for (int d = 0; d < 3; ++d) {
+      if (bx->bc[d] != NEKGPU_BC_PML) continue;
+      const bool lo_side = ec[d] < thick, hi_side = ec[d] >= nel[d] - thick;
+      if (!lo_side && !hi_side) continue;
+      double mn = coord[d][e * n3], mx = mn;
+      for (long v = 1; v < n3; ++v) {
+        mn = std::min(mn, coord[d][e * n3 + v]);
+        mx = std::max(mx, coord[d][e * n3 + v]);
+      }
+      if (lo_side) {
+        inner[2 * d] = std::max(inner[2 * d], mx);
+        outer[2 * d] = std::min(outer[2 * d], mn);
+        tag[e] |= 1 << (2 * d);
+      }
+      if (hi_side) {
+        inner[2 * d + 1] = std::min(inner[2 * d + 1], mn);
+        outer[2 * d + 1] = std::max(outer[2 * d + 1], mx);
+        tag[e] |= 1 << (2 * d + 1);
+      }
+    }
+  }
+  p.eps.resize(npts);
+  p.mu.resize(npts);
+  for (long g = 0; g < npts; ++g) {
+    p.eps[g] = bx->permittivity ? bx->permittivity[g] : 1.0;
+    p.mu[g] = bx->permeability ? bx->permeability[g] : 1.0;
+  }
+  p.sigma.assign(3 * (size_t)npts, 0.0);
+  for (long e = 0; e < nelt; ++e) {
+    if (!tag[e]) continue;
+    p.elems.push_back((int)e);
+    for (int face = 0; face < 6; ++face) {
+      if (!(tag[e] & (1 << face))) continue;
+      const int ax = face / 2;
+      const double width = std::fabs(outer[face] - inner[face]);
+      for (long v = 0; v < n3; ++v) {
+        const long j = e * n3 + v;
+        const double eta = std::sqrt(p.mu[j] / p.eps[j]);
+        const double sigmamax = -(order + 1) * std::log(referr) / (2 * eta * width);
+        const double z2o = (coord[ax][j] - inner[face]) / (outer[face] - inner[face]);
+        p.sigma[j + ax * npts] = sigmamax * std::pow(z2o, order);
+      }
+    }
+  }
+  return NEKGPU_OK;
+}
+
+// PML arrays handed over by the caller (nekgpu_mesh)
+int pml_from_mesh(const nekgpu_mesh* m, PmlHost& p) {
+  p = PmlHost();
+  if (!m->pmlsigma || m->npml <= 0) return NEKGPU_OK;
+  if (!m->pmlptr || !m->permittivity || !m->permeability) return NEKGPU_ERR_ARG;
+  const long npts = (long)m->nx1 * m->nx1 * m->nx1 * m->nelt;
+  p.sigma.assign(m->pmlsigma, m->pmlsigma + 3 * npts);
+  p.eps.assign(m->permittivity, m->permittivity + npts);
+  p.mu.assign(m->permeability, m->permeability + npts);
+  for (int l = 0; l < m->npml; ++l) {
+    const int e = m->pmlptr[l] - 1;
+    if (e < 0 || e >= m->nelt || (l > 0 && e <= p.elems.back())) return NEKGPU_ERR_ARG;
+    p.elems.push_back(e);
+  }
+  return NEKGPU_OK;
+}
+
 int build_box(const nekgpu_box* bx, BoxArrays& A, bool full) {
   const int N = bx->N, n = N + 1;
   if (N < 1 || N > 15 || bx->nelx < 1 || bx->nely < 1 || bx->nelz < 1) return NEKGPU_ERR_ARG;
@@ -426,7 +525,8 @@ int build_box(const nekgpu_box* bx, BoxArrays& A, bool full) {
   const long n2 = (long)n * n, n3 = n2 * n, npts = n3 * nelt, nxzfl = 6 * n2 * nelt;
   if (npts > (1L << 31) - 1 || nxzfl > (1L << 31) - 1) return NEKGPU_ERR_ARG;
   for (int d = 0; d < 3; ++d)
-    if (!(bx->hi[d] > bx->lo[d]) || (bx->bc[d] != NEKGPU_BC_PEC && bx->bc[d] != NEKGPU_BC_PERIODIC))
+    if (!(bx->hi[d] > bx->lo[d]) || (bx->bc[d] != NEKGPU_BC_PEC && bx->bc[d] != NEKGPU_BC_PERIODIC &&
+                                     bx->bc[d] != NEKGPU_BC_PML))
       return NEKGPU_ERR_ARG;
   std::vector<double> z, w;
   gll(N, z, w, A.D);
@@ -484,7 +584,8 @@ int build_box(const nekgpu_box* bx, BoxArrays& A, bool full) {
         const int ax = kSlotAxis[f], sd = kSlotSide[f];
         long plane = ec[ax] + (sd > 0 ? 1 : 0);
         const bool boundary = (plane == 0 || plane == nel[ax]);
-        const bool pec = boundary && bx->bc[ax] == NEKGPU_BC_PEC;
+        const int wall = !boundary ? 0 : (bx->bc[ax] == NEKGPU_BC_PEC ? 1 : (bx->bc[ax] == NEKGPU_BC_PML ? 2 : 0));
+        const bool pec = wall != 0;  // PEC and PML faces: mirror flux (cem_maxwell_pec_init)
         if (boundary && !pec) plane = plane % nel[ax];
         long long fid;
         if (ax == 0) fid = off[0] + (plane * nel[1] + ec[1]) * nel[2] + ec[2];
@@ -503,7 +604,8 @@ int build_box(const nekgpu_box* bx, BoxArrays& A, bool full) {
             const long gp = pec ? g : pe * n3 + face_vol(kSlotOpp[f], a, b, n);
             const double Zm = node_Z(bx, g), Ym = node_Y(bx, g);
             const double Zp = node_Z(bx, gp), Yp = node_Y(bx, gp);
-            const double Z0 = pec ? 2.0 * Zm : Zm + Zp, Y0 = pec ? 2.0 * Ym : Ym + Yp;
+            const double Z0 = wall == 1 ? 2.0 * Zm : (wall == 2 ? Zm : Zm + Zp);
+            const double Y0 = wall == 1 ? 2.0 * Ym : (wall == 2 ? Ym : Ym + Yp);
             A.Z1[j] = Z0 - Zm;
             A.Y1[j] = Y0 - Ym;
             A.Z0[j] = 0.5 * Z0;
@@ -536,6 +638,17 @@ int build_box(const nekgpu_box* bx, BoxArrays& A, bool full) {
   m.Z_0 = A.Z0.data(); m.Z_1 = A.Z1.data(); m.Y_0 = A.Y0.data(); m.Y_1 = A.Y1.data();
   m.ebm1 = A.ebm1.data(); m.hbm1 = A.hbm1.data();
   m.C0 = bx->C0;
+  int st = pml_from_box(bx, A, A.pml);
+  if (st) return st;
+  if (A.pml.on()) {
+    A.pmlptr1.resize(A.pml.elems.size());
+    for (size_t l = 0; l < A.pml.elems.size(); ++l) A.pmlptr1[l] = A.pml.elems[l] + 1;
+    m.pmlsigma = A.pml.sigma.data();
+    m.pmlptr = A.pmlptr1.data();
+    m.npml = (int)A.pmlptr1.size();
+    m.permittivity = A.pml.eps.data();
+    m.permeability = A.pml.mu.data();
+  }
   return NEKGPU_OK;
 }
 
@@ -575,6 +688,8 @@ void compact_from_box(const nekgpu_box* bx, const BoxArrays& A, Compact& cp) {
   cp.C0 = bx->C0;
   cp.uniform = true;
   const long npts = n3 * nelt;
+  for (int d = 0; d < 3; ++d) cp.uniform = cp.uniform && bx->bc[d] != NEKGPU_BC_PML;
+  cp.pml = A.pml;
   if (bx->permittivity)
     for (long g = 0; g < npts && cp.uniform; ++g) cp.uniform = bx->permittivity[g] == 1.0;
   if (bx->permeability)
@@ -590,7 +705,8 @@ void compact_from_box(const nekgpu_box* bx, const BoxArrays& A, Compact& cp) {
             const long j = a + (long)n * b + n2 * (f + 6 * e);
             const long g = e * n3 + face_vol(f, a, b, n);
             const long gp = pe < 0 ? g : (long)pe * n3 + face_vol(kSlotOpp[f], a, b, n);
-            face_impedance(node_Z(bx, g), node_Y(bx, g), node_Z(bx, gp), node_Y(bx, gp), pe < 0,
+            const int wall = pe >= 0 ? 0 : (bx->bc[kSlotAxis[f]] == NEKGPU_BC_PML ? 2 : 1);
+            face_impedance(node_Z(bx, g), node_Y(bx, g), node_Z(bx, gp), node_Y(bx, gp), wall,
                            bx->C0, &cp.fcoef[4 * j]);
           }
       }
@@ -673,12 +789,73 @@ int upload_plain(Context* c, const PlainHost& p) {
   cudaMemset(ff, 0, 6 * c->nxzfl * sizeof(double));
   cudaMemset(sf, 0, 6 * c->nxzfl * sizeof(double));
   a.src_w = nullptr;
+  a.bm1 = c->d_bm1;
+  if (p.pml.on()) {  // the reference's full-size PML arrays (src/PML)
+    c->npml = (int)p.pml.elems.size();
+    c->pml_elems = p.pml.elems;
+    if ((st = A.put(&c->d_pml_sigma, p.pml.sigma)) || (st = A.put(&c->d_eps, p.pml.eps)) ||
+        (st = A.put(&c->d_mu, p.pml.mu)) || (st = A.put(&c->d_pmlptr, p.pml.elems)) ||
+        (st = A.get(&c->d_pml_aux, 6 * c->npts)) || (st = A.get(&c->d_pml_k, 6 * c->npts)) ||
+        (st = A.get(&c->d_pml_res, 12 * c->npts)))
+      return st;
+    if (check_cuda(cudaMemset(c->d_pml_aux, 0, 6 * c->npts * sizeof(double))) ||
+        check_cuda(cudaMemset(c->d_pml_k, 0, 6 * c->npts * sizeof(double))) ||
+        check_cuda(cudaMemset(c->d_pml_res, 0, 12 * c->npts * sizeof(double))))
+      return NEKGPU_ERR_CUDA;
+    a.pmlsigma = c->d_pml_sigma;
+    a.eps = c->d_eps;
+    a.mu = c->d_mu;
+    a.pmlptr = c->d_pmlptr;
+    a.npml = c->npml;
+    a.pmlaux = c->d_pml_aux;
+    a.pmlk = c->d_pml_k;
+    a.pmlres = c->d_pml_res;
+  }
   return NEKGPU_OK;
 }
 
-// D for the exact-hi contractions of the mixed form: per row i, Dh on the
-// 10-bit grid of that row's largest |D(i,l)|, Df = D rounded to FP32, and
-// the remainder D - Dh split into two FP32 pieces Dm + Dl (exact to ~2^-55)
+// PML data of the fused forms (layout: PmlDev), compact over the PML elements
+int upload_pml_fused(Context* c, DevAlloc& A, const Compact& cp, PmlDev& out) {
+  out = PmlDev{};
+  if (!cp.pml.on()) return NEKGPU_OK;
+  const PmlHost& p = cp.pml;
+  const long n3 = (long)c->nx * c->nx * c->nx, npts = c->npts;
+  const long npml = (long)p.elems.size(), nn = npml * n3;
+  std::vector<int> slot(c->nelt, -1);
+  std::vector<double> d((size_t)kPmlData * nn);
+  for (long l = 0; l < npml; ++l) {
+    const long e = p.elems[l];
+    slot[e] = (int)l;
+    for (long v = 0; v < n3; ++v) {
+      const long j = e * n3 + v, q = l * n3 + v;
+      for (int ax = 0; ax < 3; ++ax) {
+        d[ax * nn + q] = p.sigma[j + ax * npts] / p.eps[j];
+        d[(3 + ax) * nn + q] = p.sigma[j + ax * npts];
+      }
+      d[6 * nn + q] = p.mu[j];
+      d[7 * nn + q] = cp.bm1[j];
+      d[8 * nn + q] = 1.0 / cp.bm1[j];
+      d[9 * nn + q] = cp.w3[v] * cp.egeom[9 * e] / cp.bm1[j];
+      d[10 * nn + q] = cp.bm1[j] / (cp.w3[v] * cp.egeom[9 * e]);
+    }
+  }
+  int st;
+  if ((st = A.put(&c->d_pml_slot, slot)) || (st = A.put(&c->d_pml_data, d)) ||
+      (st = A.get(&c->d_pml_aux, 6 * nn)) || (st = A.get(&c->d_pml_k, 6 * nn)))
+    return st;
+  if (check_cuda(cudaMemset(c->d_pml_aux, 0, 6 * nn * sizeof(double))) ||
+      check_cuda(cudaMemset(c->d_pml_k, 0, 6 * nn * sizeof(double))))
+    return NEKGPU_ERR_CUDA;
+  c->npml = (int)npml;
+  c->pml_elems = p.elems;
+  out.slot = c->d_pml_slot;
+  out.data = c->d_pml_data;
+  out.aux = c->d_pml_aux;
+  out.k = c->d_pml_k;
+  out.n = nn;
+  return NEKGPU_OK;
+}
+
 // D in the FP32 pieces of the mixed form's exact-hi contraction, as float
 // pairs [0][i + n*l] = (Dh, Df), [1][i + n*l] = (Dm, Dl) of D(i,l): Dh on a
 // 10-bit grid of row i (so every product Dh*uh with uh on a 10-bit grid has
@@ -785,7 +962,7 @@ int upload_fused(Context* c, const Compact& cp) {
     std::vector<float> tab;
     split_D(D, c->nx, tab);
     if ((st = mixed_upload_D(c->nx, tab.data(), tab.size()))) return st;
-    return NEKGPU_OK;
+    return upload_pml_fused(c, A, cp, m.pml);
   }
   if ((st = A.put(&c->d_egeom, cp.egeom))) return st;
   std::vector<float> gf(cp.egeom.begin(), cp.egeom.end());
@@ -811,7 +988,8 @@ int upload_fused(Context* c, const Compact& cp) {
     a.w[i] = cp.w[i];
     a.wf[i] = (float)cp.w[i];
   }
-  return NEKGPU_OK;
+  if (cp.pml.on() && c->form != NEKGPU_FUSED64) return NEKGPU_ERR_UNSUPPORTED;
+  return upload_pml_fused(c, A, cp, a.pml);
 }
 
 int finish_init(Context* c, int st) {
@@ -856,11 +1034,6 @@ int copy_fields_out(Context* c, const double* src, double* hn, double* en, long 
   return NEKGPU_OK;
 }
 
-double ricker(const Source& s, double t) {
-  const double pi = 4.0 * std::atan(1.0);
-  const double a = pi * s.f0 * (t - s.t0);
-  return (1.0 - 2.0 * a * a) * std::exp(-a * a);
-}
 
 int plain_stage(Context* c, int rkstep, double time, double dt) {
   int st;
@@ -869,9 +1042,11 @@ int plain_stage(Context* c, int rkstep, double time, double dt) {
   if ((st = plain_restrict_to_face(c))) return st;
   if ((st = plain_flux3d(c))) return st;
   if ((st = plain_add_flux_to_res(c))) return st;
-  if (c->src.enabled && (st = plain_usersrc(c, c->src.amp * ricker(c->src, rktime)))) return st;
+  if ((st = plain_pml_step(c))) return st;
+  if (c->src.enabled && (st = plain_usersrc(c, source_ft(c->src, rktime)))) return st;
   if ((st = plain_invqmass(c))) return st;
-  return plain_rk_update(c, c->rk_a[rkstep - 1], c->rk_b[rkstep - 1], dt);
+  if ((st = plain_rk_update(c, c->rk_a[rkstep - 1], c->rk_b[rkstep - 1], dt))) return st;
+  return plain_pml_rk_update(c, c->rk_a[rkstep - 1], c->rk_b[rkstep - 1], dt);
 }
 
 int do_stage(Context* c, int rkstep, double time, double dt) {
@@ -1024,6 +1199,7 @@ int nekgpu_box_export_d(const nekgpu_box* bx, const char* name, double* out, lon
   else if (nm == "Z_1") v = &A.Z1;
   else if (nm == "Y_0") v = &A.Y0;
   else if (nm == "Y_1") v = &A.Y1;
+  else if (nm == "pmlsigma") v = &A.pml.sigma;
   if (!v) return NEKGPU_ERR_ARG;
   *count = (long)v->size();
   if (out) std::copy(v->begin(), v->end(), out);
@@ -1045,6 +1221,9 @@ int nekgpu_box_export_i(const nekgpu_box* bx, const char* name, long long* out, 
   } else if (nm == "cempec") {
     *count = (long)A.cempec.size();
     if (out) std::copy(A.cempec.begin(), A.cempec.end(), out);
+  } else if (nm == "pmlptr") {
+    *count = (long)A.pmlptr1.size();
+    if (out) std::copy(A.pmlptr1.begin(), A.pmlptr1.end(), out);
   } else {
     return NEKGPU_ERR_ARG;
   }
@@ -1086,8 +1265,39 @@ int nekgpu_get_array(nekgpu_ctx* c, const char* name, double* out) {
   const double* d = nullptr;
   if (nm == "ebm1") d = c->d_ebm1;
   else if (nm == "hbm1") d = c->d_hbm1;
-  if (!d) return NEKGPU_ERR_ARG;
-  return check_cuda(cudaMemcpy(out, d, c->npts * sizeof(double), cudaMemcpyDeviceToHost));
+  if (d) return check_cuda(cudaMemcpy(out, d, c->npts * sizeof(double), cudaMemcpyDeviceToHost));
+  // PML arrays, 3*npts in the reference layout (zero outside the PML)
+  const bool bn = nm == "pmlbn", dn = nm == "pmldn", sg = nm == "pmlsigma";
+  if (!bn && !dn && !sg) return NEKGPU_ERR_ARG;
+  const long P = c->npts, n3 = (long)c->nx * c->nx * c->nx;
+  std::fill(out, out + 3 * P, 0.0);
+  if (!c->npml) return NEKGPU_OK;
+  if (c->form == NEKGPU_PLAIN) {
+    const double* src = sg ? c->d_pml_sigma : c->d_pml_aux + (dn ? 3 * P : 0);
+    return check_cuda(cudaMemcpy(out, src, 3 * P * sizeof(double), cudaMemcpyDeviceToHost));
+  }
+  const long nn = (long)c->npml * n3;
+  std::vector<double> h(sg ? (size_t)kPmlData * nn : 6 * (size_t)nn);
+  const double* src = sg ? c->d_pml_data : c->d_pml_aux;
+  if (check_cuda(cudaMemcpy(h.data(), src, h.size() * sizeof(double), cudaMemcpyDeviceToHost)))
+    return NEKGPU_ERR_CUDA;
+  for (long l = 0; l < c->npml; ++l)
+    for (long v = 0; v < n3; ++v) {
+      const long q = l * n3 + v, g = (long)c->pml_elems[l] * n3 + v;
+      for (int cc = 0; cc < 3; ++cc) {
+        if (sg)  // sigma = (sigma/eps) * eps is not stored; sigma itself is q = 3..5
+          out[cc * P + g] = h[(3 + cc) * nn + q];
+        else
+          out[cc * P + g] = h[((dn ? 3 : 0) + cc) * nn + q];
+      }
+    }
+  return NEKGPU_OK;
+}
+
+int nekgpu_set_source_kind(nekgpu_ctx* c, int kind) {
+  if (!c || kind < 0 || kind > 1) return NEKGPU_ERR_ARG;
+  c->src.kind = kind;
+  return NEKGPU_OK;
 }
 
 int nekgpu_set_source(nekgpu_ctx* c, int enabled, const double xc[3], double sigma, double amp,
@@ -1265,7 +1475,7 @@ int nekgpu_usersrc(nekgpu_ctx* c, double rktime) {
   int st = plain_only(c);
   if (st) return st;
   if (!c->src.enabled) return NEKGPU_OK;
-  return plain_usersrc(c, c->src.amp * ricker(c->src, rktime));
+  return plain_usersrc(c, source_ft(c->src, rktime));
 }
 int nekgpu_invqmass(nekgpu_ctx* c) {
   int st = plain_only(c);

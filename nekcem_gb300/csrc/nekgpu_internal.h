@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <string>
+#include <cmath>
 #include <vector>
 
 #include "nekcem_gpu.h"
@@ -16,6 +17,14 @@ constexpr int kMaxMixed = 10;  // nx1 limit of the parameter-resident D of the m
 // Compact description of an affine, axis-aligned hex mesh: what the fused
 // forms consume.  Built either by the box builder or by compressing the
 // reference's per-node arrays (nekgpu_init).
+// PML description (src/cem_maxwell_pml.F): elements, graded sigma, materials.
+struct PmlHost {
+  std::vector<int> elems;       // 0-based PML elements, ascending (pmlptr order)
+  std::vector<double> sigma;    // 3*npts: sigma x, y, z
+  std::vector<double> eps, mu;  // npts
+  bool on() const { return !elems.empty(); }
+};
+
 struct Compact {
   int nx = 0, nelt = 0;
   std::vector<double> D;        // nx*nx, D[i + nx*j] = D(i,j)
@@ -28,6 +37,7 @@ struct Compact {
   std::vector<double> fcoef;    // 4*nxzfl: Y02, C02Y, Z02, C02Z per face node
   bool uniform = true;          // all face coefficients equal the eps=mu=1 values
   double C0 = 1.0;
+  PmlHost pml;
 };
 
 // Full reference arrays, for the plain form (one kernel per routine).
@@ -39,12 +49,23 @@ struct PlainHost {
   std::vector<int> cempec;       // 0-based
   std::vector<int> lift_ptr, lift_slot;  // CSR volume node -> face slots (ascending)
   double C0 = 1.0;
+  PmlHost pml;
 };
 
 struct Source {
   bool enabled = false;
+  int kind = 0;  // 0 Ricker(f0, t0), 1 sin(f0 t)
   double xc[3] = {0, 0, 0}, sigma = 0, amp = 0, f0 = 0, t0 = 0;
 };
+
+// amp times the source time function at t: Ricker (1 - 2a^2) exp(-a^2),
+// a = pi f0 (t - t0), or -sin(-f0 t) (tests/3dboxpml/3dboxpml.usr:72-82)
+inline double source_ft(const Source& s, double t) {
+  if (s.kind == 1) return -s.amp * std::sin(-s.f0 * t);
+  const double pi = 4.0 * std::atan(1.0);
+  const double a = pi * s.f0 * (t - s.t0);
+  return s.amp * ((1.0 - 2.0 * a * a) * std::exp(-a * a));
+}
 
 // Kernel argument blocks ----------------------------------------------------
 
@@ -69,11 +90,36 @@ struct PlainDev {
   double* fface;  // 6*nxzfl restricted fields: fhn then fen
   double* srflx;  // 6*nxzfl
   const double* src_w;  // npts or null
+  // PML (null / 0 without): full-size arrays in the reference layout
+  const double* pmlsigma;  // 3*npts
+  const double* eps;       // npts
+  const double* mu;        // npts
+  const double* bm1;       // npts
+  const int* pmlptr;       // npml elements
+  int npml;
+  double* pmlaux;          // 6*npts: pmlbn then pmldn
+  double* pmlk;            // 6*npts: their RK registers
+  double* pmlres;          // 12*npts: respmlbn, respmldn, respmlhn, respmlen
+};
+
+// PML data of the fused forms, compact over the PML elements (slot l holds
+// element pml_elem[l]); per node of a PML element, [q][l*N3 + v]:
+//   q = 0..2 sigma/eps (x, y, z), 3..5 sigma (x, y, z), 6 mu, 7 bm1, 8 1/bm1,
+//   9 w3*rx/bm1 (the mixed form's normalised residual R: res/bm1 = R * [9]),
+//   10 bm1/(w3*rx) (a residual term t enters R as t * [10])
+constexpr int kPmlData = 11;
+struct PmlDev {
+  const int* slot;        // nelt: PML slot of the element, -1 outside
+  const double* data;     // kPmlData * n
+  double* aux;            // 6 * n: pmlbn, pmldn
+  double* k;              // 6 * n: their RK registers
+  long n;                 // npml * N3
 };
 
 struct FusedDev {
   int nelt;
   long npts;
+  PmlDev pml;
   const double* u_in;
   double* u_out;
   double* k;            // RK register read
@@ -88,6 +134,7 @@ struct FusedDev {
   double src_ft;        // amp*ricker(rktime)
   float src_ftf;
   double a, b;          // rk4a(i), rk4b(i)
+  double dt;            // for the PML auxiliary fields (coef carries dt for u)
   double C0;
   float C0f;
   int* status;
@@ -115,6 +162,8 @@ struct MixedDev {
   double a, b;
   float C0f;
   int* status;
+  PmlDev pml;
+  double dt;
 };
 
 // Reverse of one FP64 stage (nekgpu_adjoint.cu)
@@ -177,6 +226,15 @@ struct Context {
   FusedDev fargs{};
   MixedDev margs{};
   float* d_egm = nullptr;
+  // PML: plain form uses d_pml_sigma/d_eps/d_mu/d_pmlptr/d_pml_res (full
+  // size); the fused forms d_pml_slot/d_pml_data; both d_pml_aux/d_pml_k
+  // (full size for plain, compact for fused)
+  int npml = 0;
+  std::vector<int> pml_elems;
+  double *d_pml_sigma = nullptr, *d_eps = nullptr, *d_mu = nullptr, *d_pml_res = nullptr;
+  int* d_pmlptr = nullptr;
+  double *d_pml_aux = nullptr, *d_pml_k = nullptr, *d_pml_data = nullptr;
+  int* d_pml_slot = nullptr;
   // adjoint face-slot coefficients (built on first use, FP64 fused form)
   double* d_adj_slot = nullptr;
   std::vector<double> adj_jw;  // objective weights set by nekgpu_adjoint_init
@@ -206,6 +264,8 @@ int plain_add_flux_to_res(Context* c);
 int plain_usersrc(Context* c, double ft);
 int plain_invqmass(Context* c);
 int plain_rk_update(Context* c, double ca, double cb, double dt);
+int plain_pml_step(Context* c);                                   // pml_step
+int plain_pml_rk_update(Context* c, double ca, double cb, double dt);
 int plain_gs(Context* c, double* d_u, int nfld);
 
 // kernel launchers (nekgpu_fused.cu)

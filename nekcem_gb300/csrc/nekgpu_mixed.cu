@@ -288,7 +288,55 @@ __device__ __forceinline__ void line_phase(const float2* s_u2, float2* s_R2, boo
   }
 }
 
-template <int NX>
+// PML (pml_step, src/cem_maxwell_pml.F:508-590) at one node of a PML element,
+// in FP64: the auxiliary residuals from res/bm1 = R * (w3 rx / bm1), their RK
+// update (src/cem_maxwell.F:1942-1955), and the PML terms of res added to the
+// normalised residual pair R as FP32 pairs.
+template <int N3>
+__device__ __forceinline__ void pml_node(const MixedDev& a, int l, int v, long g, bool first_stage,
+                                      float* Rh, float* Rl) {
+  const long nn = a.pml.n, q = (long)l * N3 + v, P = a.npts;
+  const double* pd = a.pml.data;
+  const double sxp = pd[q], syp = pd[nn + q], szp = pd[2 * nn + q];
+  const double sigx = pd[3 * nn + q], sigy = pd[4 * nn + q], sigz = pd[5 * nn + q];
+  const double mu = pd[6 * nn + q], fac = pd[9 * nn + q], inv = pd[10 * nn + q];
+  double* aux = a.pml.aux;
+  double* kx = a.pml.k;
+  double bn[3], dn[3], hn[3], en[3], rp[6];
+  for (int c = 0; c < 3; ++c) {
+    bn[c] = aux[c * nn + q];
+    dn[c] = aux[(3 + c) * nn + q];
+    hn[c] = __ldg(a.u_in + c * P + g);
+    en[c] = __ldg(a.u_in + (3 + c) * P + g);
+  }
+  double rb[6];
+  for (int c = 0; c < 6; ++c) rb[c] = (f2d(Rh[c]) + f2d(Rl[c])) * fac;
+  rp[0] = rb[0] - syp * bn[0];
+  rp[1] = rb[1] - szp * bn[1];
+  rp[2] = rb[2] - sxp * bn[2];
+  rp[3] = rb[3] - syp * dn[0];
+  rp[4] = rb[4] - szp * dn[1];
+  rp[5] = rb[5] - sxp * dn[2];
+  double t[6];
+  t[0] = -syp * bn[0] + sxp * bn[0] - szp * mu * hn[0];
+  t[1] = -szp * bn[1] + syp * bn[1] - sxp * mu * hn[1];
+  t[2] = -sxp * bn[2] + szp * bn[2] - syp * mu * hn[2];
+  t[3] = -syp * dn[0] + sxp * dn[0] - sigz * en[0];
+  t[4] = -szp * dn[1] + syp * dn[1] - sigx * en[1];
+  t[5] = -sxp * dn[2] + szp * dn[2] - sigy * en[2];
+  for (int c = 0; c < 6; ++c) {
+    const double dR = t[c] * inv;  // res += t bm1  ->  R += t bm1 / (w3 rx)
+    float s, e;
+    two_sum(Rh[c], d2f_hi(dR), s, e);
+    Rh[c] = s;
+    Rl[c] = (Rl[c] + d2f_lo(dR)) + e;
+    const double kv = first_stage ? a.dt * rp[c] : fma(a.a, kx[c * nn + q], a.dt * rp[c]);
+    kx[c * nn + q] = kv;
+    aux[c * nn + q] = fma(a.b, kv, c < 3 ? bn[c] : dn[c - 3]);
+  }
+}
+
+template <int NX, bool PML>
 __global__ void __launch_bounds__(MCfg<NX>::NT, 3) k_mixed_stage(const MixedDev a) {
   using C = MCfg<NX>;
   constexpr int N2 = C::N2, N3 = C::N3, NT = C::NT, NF = C::NF, N3P = C::N3P;
@@ -519,6 +567,7 @@ __global__ void __launch_bounds__(MCfg<NX>::NT, 3) k_mixed_stage(const MixedDev 
     // residual pairs happens before the barrier that lets the next element's
     // TMA overwrite them.
     const int so = a.src_elem ? a.src_elem[e] : -1;
+    const int pml_l = PML ? a.pml.slot[e] : -1;
 #pragma unroll
     for (int q = 0; q < NPT; ++q) {
       const int v = tid + q * NT;
@@ -542,6 +591,7 @@ __global__ void __launch_bounds__(MCfg<NX>::NT, 3) k_mixed_stage(const MixedDev 
       if (i == 0) add(3, j + NX * k);
       if (k == 0) add(4, i + NX * j);
       if (k == NX - 1) add(5, i + NX * j);
+      if (PML && pml_l >= 0) pml_node<N3>(a, pml_l, v, (long)e * N3 + v, first_stage, Rh, Rl);
       if (so >= 0) Rl[5] = fmaf(a.src_w[(long)so * N3 + v], a.src_ftf, Rl[5]);
       const float chh = cv[q][0].x, chl = cv[q][0].y;
       const float ceh = cv[q][1].x, cel = cv[q][1].y;
@@ -577,10 +627,10 @@ __global__ void k_scale_coef_pairs(float2* coef, const double* base, long n2, do
   coef[i] = make_float2(d2f_hi(v), d2f_lo(v));
 }
 
-template <int NX>
+template <int NX, bool PML>
 int launch_mixed(Context* c, const MixedDev& a) {
   using C = MCfg<NX>;
-  auto kern = k_mixed_stage<NX>;
+  auto kern = k_mixed_stage<NX, PML>;
   static bool ready = false;
   static int grid = 0;
   if (!ready) {
@@ -633,20 +683,16 @@ int mixed_stage(Context* c, int rkstep, double time, double dt) {
   a.u_out = c->d_u[c->cur ^ 1];
   a.a = c->rk_a[rkstep - 1];
   a.b = c->rk_b[rkstep - 1];
-  if (c->src.enabled) {
-    const double rktime = time + dt * c->rk_c[rkstep - 1];
-    const double pi = 4.0 * atan(1.0);
-    const double x = pi * c->src.f0 * (rktime - c->src.t0);
-    a.src_ftf = (float)(c->src.amp * (1.0 - 2.0 * x * x) * exp(-x * x));
-  }
+  a.dt = dt;
+  if (c->src.enabled) a.src_ftf = (float)source_ft(c->src, time + dt * c->rk_c[rkstep - 1]);
   switch (c->nx) {
-    case 3: st = launch_mixed<3>(c, a); break;
-    case 4: st = launch_mixed<4>(c, a); break;
-    case 5: st = launch_mixed<5>(c, a); break;
-    case 6: st = launch_mixed<6>(c, a); break;
-    case 7: st = launch_mixed<7>(c, a); break;
-    case 8: st = launch_mixed<8>(c, a); break;
-    case 9: st = launch_mixed<9>(c, a); break;
+    case 3: st = a.pml.slot ? launch_mixed<3, true>(c, a) : launch_mixed<3, false>(c, a); break;
+    case 4: st = a.pml.slot ? launch_mixed<4, true>(c, a) : launch_mixed<4, false>(c, a); break;
+    case 5: st = a.pml.slot ? launch_mixed<5, true>(c, a) : launch_mixed<5, false>(c, a); break;
+    case 6: st = a.pml.slot ? launch_mixed<6, true>(c, a) : launch_mixed<6, false>(c, a); break;
+    case 7: st = a.pml.slot ? launch_mixed<7, true>(c, a) : launch_mixed<7, false>(c, a); break;
+    case 8: st = a.pml.slot ? launch_mixed<8, true>(c, a) : launch_mixed<8, false>(c, a); break;
+    case 9: st = a.pml.slot ? launch_mixed<9, true>(c, a) : launch_mixed<9, false>(c, a); break;
     default: return NEKGPU_ERR_UNSUPPORTED;
   }
   if (st) return st;

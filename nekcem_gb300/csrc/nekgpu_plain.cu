@@ -214,6 +214,58 @@ __global__ void k_rk(PlainDev a, double ca, double cb, double dt) {
   a.u[i] = a.u[i] + cb * kh;
 }
 
+// pml_step (src/cem_maxwell_pml.F:508-590): one thread per node of a PML
+// element; the auxiliary residuals, then their contribution to res
+__global__ void k_pml_step(PlainDev a, int n3) {
+  const long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (t >= (long)a.npml * n3) return;
+  const long P = a.npts;
+  const long j = (long)a.pmlptr[t / n3] * n3 + t % n3;
+  const double* sg = a.pmlsigma;
+  const double* bn = a.pmlaux;
+  const double* dn = a.pmlaux + 3 * P;
+  double* rb = a.pmlres;
+  double* rd = a.pmlres + 3 * P;
+  double* rh = a.pmlres + 6 * P;
+  double* re = a.pmlres + 9 * P;
+  const double* hn = a.u;
+  const double* en = a.u + 3 * P;
+  double* rsh = a.res;
+  double* rse = a.res + 3 * P;
+  const double bm1inv = 1.0 / a.bm1[j];
+  const double sigx = sg[j], sigy = sg[j + P], sigz = sg[j + 2 * P];
+  const double sxp = sigx / a.eps[j], syp = sigy / a.eps[j], szp = sigz / a.eps[j];
+  const double permeab = a.mu[j];
+  rb[j] = rsh[j] * bm1inv - syp * bn[j];
+  rb[j + P] = rsh[j + P] * bm1inv - szp * bn[j + P];
+  rb[j + 2 * P] = rsh[j + 2 * P] * bm1inv - sxp * bn[j + 2 * P];
+  rd[j] = rse[j] * bm1inv - syp * dn[j];
+  rd[j + P] = rse[j + P] * bm1inv - szp * dn[j + P];
+  rd[j + 2 * P] = rse[j + 2 * P] * bm1inv - sxp * dn[j + 2 * P];
+  rh[j] = -syp * bn[j] + sxp * bn[j] - szp * permeab * hn[j];
+  rh[j + P] = -szp * bn[j + P] + syp * bn[j + P] - sxp * permeab * hn[j + P];
+  rh[j + 2 * P] = -sxp * bn[j + 2 * P] + szp * bn[j + 2 * P] - syp * permeab * hn[j + 2 * P];
+  re[j] = -syp * dn[j] + sxp * dn[j] - sigz * en[j];
+  re[j + P] = -szp * dn[j + P] + syp * dn[j + P] - sigx * en[j + P];
+  re[j + 2 * P] = -sxp * dn[j + 2 * P] + szp * dn[j + 2 * P] - sigy * en[j + 2 * P];
+  const double b = a.bm1[j];
+  rsh[j] = rsh[j] + rh[j] * b;
+  rsh[j + P] = rsh[j + P] + rh[j + P] * b;
+  rsh[j + 2 * P] = rsh[j + 2 * P] + rh[j + 2 * P] * b;
+  rse[j] = rse[j] + re[j] * b;
+  rse[j + P] = rse[j + P] + re[j + P] * b;
+  rse[j + 2 * P] = rse[j + 2 * P] + re[j + 2 * P] * b;
+}
+
+// rk4_upd of the PML auxiliary fields (src/cem_maxwell.F:1942-1955)
+__global__ void k_pml_rk(PlainDev a, double ca, double cb, double dt) {
+  long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (i >= 6 * a.npts) return;
+  const double kh = ca * a.pmlk[i] + dt * a.pmlres[i];
+  a.pmlk[i] = kh;
+  a.pmlaux[i] = a.pmlaux[i] + cb * kh;
+}
+
 int last_error() { return check_cuda(cudaGetLastError()); }
 
 }  // namespace
@@ -274,6 +326,21 @@ int plain_usersrc(Context* c, double ft) {
 
 int plain_invqmass(Context* c) {
   k_invqmass<<<blocks_for(c->npts), kThreads, 0, c->stream>>>(c->pargs);
+  c->last_launches += 1;
+  return last_error();
+}
+
+int plain_pml_step(Context* c) {
+  if (!c->pargs.npml) return NEKGPU_OK;
+  const int n3 = c->nx * c->nx * c->nx;
+  k_pml_step<<<blocks_for((long)c->pargs.npml * n3), kThreads, 0, c->stream>>>(c->pargs, n3);
+  c->last_launches += 1;
+  return last_error();
+}
+
+int plain_pml_rk_update(Context* c, double ca, double cb, double dt) {
+  if (!c->pargs.npml) return NEKGPU_OK;
+  k_pml_rk<<<blocks_for(6 * c->npts), kThreads, 0, c->stream>>>(c->pargs, ca, cb, dt);
   c->last_launches += 1;
   return last_error();
 }

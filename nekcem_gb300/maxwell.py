@@ -46,8 +46,10 @@ class MaxwellGPU:
     @classmethod
     def from_box(cls, N: int, nel: Sequence[int], lo: Sequence[float], hi: Sequence[float],
                  bc: Sequence[int], form: str = "mixed", permittivity: Optional[np.ndarray] = None,
-                 permeability: Optional[np.ndarray] = None, C0: float = 1.0) -> "MaxwellGPU":
-        """Structured affine box (genbox + geometry + uservp of the reference)."""
+                 permeability: Optional[np.ndarray] = None, C0: float = 1.0,
+                 pml: Optional[Sequence[float]] = None) -> "MaxwellGPU":
+        """Structured affine box (genbox + geometry + uservp of the reference).
+        bc per axis: 0 PEC, 1 periodic, 2 PML; pml = (thick, order, referr)."""
         lib = L.load()
         b = L.NekgpuBox()
         b.N = int(N)
@@ -61,6 +63,8 @@ class MaxwellGPU:
                 keep.append(a)
                 setattr(b, name, _dp(a))
         b.C0 = float(C0)
+        if pml is not None:
+            b.pml_thick, b.pml_order, b.pml_referr = int(pml[0]), float(pml[1]), float(pml[2])
         h = C.c_void_p()
         L.check(lib.nekgpu_init_box(C.byref(h), C.byref(b), L.FORMS[form]), "nekgpu_init_box")
         return cls(h, L.FORMS[form], keep)
@@ -99,6 +103,11 @@ class MaxwellGPU:
         m.Z_0 = d("Z_0"); m.Z_1 = d("Z_1"); m.Y_0 = d("Y_0"); m.Y_1 = d("Y_1")
         m.ebm1 = d("ebm1"); m.hbm1 = d("hbm1")
         m.C0 = float(C0)
+        if arrays.get("pmlsigma") is not None:
+            m.pmlsigma = d("pmlsigma")
+            pp = np.ascontiguousarray(np.asarray(arrays["pmlptr"]) + 1, dtype=np.int32)
+            keep.append(pp); m.pmlptr = _ip(pp); m.npml = int(pp.size)
+            m.permittivity = d("permittivity"); m.permeability = d("permeability")
         h = C.c_void_p()
         L.check(lib.nekgpu_init(C.byref(h), C.byref(m), L.FORMS[form]), "nekgpu_init")
         return cls(h, L.FORMS[form], keep)
@@ -122,7 +131,7 @@ class MaxwellGPU:
 
     # ---- arrays ------------------------------------------------------------
     def array(self, name: str) -> np.ndarray:
-        out = np.empty(self.npts)
+        out = np.empty(3 * self.npts if name in ("pmlbn", "pmldn", "pmlsigma") else self.npts)
         L.check(L.load().nekgpu_get_array(self._h, name.encode(), _dp(out)), "nekgpu_get_array")
         return out
 
@@ -132,6 +141,10 @@ class MaxwellGPU:
     @property
     def volume(self) -> float:
         return L.load().nekgpu_volume(self._h)
+
+    def set_source_kind(self, kind: int):
+        """0: Ricker time function (default); 1: amp * sin(f0 * t)."""
+        L.check(L.load().nekgpu_set_source_kind(self._h, int(kind)), "nekgpu_set_source_kind")
 
     def set_source(self, xc, sigma, amp, f0, t0, enabled: bool = True):
         x = (C.c_double * 3)(*xc)

@@ -42,6 +42,12 @@ struct ref_ctx {
   double *hn, *en, *khn, *ken, *reshn, *resen, *fhn, *fen, *srflx;
   double *src_w; /* bm1 * exp(-r^2/(2 sigma^2)) per node, or NULL */
   double C0, src_amp, src_f0, src_t0;
+  int src_kind;
+  /* PML (src/PML): tags per element, sigma (npts,3), auxiliary fields and
+   * their RK registers and residuals (npts,3 each) */
+  int ifpml, maxpml, *pmltag, *pmlptr;
+  double *pmlsigma, *pmlbn, *pmldn, *kpmlbn, *kpmldn, *respmlbn, *respmldn, *respmlhn, *respmlen;
+  double pmlinner[6], pmlouter[6];
   double volvm1;
 };
 
@@ -484,7 +490,8 @@ ref_ctx* ref_create_box(int N, int nelx, int nely, int nelz, const double lo[3],
   /* cem_set_fc_ptr (src/cem_common.F:214-257); face global numbering with the
    * semantics of setup_dgds2 (src/nek5_connect11.F:2179-2233): the two
    * slots that share a face node carry the same positive id; a PEC face node
-   * is a singleton.  CBC codes: 0 = 'E  ' interior, 1 = 'PEC', 2 = 'P  '. */
+   * is a singleton.  CBC codes: 0 = 'E  ' interior, 1 = 'PEC', 2 = 'P  ',
+   * 3 = 'PML'. */
   c->cemface = ialloc(nxzfl);
   c->glo_face = (long long*)calloc((size_t)nxzfl, sizeof(long long));
   c->cbc = ialloc(6L * c->nelt);
@@ -499,7 +506,8 @@ ref_ctx* ref_create_box(int N, int nelx, int nely, int nelz, const double lo[3],
       int ax = slot_axis[f], sd = slot_side[f];
       int plane = ec[ax] + (sd > 0 ? 1 : 0);
       int boundary = (plane == 0 || plane == c->nel[ax]);
-      if (boundary) c->cbc[6 * e + f] = (c->bc[ax] == REF_BC_PERIODIC) ? 2 : 1;
+      if (boundary)
+        c->cbc[6 * e + f] = c->bc[ax] == REF_BC_PERIODIC ? 2 : (c->bc[ax] == REF_BC_PML ? 3 : 1);
       if (boundary && c->bc[ax] == REF_BC_PERIODIC) plane = plane % c->nel[ax];
       long long fid;
       if (ax == 0) fid = nplanes_off[0] + ((long long)plane * nely + ec[1]) * nelz + ec[2];
@@ -515,12 +523,12 @@ ref_ctx* ref_create_box(int N, int nelx, int nely, int nelz, const double lo[3],
   }
   gs_setup_local(c);
 
-  /* cem_maxwell_pec_init (src/cem_maxwell.F:1338-1366) */
+  /* cem_maxwell_pec_init (src/cem_maxwell.F:1338-1366): 'PEC' and 'PML' faces */
   c->cempec = ialloc(nxzfl);
   long l = 0;
   for (int e = 0; e < c->nelt; ++e)
     for (int f = 0; f < 6; ++f)
-      if (c->cbc[6 * e + f] == 1)
+      if (c->cbc[6 * e + f] == 1 || c->cbc[6 * e + f] == 3)
         for (long j = 0; j < c->nxzf; ++j) c->cempec[l++] = (int)(j + c->nxzf * (f + 6L * e));
   c->ncempec = l;
 
@@ -553,6 +561,10 @@ void ref_destroy(ref_ctx* c) {
                  c->khn, c->ken, c->reshn, c->resen, c->fhn, c->fen, c->srflx, c->src_w};
   for (size_t i = 0; i < sizeof(d) / sizeof(d[0]); ++i) free(d[i]);
   free(c->cemface); free(c->cbc); free(c->cempec); free(c->glo_face);
+  double* p[] = {c->pmlsigma, c->pmlbn, c->pmldn, c->kpmlbn, c->kpmldn, c->respmlbn,
+                 c->respmldn, c->respmlhn, c->respmlen};
+  for (size_t i = 0; i < sizeof(p) / sizeof(p[0]); ++i) free(p[i]);
+  free(c->pmltag); free(c->pmlptr);
   free(c->gs_order); free(c->gs_start);
   free(c);
 }
@@ -576,6 +588,10 @@ double* ref_darray(ref_ctx* c, const char* name, long* len) {
       {"resen", c->resen, 3 * c->npts}, {"fhn", c->fhn, 3 * c->nxzfl},
       {"fen", c->fen, 3 * c->nxzfl}, {"srflx", c->srflx, 6 * c->nxzfl},
       {"src_w", c->src_w, c->src_w ? c->npts : 0},
+      {"pmlsigma", c->pmlsigma, c->pmlsigma ? 3 * c->npts : 0},
+      {"pmlbn", c->pmlbn, c->pmlbn ? 3 * c->npts : 0},
+      {"pmldn", c->pmldn, c->pmldn ? 3 * c->npts : 0},
+      {"pmlinner", c->pmlinner, c->ifpml ? 6 : 0}, {"pmlouter", c->pmlouter, c->ifpml ? 6 : 0},
   };
   for (size_t i = 0; i < sizeof(t) / sizeof(t[0]); ++i)
     if (strcmp(t[i].nm, name) == 0) { if (len) *len = t[i].n; return t[i].p; }
@@ -586,6 +602,8 @@ double* ref_darray(ref_ctx* c, const char* name, long* len) {
 int* ref_iarray(ref_ctx* c, const char* name, long* len) {
   if (strcmp(name, "cemface") == 0) { if (len) *len = c->nxzfl; return c->cemface; }
   if (strcmp(name, "cbc") == 0) { if (len) *len = 6L * c->nelt; return c->cbc; }
+  if (strcmp(name, "pmltag") == 0 && c->ifpml) { if (len) *len = c->nelt; return c->pmltag; }
+  if (strcmp(name, "pmlptr") == 0 && c->ifpml) { if (len) *len = c->maxpml; return c->pmlptr; }
   if (strcmp(name, "cempec") == 0) { if (len) *len = c->ncempec; return c->cempec; }
   if (len) *len = 0;
   return NULL;
@@ -660,6 +678,8 @@ double ref_source_time(double t, double f0, double t0) {
   double a2 = a * a;
   return (1.0 - 2.0 * a2) * exp(-a2);
 }
+
+void ref_set_source_kind(ref_ctx* c, int kind) { c->src_kind = kind; }
 
 void ref_set_source(ref_ctx* c, int enabled, const double xc[3], double sigma, double amp,
                     double f0, double t0) {
@@ -840,7 +860,9 @@ void ref_add_flux_to_res(ref_ctx* c) {
 /* usersrc (src/cem_maxwell.F:503): mass-weighted E_z source */
 void ref_usersrc(ref_ctx* c, double rktime) {
   if (!c->src_w) return;
-  double ft = c->src_amp * ref_source_time(rktime, c->src_f0, c->src_t0);
+  /* kind 1: tests/3dboxpml/3dboxpml.usr:72-82, srcez - exp(..) * sin(-omega t) * bm1 */
+  double ft = c->src_kind == 1 ? -c->src_amp * sin(-c->src_f0 * rktime)
+                               : c->src_amp * ref_source_time(rktime, c->src_f0, c->src_t0);
   double* rez = c->resen + 2 * c->npts;
   for (long i = 0; i < c->npts; ++i) rez[i] = rez[i] + c->src_w[i] * ft;
 }
@@ -857,12 +879,184 @@ void ref_invqmass(ref_ctx* c) {
   }
 }
 
-/* cem_maxwell_op (src/cem_maxwell.F:484-508); userinc/userfsrc no-ops, no PML */
+/* ------------------------------------------------------------------------ */
+/* PML (src/cem_maxwell_pml.F)                                              */
+/* ------------------------------------------------------------------------ */
+
+/* slots of the negative / positive face of reference axis ax (pff order) */
+static const int neg_slot[3] = {3, 0, 4};
+static const int pos_slot[3] = {1, 2, 5};
+
+/* gs_op(gsh_face, u, 1, 4 = max, 0): every entry of a face-node group
+ * becomes the group's maximum (singletons unchanged) */
+static void gs_max(ref_ctx* c, double* v) {
+  for (int g = 0; g < c->gs_ngroups; ++g) {
+    int b = c->gs_start[g], e = c->gs_start[g + 1];
+    if (e - b < 2) continue;
+    double m = v[c->gs_order[b]];
+    for (int q = b + 1; q < e; ++q) m = v[c->gs_order[q]] > m ? v[c->gs_order[q]] : m;
+    for (int q = b; q < e; ++q) v[c->gs_order[q]] = m;
+  }
+}
+
+/* march_faces (src/cem_maxwell_pml.F:85-137) */
+static void march_faces(ref_ctx* c, double* far) {
+  long n2 = c->nxzf;
+  for (int e = 0; e < c->nelt; ++e)
+    for (int ax = 0; ax < 3; ++ax) {
+      double* pf = far + n2 * (pos_slot[ax] + 6L * e);
+      double* nf = far + n2 * (neg_slot[ax] + 6L * e);
+      for (long i = 0; i < n2; ++i) {
+        double sum = pf[i] + nf[i];
+        if (sum != 0) { pf[i] = pf[i] + 1; nf[i] = nf[i] + 1; }
+      }
+    }
+  gs_max(c, far);
+}
+
+void ref_set_pml(ref_ctx* c, int thick, double order, double referr) {
+  const int n = c->n;
+  const long n2 = c->nxzf, n3 = (long)n * n * n, np = c->npts;
+  /* pml_fill_faceary (:139-190): ones at the interior nodes of 'PML' faces,
+   * then `thick` marches */
+  double* far = dalloc(c->nxzfl);
+  for (int e = 0; e < c->nelt; ++e)
+    for (int f = 0; f < 6; ++f)
+      if (c->cbc[6 * e + f] == 3)
+        for (int b = 1; b < n - 1; ++b)
+          for (int a = 1; a < n - 1; ++a) far[a + (long)n * b + n2 * (f + 6L * e)] = 1;
+  for (int i = 0; i < thick; ++i) march_faces(c, far);
+
+  /* pml_extent_and_tags (:261-431); extents in sym order (x-, x+, y-, ...) */
+  const double inf = 1e20;
+  for (int ax = 0; ax < 3; ++ax) {
+    c->pmlouter[2 * ax] = inf;
+    c->pmlinner[2 * ax] = -inf;
+    c->pmlinner[2 * ax + 1] = inf;
+    c->pmlouter[2 * ax + 1] = -inf;
+  }
+  free(c->pmltag);
+  c->pmltag = ialloc(c->nelt);
+  const long ind = 1 + (long)n;  /* face node (1,1): a face interior point */
+  const double* coord[3] = {c->xm1, c->ym1, c->zm1};
+  const double* met[3][3] = {{c->rxm1, c->sxm1, c->txm1}, {c->rym1, c->sym1, c->tym1},
+                             {c->rzm1, c->szm1, c->tzm1}};
+  for (int e = 0; e < c->nelt; ++e)
+    for (int ax = 0; ax < 3; ++ax) {
+      double here = far[ind + n2 * (neg_slot[ax] + 6L * e)];
+      double opp = far[ind + n2 * (pos_slot[ax] + 6L * e)];
+      if (here == 0 || opp == 0) continue;
+      /* dir_local_to_global (:192-259) of the local -ax direction */
+      double loc[3] = {0, 0, 0}, glob[3];
+      loc[ax] = -1;
+      long v0 = n3 * e;
+      for (int d = 0; d < 3; ++d)
+        glob[d] = met[d][0][v0] * loc[0] + met[d][1][v0] * loc[1] + met[d][2][v0] * loc[2];
+      double big = 0;
+      int amax = 0;
+      for (int d = 0; d < 3; ++d)
+        if (fabs(glob[d]) >= big) { big = fabs(glob[d]); amax = d; }
+      int globface = 2 * amax + (glob[amax] >= 0 ? 1 : 0);
+      int ga = globface / 2;
+      int gsign = (globface % 2) * 2 - 1;
+      double mn = coord[ga][v0], mx = coord[ga][v0];
+      for (long i = 1; i < n3; ++i) {
+        double x = coord[ga][v0 + i];
+        mn = x < mn ? x : mn;
+        mx = x > mx ? x : mx;
+      }
+      if (gsign * (here - opp) > 0) { /* positive side */
+        int fp = 2 * ga + 1;
+        c->pmlinner[fp] = c->pmlinner[fp] < mn ? c->pmlinner[fp] : mn;
+        c->pmlouter[fp] = c->pmlouter[fp] > mx ? c->pmlouter[fp] : mx;
+        c->pmltag[e] |= 1 << fp;
+      }
+      if (gsign * (here - opp) < 0) { /* negative side */
+        int fm = 2 * ga;
+        c->pmlinner[fm] = c->pmlinner[fm] > mx ? c->pmlinner[fm] : mx;
+        c->pmlouter[fm] = c->pmlouter[fm] < mn ? c->pmlouter[fm] : mn;
+        c->pmltag[e] |= 1 << fm;
+      }
+    }
+  free(far);
+
+  /* pml_calc_sigma (:433-506) */
+  free(c->pmlptr);
+  c->pmlptr = ialloc(c->nelt);
+  c->maxpml = 0;
+  for (int e = 0; e < c->nelt; ++e)
+    if (c->pmltag[e]) c->pmlptr[c->maxpml++] = e;
+  double** arr[] = {&c->pmlsigma, &c->pmlbn, &c->pmldn, &c->kpmlbn, &c->kpmldn, &c->respmlbn,
+                    &c->respmldn, &c->respmlhn, &c->respmlen};
+  for (size_t i = 0; i < sizeof(arr) / sizeof(arr[0]); ++i) {
+    free(*arr[i]);
+    *arr[i] = dalloc(3 * np);
+  }
+  for (int l = 0; l < c->maxpml; ++l) {
+    int e = c->pmlptr[l];
+    for (int face = 0; face < 6; ++face) {
+      int ax = face / 2;
+      double width = fabs(c->pmlouter[face] - c->pmlinner[face]);
+      if (!(c->pmltag[e] & (1 << face))) continue;
+      for (long i = 0; i < n3; ++i) {
+        long j = i + n3 * e;
+        double eta = c->permeability[j] / c->permittivity[j];
+        eta = sqrt(eta);
+        double sigmamax = -(order + 1) * log(referr) / (2 * eta * width);
+        double z2o = (coord[ax][j] - c->pmlinner[face]) / (c->pmlouter[face] - c->pmlinner[face]);
+        c->pmlsigma[j + ax * np] = sigmamax * pow(z2o, order);
+      }
+    }
+  }
+  c->ifpml = 1;
+}
+
+/* pml_step (src/cem_maxwell_pml.F:508-590) */
+void ref_pml_step(ref_ctx* c) {
+  const long n3 = (long)c->n * c->n * c->n, np = c->npts;
+  double *sg = c->pmlsigma, *bn = c->pmlbn, *dn = c->pmldn;
+  double *rb = c->respmlbn, *rd = c->respmldn, *rh = c->respmlhn, *re = c->respmlen;
+  double *hn = c->hn, *en = c->en, *rsh = c->reshn, *rse = c->resen;
+#pragma omp parallel for schedule(static) num_threads(g_threads)
+  for (int l = 0; l < c->maxpml; ++l) {
+    long e = c->pmlptr[l];
+    for (long i = 0; i < n3; ++i) {
+      long j = i + n3 * e;
+      double bm1inv = 1.0 / c->bm1[j];
+      double sigx = sg[j], sigy = sg[j + np], sigz = sg[j + 2 * np];
+      double sxp = sigx / c->permittivity[j];
+      double syp = sigy / c->permittivity[j];
+      double szp = sigz / c->permittivity[j];
+      double permeab = c->permeability[j];
+      rb[j] = rsh[j] * bm1inv - syp * bn[j];
+      rb[j + np] = rsh[j + np] * bm1inv - szp * bn[j + np];
+      rb[j + 2 * np] = rsh[j + 2 * np] * bm1inv - sxp * bn[j + 2 * np];
+      rd[j] = rse[j] * bm1inv - syp * dn[j];
+      rd[j + np] = rse[j + np] * bm1inv - szp * dn[j + np];
+      rd[j + 2 * np] = rse[j + 2 * np] * bm1inv - sxp * dn[j + 2 * np];
+      rh[j] = -syp * bn[j] + sxp * bn[j] - szp * permeab * hn[j];
+      rh[j + np] = -szp * bn[j + np] + syp * bn[j + np] - sxp * permeab * hn[j + np];
+      rh[j + 2 * np] = -sxp * bn[j + 2 * np] + szp * bn[j + 2 * np] - syp * permeab * hn[j + 2 * np];
+      re[j] = -syp * dn[j] + sxp * dn[j] - sigz * en[j];
+      re[j + np] = -szp * dn[j + np] + syp * dn[j + np] - sigx * en[j + np];
+      re[j + 2 * np] = -sxp * dn[j + 2 * np] + szp * dn[j + 2 * np] - sigy * en[j + 2 * np];
+      rsh[j] = rsh[j] + rh[j] * c->bm1[j];
+      rsh[j + np] = rsh[j + np] + rh[j + np] * c->bm1[j];
+      rsh[j + 2 * np] = rsh[j + 2 * np] + rh[j + 2 * np] * c->bm1[j];
+      rse[j] = rse[j] + re[j] * c->bm1[j];
+      rse[j + np] = rse[j + np] + re[j + np] * c->bm1[j];
+      rse[j + 2 * np] = rse[j + 2 * np] + re[j + 2 * np] * c->bm1[j];
+    }
+  }
+}
+
+/* cem_maxwell_op (src/cem_maxwell.F:484-508); userinc/userfsrc no-ops */
 void ref_maxwell_op(ref_ctx* c, double rktime) {
   ref_cem_maxwell(c);
   ref_restrict_to_face(c);
   ref_flux3d(c);
   ref_add_flux_to_res(c);
+  if (c->ifpml) ref_pml_step(c);
   ref_usersrc(c, rktime);
   ref_invqmass(c);
 }
@@ -911,6 +1105,14 @@ void ref_rk_stage(ref_ctx* c, int rkstep, double time, double dt) {
   for (int q = 0; q < 3; ++q)
     ref_rk4_upd(c->en + q * np, c->ken + q * np, c->resen + q * np, b[rkstep - 1], a[rkstep - 1],
                 dt, np);
+  if (c->ifpml) { /* src/cem_maxwell.F:1942-1955 */
+    for (int q = 0; q < 3; ++q)
+      ref_rk4_upd(c->pmlbn + q * np, c->kpmlbn + q * np, c->respmlbn + q * np, b[rkstep - 1],
+                  a[rkstep - 1], dt, np);
+    for (int q = 0; q < 3; ++q)
+      ref_rk4_upd(c->pmldn + q * np, c->kpmldn + q * np, c->respmldn + q * np, b[rkstep - 1],
+                  a[rkstep - 1], dt, np);
+  }
 }
 
 /* cem_maxwell_op_rk (src/cem_maxwell.F:327-345) */

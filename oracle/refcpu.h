@@ -18,8 +18,10 @@ extern "C" {
 
 typedef struct ref_ctx ref_ctx;
 
-/* Box boundary kind per axis (both sides of that axis). */
-enum { REF_BC_PEC = 0, REF_BC_PERIODIC = 1 };
+/* Box boundary kind per axis (both sides of that axis): PEC walls, periodic,
+ * or 'PML' faces (a PEC wall behind perfectly matched layers, set up by
+ * ref_set_pml). */
+enum { REF_BC_PEC = 0, REF_BC_PERIODIC = 1, REF_BC_PML = 2 };
 
 /* GLL points/weights (src/nek5_speclib.F:107 ZWGLL -> ZWGLJD:240) */
 void ref_zwgll(double* z, double* w, int np);
@@ -61,6 +63,19 @@ void ref_set_flux(ref_ctx* c, double C0);
 void ref_set_source(ref_ctx* c, int enabled, const double xc[3], double sigma,
                     double amp, double f0, double t0);
 double ref_source_time(double t, double f0, double t0);
+/* time function of the source: 0 = Ricker (f0, t0), 1 = sin(f0 * t) (the
+ * Gaussian dipole of tests/3dboxpml/3dboxpml.usr:28-85, omega = f0) */
+void ref_set_source_kind(ref_ctx* c, int kind);
+
+/* PML (src/cem_maxwell_pml.F): layers of elements marched `thick` levels in
+ * from the 'PML' faces (pml_fill_faceary :139-190, march_faces :85-137 with
+ * the gs max over face nodes), element tags and extents
+ * (pml_extent_and_tags :261-431), the graded sigma profile
+ * (pml_calc_sigma :433-506; order, reflection error referr).  The auxiliary
+ * fields pmlbn, pmldn start at zero. */
+void ref_set_pml(ref_ctx* c, int thick, double order, double referr);
+/* pml_step (src/cem_maxwell_pml.F:508-590), after the lift and before usersrc */
+void ref_pml_step(ref_ctx* c);
 
 /* ---- the reference routines on the hot path ---- */
 void ref_local_grad3(double* ur, double* us, double* ut, const double* u, int n,

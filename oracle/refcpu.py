@@ -15,7 +15,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "librefcpu.so")
-BC_PEC, BC_PERIODIC = 0, 1
+BC_PEC, BC_PERIODIC, BC_PML = 0, 1, 2
 
 
 def build(force: bool = False) -> str:
@@ -56,6 +56,9 @@ def lib():
         L.ref_set_materials.argtypes = [vp, dp, dp]
         L.ref_set_flux.argtypes = [vp, C.c_double]
         L.ref_set_source.argtypes = [vp, ip, dp, C.c_double, C.c_double, C.c_double, C.c_double]
+        L.ref_set_source_kind.argtypes = [vp, ip]
+        L.ref_set_pml.argtypes = [vp, ip, C.c_double, C.c_double]
+        L.ref_pml_step.argtypes = [vp]
         L.ref_source_time.restype = C.c_double
         L.ref_source_time.argtypes = [C.c_double, C.c_double, C.c_double]
         for nm in ("ref_cem_maxwell", "ref_restrict_to_face", "ref_flux3d", "ref_flux_pre",
@@ -172,6 +175,12 @@ class RefBox:
 
     def set_flux(self, C0: float):
         lib().ref_set_flux(self._c, float(C0))
+
+    def set_pml(self, thick: int, order: float, referr: float):
+        lib().ref_set_pml(self._c, int(thick), float(order), float(referr))
+
+    def set_source_kind(self, kind: int):
+        lib().ref_set_source_kind(self._c, int(kind))
 
     def set_source(self, xc, sigma, amp, f0, t0, enabled=True):
         xa = (C.c_double * 3)(*xc)

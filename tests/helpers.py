@@ -22,10 +22,15 @@ def oracle_arrays(ref: R.RefBox) -> dict:
     out["cemface"] = ref.i("cemface").copy()
     out["cempec"] = ref.i("cempec").copy()
     out["glo_face"] = ref.l("glo_face").copy()
+    if getattr(ref, "pml", None):
+        out["pmlsigma"] = ref.d("pmlsigma").copy()
+        out["pmlptr"] = ref.i("pmlptr").copy()
+        out["permittivity"] = ref.d("permittivity").copy()
+        out["permeability"] = ref.d("permeability").copy()
     return out
 
 
-def make_ref(N, nel, lo, hi, bc, eps=None, mu=None, C0=1.0, threads=0):
+def make_ref(N, nel, lo, hi, bc, eps=None, mu=None, C0=1.0, threads=0, pml=None):
     if threads:
         R.set_threads(threads)
     ref = R.RefBox(N, nel, lo, hi, bc)
@@ -35,6 +40,9 @@ def make_ref(N, nel, lo, hi, bc, eps=None, mu=None, C0=1.0, threads=0):
         m = np.ones(ref.npts) if mu is None else (mu(x, y, z) if callable(mu) else mu)
         ref.set_materials(np.asarray(e, float), np.asarray(m, float))
     ref.set_flux(C0)
+    ref.pml = pml
+    if pml is not None:
+        ref.set_pml(*pml)
     return ref
 
 
@@ -48,7 +56,8 @@ def gpu_from_box(ref: R.RefBox, form: str, C0: float = 1.0) -> MaxwellGPU:
     uniform = np.all(eps == 1.0) and np.all(mu == 1.0)
     return MaxwellGPU.from_box(ref.N, ref.nel, ref.lo, ref.hi, ref.bc, form=form,
                                permittivity=None if uniform else eps,
-                               permeability=None if uniform else mu, C0=C0)
+                               permeability=None if uniform else mu, C0=C0,
+                               pml=getattr(ref, "pml", None))
 
 
 def random_fields(npts: int, seed: int):

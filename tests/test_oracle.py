@@ -143,3 +143,47 @@ def test_dt_rule():
     assert abs(cases.get_dxmin(x, y, z, c.N + 1, c.nelt) - m.dxmin()) < 1e-15
     z7, _ = R.zwgll(8)
     np.testing.assert_allclose(c.timestep(x, y, z), 0.5 * (z7[1] - z7[0]) * 0.125, rtol=1e-12)
+
+
+# ---- PML (src/cem_maxwell_pml.F) -------------------------------------------------
+def test_oracle_pml_layers_and_sigma():
+    """6^3 box on [-1,1]^3 with 'PML' on every face, one layer: the outer
+    shell of 152 elements is tagged, the extents are the layer boundaries and
+    sigma grows as sigmamax ((x - inner)/(outer - inner))^order with
+    sigmamax = -(order + 1) ln(referr) / (2 eta width)."""
+    ref = R.RefBox(3, (6, 6, 6), (-1, -1, -1), (1, 1, 1), (2, 2, 2))
+    ref.set_pml(1, 3.0, 1e-8)
+    tag = ref.i("pmltag")
+    assert (tag != 0).sum() == 6 ** 3 - 4 ** 3
+    np.testing.assert_allclose(ref.d("pmlinner"), [-2 / 3, 2 / 3] * 3, rtol=1e-14)
+    np.testing.assert_allclose(ref.d("pmlouter"), [-1, 1] * 3, rtol=1e-14)
+    x = ref.coords()[0]
+    sx = ref.d("pmlsigma")[:ref.npts]
+    smax = -(3.0 + 1) * np.log(1e-8) / (2 * 1.0 * (1 / 3))
+    right = x > 2 / 3
+    np.testing.assert_allclose(sx[right], smax * ((x[right] - 2 / 3) / (1 / 3)) ** 3, rtol=1e-12,
+                               atol=1e-12)
+    assert np.all(sx[np.abs(x) < 2 / 3 - 1e-12] == 0)
+    # PML faces are in the PEC list and are not doubled in the materials
+    assert R.lib().ref_size(ref._c, b"ncempec") == 6 * 36 * 16
+    assert np.all(ref.d("Z_1")[ref.i("cempec")] == 0)
+
+
+def test_oracle_3dboxpml_short_run_bounded():
+    """The reference's tests/3dboxpml setup (6^3 el on [-1,1]^3, all faces
+    'PML', thickness 1, order 3, error 1e-8, Gaussian dipole sin(2t), zero
+    initial fields, dt = 0.1 dxmin) at N=4 for 300 steps: the fields stay
+    below the reference's bound 1 (L2 and Linf), and the PML elements carry
+    non-zero auxiliary fields once the wave reaches them."""
+    R.set_threads(os.cpu_count() or 1)
+    ref = R.RefBox(4, (6, 6, 6), (-1, -1, -1), (1, 1, 1), (2, 2, 2))
+    ref.set_pml(1, 3.0, 1e-8)
+    ref.set_source_kind(1)
+    ref.set_source((0.0, 0.0, 0.0), 0.1, 1.0, 2.0, 0.0)
+    dt = 0.1 * ref.dxmin()
+    ref.set_state(np.zeros((3, ref.npts)), np.zeros((3, ref.npts)))
+    ref.run(300, 0.0, dt)
+    for comp in list(ref.hn) + list(ref.en):
+        l2, li = ref.cem_error(comp.copy(), np.zeros(ref.npts))
+        assert l2 <= 1.0 and li <= 1.0
+    assert np.abs(ref.d("pmldn")).max() > 0
