@@ -263,6 +263,23 @@ int nekgpu_adjoint_init(nekgpu_ctx* ctx, const double* jw, int stride);
 int nekgpu_adjoint_run(nekgpu_ctx* ctx, int nsteps, double t0, double dt, double* J,
                        double* dJdeps);
 
+/* ---- output ------------------------------------------------------------------ */
+/* The reference's VTK output for param(81) = 3 (cem_out_fields3,
+ * src/io.F:562-640; src/io_vtkbin.c writeheader/writenodes/write3dcells/
+ * writefield; cells of vtk_dump_header_nonswap, src/io_dumpvtk.F:718-810):
+ * legacy binary (big-endian), FP32 points and VECTORS "E ", "H " of the
+ * current state and, when solhn/solen are given (3 x ld host arrays, the
+ * analytic fields shn/sen), "solE", "solH".  Needs the node coordinates. */
+int nekgpu_write_vtk(nekgpu_ctx* ctx, const char* path, const double* solhn, const double* solen,
+                     long ld);
+/* Checkpoints of the device state (fields, RK register, PML auxiliary fields
+ * and registers, raw FP64) with the time and step number; loading one into a
+ * context of the same form and mesh (else NEKGPU_ERR_MESH) continues the run
+ * bit for bit.  No counterpart in the reference's non-MPI build, whose
+ * restart writers are empty (src/io_vtkbin.c:307-322). */
+int nekgpu_checkpoint_save(nekgpu_ctx* ctx, const char* path, double time, long istep);
+int nekgpu_checkpoint_load(nekgpu_ctx* ctx, const char* path, double* time, long* istep);
+
 /* ---- timing ---------------------------------------------------------------- */
 /* Runs nsteps steps between CUDA events on the context stream and returns the
  * elapsed device milliseconds (state advances; *time += nsteps*dt). */

@@ -29,6 +29,7 @@ SOURCES = {
     "nekgpu_noalloc.cu": [],
     "nekgpu_adjoint.cu": [],
     "nekgpu_adjoint_host.cpp": ["-Xcompiler", "-ffp-contract=off"],
+    "nekgpu_io.cpp": [],
 }
 
 

@@ -271,3 +271,27 @@ class MaxwellGPU:
         L.check(L.load().nekgpu_adjoint_run(self._h, int(nsteps), float(t0), float(dt), C.byref(J),
                                             _dp(out)), "nekgpu_adjoint_run")
         return J.value, out
+
+    # ---- output ----------------------------------------------------------------
+    def write_vtk(self, path: str, sol: Optional[tuple] = None):
+        """The reference's param(81)=3 VTK file of the current state; sol =
+        (solH, solE) adds the analytic fields."""
+        lib = L.load()
+        if sol is None:
+            L.check(lib.nekgpu_write_vtk(self._h, str(path).encode(), None, None, 0), "nekgpu_write_vtk")
+            return
+        sh = np.ascontiguousarray(sol[0], dtype=np.float64).reshape(3, self.npts)
+        se = np.ascontiguousarray(sol[1], dtype=np.float64).reshape(3, self.npts)
+        L.check(lib.nekgpu_write_vtk(self._h, str(path).encode(), _dp(sh), _dp(se), self.npts),
+                "nekgpu_write_vtk")
+
+    def checkpoint_save(self, path: str, time: float, istep: int = 0):
+        L.check(L.load().nekgpu_checkpoint_save(self._h, str(path).encode(), float(time), int(istep)),
+                "nekgpu_checkpoint_save")
+
+    def checkpoint_load(self, path: str):
+        """Returns (time, istep) of the checkpoint."""
+        t = C.c_double(); n = C.c_long()
+        L.check(L.load().nekgpu_checkpoint_load(self._h, str(path).encode(), C.byref(t), C.byref(n)),
+                "nekgpu_checkpoint_load")
+        return t.value, n.value
