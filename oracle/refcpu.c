@@ -379,8 +379,43 @@ static void genxyz_box(ref_ctx* c) {
   }
 }
 
+/* Smooth interior deformation of the box (a usrdat2-style user mapping,
+ * tests/3dboxpml/3dboxpml.usr:159-194 shows the hook): every point moves by
+ * amp * L_d * s * sin(2 pi xi_(d+1)), s = sin(pi xi_x) sin(pi xi_y) sin(pi xi_z),
+ * xi the point's position in [0,1] per axis.  The domain boundary does not
+ * move, so the face pairing and PEC/periodic faces stay as they are, while
+ * the elements become curvilinear. */
+static void map_box(ref_ctx* c, double amp) {
+  const double pi = 4.0 * atan(1.0);
+  for (long i = 0; i < c->npts; ++i) {
+    double xi[3] = {(c->xm1[i] - c->lo[0]) / (c->hi[0] - c->lo[0]),
+                    (c->ym1[i] - c->lo[1]) / (c->hi[1] - c->lo[1]),
+                    (c->zm1[i] - c->lo[2]) / (c->hi[2] - c->lo[2])};
+    double s = sin(pi * xi[0]) * sin(pi * xi[1]) * sin(pi * xi[2]);
+    double dx = amp * (c->hi[0] - c->lo[0]) * s * sin(2 * pi * xi[1]);
+    double dy = amp * (c->hi[1] - c->lo[1]) * s * sin(2 * pi * xi[2]);
+    double dz = amp * (c->hi[2] - c->lo[2]) * s * sin(2 * pi * xi[0]);
+    c->xm1[i] += dx;
+    c->ym1[i] += dy;
+    c->zm1[i] += dz;
+  }
+}
+
+static ref_ctx* create_box(int N, int nelx, int nely, int nelz, const double lo[3],
+                           const double hi[3], const int bc[3], double amp);
+
 ref_ctx* ref_create_box(int N, int nelx, int nely, int nelz, const double lo[3],
                         const double hi[3], const int bc[3]) {
+  return create_box(N, nelx, nely, nelz, lo, hi, bc, 0.0);
+}
+
+ref_ctx* ref_create_box_mapped(int N, int nelx, int nely, int nelz, const double lo[3],
+                               const double hi[3], const int bc[3], double amp) {
+  return create_box(N, nelx, nely, nelz, lo, hi, bc, amp);
+}
+
+static ref_ctx* create_box(int N, int nelx, int nely, int nelz, const double lo[3],
+                           const double hi[3], const int bc[3], double amp) {
   if (N < 1 || N > 15 || nelx < 1 || nely < 1 || nelz < 1) return NULL;
   ref_ctx* c = (ref_ctx*)calloc(1, sizeof(ref_ctx));
   int n = N + 1;
@@ -407,6 +442,7 @@ ref_ctx* ref_create_box(int N, int nelx, int nely, int nelz, const double lo[3],
 
   c->xm1 = dalloc(npts); c->ym1 = dalloc(npts); c->zm1 = dalloc(npts);
   genxyz_box(c);
+  if (amp != 0.0) map_box(c, amp);
 
   /* XYZRST (src/nek5_coef.F:877-924) + GLMAPM1 (555-635) + GEODAT1 bm1 (758) */
   double *xr = dalloc(npts), *yr = dalloc(npts), *zr = dalloc(npts);

@@ -39,6 +39,10 @@ double ref_pnleg(double z, int n);
  */
 ref_ctx* ref_create_box(int N, int nelx, int nely, int nelz, const double lo[3],
                         const double hi[3], const int bc[3]);
+/* the same box with a smooth interior deformation of amplitude amp (curved,
+ * non-affine elements; the domain boundary stays in place) */
+ref_ctx* ref_create_box_mapped(int N, int nelx, int nely, int nelz, const double lo[3],
+                               const double hi[3], const int bc[3], double amp);
 void ref_destroy(ref_ctx* c);
 
 /* Named array access (the reference's COMMON arrays).  Returns NULL for an

@@ -42,6 +42,8 @@ def lib():
         vp, ip, dp = C.c_void_p, C.c_int, C.POINTER(C.c_double)
         L.ref_create_box.restype = vp
         L.ref_create_box.argtypes = [ip, ip, ip, ip, dp, dp, C.POINTER(C.c_int)]
+        L.ref_create_box_mapped.restype = vp
+        L.ref_create_box_mapped.argtypes = [ip, ip, ip, ip, dp, dp, C.POINTER(C.c_int), C.c_double]
         L.ref_destroy.argtypes = [vp]
         L.ref_darray.restype = dp
         L.ref_darray.argtypes = [vp, C.c_char_p, C.POINTER(C.c_long)]
@@ -113,12 +115,16 @@ def set_threads(n: int):
 class RefBox:
     """Oracle for one structured affine box mesh (reference COMMON arrays)."""
 
-    def __init__(self, N, nel, lo, hi, bc):
+    def __init__(self, N, nel, lo, hi, bc, deform: float = 0.0):
         L = lib()
         lo_a = (C.c_double * 3)(*lo); hi_a = (C.c_double * 3)(*hi)
         bc_a = (C.c_int * 3)(*bc)
-        self._c = L.ref_create_box(int(N), int(nel[0]), int(nel[1]), int(nel[2]),
-                                   lo_a, hi_a, bc_a)
+        if deform:
+            self._c = L.ref_create_box_mapped(int(N), int(nel[0]), int(nel[1]), int(nel[2]),
+                                              lo_a, hi_a, bc_a, float(deform))
+        else:
+            self._c = L.ref_create_box(int(N), int(nel[0]), int(nel[1]), int(nel[2]),
+                                       lo_a, hi_a, bc_a)
         if not self._c:
             raise ValueError("ref_create_box rejected the mesh")
         self.N, self.nel, self.lo, self.hi, self.bc = N, tuple(nel), tuple(lo), tuple(hi), tuple(bc)

@@ -30,10 +30,10 @@ def oracle_arrays(ref: R.RefBox) -> dict:
     return out
 
 
-def make_ref(N, nel, lo, hi, bc, eps=None, mu=None, C0=1.0, threads=0, pml=None):
+def make_ref(N, nel, lo, hi, bc, eps=None, mu=None, C0=1.0, threads=0, pml=None, deform=0.0):
     if threads:
         R.set_threads(threads)
-    ref = R.RefBox(N, nel, lo, hi, bc)
+    ref = R.RefBox(N, nel, lo, hi, bc, deform=deform)
     if eps is not None or mu is not None:
         x, y, z = ref.coords()
         e = np.ones(ref.npts) if eps is None else (eps(x, y, z) if callable(eps) else eps)

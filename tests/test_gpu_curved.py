@@ -1,0 +1,70 @@
+"""Curvilinear (non-affine) elements: boxes with a smooth interior
+deformation (per-node metrics, curved faces with per-node normals and areas).
+The plain form runs them from the reference's arrays bit for bit against the
+oracle; the cavity mode (whose walls do not move) keeps its accuracy; the
+fused forms, which need affine elements, refuse them."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from helpers import gpu_from_ref, make_ref, smooth_fields
+from nekcem_gb300 import cases
+from nekcem_gb300 import _lib as L
+
+pytestmark = pytest.mark.gpu
+
+CURVED = [
+    dict(N=4, nel=(3, 3, 3), bc=(0, 0, 0), deform=0.05),
+    dict(N=5, nel=(2, 3, 2), bc=(1, 0, 1), deform=0.08),
+    dict(N=7, nel=(2, 2, 2), bc=(1, 1, 1), deform=0.04),
+]
+
+
+@pytest.mark.parametrize("m", CURVED, ids=["pec_n4", "mixed_bc_n5", "periodic_n7"])
+@pytest.mark.parametrize("materials", [False, True])
+def test_plain_curved_bit_exact(m, materials):
+    eps = (lambda x, y, z: 1.0 + 0.5 * np.sin(2 * x) ** 2) if materials else None
+    ref = make_ref(m["N"], m["nel"], (0, 0, 0), (1, 1, 1), m["bc"], eps=eps, deform=m["deform"])
+    assert np.abs(ref.d("rym1")).max() > 1e-3  # the metrics are not diagonal
+    g = gpu_from_ref(ref, "plain")
+    H, E = smooth_fields(ref, 5)
+    ref.set_state(H, E); g.set_state(H, E)
+    dt = 0.2 * ref.dxmin()
+    ref.run(5, 0.0, dt); g.run(5, 0.0, dt)
+    gH, gE = g.get_state()
+    np.testing.assert_array_equal(gH, ref.hn)
+    np.testing.assert_array_equal(gE, ref.en)
+    g.close(); ref.close()
+
+
+def test_curved_cavity_keeps_its_accuracy():
+    """TM110 cavity on a deformed 4^3, N=7 mesh (the walls stay put, so the
+    analytic mode is unchanged): after 300 steps the L2 error stays small.
+    It is larger than on the affine mesh (9e-10 there): the curved geometry
+    is only represented to the GLL interpolant's accuracy and the metric
+    products alias (the reference's dealiased curl, maxwell_wght_dcurl,
+    addresses the latter)."""
+    res = {}
+    for deform in (0.0, 0.04):
+        ref = make_ref(7, (4, 4, 4), (0, 0, 0), (1, 1, 1), (0, 0, 0), deform=deform)
+        g = gpu_from_ref(ref, "plain")
+        x, y, z = (a.copy() for a in ref.coords())
+        c = cases.make("cavity")
+        dt = 0.5 * cases.min_gll_spacing(x, y, z, 8, 64) * 0.5
+        g.set_state(*c.exact(x, y, z, 0.0))
+        t = g.run(300, 0.0, dt)
+        l2, _ = g.cem_error(*c.exact(x, y, z, t))
+        res[deform] = float(np.sqrt(np.sum(l2 ** 2)))
+        g.close(); ref.close()
+    assert res[0.0] < 1e-8, res
+    assert res[0.04] < 1e-6, res
+
+
+@pytest.mark.parametrize("form", ["fused64", "mixed"])
+def test_fused_forms_refuse_curved_meshes(form):
+    ref = make_ref(4, (2, 2, 2), (0, 0, 0), (1, 1, 1), (0, 0, 0), deform=0.05)
+    with pytest.raises(L.NekgpuError) as e:
+        gpu_from_ref(ref, form)
+    assert e.value.status == -2
+    ref.close()
