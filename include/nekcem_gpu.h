@@ -173,6 +173,28 @@ int nekgpu_set_source_kind(nekgpu_ctx* ctx, int kind);
 int nekgpu_set_source(nekgpu_ctx* ctx, int enabled, const double xc[3], double sigma,
                       double amp, double f0, double t0);
 
+/* ---- dispersive media ---------------------------------------------------- */
+#define NEKGPU_DRUDE 1
+#define NEKGPU_LORENTZ 2
+/* Polarisation currents at listed nodes, advanced with every RK stage inside
+ * usersrc before the volume source, as tests/drude/drude.usr:167 and
+ * tests/lorentz/lorentz.usr:174 call them:
+ *   NEKGPU_DRUDE (cem_maxwell_drude, src/cem_maxwell.F:3095-3147):
+ *     params(ld,2) = a, b;  resE -= J bm1,  dJ/dt = -a J + b E
+ *   NEKGPU_LORENTZ (cem_maxwell_lorentz, src/cem_maxwell.F:3149-3212):
+ *     params(ld,3) = a, b, c;  resE -= J1 bm1,  dJ1/dt = -a J1 - b J2 + c E,
+ *     dJ2/dt = J1
+ * index: n 1-based node numbers (drudeindex / lorentzindex); a node may be in
+ * one list once.  A call replaces that model's list (n = 0 removes it) and
+ * restarts every current and its RK register at zero.  NEKGPU_PLAIN,
+ * NEKGPU_FUSED64 and NEKGPU_MIXED (currents in FP64 in all three). */
+int nekgpu_set_dispersive(nekgpu_ctx* ctx, int model, const double* params, long ld,
+                          const int* index, long n);
+/* The currents in the reference layout, jn(ld,3) (Drude) or jn(ld,3,2)
+ * (Lorentz: J1 then J2); only listed nodes are read, other nodes read 0. */
+int nekgpu_set_current(nekgpu_ctx* ctx, int model, const double* jn, long ld);
+int nekgpu_get_current(nekgpu_ctx* ctx, int model, double* jn, long ld);
+
 /* ---- state --------------------------------------------------------------- */
 /* hn(ld,3), en(ld,3) host arrays, ld >= npts (lpts1 in the reference). */
 int nekgpu_set_state(nekgpu_ctx* ctx, const double* hn, const double* en, long ld);
@@ -273,7 +295,8 @@ int nekgpu_adjoint_run(nekgpu_ctx* ctx, int nsteps, double t0, double dt, double
 int nekgpu_write_vtk(nekgpu_ctx* ctx, const char* path, const double* solhn, const double* solen,
                      long ld);
 /* Checkpoints of the device state (fields, RK register, PML auxiliary fields
- * and registers, raw FP64) with the time and step number; loading one into a
+ * and dispersive currents with their registers, raw FP64) with the time and
+ * step number; loading one into a
  * context of the same form and mesh (else NEKGPU_ERR_MESH) continues the run
  * bit for bit.  No counterpart in the reference's non-MPI build, whose
  * restart writers are empty (src/io_vtkbin.c:307-322). */

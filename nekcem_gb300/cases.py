@@ -207,6 +207,65 @@ def gaussian_pulse_ez(center, sigma):
     return init
 
 
+class DispersiveWave:
+    """Plane wave along x (E_y, H_z) in a uniform dispersive medium, the
+    analytic mode of the Maxwell system with the reference's polarisation
+    currents (cem_maxwell_drude / cem_maxwell_lorentz,
+    src/cem_maxwell.F:3095-3212):
+
+        eps dE/dt = curl H - J1,   mu dH/dt = -curl E,
+        Drude:   dJ1/dt = -a J1 + b E
+        Lorentz: dJ1/dt = -a J1 - b J2 + c E,   dJ2/dt = J1
+
+    Fields are Re(X exp(i(k x - w t))) with E_y amplitude 1 and the complex
+    frequency w a root of the dispersion relation (the least damped root with
+    Re w > 0, the upper branch when there are two)."""
+
+    def __init__(self, model: str, a: float, b: float, c: float = 0.0, k: float = 1.0,
+                 eps: float = 1.0, mu: float = 1.0):
+        self.model, self.a, self.b, self.c = model, a, b, c
+        self.k, self.eps, self.mu = k, eps, mu
+        k2 = k * k / mu
+        if model == "drude":
+            poly = [-1j * eps, a * eps, 1j * (k2 + b), -a * k2]
+        elif model == "lorentz":
+            poly = [-eps, -1j * a * eps, eps * b + k2 + c, 1j * a * k2, -b * k2]
+        else:
+            raise KeyError(model)
+        roots = [w for w in np.roots(poly) if w.real > 1e-9]
+        self.omega = max(roots, key=lambda w: (round(w.imag, 12), w.real))
+        w = self.omega
+        self.Hh = k / (mu * w)
+        if model == "drude":
+            self.J1 = b / (a - 1j * w)
+            self.J2 = 0.0
+        else:
+            den = b - w * w - 1j * a * w
+            self.J1 = c * (-1j * w) / den
+            self.J2 = c / den
+
+    def residual(self) -> float:
+        """|-i w eps E + i k H + J1| of the E equation (0 up to rounding)"""
+        w = self.omega
+        return abs(-1j * w * self.eps + 1j * self.k * self.Hh + self.J1)
+
+    def exact(self, x, y, z, t):
+        ph = np.exp(1j * (self.k * np.asarray(x) - self.omega * t))
+        zero = np.zeros(np.shape(x))
+        H = np.stack([zero, zero, (self.Hh * ph).real])
+        E = np.stack([zero, (ph).real, zero])
+        return H, E
+
+    def currents(self, x, y, z, t):
+        """J1 (3, n) for Drude; J1 then J2 (6, n) for Lorentz"""
+        ph = np.exp(1j * (self.k * np.asarray(x) - self.omega * t))
+        zero = np.zeros(np.shape(x))
+        J = [zero, (self.J1 * ph).real, zero]
+        if self.model == "lorentz":
+            J += [zero, (self.J2 * ph).real, zero]
+        return np.stack(J)
+
+
 def zero_fields(x, y, z):
     return np.zeros((3, x.size)), np.zeros((3, x.size))
 

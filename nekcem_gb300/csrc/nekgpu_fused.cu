@@ -169,7 +169,7 @@ struct Cfg {
   static constexpr int kMinBlocks = kMixed ? (NT <= 256 ? 4 : (NT <= 512 ? 2 : 1)) : 1;
 };
 
-template <int NX, typename T, bool PML>
+template <int NX, typename T, bool EXT>
 __global__ void __launch_bounds__(Cfg<NX, T>::NT, Cfg<NX, T>::kMinBlocks)
     k_fused_stage(const FusedDev a) {
   using C = Cfg<NX, T>;
@@ -390,7 +390,7 @@ __global__ void __launch_bounds__(Cfg<NX, T>::NT, Cfg<NX, T>::kMinBlocks)
       // ---- PML (pml_step, src/cem_maxwell_pml.F:508-590), FP64 form only:
       // auxiliary residuals from the residual so far, their RK update
       // (src/cem_maxwell.F:1942-1955), and their contribution to res
-      if (PML && !C::kMixed) {
+      if (EXT && !C::kMixed && a.pml.slot) {
         const int l = a.pml.slot[e];
         if (l >= 0) {
           const long nn = a.pml.n, q = (long)l * N3 + tid;
@@ -428,6 +428,38 @@ __global__ void __launch_bounds__(Cfg<NX, T>::NT, Cfg<NX, T>::kMinBlocks)
             const double kv = first_stage ? a.dt * rp[cc] : fma(a.a, kx[cc * nn + q], a.dt * rp[cc]);
             kx[cc * nn + q] = kv;
             aux[cc * nn + q] = fma(a.b, kv, cc < 3 ? bn[cc] : dn[cc - 3]);
+          }
+        }
+      }
+      // ---- dispersive currents inside usersrc (cem_maxwell_drude /
+      // cem_maxwell_lorentz, src/cem_maxwell.F:3095-3212), FP64 form only:
+      // resE -= J1 bm1, the currents' residuals and their RK update
+      if (EXT && !C::kMixed && a.disp.slot) {
+        const int l = a.disp.slot[e];
+        if (l >= 0) {
+          const DispDev& d = a.disp;
+          const long nn = d.n, q = (long)l * N3 + tid;
+          const int kind = (int)d.data[q];
+          if (kind != 0) {
+            const double pa = d.data[nn + q], pb = d.data[2 * nn + q], pc = d.data[3 * nn + q];
+            const double bm1 = d.data[4 * nn + q];
+            const double* en = s_u64 + 3 * N3;
+#pragma unroll
+            for (int cc = 0; cc < 3; ++cc) {
+              const double j1 = d.aux[cc * nn + q], ev = en[cc * N3 + tid];
+              res[3 + cc] = (T)((double)res[3 + cc] - j1 * bm1);
+              double r1 = -pa * j1 + pb * ev;
+              if (kind == 2) {
+                const double j2 = d.aux[(3 + cc) * nn + q];
+                r1 = -pa * j1 - pb * j2 + pc * ev;
+                const double k2 = first_stage ? a.dt * j1 : fma(a.a, d.k[(3 + cc) * nn + q], a.dt * j1);
+                d.k[(3 + cc) * nn + q] = k2;
+                d.aux[(3 + cc) * nn + q] = fma(a.b, k2, j2);
+              }
+              const double k1 = first_stage ? a.dt * r1 : fma(a.a, d.k[cc * nn + q], a.dt * r1);
+              d.k[cc * nn + q] = k1;
+              d.aux[cc * nn + q] = fma(a.b, k1, j1);
+            }
           }
         }
       }
@@ -473,12 +505,12 @@ __global__ void k_scale_coef(double* coef, const double* base, long n2, double d
   coef[i] = dt * base[i];
 }
 
-// PML: the variant with the PML branch (a separate instantiation, so that
-// meshes without PML keep the kernel's register budget)
-template <int NX, typename T, bool PML>
+// EXT: the variant with the PML and dispersive-current branches (a separate
+// instantiation, so that meshes without them keep the kernel's register budget)
+template <int NX, typename T, bool EXT>
 int launch(Context* c, const FusedDev& a) {
   using C = Cfg<NX, T>;
-  auto kern = k_fused_stage<NX, T, PML>;
+  auto kern = k_fused_stage<NX, T, EXT>;
   static bool ready = false;
   static int grid = 0;
   if (!ready) {
@@ -500,23 +532,23 @@ int launch(Context* c, const FusedDev& a) {
   return check_cuda(cudaGetLastError());
 }
 
-template <typename T, bool PML>
+template <typename T, bool EXT>
 int dispatch_nx(Context* c, const FusedDev& a) {
   switch (c->nx) {
-    case 3: return launch<3, T, PML>(c, a);
-    case 4: return launch<4, T, PML>(c, a);
-    case 5: return launch<5, T, PML>(c, a);
-    case 6: return launch<6, T, PML>(c, a);
-    case 7: return launch<7, T, PML>(c, a);
-    case 8: return launch<8, T, PML>(c, a);
-    case 9: return launch<9, T, PML>(c, a);
+    case 3: return launch<3, T, EXT>(c, a);
+    case 4: return launch<4, T, EXT>(c, a);
+    case 5: return launch<5, T, EXT>(c, a);
+    case 6: return launch<6, T, EXT>(c, a);
+    case 7: return launch<7, T, EXT>(c, a);
+    case 8: return launch<8, T, EXT>(c, a);
+    case 9: return launch<9, T, EXT>(c, a);
     default: return NEKGPU_ERR_UNSUPPORTED;
   }
 }
 
 template <typename T>
 int dispatch(Context* c, const FusedDev& a) {
-  return a.pml.slot ? dispatch_nx<T, true>(c, a) : dispatch_nx<T, false>(c, a);
+  return (a.pml.slot || a.disp.slot) ? dispatch_nx<T, true>(c, a) : dispatch_nx<T, false>(c, a);
 }
 
 }  // namespace

@@ -1043,6 +1043,7 @@ int plain_stage(Context* c, int rkstep, double time, double dt) {
   if ((st = plain_flux3d(c))) return st;
   if ((st = plain_add_flux_to_res(c))) return st;
   if ((st = plain_pml_step(c))) return st;
+  if ((st = plain_dispersive(c, c->rk_a[rkstep - 1], c->rk_b[rkstep - 1], dt))) return st;
   if (c->src.enabled && (st = plain_usersrc(c, source_ft(c->src, rktime)))) return st;
   if ((st = plain_invqmass(c))) return st;
   if ((st = plain_rk_update(c, c->rk_a[rkstep - 1], c->rk_b[rkstep - 1], dt))) return st;
@@ -1298,6 +1299,119 @@ int nekgpu_set_source_kind(nekgpu_ctx* c, int kind) {
   if (!c || kind < 0 || kind > 1) return NEKGPU_ERR_ARG;
   c->src.kind = kind;
   return NEKGPU_OK;
+}
+
+// Dispersive media: the per-node model and parameters live on the host; each
+// call rebuilds the compact per-element device arrays of all listed nodes.
+int nekgpu_set_dispersive(nekgpu_ctx* c, int model, const double* params, long ld,
+                          const int* index, long n) {
+  if (!c || (model != NEKGPU_DRUDE && model != NEKGPU_LORENTZ) || n < 0 ||
+      (n > 0 && (!params || !index || ld < c->npts)))
+    return NEKGPU_ERR_ARG;
+  if (c->form == NEKGPU_MIXED_NAIVE) return NEKGPU_ERR_UNSUPPORTED;
+  const long P = c->npts, n3 = (long)c->nx * c->nx * c->nx;
+  std::vector<signed char> kind = c->disp_kind;
+  std::vector<double> par = c->disp_par;
+  if (kind.empty()) {
+    kind.assign(P, 0);
+    par.assign(3 * P, 0.0);
+  }
+  for (long j = 0; j < P; ++j)
+    if (kind[j] == model) kind[j] = 0;
+  for (long i = 0; i < n; ++i) {
+    const long j = (long)index[i] - 1;
+    if (j < 0 || j >= P || kind[j] != 0) return NEKGPU_ERR_ARG;  // out of range or listed twice
+    kind[j] = (signed char)model;
+    par[j] = params[j];
+    par[P + j] = params[ld + j];
+    par[2 * P + j] = model == NEKGPU_LORENTZ ? params[2 * ld + j] : 0.0;
+  }
+  std::vector<int> slot(c->nelt, -1), elems;
+  for (int e = 0; e < c->nelt; ++e)
+    for (long v = 0; v < n3; ++v)
+      if (kind[e * n3 + v]) {
+        slot[e] = (int)elems.size();
+        elems.push_back(e);
+        break;
+      }
+  const long nn = (long)elems.size() * n3;
+  DispDev d{};
+  if (nn) {
+    std::vector<double> data((size_t)kDispData * nn, 0.0);
+    for (size_t l = 0; l < elems.size(); ++l)
+      for (long v = 0; v < n3; ++v) {
+        const long j = elems[l] * n3 + v, q = (long)l * n3 + v;
+        data[q] = kind[j];
+        for (int p = 0; p < 3; ++p) data[(1 + p) * nn + q] = par[p * P + j];
+        data[4 * nn + q] = c->host_bm1[j];
+        if (!c->host_rx.empty())
+          data[5 * nn + q] = c->host_bm1[j] / (c->host_w3[v] * c->host_rx[elems[l]]);
+      }
+    DevAlloc A(c);
+    int* d_slot;
+    int* d_elem;
+    double *d_data, *d_aux, *d_k;
+    int st;
+    if ((st = A.put(&d_slot, slot)) || (st = A.put(&d_elem, elems)) || (st = A.put(&d_data, data)) ||
+        (st = A.get(&d_aux, 6 * nn)) || (st = A.get(&d_k, 6 * nn)))
+      return st;
+    if (check_cuda(cudaMemset(d_aux, 0, 6 * nn * sizeof(double))) ||
+        check_cuda(cudaMemset(d_k, 0, 6 * nn * sizeof(double))))
+      return NEKGPU_ERR_CUDA;
+    d = DispDev{d_slot, d_elem, d_data, d_aux, d_k, nn};
+  }
+  c->disp_kind.swap(kind);
+  c->disp_par.swap(par);
+  c->disp_slot.swap(slot);
+  c->disp_elems.swap(elems);
+  c->d_disp_slot = const_cast<int*>(d.slot);
+  c->d_disp_elem = const_cast<int*>(d.elem);
+  c->d_disp_data = const_cast<double*>(d.data);
+  c->d_disp_aux = d.aux;
+  c->d_disp_k = d.k;
+  c->disp_n = nn;
+  c->pargs.disp = d;
+  c->fargs.disp = d;
+  c->margs.disp = d;
+  return NEKGPU_OK;
+}
+
+static int current_copy(nekgpu_ctx* c, int model, double* jn, long ld, bool to_device) {
+  if (!c || (model != NEKGPU_DRUDE && model != NEKGPU_LORENTZ) || !jn || ld < c->npts)
+    return NEKGPU_ERR_ARG;
+  const long P = c->npts, n3 = (long)c->nx * c->nx * c->nx, nn = c->disp_n;
+  const int nc = model == NEKGPU_DRUDE ? 3 : 6;
+  std::vector<double> aux(6 * nn);
+  if (nn && check_cuda(cudaStreamSynchronize(c->stream))) return NEKGPU_ERR_CUDA;
+  if (nn && check_cuda(cudaMemcpy(aux.data(), c->d_disp_aux, aux.size() * sizeof(double),
+                                  cudaMemcpyDeviceToHost)))
+    return NEKGPU_ERR_CUDA;
+  if (!to_device)
+    for (int q = 0; q < nc; ++q) std::fill(jn + q * ld, jn + q * ld + P, 0.0);
+  for (size_t l = 0; l < c->disp_elems.size(); ++l)
+    for (long v = 0; v < n3; ++v) {
+      const long j = (long)c->disp_elems[l] * n3 + v, t = (long)l * n3 + v;
+      if (c->disp_kind[j] != model) continue;
+      for (int q = 0; q < nc; ++q) {
+        if (to_device)
+          aux[q * nn + t] = jn[q * ld + j];
+        else
+          jn[q * ld + j] = aux[q * nn + t];
+      }
+    }
+  if (to_device && nn &&
+      check_cuda(cudaMemcpy(c->d_disp_aux, aux.data(), aux.size() * sizeof(double),
+                            cudaMemcpyHostToDevice)))
+    return NEKGPU_ERR_CUDA;
+  return NEKGPU_OK;
+}
+
+int nekgpu_set_current(nekgpu_ctx* c, int model, const double* jn, long ld) {
+  return current_copy(c, model, const_cast<double*>(jn), ld, true);
+}
+
+int nekgpu_get_current(nekgpu_ctx* c, int model, double* jn, long ld) {
+  return current_copy(c, model, jn, ld, false);
 }
 
 int nekgpu_set_source(nekgpu_ctx* c, int enabled, const double xc[3], double sigma, double amp,

@@ -69,6 +69,21 @@ inline double source_ft(const Source& s, double t) {
 
 // Kernel argument blocks ----------------------------------------------------
 
+// Dispersive currents (cem_maxwell_drude / cem_maxwell_lorentz), compact over
+// the elements holding listed nodes (slot l holds element elem[l]); per node
+// [q][l*N3 + v]: q = 0 kind (0 none, 1 Drude, 2 Lorentz), 1 a, 2 b, 3 c,
+// 4 bm1, 5 bm1/(w3*rx) (a residual term t enters the mixed form's R as
+// t * [5]).  aux: J1 (3 rows) then J2 (3 rows, Lorentz); k: their registers.
+constexpr int kDispData = 6;
+struct DispDev {
+  const int* slot;  // nelt: slot of the element, -1 without listed nodes
+  const int* elem;  // nslot: element of each slot
+  const double* data;
+  double* aux;      // 6 * n
+  double* k;        // 6 * n
+  long n;           // nslot * N3
+};
+
 struct PlainDev {
   int nx, nelt;
   long npts, nxzfl;
@@ -100,6 +115,7 @@ struct PlainDev {
   double* pmlaux;          // 6*npts: pmlbn then pmldn
   double* pmlk;            // 6*npts: their RK registers
   double* pmlres;          // 12*npts: respmlbn, respmldn, respmlhn, respmlen
+  DispDev disp;
 };
 
 // PML data of the fused forms, compact over the PML elements (slot l holds
@@ -120,6 +136,7 @@ struct FusedDev {
   int nelt;
   long npts;
   PmlDev pml;
+  DispDev disp;
   const double* u_in;
   double* u_out;
   double* k;            // RK register read
@@ -163,6 +180,7 @@ struct MixedDev {
   float C0f;
   int* status;
   PmlDev pml;
+  DispDev disp;
   double dt;
 };
 
@@ -235,6 +253,15 @@ struct Context {
   int* d_pmlptr = nullptr;
   double *d_pml_aux = nullptr, *d_pml_k = nullptr, *d_pml_data = nullptr;
   int* d_pml_slot = nullptr;
+  // dispersive currents: per node model (0 none, 1 Drude, 2 Lorentz) and
+  // parameters a, b, c on the host; the device side in DispDev (all forms)
+  std::vector<signed char> disp_kind;
+  std::vector<double> disp_par;  // 3*npts
+  std::vector<int> disp_slot;    // nelt
+  std::vector<int> disp_elems;
+  double *d_disp_data = nullptr, *d_disp_aux = nullptr, *d_disp_k = nullptr;
+  int *d_disp_slot = nullptr, *d_disp_elem = nullptr;
+  long disp_n = 0;
   // adjoint face-slot coefficients (built on first use, FP64 fused form)
   double* d_adj_slot = nullptr;
   std::vector<double> adj_jw;  // objective weights set by nekgpu_adjoint_init
@@ -266,6 +293,8 @@ int plain_invqmass(Context* c);
 int plain_rk_update(Context* c, double ca, double cb, double dt);
 int plain_pml_step(Context* c);                                   // pml_step
 int plain_pml_rk_update(Context* c, double ca, double cb, double dt);
+// cem_maxwell_drude / cem_maxwell_lorentz with the currents' rk4_upd
+int plain_dispersive(Context* c, double ca, double cb, double dt);
 int plain_gs(Context* c, double* d_u, int nfld);
 
 // kernel launchers (nekgpu_fused.cu)

@@ -64,6 +64,7 @@ struct CkHeader {
   int32_t version, form, nx1, npml;
   int64_t nelt, npts, aux_len, istep;
   double time;
+  int64_t disp_len;  // 6 * nodes of the elements holding dispersive currents
 };
 
 }  // namespace
@@ -131,9 +132,10 @@ extern "C" int nekgpu_write_vtk(nekgpu_ctx* c, const char* path, const double* s
 }
 
 // ---- checkpoints -----------------------------------------------------------
-// Raw device state: the fields, the RK register and (with PML) the auxiliary
-// fields with their registers, as the context holds them; reloaded into a
-// context of the same form and mesh the run continues bit for bit.
+// Raw device state: the fields, the RK register, (with PML) the auxiliary
+// fields and (with dispersive media) the currents, each with its registers,
+// as the context holds them; reloaded into a context of the same form, mesh
+// and dispersive lists the run continues bit for bit.
 namespace {
 
 const double* state_ptr(Context* c) { return c->form == NEKGPU_PLAIN ? c->d_u[0] : c->d_u[c->cur]; }
@@ -149,7 +151,7 @@ extern "C" int nekgpu_checkpoint_save(nekgpu_ctx* c, const char* path, double ti
   if (!c->have_state) return NEKGPU_ERR_STATE;
   CkHeader h{};
   std::memcpy(h.magic, "NEKGPUCK", 8);
-  h.version = 1;
+  h.version = 2;
   h.form = c->form;
   h.nx1 = c->nx;
   h.npml = c->npml;
@@ -158,8 +160,9 @@ extern "C" int nekgpu_checkpoint_save(nekgpu_ctx* c, const char* path, double ti
   h.aux_len = aux_len(c);
   h.istep = istep;
   h.time = time;
+  h.disp_len = 6 * c->disp_n;
   const long ns = 6 * c->npts;
-  std::vector<double> buf(2 * ns + 2 * h.aux_len);
+  std::vector<double> buf(2 * ns + 2 * h.aux_len + 2 * h.disp_len);
   if (check_cuda(cudaStreamSynchronize(c->stream)) ||
       check_cuda(cudaMemcpy(buf.data(), state_ptr(c), ns * 8, cudaMemcpyDeviceToHost)) ||
       check_cuda(cudaMemcpy(buf.data() + ns, c->d_k, ns * 8, cudaMemcpyDeviceToHost)))
@@ -168,6 +171,11 @@ extern "C" int nekgpu_checkpoint_save(nekgpu_ctx* c, const char* path, double ti
       (check_cuda(cudaMemcpy(buf.data() + 2 * ns, c->d_pml_aux, h.aux_len * 8, cudaMemcpyDeviceToHost)) ||
        check_cuda(cudaMemcpy(buf.data() + 2 * ns + h.aux_len, c->d_pml_k, h.aux_len * 8,
                              cudaMemcpyDeviceToHost))))
+    return NEKGPU_ERR_CUDA;
+  double* dd = buf.data() + 2 * ns + 2 * h.aux_len;
+  if (h.disp_len &&
+      (check_cuda(cudaMemcpy(dd, c->d_disp_aux, h.disp_len * 8, cudaMemcpyDeviceToHost)) ||
+       check_cuda(cudaMemcpy(dd + h.disp_len, c->d_disp_k, h.disp_len * 8, cudaMemcpyDeviceToHost))))
     return NEKGPU_ERR_CUDA;
   FILE* f = std::fopen(path, "wb");
   if (!f) return NEKGPU_ERR_ARG;
@@ -183,14 +191,14 @@ extern "C" int nekgpu_checkpoint_load(nekgpu_ctx* c, const char* path, double* t
   if (!f) return NEKGPU_ERR_ARG;
   CkHeader h{};
   bool ok = std::fread(&h, sizeof(h), 1, f) == 1 && std::memcmp(h.magic, "NEKGPUCK", 8) == 0 &&
-            h.version == 1;
+            h.version == 2;
   if (ok && (h.form != c->form || h.nx1 != c->nx || h.nelt != c->nelt || h.npts != c->npts ||
-             h.npml != c->npml || h.aux_len != aux_len(c))) {
+             h.npml != c->npml || h.aux_len != aux_len(c) || h.disp_len != 6 * c->disp_n)) {
     std::fclose(f);
     return NEKGPU_ERR_MESH;  // a checkpoint of another mesh or form
   }
   const long ns = 6 * c->npts;
-  std::vector<double> buf(ok ? 2 * ns + 2 * h.aux_len : 0);
+  std::vector<double> buf(ok ? 2 * ns + 2 * h.aux_len + 2 * h.disp_len : 0);
   ok = ok && std::fread(buf.data(), 8, buf.size(), f) == buf.size();
   std::fclose(f);
   if (!ok) return NEKGPU_ERR_ARG;
@@ -203,6 +211,11 @@ extern "C" int nekgpu_checkpoint_load(nekgpu_ctx* c, const char* path, double* t
       (check_cuda(cudaMemcpy(c->d_pml_aux, buf.data() + 2 * ns, h.aux_len * 8, cudaMemcpyHostToDevice)) ||
        check_cuda(cudaMemcpy(c->d_pml_k, buf.data() + 2 * ns + h.aux_len, h.aux_len * 8,
                              cudaMemcpyHostToDevice))))
+    return NEKGPU_ERR_CUDA;
+  const double* dd = buf.data() + 2 * ns + 2 * h.aux_len;
+  if (h.disp_len &&
+      (check_cuda(cudaMemcpy(c->d_disp_aux, dd, h.disp_len * 8, cudaMemcpyHostToDevice)) ||
+       check_cuda(cudaMemcpy(c->d_disp_k, dd + h.disp_len, h.disp_len * 8, cudaMemcpyHostToDevice))))
     return NEKGPU_ERR_CUDA;
   c->have_state = true;
   if (time) *time = h.time;

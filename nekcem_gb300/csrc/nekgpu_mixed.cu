@@ -336,7 +336,42 @@ __device__ __forceinline__ void pml_node(const MixedDev& a, int l, int v, long g
   }
 }
 
-template <int NX, bool PML>
+// Dispersive currents (cem_maxwell_drude / cem_maxwell_lorentz,
+// src/cem_maxwell.F:3095-3212) at one node of an element holding listed
+// nodes, in FP64: resE -= J1 bm1 enters the normalised residual pair as
+// -J1 * bm1/(w3 rx), and the currents take their RK update.
+template <int N3>
+__device__ __forceinline__ void disp_node(const MixedDev& a, int l, int v, long g, bool first_stage,
+                                          float* Rh, float* Rl) {
+  const DispDev& d = a.disp;
+  const long nn = d.n, q = (long)l * N3 + v, P = a.npts;
+  const int kind = (int)d.data[q];
+  if (kind == 0) return;
+  const double pa = d.data[nn + q], pb = d.data[2 * nn + q], pc = d.data[3 * nn + q];
+  const double inv = d.data[5 * nn + q];
+  for (int c = 0; c < 3; ++c) {
+    const double j1 = d.aux[c * nn + q], ev = __ldg(a.u_in + (3 + c) * P + g);
+    const double dR = -(j1 * inv);
+    float s, e;
+    two_sum(Rh[3 + c], d2f_hi(dR), s, e);
+    Rh[3 + c] = s;
+    Rl[3 + c] = (Rl[3 + c] + d2f_lo(dR)) + e;
+    double r1 = -pa * j1 + pb * ev;
+    if (kind == 2) {
+      const double j2 = d.aux[(3 + c) * nn + q];
+      r1 = -pa * j1 - pb * j2 + pc * ev;
+      const double k2 = first_stage ? a.dt * j1 : fma(a.a, d.k[(3 + c) * nn + q], a.dt * j1);
+      d.k[(3 + c) * nn + q] = k2;
+      d.aux[(3 + c) * nn + q] = fma(a.b, k2, j2);
+    }
+    const double k1 = first_stage ? a.dt * r1 : fma(a.a, d.k[c * nn + q], a.dt * r1);
+    d.k[c * nn + q] = k1;
+    d.aux[c * nn + q] = fma(a.b, k1, j1);
+  }
+}
+
+// EXT: the variant with the PML and dispersive-current branches
+template <int NX, bool EXT>
 __global__ void __launch_bounds__(MCfg<NX>::NT, 3) k_mixed_stage(const MixedDev a) {
   using C = MCfg<NX>;
   constexpr int N2 = C::N2, N3 = C::N3, NT = C::NT, NF = C::NF, N3P = C::N3P;
@@ -567,7 +602,8 @@ __global__ void __launch_bounds__(MCfg<NX>::NT, 3) k_mixed_stage(const MixedDev 
     // residual pairs happens before the barrier that lets the next element's
     // TMA overwrite them.
     const int so = a.src_elem ? a.src_elem[e] : -1;
-    const int pml_l = PML ? a.pml.slot[e] : -1;
+    const int pml_l = (EXT && a.pml.slot) ? a.pml.slot[e] : -1;
+    const int disp_l = (EXT && a.disp.slot) ? a.disp.slot[e] : -1;
 #pragma unroll
     for (int q = 0; q < NPT; ++q) {
       const int v = tid + q * NT;
@@ -591,7 +627,8 @@ __global__ void __launch_bounds__(MCfg<NX>::NT, 3) k_mixed_stage(const MixedDev 
       if (i == 0) add(3, j + NX * k);
       if (k == 0) add(4, i + NX * j);
       if (k == NX - 1) add(5, i + NX * j);
-      if (PML && pml_l >= 0) pml_node<N3>(a, pml_l, v, (long)e * N3 + v, first_stage, Rh, Rl);
+      if (EXT && pml_l >= 0) pml_node<N3>(a, pml_l, v, (long)e * N3 + v, first_stage, Rh, Rl);
+      if (EXT && disp_l >= 0) disp_node<N3>(a, disp_l, v, (long)e * N3 + v, first_stage, Rh, Rl);
       if (so >= 0) Rl[5] = fmaf(a.src_w[(long)so * N3 + v], a.src_ftf, Rl[5]);
       const float chh = cv[q][0].x, chl = cv[q][0].y;
       const float ceh = cv[q][1].x, cel = cv[q][1].y;
@@ -627,10 +664,10 @@ __global__ void k_scale_coef_pairs(float2* coef, const double* base, long n2, do
   coef[i] = make_float2(d2f_hi(v), d2f_lo(v));
 }
 
-template <int NX, bool PML>
+template <int NX, bool EXT>
 int launch_mixed(Context* c, const MixedDev& a) {
   using C = MCfg<NX>;
-  auto kern = k_mixed_stage<NX, PML>;
+  auto kern = k_mixed_stage<NX, EXT>;
   static bool ready = false;
   static int grid = 0;
   if (!ready) {
@@ -685,14 +722,15 @@ int mixed_stage(Context* c, int rkstep, double time, double dt) {
   a.b = c->rk_b[rkstep - 1];
   a.dt = dt;
   if (c->src.enabled) a.src_ftf = (float)source_ft(c->src, time + dt * c->rk_c[rkstep - 1]);
+  const bool ext = a.pml.slot || a.disp.slot;
   switch (c->nx) {
-    case 3: st = a.pml.slot ? launch_mixed<3, true>(c, a) : launch_mixed<3, false>(c, a); break;
-    case 4: st = a.pml.slot ? launch_mixed<4, true>(c, a) : launch_mixed<4, false>(c, a); break;
-    case 5: st = a.pml.slot ? launch_mixed<5, true>(c, a) : launch_mixed<5, false>(c, a); break;
-    case 6: st = a.pml.slot ? launch_mixed<6, true>(c, a) : launch_mixed<6, false>(c, a); break;
-    case 7: st = a.pml.slot ? launch_mixed<7, true>(c, a) : launch_mixed<7, false>(c, a); break;
-    case 8: st = a.pml.slot ? launch_mixed<8, true>(c, a) : launch_mixed<8, false>(c, a); break;
-    case 9: st = a.pml.slot ? launch_mixed<9, true>(c, a) : launch_mixed<9, false>(c, a); break;
+    case 3: st = ext ? launch_mixed<3, true>(c, a) : launch_mixed<3, false>(c, a); break;
+    case 4: st = ext ? launch_mixed<4, true>(c, a) : launch_mixed<4, false>(c, a); break;
+    case 5: st = ext ? launch_mixed<5, true>(c, a) : launch_mixed<5, false>(c, a); break;
+    case 6: st = ext ? launch_mixed<6, true>(c, a) : launch_mixed<6, false>(c, a); break;
+    case 7: st = ext ? launch_mixed<7, true>(c, a) : launch_mixed<7, false>(c, a); break;
+    case 8: st = ext ? launch_mixed<8, true>(c, a) : launch_mixed<8, false>(c, a); break;
+    case 9: st = ext ? launch_mixed<9, true>(c, a) : launch_mixed<9, false>(c, a); break;
     default: return NEKGPU_ERR_UNSUPPORTED;
   }
   if (st) return st;

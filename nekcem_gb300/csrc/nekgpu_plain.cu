@@ -266,9 +266,54 @@ __global__ void k_pml_rk(PlainDev a, double ca, double cb, double dt) {
   a.pmlaux[i] = a.pmlaux[i] + cb * kh;
 }
 
+// cem_maxwell_drude (src/cem_maxwell.F:3095-3147) and cem_maxwell_lorentz
+// (:3149-3212) at one node of an element holding listed nodes, followed by
+// the rk4_upd of its currents; unlisted nodes (kind 0) are left alone, as the
+// reference's rk4_upd leaves a zero current with a zero residual.
+__global__ void k_dispersive(PlainDev a, int n3, double ca, double cb, double dt) {
+  const long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  const DispDev& d = a.disp;
+  if (t >= d.n) return;
+  const long nn = d.n, P = a.npts;
+  const int kind = (int)d.data[t];
+  if (kind == 0) return;
+  const long j = (long)d.elem[t / n3] * n3 + t % n3;
+  const double pa = d.data[nn + t], pb = d.data[2 * nn + t], pc = d.data[3 * nn + t];
+  const double bm1 = d.data[4 * nn + t];
+  const double* en = a.u + 3 * P;
+  double* rse = a.res + 3 * P;
+  for (int q = 0; q < 3; ++q) {
+    const double j1 = d.aux[q * nn + t];
+    rse[j + q * P] = rse[j + q * P] - j1 * bm1;
+    if (kind == 1) {
+      const double r = -pa * j1 + pb * en[j + q * P];
+      const double kh = ca * d.k[q * nn + t] + dt * r;
+      d.k[q * nn + t] = kh;
+      d.aux[q * nn + t] = j1 + cb * kh;
+    } else {
+      const double j2 = d.aux[(3 + q) * nn + t];
+      const double r1 = -pa * j1 - pb * j2 + pc * en[j + q * P];
+      const double k1 = ca * d.k[q * nn + t] + dt * r1;
+      const double k2 = ca * d.k[(3 + q) * nn + t] + dt * j1;
+      d.k[q * nn + t] = k1;
+      d.k[(3 + q) * nn + t] = k2;
+      d.aux[q * nn + t] = j1 + cb * k1;
+      d.aux[(3 + q) * nn + t] = j2 + cb * k2;
+    }
+  }
+}
+
 int last_error() { return check_cuda(cudaGetLastError()); }
 
 }  // namespace
+
+int plain_dispersive(Context* c, double ca, double cb, double dt) {
+  if (!c->pargs.disp.n) return NEKGPU_OK;
+  const int n3 = c->nx * c->nx * c->nx;
+  k_dispersive<<<blocks_for(c->pargs.disp.n), kThreads, 0, c->stream>>>(c->pargs, n3, ca, cb, dt);
+  c->last_launches += 1;
+  return last_error();
+}
 
 int plain_cem_maxwell(Context* c) {
   const int n = c->nx, n3 = n * n * n;

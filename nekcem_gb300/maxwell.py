@@ -151,6 +151,39 @@ class MaxwellGPU:
         L.check(L.load().nekgpu_set_source(self._h, 1 if enabled else 0, x, sigma, amp, f0, t0),
                 "nekgpu_set_source")
 
+    # ---- dispersive media (cem_maxwell_drude / cem_maxwell_lorentz) ----------
+    DRUDE, LORENTZ = 1, 2
+
+    def set_dispersive(self, model: int, params, index):
+        """Polarisation currents at the 0-based nodes ``index``: Drude
+        (params (2, npts) = a, b) or Lorentz (params (3, npts) = a, b, c).
+        Replaces the model's list and restarts all currents at zero."""
+        ncol = 2 if model == self.DRUDE else 3
+        index = np.ascontiguousarray(index, dtype=np.int32).reshape(-1) + 1
+        n = int(index.size)
+        if n:
+            params = np.ascontiguousarray(params, dtype=np.float64).reshape(ncol, self.npts)
+            pp, ld = _dp(params), self.npts
+        else:
+            pp, ld = None, self.npts
+        L.check(L.load().nekgpu_set_dispersive(self._h, int(model), pp, ld,
+                                               index.ctypes.data_as(L.ip), n),
+                "nekgpu_set_dispersive")
+
+    def set_current(self, model: int, J):
+        nc = 3 if model == self.DRUDE else 6
+        J = np.ascontiguousarray(J, dtype=np.float64).reshape(nc, self.npts)
+        L.check(L.load().nekgpu_set_current(self._h, int(model), _dp(J), self.npts),
+                "nekgpu_set_current")
+
+    def get_current(self, model: int) -> np.ndarray:
+        """(3, npts) Drude J or (6, npts) Lorentz J1, J2; zero off the lists"""
+        nc = 3 if model == self.DRUDE else 6
+        J = np.empty((nc, self.npts))
+        L.check(L.load().nekgpu_get_current(self._h, int(model), _dp(J), self.npts),
+                "nekgpu_get_current")
+        return J
+
     # ---- fields (Fortran hn(npts,3), en(npts,3) as (3, npts)) --------------
     def set_state(self, H: np.ndarray, E: np.ndarray):
         H = np.ascontiguousarray(H, dtype=np.float64).reshape(3, self.npts)

@@ -48,6 +48,16 @@ struct ref_ctx {
   int ifpml, maxpml, *pmltag, *pmlptr;
   double *pmlsigma, *pmlbn, *pmldn, *kpmlbn, *kpmldn, *respmlbn, *respmldn, *respmlhn, *respmlen;
   double pmlinner[6], pmlouter[6];
+  /* dispersive media (the /userdrude/ and /userlorentz/ blocks of
+   * tests/drude/drude.usr and tests/lorentz/lorentz.usr): per node parameters
+   * (npts,2) / (npts,3), 0-based index lists, currents jn(npts,3) /
+   * jn(npts,3,2) with their RK registers and residuals */
+  long ndrude, nlorentz;
+  int *drudeindex, *lorentzindex;
+  double *drudeparams, *djn, *dkjn, *dresjn;
+  double *lorentzparams, *ljn, *lkjn, *lresjn;
+  int rkstep_now; /* stage of the op in progress (0 outside ref_rk_stage) */
+  double dt_now;
   double volvm1;
 };
 
@@ -601,6 +611,10 @@ void ref_destroy(ref_ctx* c) {
                  c->respmldn, c->respmlhn, c->respmlen};
   for (size_t i = 0; i < sizeof(p) / sizeof(p[0]); ++i) free(p[i]);
   free(c->pmltag); free(c->pmlptr);
+  double* q[] = {c->drudeparams, c->djn, c->dkjn, c->dresjn,
+                 c->lorentzparams, c->ljn, c->lkjn, c->lresjn};
+  for (size_t i = 0; i < sizeof(q) / sizeof(q[0]); ++i) free(q[i]);
+  free(c->drudeindex); free(c->lorentzindex);
   free(c->gs_order); free(c->gs_start);
   free(c);
 }
@@ -628,6 +642,8 @@ double* ref_darray(ref_ctx* c, const char* name, long* len) {
       {"pmlbn", c->pmlbn, c->pmlbn ? 3 * c->npts : 0},
       {"pmldn", c->pmldn, c->pmldn ? 3 * c->npts : 0},
       {"pmlinner", c->pmlinner, c->ifpml ? 6 : 0}, {"pmlouter", c->pmlouter, c->ifpml ? 6 : 0},
+      {"drudejn", c->djn, c->djn ? 3 * c->npts : 0},
+      {"lorentzjn", c->ljn, c->ljn ? 6 * c->npts : 0},
   };
   for (size_t i = 0; i < sizeof(t) / sizeof(t[0]); ++i)
     if (strcmp(t[i].nm, name) == 0) { if (len) *len = t[i].n; return t[i].p; }
@@ -893,6 +909,84 @@ void ref_add_flux_to_res(ref_ctx* c) {
     }
 }
 
+/* ------------------------------------------------------------------------ */
+/* Dispersive media, called from usersrc (tests/drude/drude.usr:167,        */
+/* tests/lorentz/lorentz.usr:174)                                           */
+/* ------------------------------------------------------------------------ */
+
+/* Drude and Lorentz parameters at the listed nodes (0-based); the currents,
+ * their RK registers and residuals restart at zero (uservp, rzero) */
+void ref_set_drude(ref_ctx* c, const double* params, const int* index, long n) {
+  long np = c->npts;
+  free(c->drudeparams); free(c->djn); free(c->dkjn); free(c->dresjn); free(c->drudeindex);
+  c->drudeparams = dalloc(2 * np);
+  memcpy(c->drudeparams, params, 2 * np * sizeof(double));
+  c->djn = dalloc(3 * np); c->dkjn = dalloc(3 * np); c->dresjn = dalloc(3 * np);
+  c->drudeindex = ialloc(n);
+  memcpy(c->drudeindex, index, (size_t)n * sizeof(int));
+  c->ndrude = n;
+}
+
+void ref_set_lorentz(ref_ctx* c, const double* params, const int* index, long n) {
+  long np = c->npts;
+  free(c->lorentzparams); free(c->ljn); free(c->lkjn); free(c->lresjn); free(c->lorentzindex);
+  c->lorentzparams = dalloc(3 * np);
+  memcpy(c->lorentzparams, params, 3 * np * sizeof(double));
+  c->ljn = dalloc(6 * np); c->lkjn = dalloc(6 * np); c->lresjn = dalloc(6 * np);
+  c->lorentzindex = ialloc(n);
+  memcpy(c->lorentzindex, index, (size_t)n * sizeof(int));
+  c->nlorentz = n;
+}
+
+/* cem_maxwell_drude (src/cem_maxwell.F:3095-3147): resE -= jn bm1,
+ * resjn = -a jn + b en at the listed nodes, then rk4_upd of jn on all nodes */
+static void drude_step(ref_ctx* c, int rkstep, double dt) {
+  long np = c->npts;
+  const double* pa = c->drudeparams;
+  for (long i = 0; i < c->ndrude; ++i) {
+    long j = c->drudeindex[i];
+    double a = pa[j], b = pa[np + j];
+    for (int q = 0; q < 3; ++q) {
+      c->resen[j + q * np] = c->resen[j + q * np] - c->djn[j + q * np] * c->bm1[j];
+      c->dresjn[j + q * np] = -a * c->djn[j + q * np] + b * c->en[j + q * np];
+    }
+  }
+  double ra[5], rb[5], rc[6];
+  ref_rk_coeffs(ra, rb, rc);
+  for (int q = 0; q < 3; ++q)
+    ref_rk4_upd(c->djn + q * np, c->dkjn + q * np, c->dresjn + q * np, rb[rkstep - 1],
+                ra[rkstep - 1], dt, np);
+}
+
+/* cem_maxwell_lorentz (src/cem_maxwell.F:3149-3212): resE -= jn1 bm1,
+ * resjn1 = -a jn1 - b jn2 + c en, resjn2 = jn1, then rk4_upd of both */
+static void lorentz_step(ref_ctx* c, int rkstep, double dt) {
+  long np = c->npts;
+  const double* pa = c->lorentzparams;
+  double* j1 = c->ljn;
+  double* j2 = c->ljn + 3 * np;
+  for (long i = 0; i < c->nlorentz; ++i) {
+    long j = c->lorentzindex[i];
+    double a = pa[j], b = pa[np + j], cc = pa[2 * np + j];
+    for (int q = 0; q < 3; ++q) {
+      c->resen[j + q * np] = c->resen[j + q * np] - j1[j + q * np] * c->bm1[j];
+      c->lresjn[j + q * np] = -a * j1[j + q * np] - b * j2[j + q * np] + cc * c->en[j + q * np];
+      c->lresjn[j + (3 + q) * np] = j1[j + q * np];
+    }
+  }
+  double ra[5], rb[5], rc[6];
+  ref_rk_coeffs(ra, rb, rc);
+  for (int q = 0; q < 6; ++q)
+    ref_rk4_upd(c->ljn + q * np, c->lkjn + q * np, c->lresjn + q * np, rb[rkstep - 1],
+                ra[rkstep - 1], dt, np);
+}
+
+/* the dispersive currents inside usersrc, before the volume source */
+void ref_dispersive(ref_ctx* c, int rkstep, double dt) {
+  if (c->djn) drude_step(c, rkstep, dt);
+  if (c->ljn) lorentz_step(c, rkstep, dt);
+}
+
 /* usersrc (src/cem_maxwell.F:503): mass-weighted E_z source */
 void ref_usersrc(ref_ctx* c, double rktime) {
   if (!c->src_w) return;
@@ -1093,6 +1187,7 @@ void ref_maxwell_op(ref_ctx* c, double rktime) {
   ref_flux3d(c);
   ref_add_flux_to_res(c);
   if (c->ifpml) ref_pml_step(c);
+  if (c->rkstep_now > 0) ref_dispersive(c, c->rkstep_now, c->dt_now);
   ref_usersrc(c, rktime);
   ref_invqmass(c);
 }
@@ -1133,7 +1228,10 @@ void ref_rk_stage(ref_ctx* c, int rkstep, double time, double dt) {
   double a[5], b[5], cc[6];
   ref_rk_coeffs(a, b, cc);
   double rktime = time + dt * cc[rkstep - 1];
+  c->rkstep_now = rkstep;
+  c->dt_now = dt;
   ref_maxwell_op(c, rktime);
+  c->rkstep_now = 0;
   long np = c->npts;
   for (int q = 0; q < 3; ++q)
     ref_rk4_upd(c->hn + q * np, c->khn + q * np, c->reshn + q * np, b[rkstep - 1], a[rkstep - 1],

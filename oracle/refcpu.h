@@ -81,6 +81,16 @@ void ref_set_pml(ref_ctx* c, int thick, double order, double referr);
 /* pml_step (src/cem_maxwell_pml.F:508-590), after the lift and before usersrc */
 void ref_pml_step(ref_ctx* c);
 
+/* Dispersive media (cem_maxwell_drude / cem_maxwell_lorentz,
+ * src/cem_maxwell.F:3095-3212, called from usersrc in tests/drude and
+ * tests/lorentz).  params: Drude (npts,2) = a, b; Lorentz (npts,3) = a, b, c;
+ * index: n 0-based nodes.  Inside ref_rk_stage the currents are advanced with
+ * the stage (before the volume source); the currents are the darrays
+ * "drudejn" (npts,3) and "lorentzjn" (npts,3,2), zero after these calls. */
+void ref_set_drude(ref_ctx* c, const double* params, const int* index, long n);
+void ref_set_lorentz(ref_ctx* c, const double* params, const int* index, long n);
+void ref_dispersive(ref_ctx* c, int rkstep, double dt);
+
 /* ---- the reference routines on the hot path ---- */
 void ref_local_grad3(double* ur, double* us, double* ut, const double* u, int n,
                      const double* D, const double* Dt);

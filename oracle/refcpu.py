@@ -61,6 +61,8 @@ def lib():
         L.ref_set_source_kind.argtypes = [vp, ip]
         L.ref_set_pml.argtypes = [vp, ip, C.c_double, C.c_double]
         L.ref_pml_step.argtypes = [vp]
+        L.ref_set_drude.argtypes = [vp, dp, C.POINTER(C.c_int), C.c_long]
+        L.ref_set_lorentz.argtypes = [vp, dp, C.POINTER(C.c_int), C.c_long]
         L.ref_source_time.restype = C.c_double
         L.ref_source_time.argtypes = [C.c_double, C.c_double, C.c_double]
         for nm in ("ref_cem_maxwell", "ref_restrict_to_face", "ref_flux3d", "ref_flux_pre",
@@ -184,6 +186,33 @@ class RefBox:
 
     def set_pml(self, thick: int, order: float, referr: float):
         lib().ref_set_pml(self._c, int(thick), float(order), float(referr))
+
+    def _set_dispersive(self, fn, params, index, ncol):
+        params = np.ascontiguousarray(params, dtype=np.float64).reshape(-1)
+        assert params.size == ncol * self.npts
+        index = np.ascontiguousarray(index, dtype=np.int32)
+        assert index.size == 0 or (index.min() >= 0 and index.max() < self.npts)
+        fn(self._c, _dp(params), index.ctypes.data_as(C.POINTER(C.c_int)), int(index.size))
+
+    def set_drude(self, a, b, index):
+        """Drude current jn at the 0-based nodes ``index`` (cem_maxwell_drude):
+        dJ/dt = -a J + b E, resE -= J bm1; a, b per node (npts each)."""
+        self._set_dispersive(lib().ref_set_drude, np.stack([a, b]), index, 2)
+
+    def set_lorentz(self, a, b, c, index):
+        """Lorentz currents (cem_maxwell_lorentz): dJ1/dt = -a J1 - b J2 + c E,
+        dJ2/dt = J1, resE -= J1 bm1."""
+        self._set_dispersive(lib().ref_set_lorentz, np.stack([a, b, c]), index, 3)
+
+    @property
+    def drude_jn(self):
+        """(3, npts) view of the Drude current"""
+        return self.d("drudejn").reshape(3, self.npts)
+
+    @property
+    def lorentz_jn(self):
+        """(6, npts) view of the Lorentz currents: J1 (3 rows) then J2"""
+        return self.d("lorentzjn").reshape(6, self.npts)
 
     def set_source_kind(self, kind: int):
         lib().ref_set_source_kind(self._c, int(kind))
