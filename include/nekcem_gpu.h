@@ -141,6 +141,15 @@ int nekgpu_init(nekgpu_ctx** ctx, const nekgpu_mesh* mesh, int form);
 /* Builds the box case on the host (GLL points, geometry, face pairing,
  * materials) and uploads it. */
 int nekgpu_init_box(nekgpu_ctx** ctx, const nekgpu_box* box, int form);
+/* The 2-D forms (the reference's ldim = 2 build): imode 1 = TE (E1, E2, H3),
+ * 2 = TM (H1, H2, E3), param(4).  The mesh holds the 2-D arrays: w3mn nx1^2,
+ * rxmn/rymn/sxmn/symn (the 2-D cofactors of GLMAPM1), face arrays of
+ * nxzfl = 4 nx1 nelt slots in the reference's 2-D face numbering; the z
+ * metrics, unzm and zmn are not read.  One kernel per RK stage in the
+ * reference's FP64 arithmetic (bit-identical to the CPU path); fields keep
+ * the (ld,3) layout with the inactive components left as set.  No source,
+ * dispersive media, PML, adjoint or VTK output in 2-D. */
+int nekgpu_init2d(nekgpu_ctx** ctx, const nekgpu_mesh* mesh, int imode);
 int nekgpu_finalize(nekgpu_ctx* ctx);
 
 /* Host-only (no GPU needed): the box builder's reference-layout arrays, for

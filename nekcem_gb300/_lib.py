@@ -64,6 +64,7 @@ SIGNATURES = [
     ("nekgpu_device_check", C.c_int, [C.c_int]),
     ("nekgpu_init", C.c_int, [C.POINTER(C.c_void_p), C.POINTER(NekgpuMesh), C.c_int]),
     ("nekgpu_init_box", C.c_int, [C.POINTER(C.c_void_p), C.POINTER(NekgpuBox), C.c_int]),
+    ("nekgpu_init2d", C.c_int, [C.POINTER(C.c_void_p), C.POINTER(NekgpuMesh), C.c_int]),
     ("nekgpu_finalize", C.c_int, [C.c_void_p]),
     ("nekgpu_box_export_d", C.c_int, [C.POINTER(NekgpuBox), C.c_char_p, dp, C.POINTER(C.c_long)]),
     ("nekgpu_box_export_i", C.c_int, [C.POINTER(NekgpuBox), C.c_char_p, lp, C.POINTER(C.c_long)]),

@@ -30,6 +30,7 @@ SOURCES = {
     "nekgpu_adjoint.cu": [],
     "nekgpu_adjoint_host.cpp": ["-Xcompiler", "-ffp-contract=off"],
     "nekgpu_io.cpp": [],
+    "nekgpu_2d.cu": ["--fmad=false"],
 }
 
 

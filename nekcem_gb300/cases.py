@@ -151,6 +151,58 @@ def sol_planewave(x, y, z, t):
 
 # ---- materials and sources -----------------------------------------------------
 
+TE, TM = 1, 2
+
+
+def sol_2dboxpec(mode: int):
+    """tests/2dboxpec/2dboxpec.usr usersol: [-1,1]^2 PEC, w = 1.5 pi,
+    omega = sqrt(2); TM: Hx, Hy, Ez; TE: Hz, Ex, Ey."""
+    ww, om = 1.5 * np.pi, np.sqrt(2.0)
+
+    def sol(x, y, z, t):
+        tmph = np.sin(ww * om * t) / om
+        tmpe = np.cos(ww * om * t)
+        zero = np.zeros_like(x)
+        if mode == TM:
+            H = np.stack([np.cos(ww * x) * np.sin(ww * y) * tmph,
+                          -np.sin(ww * x) * np.cos(ww * y) * tmph, zero])
+            E = np.stack([zero, zero, np.cos(ww * x) * np.cos(ww * y) * tmpe])
+        else:
+            H = np.stack([zero, zero, np.sin(ww * x) * np.sin(ww * y) * tmpe])
+            E = np.stack([np.sin(ww * x) * np.cos(ww * y) * tmph,
+                          -np.cos(ww * x) * np.sin(ww * y) * tmph, zero])
+        return H, E
+    return sol
+
+
+def sol_2dboxper(mode: int):
+    """tests/2dboxper/2dboxper.usr usersol: [0,2pi]^2 periodic, omega = sqrt(2)."""
+    om = np.sqrt(2.0)
+
+    def sol(x, y, z, t):
+        zero = np.zeros_like(x)
+        if mode == TM:
+            tmph, tmpe = np.sin(om * t) / om, np.cos(om * t)
+            H = np.stack([np.cos(x) * np.sin(y) * tmph, -np.sin(x) * np.cos(y) * tmph, zero])
+            E = np.stack([zero, zero, np.cos(x) * np.cos(y) * tmpe])
+        else:
+            tmph, tmpe = np.cos(om * t), np.sin(om * t) / om
+            H = np.stack([zero, zero, np.sin(x) * np.sin(y) * tmph])
+            E = np.stack([np.sin(x) * np.cos(y) * tmpe, -np.cos(x) * np.sin(y) * tmpe, zero])
+        return H, E
+    return sol
+
+
+# the reference's 2-D known-answer cases: 3x3 quadrilaterals, N=8, dt 0.005,
+# 1000 steps; tolerances per active component (userchk)
+CASES_2D = {
+    "2dboxpec": dict(N=8, nel=(3, 3), lo=(-1.0, -1.0), hi=(1.0, 1.0), bc=(PEC, PEC), dt=0.005,
+                     nsteps=1000, sol=sol_2dboxpec, l2tol=1e-6, linftol=1e-5),
+    "2dboxper": dict(N=8, nel=(3, 3), lo=(0.0, 0.0), hi=(TWO_PI, TWO_PI), bc=(PERIODIC, PERIODIC),
+                     dt=0.005, nsteps=1000, sol=sol_2dboxper, l2tol=5e-8, linftol=5e-7),
+}
+
+
 def eps_sphere(x, y, z, center=(0.5, 0.5, 0.5), radius=0.25, inside=4.0):
     r2 = (x - center[0]) ** 2 + (y - center[1]) ** 2 + (z - center[2]) ** 2
     return np.where(r2 < radius * radius, inside, 1.0)

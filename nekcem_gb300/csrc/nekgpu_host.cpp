@@ -857,10 +857,10 @@ int upload_pml_fused(Context* c, DevAlloc& A, const Compact& cp, PmlDev& out) {
 }
 
 // D in the FP32 pieces of the mixed form's exact-hi contraction, as float
-// pairs [0][i + n*l] = (Dh, Df), [1][i + n*l] = (Dm, Dl) of D(i,l): Dh on a
-// 10-bit grid of row i (so every product Dh*uh with uh on a 10-bit grid has
-// at most 21 bits and the sum over <= 16 terms stays exact in FP32),
-// Df = RN32(D), Dm = RN32(D - Dh), Dl = RN32(D - Dh - Dm).
+// pairs [0][i + n*l] = (Dh, Df) of D(i,l) and [1][j + H*l] =
+// (Dm(2j,l), Dm(2j+1,l)), H = (n+1)/2: Dh on a 10-bit grid of row i (so every
+// product Dh*uh with uh on a 10-bit grid has at most 21 bits and the sum over
+// <= 16 terms stays exact in FP32), Df = RN32(D), Dm = RN32(D - Dh).
 void split_D(const std::vector<double>& D, int n, std::vector<float>& tab) {
   const int M2 = kMaxMixed * kMaxMixed;
   tab.assign(4 * (size_t)M2, 0.0f);
@@ -873,12 +873,10 @@ void split_D(const std::vector<double>& D, int n, std::vector<float>& tab) {
     for (int l = 0; l < n; ++l) {
       const size_t k = i + (size_t)n * l;
       const double h = std::nearbyint(D[k] / qd) * qd;  // at most 11 significant bits
-      const double r = D[k] - h;
-      const float m = (float)r;
       tab[2 * k] = (float)h;
       tab[2 * k + 1] = (float)D[k];
-      tab[2 * (M2 + k)] = m;
-      tab[2 * (M2 + k) + 1] = (float)(r - (double)m);
+      const size_t kp = (size_t)(i / 2) + (size_t)((n + 1) / 2) * l;
+      tab[2 * (M2 + kp) + (i & 1)] = (float)(D[k] - h);
     }
   }
 }
@@ -1052,6 +1050,7 @@ int plain_stage(Context* c, int rkstep, double time, double dt) {
 
 int do_stage(Context* c, int rkstep, double time, double dt) {
   if (rkstep < 1 || rkstep > 5) return NEKGPU_ERR_ARG;
+  if (c->ndim == 2) return stage2d(c, rkstep, time, dt);
   if (c->form == NEKGPU_PLAIN) return plain_stage(c, rkstep, time, dt);
   if (c->form == NEKGPU_MIXED) return mixed_stage(c, rkstep, time, dt);
   return fused_stage(c, rkstep, time, dt);
@@ -1138,6 +1137,93 @@ int nekgpu_init(nekgpu_ctx** ctx, const nekgpu_mesh* m, int form) {
     c->host_x.assign(m->xmn, m->xmn + c->npts);
     c->host_y.assign(m->ymn, m->ymn + c->npts);
     c->host_z.assign(m->zmn, m->zmn + c->npts);
+  }
+  st = finish_init(c, st);
+  if (st) {
+    delete c;
+    return st;
+  }
+  *ctx = c;
+  return NEKGPU_OK;
+}
+
+int nekgpu_init2d(nekgpu_ctx** ctx, const nekgpu_mesh* m, int imode) {
+  if (!ctx || !m || (imode != 1 && imode != 2)) return NEKGPU_ERR_ARG;
+  *ctx = nullptr;
+  if (m->nx1 < 2 || m->nx1 > kMaxNx || m->nelt < 1 || !m->dxm1 || !m->w3mn || !m->bmn ||
+      !m->unxm || !m->unym || !m->aream || !m->cemface || !m->glo_face || !m->Z_0 || !m->Z_1 ||
+      !m->Y_0 || !m->Y_1 || !m->ebm1 || !m->hbm1 || !m->rxmn || !m->rymn || !m->sxmn ||
+      !m->symn || m->ncempec < 0 || (m->ncempec > 0 && !m->cempec))
+    return NEKGPU_ERR_ARG;
+  const int n = m->nx1;
+  const long n2 = (long)n * n, npts = n2 * m->nelt, nxzfl = 4L * n * m->nelt;
+  // the reference's 2-D face numbering: slot a + n*(f + 4e), f in pff order,
+  // a ascending along the face (cem_set_fc_ptr with SKPDAT for NZ = 1)
+  std::vector<int> cemface(nxzfl), partner(nxzfl, -1), pec(nxzfl, 0);
+  for (long e = 0; e < m->nelt; ++e)
+    for (int f = 0; f < 4; ++f)
+      for (int a = 0; a < n; ++a) {
+        const long js = a + (long)n * (f + 4 * e);
+        const long vloc = f == 0 ? a : (f == 1 ? n - 1 + n * a : (f == 2 ? a + n * (n - 1) : n * a));
+        if (m->cemface[js] - 1 != e * n2 + vloc) return NEKGPU_ERR_MESH;
+        cemface[js] = (int)(e * n2 + vloc);
+      }
+  std::vector<int> pairs, single;
+  int st = pairs_from_ids(m->glo_face, nxzfl, pairs, single);
+  if (st) return st;
+  for (size_t q = 0; q + 1 < pairs.size(); q += 2) {
+    partner[pairs[q]] = pairs[q + 1];
+    partner[pairs[q + 1]] = pairs[q];
+  }
+  for (int j = 0; j < m->ncempec; ++j) {
+    const int sl = m->cempec[j] - 1;
+    if (sl < 0 || sl >= nxzfl || partner[sl] >= 0) return NEKGPU_ERR_MESH;
+    pec[sl] = 1;
+  }
+  nekgpu_ctx* c = new (std::nothrow) nekgpu_ctx();
+  if (!c) return NEKGPU_ERR_NOMEM;
+  st = common_setup(c, NEKGPU_FUSED64, n, m->nelt);
+  if (!st) {
+    c->ndim = 2;
+    c->imode = imode;
+    c->npts = npts;
+    c->nxzfl = nxzfl;
+    DevAlloc A(c);
+    std::vector<double> bm1(m->bmn, m->bmn + npts), eb(m->ebm1, m->ebm1 + npts),
+        hb(m->hbm1, m->hbm1 + npts);
+    if (!st) st = A.get(&c->d_u[0], 6 * npts);
+    if (!st) st = A.get(&c->d_u[1], 6 * npts);
+    if (!st) st = upload_common(c, A, bm1, eb, hb);
+    Stage2dDev& a = c->s2;
+    a = Stage2dDev{};
+    a.nx = n; a.nelt = m->nelt; a.imode = imode; a.npts = npts; a.nxzfl = nxzfl;
+    a.C0 = m->C0;
+    a.ebm1 = c->d_ebm1;
+    a.hbm1 = c->d_hbm1;
+    std::vector<double> D(m->dxm1, m->dxm1 + n2), Dt(n2);
+    for (int i = 0; i < n; ++i)
+      for (int j = 0; j < n; ++j) Dt[j + (size_t)n * i] = D[i + (size_t)n * j];
+    const double* nsrc[4] = {m->rxmn, m->rymn, m->sxmn, m->symn};
+    const double** ndst[4] = {&a.rx, &a.ry, &a.sx, &a.sy};
+    const double* fsrc[7] = {m->unxm, m->unym, m->aream, m->Z_0, m->Z_1, m->Y_0, m->Y_1};
+    const double** fdst[7] = {&a.unx, &a.uny, &a.area, &a.Z0, &a.Z1, &a.Y0, &a.Y1};
+    double* d;
+    if (!st && !(st = A.put(&d, D))) a.D = d;
+    if (!st && !(st = A.put(&d, Dt))) a.Dt = d;
+    if (!st && !(st = A.put(&d, std::vector<double>(m->w3mn, m->w3mn + n2)))) a.w3 = d;
+    for (int q = 0; q < 4 && !st; ++q)
+      if (!(st = A.put(&d, std::vector<double>(nsrc[q], nsrc[q] + npts)))) *ndst[q] = d;
+    for (int q = 0; q < 7 && !st; ++q)
+      if (!(st = A.put(&d, std::vector<double>(fsrc[q], fsrc[q] + nxzfl)))) *fdst[q] = d;
+    int* di;
+    if (!st && !(st = A.put(&di, cemface))) a.cemface = di;
+    if (!st && !(st = A.put(&di, partner))) a.partner = di;
+    if (!st && !(st = A.put(&di, pec))) a.pec = di;
+    if (!st && m->xmn && m->ymn) {
+      c->host_x.assign(m->xmn, m->xmn + npts);
+      c->host_y.assign(m->ymn, m->ymn + npts);
+      c->host_z.assign(npts, 0.0);
+    }
   }
   st = finish_init(c, st);
   if (st) {
@@ -1308,7 +1394,7 @@ int nekgpu_set_dispersive(nekgpu_ctx* c, int model, const double* params, long l
   if (!c || (model != NEKGPU_DRUDE && model != NEKGPU_LORENTZ) || n < 0 ||
       (n > 0 && (!params || !index || ld < c->npts)))
     return NEKGPU_ERR_ARG;
-  if (c->form == NEKGPU_MIXED_NAIVE) return NEKGPU_ERR_UNSUPPORTED;
+  if (c->form == NEKGPU_MIXED_NAIVE || c->ndim == 2) return NEKGPU_ERR_UNSUPPORTED;
   const long P = c->npts, n3 = (long)c->nx * c->nx * c->nx;
   std::vector<signed char> kind = c->disp_kind;
   std::vector<double> par = c->disp_par;
@@ -1427,6 +1513,7 @@ int nekgpu_set_source(nekgpu_ctx* c, int enabled, const double xc[3], double sig
     return NEKGPU_OK;
   }
   if (!xc || !(sigma > 0)) return NEKGPU_ERR_ARG;
+  if (c->ndim == 2) return NEKGPU_ERR_UNSUPPORTED;  // 3-D volume source only
   if ((long)c->host_x.size() != c->npts) return NEKGPU_ERR_STATE;  // needs coordinates
   const double s2 = 2.0 * sigma * sigma;
   std::vector<double> g(c->npts);

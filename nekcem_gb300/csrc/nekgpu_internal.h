@@ -207,8 +207,28 @@ struct AdjointDev {
 };
 
 
+// 2-D TE / TM stage (nekgpu_2d.cu): the reference's ldim = 2 arrays as given
+struct Stage2dDev {
+  int nx, nelt, imode;  // imode 1 TE (E1, E2, H3), 2 TM (H1, H2, E3)
+  long npts, nxzfl;
+  const double *D, *Dt, *w3;        // nx^2 each
+  const double *rx, *ry, *sx, *sy;  // npts
+  const double *unx, *uny, *area, *Z0, *Z1, *Y0, *Y1;  // nxzfl
+  const double *ebm1, *hbm1;        // npts
+  const int* cemface;               // nxzfl, 0-based volume node
+  const int* partner;               // nxzfl: the other slot of the face node, -1 if none
+  const int* pec;                   // nxzfl: 1 on PEC slots
+  double C0;
+  const double* u_in;
+  double* u_out;
+  double* k;
+  double ca, cb, dt;
+};
+
 struct Context {
   int form = NEKGPU_MIXED;
+  int ndim = 3, imode = 3;  // ndim 2: TE (imode 1) or TM (imode 2) quadrilateral mesh
+  Stage2dDev s2{};
   int device = 0;
   int nx = 0, nelt = 0;
   long npts = 0, nxzfl = 0;
@@ -309,10 +329,13 @@ int scale_coef(Context* c, double dt);
 int mixed_stage(Context* c, int rkstep, double time, double dt);
 // the mixed form keeps dt-scaled coefficients as (hi, lo) float pairs in d_coef
 int scale_coef_pairs(Context* c, double dt);
-// D(i,j) at [i + nx*j] in four FP32 pieces: Dh on a 10-bit grid per row
-// (exact products with the 10-bit uh), Df = D rounded, and the remainder
-// D - Dh = Dm + Dl to ~2^-55; uploaded once per nx
-int mixed_upload_D(int nx, const float* tab, size_t count);  // even-odd D pieces
+// D(i,j) in three FP32 pieces: Dh on a 10-bit grid per row (exact products
+// with the 10-bit uh), Df = D rounded, and the remainder Dm = RN32(D - Dh),
+// as float pairs (layout in nekgpu_mixed.cu); uploaded once per nx
+int mixed_upload_D(int nx, const float* tab, size_t count);
+
+// nekgpu_2d.cu: one 2-D TE / TM stage in the reference's arithmetic
+int stage2d(Context* c, int rkstep, double time, double dt);
 
 // nekgpu_adjoint.cu
 int adjoint_stage(Context* c, const AdjointDev& a);

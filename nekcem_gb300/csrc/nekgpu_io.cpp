@@ -73,6 +73,7 @@ extern "C" int nekgpu_write_vtk(nekgpu_ctx* c, const char* path, const double* s
                                 const double* solen, long ld) {
   if (!c || !path || (solhn == nullptr) != (solen == nullptr) || (solhn && ld < c->npts))
     return NEKGPU_ERR_ARG;
+  if (c->ndim == 2) return NEKGPU_ERR_UNSUPPORTED;  // hexahedral cells only
   if ((long)c->host_x.size() != c->npts || !c->have_state) return NEKGPU_ERR_STATE;
   const long P = c->npts;
   const int n = c->nx;

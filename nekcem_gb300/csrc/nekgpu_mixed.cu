@@ -12,16 +12,20 @@
 //  * Exact-hi contractions.  Per element and field component, u is split into
 //    uh = u rounded to a 10-bit grid q (q from the element's largest |u|) and
 //    ul = u - uh; each row of D is split the same way into Dh (10 bits) plus
-//    a remainder kept as two FP32 pieces Dm + Dl (so D itself is represented
-//    to ~2^-55: a rounded D would perturb the operator and drift the phase).
-//    Every product Dh*uh is an integer multiple of q*qD below 2^20 q*qD, so
-//    the FP32 sum over the <= 16 terms is exact.  The small remainder
-//    sum(D*ul + (Dm + Dl)*uh) is summed in FP32 beside it.  The FP32 rounding
-//    error is ~2^-34 of sum|D||u| instead of ~2^-24.
+//    the remainder Dm = RN32(D - Dh), so D itself is represented to ~2^-34 of
+//    its row (a D rounded to FP32, 2^-24, perturbs the operator enough to
+//    drift the phase over thousands of steps; 2^-34 does not: the plane-wave
+//    and cavity errors stay at the FP64 form's).  Every product Dh*uh is an
+//    integer multiple of q*qD below 2^20 q*qD, so the FP32 sum over the <= 16
+//    terms is exact.  The small remainder sum(Df*ul + Dm*uh) is summed in FP32
+//    beside it.  The FP32 rounding error is ~2^-34 of sum|D||u| instead of
+//    ~2^-24.
 //  * Thread per line.  Each thread contracts one GLL line at a time, so every
-//    D coefficient is a compile-time constant-bank operand.  The four
-//    products of a term run as two packed FP32x2 FMAs (sm_100 family):
-//    (hi, lo) += (Dh, Df) * (uh, ul) and (m, l) += (Dm, Dl) * (uh, uh).
+//    D coefficient is a compile-time constant-bank operand.  The three
+//    products of a term run as packed FP32x2 FMAs (sm_100 family), one and a
+//    half per term: (hi_i, lo_i) += (Dh, Df)(i,l) * (uh, ul)_l for every
+//    output i and (m_i, m_i+1) += (Dm(i,l), Dm(i+1,l)) * (uh, uh)_l for every
+//    pair of outputs.
 //  * Normalised residual.  For an affine axis-aligned element the mass
 //    cancels the GLL weights and metrics: res/(bm1*2/hx) = d_s Hz - d_t Hy
 //    (+ face terms flux*area/(bm1*2/hx)), etc.  All FP32 coefficients are then
@@ -151,9 +155,10 @@ __device__ __forceinline__ int face_vol(int f, int a, int b) {
 
 // D of order nx-1 in the FP32 pieces of the exact-hi contraction, as float
 // pairs indexed by nx so that every coefficient is a compile-time
-// constant-bank operand: [nx][0][i + nx*l] = (Dh, Df), [nx][1][i + nx*l] =
-// (Dm, Dl) of D(i,l).  Dh is D on a 10-bit grid of its row, Df = RN32(D),
-// Dm = RN32(D - Dh), Dl = RN32(D - Dh - Dm).  D depends only on nx.
+// constant-bank operand: [nx][0][i + nx*l] = (Dh, Df) of D(i,l),
+// [nx][1][j + H*l] = (Dm(2j,l), Dm(2j+1,l)) with H = (nx+1)/2 (zero past the
+// last row).  Dh is D on a 10-bit grid of its row, Df = RN32(D),
+// Dm = RN32(D - Dh).  D depends only on nx.
 __constant__ float2 c_mixD[kMaxMixed + 1][2][kMaxMixed * kMaxMixed];
 
 // A copy of the thread index the compiler cannot see through: index math
@@ -237,28 +242,27 @@ __device__ __forceinline__ void line_phase(const float2* s_u2, float2* s_R2, boo
 #pragma unroll
       for (int l = 0; l < NX; ++l) u[l] = pu[line_node<NX, DIR>(la, lb, l)];
       // all NX outputs of the line at once, packed in float pairs:
-      //   (hi, lo) += (Dh, Df) * (uh, ul)   hi exact
-      //   (m, l)   += (Dm, Dl) * (uh, uh)
-      float2 x[NX], y[NX];
+      //   (hi_i, lo_i)   += (Dh, Df)(i,l) * (uh, ul)_l      hi exact
+      //   (m_i, m_i+1)   += (Dm(i,l), Dm(i+1,l)) * (uh, uh)_l
+      constexpr int H = (NX + 1) / 2;
+      float2 x[NX], y[H];
 #pragma unroll
-      for (int i = 0; i < NX; ++i) {
-        x[i] = __fmul2_rn(c_mixD[NX][0][i], u[0]);
-        y[i] = __fmul2_rn(c_mixD[NX][1][i], make_float2(u[0].x, u[0].x));
-      }
+      for (int i = 0; i < NX; ++i) x[i] = __fmul2_rn(c_mixD[NX][0][i], u[0]);
+#pragma unroll
+      for (int i = 0; i < H; ++i) y[i] = __fmul2_rn(c_mixD[NX][1][i], make_float2(u[0].x, u[0].x));
 #pragma unroll
       for (int l = 1; l < NX; ++l) {
         const float2 uu = make_float2(u[l].x, u[l].x);
 #pragma unroll
-        for (int i = 0; i < NX; ++i) {
-          x[i] = __ffma2_rn(c_mixD[NX][0][i + NX * l], u[l], x[i]);
-          y[i] = __ffma2_rn(c_mixD[NX][1][i + NX * l], uu, y[i]);
-        }
+        for (int i = 0; i < NX; ++i) x[i] = __ffma2_rn(c_mixD[NX][0][i + NX * l], u[l], x[i]);
+#pragma unroll
+        for (int i = 0; i < H; ++i) y[i] = __ffma2_rn(c_mixD[NX][1][i + H * l], uu, y[i]);
       }
       float hi[NX], lo[NX];
 #pragma unroll
       for (int i = 0; i < NX; ++i) {
         hi[i] = x[i].x;
-        lo[i] = x[i].y + (y[i].x + y[i].y);
+        lo[i] = x[i].y + ((i & 1) ? y[i / 2].y : y[i / 2].x);
       }
       float2* R0 = s_R2 + rt * C::N3P;
 #pragma unroll

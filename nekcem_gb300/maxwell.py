@@ -76,7 +76,23 @@ class MaxwellGPU:
         them).  ``arrays`` holds the COMMON arrays by their Fortran names;
         ``cemface``/``cempec`` are 0-based here and converted to Fortran's
         1-based convention."""
-        lib = L.load()
+        m, keep = cls._mesh(arrays, nx1, nelt, C0)
+        h = C.c_void_p()
+        L.check(L.load().nekgpu_init(C.byref(h), C.byref(m), L.FORMS[form]), "nekgpu_init")
+        return cls(h, L.FORMS[form], keep)
+
+    @classmethod
+    def from_arrays2d(cls, arrays: dict, nx1: int, nelt: int, mode: int,
+                      C0: float = 1.0) -> "MaxwellGPU":
+        """2-D TE (mode 1) or TM (mode 2) context from the reference's ldim = 2
+        arrays (nekgpu_init2d); z-metric arrays are not read."""
+        m, keep = cls._mesh(arrays, nx1, nelt, C0)
+        h = C.c_void_p()
+        L.check(L.load().nekgpu_init2d(C.byref(h), C.byref(m), int(mode)), "nekgpu_init2d")
+        return cls(h, L.FORMS["fused64"], keep)
+
+    @staticmethod
+    def _mesh(arrays: dict, nx1: int, nelt: int, C0: float):
         m = L.NekgpuMesh()
         m.nx1, m.nelt = int(nx1), int(nelt)
         keep = []
@@ -108,9 +124,7 @@ class MaxwellGPU:
             pp = np.ascontiguousarray(np.asarray(arrays["pmlptr"]) + 1, dtype=np.int32)
             keep.append(pp); m.pmlptr = _ip(pp); m.npml = int(pp.size)
             m.permittivity = d("permittivity"); m.permeability = d("permeability")
-        h = C.c_void_p()
-        L.check(lib.nekgpu_init(C.byref(h), C.byref(m), L.FORMS[form]), "nekgpu_init")
-        return cls(h, L.FORMS[form], keep)
+        return m, keep
 
     def close(self):
         if getattr(self, "_h", None):

@@ -28,6 +28,7 @@ int ref_get_threads(void) { return g_threads; }
 
 struct ref_ctx {
   int N, n, nelt, nel[3], bc[3];
+  int ndim, imode, nfaces; /* 3, 3, 6; or 2 with imode 1 (TE) / 2 (TM), 4 */
   long npts, nxzf, nxzfl, ncempec;
   double lo[3], hi[3];
   double *zgm1, *wxm1, *dxm1, *dxtm1, *w3m1;
@@ -430,6 +431,7 @@ static ref_ctx* create_box(int N, int nelx, int nely, int nelz, const double lo[
   ref_ctx* c = (ref_ctx*)calloc(1, sizeof(ref_ctx));
   int n = N + 1;
   c->N = N; c->n = n;
+  c->ndim = 3; c->imode = 3; c->nfaces = 6;
   c->nel[0] = nelx; c->nel[1] = nely; c->nel[2] = nelz;
   c->nelt = nelx * nely * nelz;
   for (int d = 0; d < 3; ++d) { c->lo[d] = lo[d]; c->hi[d] = hi[d]; c->bc[d] = bc[d]; }
@@ -653,7 +655,7 @@ double* ref_darray(ref_ctx* c, const char* name, long* len) {
 
 int* ref_iarray(ref_ctx* c, const char* name, long* len) {
   if (strcmp(name, "cemface") == 0) { if (len) *len = c->nxzfl; return c->cemface; }
-  if (strcmp(name, "cbc") == 0) { if (len) *len = 6L * c->nelt; return c->cbc; }
+  if (strcmp(name, "cbc") == 0) { if (len) *len = (long)c->nfaces * c->nelt; return c->cbc; }
   if (strcmp(name, "pmltag") == 0 && c->ifpml) { if (len) *len = c->nelt; return c->pmltag; }
   if (strcmp(name, "pmlptr") == 0 && c->ifpml) { if (len) *len = c->maxpml; return c->pmlptr; }
   if (strcmp(name, "cempec") == 0) { if (len) *len = c->ncempec; return c->cempec; }
@@ -699,11 +701,12 @@ void ref_set_materials(ref_ctx* c, const double* permittivity, const double* per
   memcpy(c->Y_0, c->yconduc, sizeof(double) * nxzfl);
   ref_gs_op_fields(c, c->Z_0, nxzfl, 1);
   ref_gs_op_fields(c, c->Y_0, nxzfl, 1);
+  int nf = c->nfaces;
   for (int e = 0; e < c->nelt; ++e)
-    for (int f = 0; f < 6; ++f)
-      if (c->cbc[6 * e + f] == 1)
+    for (int f = 0; f < nf; ++f)
+      if (c->cbc[nf * e + f] == 1)
         for (long j = 0; j < c->nxzf; ++j) {
-          long i = j + c->nxzf * (f + 6L * e);
+          long i = j + c->nxzf * (f + (long)nf * e);
           c->Y_0[i] = 2.0 * c->Y_0[i];
           c->Z_0[i] = 2.0 * c->Z_0[i];
         }
@@ -782,8 +785,15 @@ void ref_wght_curl(ref_ctx* c, double* w1, double* w2, double* w3, const double*
   }
 }
 
+static void cem_maxwell_2d(ref_ctx* c);
+static void restrict_2d(ref_ctx* c);
+static void flux2d(ref_ctx* c);
+static void lift_2d(ref_ctx* c);
+static void invqmass_2d(ref_ctx* c);
+
 /* cem_maxwell 3-D branch (src/cem_maxwell.F:574-582) */
 void ref_cem_maxwell(ref_ctx* c) {
+  if (c->ndim == 2) { cem_maxwell_2d(c); return; }
   long np = c->npts;
   ref_wght_curl(c, c->resen, c->resen + np, c->resen + 2 * np, c->hn, c->hn + np, c->hn + 2 * np);
   ref_wght_curl(c, c->reshn, c->reshn + np, c->reshn + 2 * np, c->en, c->en + np, c->en + 2 * np);
@@ -793,6 +803,7 @@ void ref_cem_maxwell(ref_ctx* c) {
 
 /* cem_maxwell_restrict_to_face (src/cem_maxwell.F:604-623) */
 void ref_restrict_to_face(ref_ctx* c) {
+  if (c->ndim == 2) { restrict_2d(c); return; }
   long np = c->npts, nf = c->nxzfl;
 #pragma omp parallel for schedule(static) num_threads(g_threads)
   for (long j = 0; j < nf; ++j) {
@@ -882,6 +893,7 @@ void ref_flux_upwind(ref_ctx* c) {
 
 /* cem_maxwell_flux3d (src/cem_maxwell.F:922-1002); userfsrc is a no-op */
 void ref_flux3d(ref_ctx* c) {
+  if (c->ndim == 2) { flux2d(c); return; }
   ref_flux_pre(c);
   ref_gs_op_fields(c, c->srflx, c->nxzfl, 6);
   if (c->ncempec > 0) ref_flux_pec(c);
@@ -893,6 +905,7 @@ void ref_flux3d(ref_ctx* c) {
  * below keeps that order because an element's slots are contiguous and only
  * touch that element's nodes. */
 void ref_add_flux_to_res(ref_ctx* c) {
+  if (c->ndim == 2) { lift_2d(c); return; }
   long k = c->nxzfl, np = c->npts, per = 6 * c->nxzf;
   double* s = c->srflx;
 #pragma omp parallel for schedule(static) num_threads(g_threads)
@@ -999,6 +1012,7 @@ void ref_usersrc(ref_ctx* c, double rktime) {
 
 /* cem_maxwell_invqmass, CPU branch (src/cem_maxwell.F:1878-1886) */
 void ref_invqmass(ref_ctx* c) {
+  if (c->ndim == 2) { invqmass_2d(c); return; }
   long np = c->npts;
 #pragma omp parallel for schedule(static) num_threads(g_threads)
   for (long i = 0; i < np; ++i) {
@@ -1233,6 +1247,17 @@ void ref_rk_stage(ref_ctx* c, int rkstep, double time, double dt) {
   ref_maxwell_op(c, rktime);
   c->rkstep_now = 0;
   long np = c->npts;
+  if (c->ndim == 2) { /* rk_maxwell_ab TM / TE branches (src/cem_maxwell.F:1925-1932) */
+    double* u[3]; double* k[3]; double* r[3];
+    int tm = c->imode == 2;
+    u[0] = (tm ? c->hn : c->en); k[0] = (tm ? c->khn : c->ken); r[0] = (tm ? c->reshn : c->resen);
+    u[1] = u[0] + np; k[1] = k[0] + np; r[1] = r[0] + np;
+    u[2] = (tm ? c->en : c->hn) + 2 * np; k[2] = (tm ? c->ken : c->khn) + 2 * np;
+    r[2] = (tm ? c->resen : c->reshn) + 2 * np;
+    for (int q = 0; q < 3; ++q)
+      ref_rk4_upd(u[q], k[q], r[q], b[rkstep - 1], a[rkstep - 1], dt, np);
+    return;
+  }
   for (int q = 0; q < 3; ++q)
     ref_rk4_upd(c->hn + q * np, c->khn + q * np, c->reshn + q * np, b[rkstep - 1], a[rkstep - 1],
                 dt, np);
@@ -1267,6 +1292,22 @@ double ref_get_dxmin(const ref_ctx* c) {
   int n = c->n;
   double d2m = 1.0e20;
   const double *x = c->xm1, *y = c->ym1, *z = c->zm1;
+  if (c->ndim == 2) { /* the 2D branch */
+    for (int e = 0; e < c->nelt; ++e)
+      for (int j = 1; j < n - 1; ++j)
+        for (int i = 1; i < n - 1; ++i) {
+          long o = (long)n * n * e;
+          double dx = x[o + i + 1 + n * j] - x[o + i - 1 + n * j];
+          double dy = y[o + i + 1 + n * j] - y[o + i - 1 + n * j];
+          double d2 = dx * dx + dy * dy;
+          d2m = d2 < d2m ? d2 : d2m;
+          dx = x[o + i + n * (j + 1)] - x[o + i + n * (j - 1)];
+          dy = y[o + i + n * (j + 1)] - y[o + i + n * (j - 1)];
+          d2 = dx * dx + dy * dy;
+          d2m = d2 < d2m ? d2 : d2m;
+        }
+    return sqrt(d2m) / 2.0;
+  }
 #define IDX(i, j, k, e) ((long)(i) + (long)n * (j) + (long)n * n * (k) + (long)n * n * n * (e))
   for (int e = 0; e < c->nelt; ++e)
     for (int k = 1; k < n - 1; ++k)
@@ -1308,3 +1349,336 @@ void ref_cem_error(const ref_ctx* c, const double* u, const double* exact, long 
   *l2 = s;
   *linf = m;
 }
+
+/* ------------------------------------------------------------------------ */
+/* 2-D TE / TM forms (imode 1 / 2): the ldim=2 branches of the routines     */
+/* above, on a box of quadrilaterals                                         */
+/* ------------------------------------------------------------------------ */
+
+/* face slot f (0..3, pff order: s=-1, r=+1, s=+1, r=-1) node a -> volume
+ * index within the element; SKPDAT walks every 2-D face in ascending
+ * coordinate order (src/nek5_connect11.F:1483-1530 with NZ = 1) */
+static int face_vol_2d(int f, int a, int n) {
+  switch (f) {
+    case 0: return a;
+    case 1: return n - 1 + n * a;
+    case 2: return a + n * (n - 1);
+    default: return n * a;
+  }
+}
+
+/* the three active components of the mode: TM (imode 2) H1, H2, E3;
+ * TE (imode 1) E1, E2, H3 */
+static void mode_fields(ref_ctx* c, double* base_h, double* base_e, long ld, double* out[3]) {
+  if (c->imode == 2) {
+    out[0] = base_h; out[1] = base_h + ld; out[2] = base_e + 2 * ld;
+  } else {
+    out[0] = base_e; out[1] = base_e + ld; out[2] = base_h + 2 * ld;
+  }
+}
+
+/* maxwell_wght_curl, ldim = 2 (src/cem_maxwell.F:1500-1536) with
+ * local_grad2 (src/nek5_grad.F:21-34) */
+static void wght_curl_2d(ref_ctx* c, double* w1, double* w2, double* w3, const double* u1,
+                         const double* u2, const double* u3) {
+  int n = c->n;
+  long n2 = (long)n * n;
+#pragma omp parallel for schedule(static) num_threads(g_threads)
+  for (int e = 0; e < c->nelt; ++e) {
+    double u1r[256], u1s[256], u2r[256], u2s[256], u3r[256], u3s[256];
+    long o = n2 * e;
+    mxm(c->dxm1, n, u1 + o, n, u1r, n);
+    mxm(u1 + o, n, c->dxtm1, n, u1s, n);
+    mxm(c->dxm1, n, u2 + o, n, u2r, n);
+    mxm(u2 + o, n, c->dxtm1, n, u2s, n);
+    mxm(c->dxm1, n, u3 + o, n, u3r, n);
+    mxm(u3 + o, n, c->dxtm1, n, u3s, n);
+    for (long i = 0; i < n2; ++i) {
+      long k = i + o;
+      double u1rw = u1r[i] * c->w3m1[i], u1sw = u1s[i] * c->w3m1[i];
+      double u2rw = u2r[i] * c->w3m1[i], u2sw = u2s[i] * c->w3m1[i];
+      double u3rw = u3r[i] * c->w3m1[i], u3sw = u3s[i] * c->w3m1[i];
+      double rx = c->rxm1[k], sx = c->sxm1[k], ry = c->rym1[k], sy = c->sym1[k];
+      w1[k] = (u3rw * ry + u3sw * sy);
+      w2[k] = -(u3rw * rx + u3sw * sx);
+      w3[k] = (u2rw * rx + u2sw * sx - u1rw * ry - u1sw * sy);
+    }
+  }
+}
+
+/* cem_maxwell TM / TE branches (src/cem_maxwell.F:584-595) */
+static void cem_maxwell_2d(ref_ctx* c) {
+  long np = c->npts;
+  double *u[3], *r[3];
+  mode_fields(c, c->hn, c->en, np, u);
+  mode_fields(c, c->reshn, c->resen, np, r);
+  wght_curl_2d(c, r[0], r[1], r[2], u[0], u[1], u[2]);
+  if (c->imode == 2) { /* chsign resHN(1,1), resHN(1,2) */
+    for (long i = 0; i < np; ++i) { r[0][i] = -r[0][i]; r[1][i] = -r[1][i]; }
+  } else { /* chsign resHN(1,3) */
+    for (long i = 0; i < np; ++i) r[2][i] = -r[2][i];
+  }
+}
+
+/* cem_maxwell_restrict_to_face TM / TE branches (src/cem_maxwell.F:616-637) */
+static void restrict_2d(ref_ctx* c) {
+  long np = c->npts, nf = c->nxzfl;
+  for (long j = 0; j < nf; ++j) {
+    long i = c->cemface[j];
+    for (int q = 0; q < 3; ++q) { c->fhn[j + q * nf] = 0.0; c->fen[j + q * nf] = 0.0; }
+    if (c->imode == 2) {
+      c->fhn[j] = c->hn[i];
+      c->fhn[j + nf] = c->hn[i + np];
+      c->fen[j + 2 * nf] = c->en[i + 2 * np];
+    } else {
+      c->fhn[j + 2 * nf] = c->hn[i + 2 * np];
+      c->fen[j] = c->en[i];
+      c->fen[j + nf] = c->en[i + np];
+    }
+  }
+}
+
+/* cem_maxwell_flux2d (src/cem_maxwell.F:811-920) with gs_op_fields over 3
+ * fields and the TM / TE branches of cem_maxwell_flux_pec (:1408-1421) */
+static void flux2d(ref_ctx* c) {
+  long k = c->nxzfl;
+  double* s = c->srflx;
+  double C0 = c->C0;
+  const double *fh = c->fhn, *fe = c->fen;
+  for (long i = 0; i < k; ++i) {
+    double nx = c->unx[i], ny = c->uny[i];
+    if (c->imode == 2) {
+      s[0 * k + i] = -ny * fe[2 * k + i];
+      s[1 * k + i] = nx * fe[2 * k + i];
+      s[2 * k + i] = -nx * fh[1 * k + i] + ny * fh[0 * k + i];
+    } else {
+      s[0 * k + i] = -ny * fh[2 * k + i];
+      s[1 * k + i] = nx * fh[2 * k + i];
+      s[2 * k + i] = -nx * fe[1 * k + i] + ny * fe[0 * k + i];
+    }
+  }
+  ref_gs_op_fields(c, s, k, 3);
+  for (long j = 0; j < c->ncempec; ++j) {
+    long i = c->cempec[j];
+    if (c->imode == 2) {
+      s[0 * k + i] = 2.0 * s[0 * k + i];
+      s[1 * k + i] = 2.0 * s[1 * k + i];
+      s[2 * k + i] = 0.0;
+    } else {
+      s[0 * k + i] = 0.0;
+      s[1 * k + i] = 0.0;
+      s[2 * k + i] = 2.0 * s[2 * k + i];
+    }
+  }
+  for (long i = 0; i < k; ++i) {
+    double Y0 = c->Y_0[i], Y1 = c->Y_1[i], Z0 = c->Z_0[i], Z1 = c->Z_1[i];
+    double nx = c->unx[i], ny = c->uny[i];
+    if (c->imode == 2) {
+      double fu1 = ny * s[2 * k + i];
+      double fu2 = -nx * s[2 * k + i];
+      double fw3 = nx * s[1 * k + i] - ny * s[0 * k + i];
+      s[0 * k + i] = 0.5 / Y0 * (-Y1 * s[0 * k + i] - C0 * fu1);
+      s[1 * k + i] = 0.5 / Y0 * (-Y1 * s[1 * k + i] - C0 * fu2);
+      s[2 * k + i] = 0.5 / Z0 * (Z1 * s[2 * k + i] - C0 * fw3);
+    } else {
+      double fw1 = ny * s[2 * k + i];
+      double fw2 = -nx * s[2 * k + i];
+      double fu3 = nx * s[1 * k + i] - ny * s[0 * k + i];
+      s[0 * k + i] = 0.5 / Z0 * (Z1 * s[0 * k + i] - C0 * fw1);
+      s[1 * k + i] = 0.5 / Z0 * (Z1 * s[1 * k + i] - C0 * fw2);
+      s[2 * k + i] = 0.5 / Y0 * (-Y1 * s[2 * k + i] - C0 * fu3);
+    }
+  }
+}
+
+/* cem_maxwell_add_flux_to_res TM / TE branches (src/cem_maxwell.F:736-755) */
+static void lift_2d(ref_ctx* c) {
+  long k = c->nxzfl, np = c->npts;
+  double* s = c->srflx;
+  double* r[3];
+  mode_fields(c, c->reshn, c->resen, np, r);
+  for (long j = 0; j < k; ++j) {
+    long i = c->cemface[j];
+    double a = c->area[j];
+    r[0][i] = r[0][i] + a * s[0 * k + j];
+    r[1][i] = r[1][i] + a * s[1 * k + j];
+    r[2][i] = r[2][i] + a * s[2 * k + j];
+  }
+}
+
+/* cem_maxwell_invqmass TM / TE branches (src/cem_maxwell.F:1887-1898) */
+static void invqmass_2d(ref_ctx* c) {
+  long np = c->npts;
+  for (long i = 0; i < np; ++i) {
+    if (c->imode == 2) {
+      c->reshn[i] = c->reshn[i] * c->hbm1[i];
+      c->reshn[i + np] = c->reshn[i + np] * c->hbm1[i];
+      c->resen[i + 2 * np] = c->resen[i + 2 * np] * c->ebm1[i];
+    } else {
+      c->resen[i] = c->resen[i] * c->ebm1[i];
+      c->resen[i + np] = c->resen[i + np] * c->ebm1[i];
+      c->reshn[i + 2 * np] = c->reshn[i + 2 * np] * c->hbm1[i];
+    }
+  }
+}
+
+/* A box [lo,hi]^2 of nelx x nely quadrilaterals, N <= 15, for imode 1 (TE)
+ * or 2 (TM): GENWZ, genxyz (bilinear corner map), XYZRST + GLMAPM1 ldim=2
+ * (src/nek5_coef.F:555-613), bm1 = jac w3, AREA2 (:1020-1095) and the 2-D
+ * face numbering of cem_set_fc_ptr. */
+ref_ctx* ref_create_box2d(int N, int nelx, int nely, const double lo[2], const double hi[2],
+                          const int bc[2], int imode) {
+  if (N < 1 || N > 15 || nelx < 1 || nely < 1 || (imode != 1 && imode != 2)) return NULL;
+  if (bc[0] == REF_BC_PML || bc[1] == REF_BC_PML) return NULL;
+  ref_ctx* c = (ref_ctx*)calloc(1, sizeof(ref_ctx));
+  int n = N + 1;
+  c->N = N; c->n = n;
+  c->ndim = 2; c->imode = imode; c->nfaces = 4;
+  c->nel[0] = nelx; c->nel[1] = nely; c->nel[2] = 1;
+  c->nelt = nelx * nely;
+  for (int d = 0; d < 2; ++d) { c->lo[d] = lo[d]; c->hi[d] = hi[d]; c->bc[d] = bc[d]; }
+  c->lo[2] = 0.0; c->hi[2] = 0.0; c->bc[2] = REF_BC_PERIODIC;
+  long n2 = (long)n * n;
+  c->npts = n2 * c->nelt;
+  c->nxzf = n;
+  c->nxzfl = 4L * n * c->nelt;
+  long npts = c->npts, nxzfl = c->nxzfl;
+
+  c->zgm1 = dalloc(n); c->wxm1 = dalloc(n);
+  c->dxm1 = dalloc(n * n); c->dxtm1 = dalloc(n * n);
+  c->w3m1 = dalloc(n2);
+  ref_zwgll(c->zgm1, c->wxm1, n);
+  ref_dgll(c->dxm1, c->dxtm1, c->zgm1, n);
+  for (int iy = 0; iy < n; ++iy)
+    for (int ix = 0; ix < n; ++ix) c->w3m1[ix + n * iy] = c->wxm1[ix] * c->wxm1[iy];
+
+  c->xm1 = dalloc(npts); c->ym1 = dalloc(npts); c->zm1 = dalloc(npts);
+  for (int e = 0; e < c->nelt; ++e) {
+    int ec[2] = {e % nelx, e / nelx};
+    double cb[2][2];
+    for (int d = 0; d < 2; ++d) {
+      double L = c->hi[d] - c->lo[d];
+      cb[d][0] = c->lo[d] + L * (double)ec[d] / (double)c->nel[d];
+      cb[d][1] = c->lo[d] + L * (double)(ec[d] + 1) / (double)c->nel[d];
+    }
+    double h[16][2];
+    for (int i = 0; i < n; ++i) {
+      h[i][0] = (1.0 - c->zgm1[i]) * 0.5;
+      h[i][1] = (1.0 + c->zgm1[i]) * 0.5;
+    }
+    for (int iyt = 0; iyt < 2; ++iyt)
+      for (int ixt = 0; ixt < 2; ++ixt)
+        for (int j = 0; j < n; ++j)
+          for (int i = 0; i < n; ++i) {
+            double hh = h[i][ixt] * h[j][iyt];
+            long idx = i + (long)n * j + n2 * e;
+            c->xm1[idx] = c->xm1[idx] + hh * cb[0][ixt];
+            c->ym1[idx] = c->ym1[idx] + hh * cb[1][iyt];
+          }
+  }
+
+  double *xr = dalloc(npts), *yr = dalloc(npts), *xs = dalloc(npts), *ys = dalloc(npts);
+  for (int e = 0; e < c->nelt; ++e) {
+    long o = n2 * e;
+    mxm(c->dxm1, n, c->xm1 + o, n, xr + o, n);
+    mxm(c->xm1 + o, n, c->dxtm1, n, xs + o, n);
+    mxm(c->dxm1, n, c->ym1 + o, n, yr + o, n);
+    mxm(c->ym1 + o, n, c->dxtm1, n, ys + o, n);
+  }
+  c->rxm1 = dalloc(npts); c->rym1 = dalloc(npts); c->rzm1 = dalloc(npts);
+  c->sxm1 = dalloc(npts); c->sym1 = dalloc(npts); c->szm1 = dalloc(npts);
+  c->txm1 = dalloc(npts); c->tym1 = dalloc(npts); c->tzm1 = dalloc(npts);
+  c->jacm1 = dalloc(npts); c->bm1 = dalloc(npts);
+  for (long i = 0; i < npts; ++i) {
+    double jac = 0.0;
+    jac = jac + xr[i] * ys[i];
+    jac = jac - xs[i] * yr[i];
+    c->jacm1[i] = jac;
+    c->rxm1[i] = ys[i];
+    c->rym1[i] = -xs[i];
+    c->sxm1[i] = -yr[i];
+    c->sym1[i] = xr[i];
+    c->tzm1[i] = 1.0;
+  }
+  for (int e = 0; e < c->nelt; ++e)
+    for (long i = 0; i < n2; ++i) c->bm1[n2 * e + i] = c->jacm1[n2 * e + i] * c->w3m1[i];
+  c->volvm1 = 0.0;
+  for (long i = 0; i < npts; ++i) c->volvm1 += c->bm1[i];
+
+  /* AREA2 with SETWGTR (non-axisymmetric: the GLL weights) */
+  c->unx = dalloc(nxzfl); c->uny = dalloc(nxzfl); c->unz = dalloc(nxzfl); c->area = dalloc(nxzfl);
+  for (int e = 0; e < c->nelt; ++e)
+    for (int f = 0; f < 4; ++f)
+      for (int a = 0; a < n; ++a) {
+        long v = n2 * e + face_vol_2d(f, a, n);
+        long j = a + (long)n * (f + 4L * e);
+        double tx, ty, len;
+        if (f == 0 || f == 2) { /* "S": xr, yr */
+          len = sqrt(xr[v] * xr[v] + yr[v] * yr[v]);
+          tx = xr[v] / len;
+          ty = yr[v] / len;
+          if (f == 2) { tx = -xr[v] / len; ty = -yr[v] / len; }
+        } else { /* "R": xs, ys */
+          len = sqrt(xs[v] * xs[v] + ys[v] * ys[v]);
+          tx = xs[v] / len;
+          ty = ys[v] / len;
+          if (f == 3) { tx = -xs[v] / len; ty = -ys[v] / len; }
+        }
+        c->unx[j] = ty;
+        c->uny[j] = -tx;
+        c->area[j] = len * c->wxm1[a];
+      }
+  free(xr); free(yr); free(xs); free(ys);
+
+  /* cem_set_fc_ptr and the face pairing (one id per face-node position;
+   * periodic axes wrap) */
+  c->cemface = ialloc(nxzfl);
+  c->glo_face = (long long*)calloc((size_t)nxzfl, sizeof(long long));
+  c->cbc = ialloc(4L * c->nelt);
+  long long yoff = (long long)(nelx + 1) * nely;
+  for (int e = 0; e < c->nelt; ++e) {
+    int ec[2] = {e % nelx, e / nelx};
+    for (int f = 0; f < 4; ++f) {
+      int ax = slot_axis[f], sd = slot_side[f];
+      int plane = ec[ax] + (sd > 0 ? 1 : 0);
+      int boundary = (plane == 0 || plane == c->nel[ax]);
+      if (boundary) c->cbc[4 * e + f] = c->bc[ax] == REF_BC_PERIODIC ? 2 : 1;
+      if (boundary && c->bc[ax] == REF_BC_PERIODIC) plane = plane % c->nel[ax];
+      long long fid = ax == 0 ? (long long)plane * nely + ec[1]
+                              : yoff + (long long)plane * nelx + ec[0];
+      for (int a = 0; a < n; ++a) {
+        long j = a + (long)n * (f + 4L * e);
+        c->cemface[j] = (int)(n2 * e + face_vol_2d(f, a, n));
+        c->glo_face[j] = fid * (long long)n + a + 1;
+      }
+    }
+  }
+  gs_setup_local(c);
+  c->cempec = ialloc(nxzfl);
+  long l = 0;
+  for (int e = 0; e < c->nelt; ++e)
+    for (int f = 0; f < 4; ++f)
+      if (c->cbc[4 * e + f] == 1)
+        for (long j = 0; j < n; ++j) c->cempec[l++] = (int)(j + (long)n * (f + 4L * e));
+  c->ncempec = l;
+
+  c->hn = dalloc(3 * npts); c->en = dalloc(3 * npts);
+  c->khn = dalloc(3 * npts); c->ken = dalloc(3 * npts);
+  c->reshn = dalloc(3 * npts); c->resen = dalloc(3 * npts);
+  c->fhn = dalloc(3 * nxzfl); c->fen = dalloc(3 * nxzfl);
+  c->srflx = dalloc(6 * nxzfl);
+  c->permittivity = dalloc(npts); c->permeability = dalloc(npts);
+  c->impede = dalloc(npts); c->conduc = dalloc(npts);
+  c->zimpede = dalloc(nxzfl); c->yconduc = dalloc(nxzfl);
+  c->Z_0 = dalloc(nxzfl); c->Z_1 = dalloc(nxzfl); c->Y_0 = dalloc(nxzfl); c->Y_1 = dalloc(nxzfl);
+  c->ebm1 = dalloc(npts); c->hbm1 = dalloc(npts);
+  c->C0 = 1.0;
+  double* one = dalloc(npts);
+  for (long i = 0; i < npts; ++i) one[i] = 1.0;
+  ref_set_materials(c, one, one);
+  free(one);
+  return c;
+}
+
+int ref_ndim(const ref_ctx* c) { return c->ndim; }
+int ref_imode(const ref_ctx* c) { return c->imode; }

@@ -43,6 +43,13 @@ ref_ctx* ref_create_box(int N, int nelx, int nely, int nelz, const double lo[3],
  * non-affine elements; the domain boundary stays in place) */
 ref_ctx* ref_create_box_mapped(int N, int nelx, int nely, int nelz, const double lo[3],
                                const double hi[3], const int bc[3], double amp);
+/* 2-D box of nelx x nely quadrilaterals for the TE (imode 1: E1, E2, H3) or
+ * TM (imode 2: H1, H2, E3) form (the reference's ldim = 2 build, param(4));
+ * lo/hi/bc per axis x, y.  The routines below take their 2-D branches. */
+ref_ctx* ref_create_box2d(int N, int nelx, int nely, const double lo[2], const double hi[2],
+                          const int bc[2], int imode);
+int ref_ndim(const ref_ctx* c);
+int ref_imode(const ref_ctx* c);
 void ref_destroy(ref_ctx* c);
 
 /* Named array access (the reference's COMMON arrays).  Returns NULL for an

@@ -61,6 +61,8 @@ def lib():
         L.ref_set_source_kind.argtypes = [vp, ip]
         L.ref_set_pml.argtypes = [vp, ip, C.c_double, C.c_double]
         L.ref_pml_step.argtypes = [vp]
+        L.ref_create_box2d.restype = vp
+        L.ref_create_box2d.argtypes = [ip, ip, ip, dp, dp, C.POINTER(C.c_int), ip]
         L.ref_set_drude.argtypes = [vp, dp, C.POINTER(C.c_int), C.c_long]
         L.ref_set_lorentz.argtypes = [vp, dp, C.POINTER(C.c_int), C.c_long]
         L.ref_source_time.restype = C.c_double
@@ -266,3 +268,25 @@ class RefBox:
 
     def coords(self):
         return self.d("xm1"), self.d("ym1"), self.d("zm1")
+
+
+class RefBox2D(RefBox):
+    """Oracle for a 2-D box of quadrilaterals in the TE (mode 1: E1, E2, H3) or
+    TM (mode 2: H1, H2, E3) form.  Fields keep the 3-component layout (the
+    inactive components stay zero); ``coords()`` gives x, y (z = 0)."""
+
+    def __init__(self, N, nel, lo, hi, bc, mode: int):
+        L = lib()
+        lo_a = (C.c_double * 2)(*lo); hi_a = (C.c_double * 2)(*hi)
+        bc_a = (C.c_int * 2)(*bc)
+        self._c = L.ref_create_box2d(int(N), int(nel[0]), int(nel[1]), lo_a, hi_a, bc_a, int(mode))
+        if not self._c:
+            raise ValueError("ref_create_box2d rejected the mesh")
+        self.N, self.nel, self.lo, self.hi, self.bc = N, tuple(nel), tuple(lo), tuple(hi), tuple(bc)
+        self.mode = int(mode)
+        self.n = N + 1
+        self.nelt = int(L.ref_size(self._c, b"nelt"))
+        self.npts = int(L.ref_size(self._c, b"npts"))
+        self.nxzf = int(L.ref_size(self._c, b"nxzf"))
+        self.nxzfl = int(L.ref_size(self._c, b"nxzfl"))
+

@@ -1,0 +1,153 @@
+"""2-D TE / TM forms (the reference's ldim = 2 build, param(4) = 1 TE, 2 TM).
+
+CPU: the oracle's 2-D branches pass the reference's own known-answer tests,
+tests/2dboxpec and tests/2dboxper (3x3 quadrilaterals, N=8, dt 0.005, 1000
+steps, per-component L2 / Linf tolerances of their userchk), for TE and TM.
+GPU: nekgpu_init2d from the oracle's arrays matches the oracle bit for bit
+(PEC, periodic and mixed boxes, with and without materials) and passes the
+same known answers; what 2-D does not support is refused.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from helpers import oracle_arrays
+from nekcem_gb300 import MaxwellGPU, cases
+from nekcem_gb300 import _lib as L
+from oracle import refcpu as R
+
+TE, TM = cases.TE, cases.TM
+PEC, PER = 0, 1
+
+
+def known_answer(name, mode, gpu: bool):
+    cs = cases.CASES_2D[name]
+    ref = R.RefBox2D(cs["N"], cs["nel"], cs["lo"], cs["hi"], cs["bc"], mode)
+    x, y, z = (a.copy() for a in ref.coords())
+    sol = cs["sol"](mode)
+    H, E = sol(x, y, z, 0.0)
+    if gpu:
+        g = MaxwellGPU.from_arrays2d(oracle_arrays(ref), ref.n, ref.nelt, mode)
+        g.set_state(H, E)
+        t = g.run(cs["nsteps"], 0.0, cs["dt"])
+        Hg, Eg = g.get_state()
+        g.close()
+    else:
+        ref.set_state(H, E)
+        ref.run(cs["nsteps"], 0.0, cs["dt"])
+        t = cs["nsteps"] * cs["dt"]
+        Hg, Eg = ref.hn.copy(), ref.en.copy()
+    Hx, Ex = sol(x, y, z, t)
+    res = []
+    for a, b in [(Hg[q], Hx[q]) for q in range(3)] + [(Eg[q], Ex[q]) for q in range(3)]:
+        res.append(ref.cem_error(a, b))
+    ref.close()
+    active = [0, 1, 5] if mode == TM else [2, 3, 4]
+    for q in range(6):
+        l2, li = res[q]
+        if q in active:
+            assert l2 <= cs["l2tol"] and li <= cs["linftol"], (name, mode, q, l2, li)
+        else:
+            assert l2 == 0.0 and li == 0.0, (name, mode, q, l2, li)
+    return res
+
+
+@pytest.mark.parametrize("name", list(cases.CASES_2D))
+@pytest.mark.parametrize("mode", [TE, TM])
+def test_oracle_2d_known_answers(name, mode):
+    known_answer(name, mode, gpu=False)
+
+
+def test_oracle_2d_geometry():
+    """Affine quads: cofactors, Jacobian, normals and edge weights."""
+    ref = R.RefBox2D(4, (3, 2), (0.0, -1.0), (1.5, 1.0), (PEC, PER), TE)
+    hx, hy = 0.5, 1.0
+    np.testing.assert_allclose(ref.d("rxm1"), hy / 2, rtol=1e-12)
+    np.testing.assert_allclose(ref.d("sym1"), hx / 2, rtol=1e-12)
+    np.testing.assert_allclose(ref.d("rym1"), 0, atol=1e-13)
+    np.testing.assert_allclose(ref.d("jacm1"), hx * hy / 4, rtol=1e-12)
+    assert ref.volvm1 == pytest.approx(1.5 * 2.0, rel=1e-12)
+    n = ref.n
+    unx = ref.d("unx").reshape(-1, 4, n)
+    uny = ref.d("uny").reshape(-1, 4, n)
+    np.testing.assert_array_equal(uny[:, 0], -1.0)  # s = -1 face
+    np.testing.assert_array_equal(unx[:, 1], 1.0)   # r = +1
+    np.testing.assert_array_equal(uny[:, 2], 1.0)   # s = +1
+    np.testing.assert_array_equal(unx[:, 3], -1.0)  # r = -1
+    w = ref.d("wxm1")
+    area = ref.d("area").reshape(-1, 4, n)
+    np.testing.assert_allclose(area[:, 0], np.broadcast_to(hx / 2 * w, area[:, 0].shape), rtol=1e-12)
+    np.testing.assert_allclose(area[:, 1], np.broadcast_to(hy / 2 * w, area[:, 1].shape), rtol=1e-12)
+    assert len(ref.i("cempec")) == 4 * n  # two faces on each x wall (y is periodic)
+    ref.close()
+
+
+# ---- GPU ----------------------------------------------------------------------------
+MESHES_2D = {
+    "pec": dict(N=5, nel=(3, 2), lo=(0.0, 0.0), hi=(1.5, 1.0), bc=(PEC, PEC)),
+    "periodic": dict(N=8, nel=(2, 3), lo=(0.0, 0.0), hi=(1.0, 1.0), bc=(PER, PER)),
+    "mixed": dict(N=7, nel=(4, 2), lo=(-1.0, 0.0), hi=(1.0, 0.5), bc=(PER, PEC)),
+}
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", list(MESHES_2D))
+@pytest.mark.parametrize("mode", [TE, TM])
+@pytest.mark.parametrize("materials", [False, True])
+def test_2d_bit_exact(name, mode, materials):
+    b = MESHES_2D[name]
+    ref = R.RefBox2D(b["N"], b["nel"], b["lo"], b["hi"], b["bc"], mode)
+    x, y, z = ref.coords()
+    if materials:
+        ref.set_materials(1.0 + 0.5 * np.sin(3 * x) ** 2, 1.0 + 0.3 * np.cos(2 * y) ** 2)
+    g = MaxwellGPU.from_arrays2d(oracle_arrays(ref), ref.n, ref.nelt, mode)
+    rng = np.random.default_rng(mode * 10 + len(name))
+    H = rng.standard_normal((3, ref.npts))
+    E = rng.standard_normal((3, ref.npts))
+    ref.set_state(H, E)
+    g.set_state(H, E)
+    dt = 0.2 * ref.dxmin()
+    ref.run(5, 0.0, dt)
+    g.run(5, 0.0, dt)
+    Hg, Eg = g.get_state()
+    np.testing.assert_array_equal(Hg, ref.hn)
+    np.testing.assert_array_equal(Eg, ref.en)
+    g.close(); ref.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", list(cases.CASES_2D))
+@pytest.mark.parametrize("mode", [TE, TM])
+def test_2d_known_answers_gpu(name, mode):
+    known_answer(name, mode, gpu=True)
+
+
+@pytest.mark.gpu
+def test_2d_refusals(tmp_path):
+    ref = R.RefBox2D(3, (2, 2), (0.0, 0.0), (1.0, 1.0), (PEC, PEC), TM)
+    arrays = oracle_arrays(ref)
+    g = MaxwellGPU.from_arrays2d(arrays, ref.n, ref.nelt, TM)
+    g.set_state(np.zeros((3, g.npts)), np.zeros((3, g.npts)))
+    calls = [
+        lambda: g.set_source((0.5, 0.5, 0.0), 0.1, 1.0, 1.0, 0.0),
+        lambda: g.set_dispersive(g.DRUDE, np.ones((2, g.npts)), np.arange(3)),
+        lambda: g.adjoint_gradient(1, 0.0, 0.01, np.ones(g.npts)),
+        lambda: g.write_vtk(str(tmp_path / "x.vtk")),
+    ]
+    for call in calls:
+        with pytest.raises(L.NekgpuError) as e:
+            call()
+        assert e.value.status == -8
+    g.close()
+    bad = dict(arrays)
+    cf = bad["cemface"].copy()
+    cf[[0, 1]] = cf[[1, 0]]  # not the reference's face numbering
+    bad["cemface"] = cf
+    with pytest.raises(L.NekgpuError) as e:
+        MaxwellGPU.from_arrays2d(bad, ref.n, ref.nelt, TM)
+    assert e.value.status == -2
+    with pytest.raises(L.NekgpuError) as e:
+        MaxwellGPU.from_arrays2d(arrays, ref.n, ref.nelt, 3)
+    assert e.value.status == -1
+    ref.close()
