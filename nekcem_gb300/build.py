@@ -31,6 +31,7 @@ SOURCES = {
     "nekgpu_adjoint_host.cpp": ["-Xcompiler", "-ffp-contract=off"],
     "nekgpu_io.cpp": [],
     "nekgpu_2d.cu": ["--fmad=false"],
+    "nekgpu_curved.cu": [],
 }
 
 

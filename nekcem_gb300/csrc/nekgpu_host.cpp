@@ -990,6 +990,94 @@ int upload_fused(Context* c, const Compact& cp) {
   return upload_pml_fused(c, A, cp, a.pml);
 }
 
+// Curvilinear mesh for the fused FP64 form: the reference's per-node metrics
+// and face arrays as given; face node partners from the gs ids.  The
+// reference's face numbering is required (the lift finds a node's face
+// slots from its position in the element).
+int upload_curved(Context* c, const nekgpu_mesh* m) {
+  const int n = m->nx1;
+  const long n2 = (long)n * n, n3 = n2 * n, npts = n3 * m->nelt, nxzfl = 6 * n2 * m->nelt;
+  if (n < 3 || n > 8) return NEKGPU_ERR_UNSUPPORTED;
+  if (m->npml > 0) return NEKGPU_ERR_UNSUPPORTED;  // no PML on curvilinear meshes
+  for (long e = 0; e < m->nelt; ++e)
+    for (int f = 0; f < 6; ++f)
+      for (int b = 0; b < n; ++b)
+        for (int a = 0; a < n; ++a) {
+          const long j = a + (long)n * b + n2 * (f + 6 * e);
+          if (m->cemface[j] - 1 != e * n3 + face_vol(f, a, b, n)) return NEKGPU_ERR_MESH;
+        }
+  std::vector<int> pairs, single, partner(nxzfl, -2);
+  int st = pairs_from_ids(m->glo_face, nxzfl, pairs, single);
+  if (st) return st;
+  for (size_t q = 0; q + 1 < pairs.size(); q += 2) {
+    partner[pairs[q]] = m->cemface[pairs[q + 1]] - 1;
+    partner[pairs[q + 1]] = m->cemface[pairs[q]] - 1;
+  }
+  for (int j = 0; j < m->ncempec; ++j) {
+    const int sl = m->cempec[j] - 1;
+    if (sl < 0 || sl >= nxzfl || partner[sl] != -2) return NEKGPU_ERR_MESH;
+    partner[sl] = -1;
+  }
+  for (long j = 0; j < nxzfl; ++j)
+    if (partner[j] == -2) return NEKGPU_ERR_MESH;  // a face node with no partner and no wall
+  DevAlloc A(c);
+  std::vector<double> bm1(m->bmn, m->bmn + npts), eb(m->ebm1, m->ebm1 + npts),
+      hb(m->hbm1, m->hbm1 + npts);
+  if ((st = A.get(&c->d_u[0], 6 * npts)) || (st = A.get(&c->d_u[1], 6 * npts))) return st;
+  if ((st = upload_common(c, A, bm1, eb, hb))) return st;
+  if ((st = A.get(&c->d_coef, 2 * npts))) return st;
+  std::vector<double> base(2 * npts);
+  for (long g = 0; g < npts; ++g) {
+    base[g] = hb[g];
+    base[npts + g] = eb[g];
+  }
+  if ((st = A.put(&c->d_cbase, base))) return st;
+  c->coef_dt = std::nan("");
+  const double* mt[9] = {m->rxmn, m->rymn, m->rzmn, m->sxmn, m->symn, m->szmn, m->txmn, m->tymn, m->tzmn};
+  std::vector<double> metrics(9 * (size_t)npts), face(4 * (size_t)nxzfl), fcoef(4 * (size_t)nxzfl);
+  for (int q = 0; q < 9; ++q) std::copy(mt[q], mt[q] + npts, metrics.begin() + q * npts);
+  bool uniform = true;
+  for (long j = 0; j < nxzfl; ++j) {
+    face[j] = m->unxm[j];
+    face[nxzfl + j] = m->unym[j];
+    face[2 * nxzfl + j] = m->unzm[j];
+    face[3 * nxzfl + j] = m->aream[j];
+    const double Y0 = m->Y_0[j], Y1 = m->Y_1[j], Z0 = m->Z_0[j], Z1 = m->Z_1[j];
+    const double o[4] = {-0.5 / Y0 * Y1, 0.5 / Y0 * m->C0, 0.5 / Z0 * Z1, 0.5 / Z0 * m->C0};
+    for (int q = 0; q < 4; ++q) fcoef[q * nxzfl + j] = o[q];
+    uniform = uniform && o[0] == -0.5 && o[1] == 0.5 && o[2] == 0.5 && o[3] == 0.5;
+  }
+  CurvedDev& a = c->cargs;
+  a = CurvedDev{};
+  double* d;
+  int* di;
+  if ((st = A.put(&d, metrics))) return st;
+  a.metrics = d;
+  if ((st = A.put(&d, std::vector<double>(m->w3mn, m->w3mn + n3)))) return st;
+  a.w3 = d;
+  if ((st = A.put(&d, face))) return st;
+  a.face = d;
+  if (!uniform) {
+    if ((st = A.put(&d, fcoef))) return st;
+    a.fcoef = d;
+  }
+  if ((st = A.put(&di, partner))) return st;
+  a.partner = di;
+  a.nelt = m->nelt;
+  a.npts = npts;
+  a.nxzfl = nxzfl;
+  a.k = c->d_k;
+  a.coef = c->d_coef;
+  for (long i = 0; i < n2; ++i) a.D[i] = m->dxm1[i];
+  c->host_w3.assign(m->w3mn, m->w3mn + n3);
+  c->curved = true;
+  // the fused arguments carry the source weights for the curved kernel too
+  c->fargs = FusedDev{};
+  c->fargs.nelt = m->nelt;
+  c->fargs.npts = npts;
+  return NEKGPU_OK;
+}
+
 int finish_init(Context* c, int st) {
   if (st) {
     free_all(c);
@@ -1051,6 +1139,7 @@ int plain_stage(Context* c, int rkstep, double time, double dt) {
 int do_stage(Context* c, int rkstep, double time, double dt) {
   if (rkstep < 1 || rkstep > 5) return NEKGPU_ERR_ARG;
   if (c->ndim == 2) return stage2d(c, rkstep, time, dt);
+  if (c->curved) return curved_stage(c, rkstep, time, dt);
   if (c->form == NEKGPU_PLAIN) return plain_stage(c, rkstep, time, dt);
   if (c->form == NEKGPU_MIXED) return mixed_stage(c, rkstep, time, dt);
   return fused_stage(c, rkstep, time, dt);
@@ -1130,8 +1219,14 @@ int nekgpu_init(nekgpu_ctx** ctx, const nekgpu_mesh* m, int form) {
   } else {
     Compact cp;
     st = build_compact(m, cp);
-    if (!st) st = common_setup(c, form, m->nx1, m->nelt);
-    if (!st) st = upload_fused(c, cp);
+    if (st == NEKGPU_ERR_MESH && form == NEKGPU_FUSED64) {
+      // not affine: the curvilinear variant of the fused FP64 form
+      st = common_setup(c, form, m->nx1, m->nelt);
+      if (!st) st = upload_curved(c, m);
+    } else {
+      if (!st) st = common_setup(c, form, m->nx1, m->nelt);
+      if (!st) st = upload_fused(c, cp);
+    }
   }
   if (!st && m->xmn && m->ymn && m->zmn) {
     c->host_x.assign(m->xmn, m->xmn + c->npts);
@@ -1394,7 +1489,7 @@ int nekgpu_set_dispersive(nekgpu_ctx* c, int model, const double* params, long l
   if (!c || (model != NEKGPU_DRUDE && model != NEKGPU_LORENTZ) || n < 0 ||
       (n > 0 && (!params || !index || ld < c->npts)))
     return NEKGPU_ERR_ARG;
-  if (c->form == NEKGPU_MIXED_NAIVE || c->ndim == 2) return NEKGPU_ERR_UNSUPPORTED;
+  if (c->form == NEKGPU_MIXED_NAIVE || c->ndim == 2 || c->curved) return NEKGPU_ERR_UNSUPPORTED;
   const long P = c->npts, n3 = (long)c->nx * c->nx * c->nx;
   std::vector<signed char> kind = c->disp_kind;
   std::vector<double> par = c->disp_par;

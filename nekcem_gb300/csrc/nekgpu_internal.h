@@ -207,6 +207,27 @@ struct AdjointDev {
 };
 
 
+// Curvilinear hexahedra in the fused FP64 form (nekgpu_curved.cu): per-node
+// metrics and per-face-node geometry as the reference holds them
+struct CurvedDev {
+  int nelt;
+  long npts, nxzfl;
+  const double* u_in;
+  double* u_out;
+  double* k;
+  const double* coef;     // 2*npts: dt*hbm1 then dt*ebm1
+  const double* metrics;  // 9*npts: rx, ry, rz, sx, sy, sz, tx, ty, tz (cofactors)
+  const double* w3;       // nx^3
+  const double* face;     // 4*nxzfl: unx, uny, unz, area
+  const double* fcoef;    // 4*nxzfl: Y02, C02Y, Z02, C02Z
+  const int* partner;     // nxzfl: volume node across the face, -1 on PEC faces
+  const int* src_elem;    // nelt or null
+  const double* src_w;    // nx^3 per source element
+  double src_ft;
+  double a, b;
+  double D[kMaxNx * kMaxNx];  // D(i,j) at [i + nx*j]
+};
+
 // 2-D TE / TM stage (nekgpu_2d.cu): the reference's ldim = 2 arrays as given
 struct Stage2dDev {
   int nx, nelt, imode;  // imode 1 TE (E1, E2, H3), 2 TM (H1, H2, E3)
@@ -229,6 +250,8 @@ struct Context {
   int form = NEKGPU_MIXED;
   int ndim = 3, imode = 3;  // ndim 2: TE (imode 1) or TM (imode 2) quadrilateral mesh
   Stage2dDev s2{};
+  bool curved = false;      // fused FP64 form on a curvilinear mesh (nekgpu_curved.cu)
+  CurvedDev cargs{};
   int device = 0;
   int nx = 0, nelt = 0;
   long npts = 0, nxzfl = 0;
@@ -333,6 +356,9 @@ int scale_coef_pairs(Context* c, double dt);
 // with the 10-bit uh), Df = D rounded, and the remainder Dm = RN32(D - Dh),
 // as float pairs (layout in nekgpu_mixed.cu); uploaded once per nx
 int mixed_upload_D(int nx, const float* tab, size_t count);
+
+// nekgpu_curved.cu: one fused FP64 stage on a curvilinear mesh
+int curved_stage(Context* c, int rkstep, double time, double dt);
 
 // nekgpu_2d.cu: one 2-D TE / TM stage in the reference's arithmetic
 int stage2d(Context* c, int rkstep, double time, double dt);

@@ -1,14 +1,15 @@
 """Curvilinear (non-affine) elements: boxes with a smooth interior
 deformation (per-node metrics, curved faces with per-node normals and areas).
 The plain form runs them from the reference's arrays bit for bit against the
-oracle; the cavity mode (whose walls do not move) keeps its accuracy; the
-fused forms, which need affine elements, refuse them."""
+oracle; the fused FP64 form runs them through its curvilinear kernel at
+1e-12 per step; the cavity mode (whose walls do not move) keeps its accuracy
+on both; the mixed form, which needs affine elements, refuses them."""
 from __future__ import annotations
 
 import numpy as np
 import pytest
 
-from helpers import gpu_from_ref, make_ref, smooth_fields
+from helpers import gpu_from_ref, make_ref, rel_err, smooth_fields
 from nekcem_gb300 import cases
 from nekcem_gb300 import _lib as L
 
@@ -38,7 +39,31 @@ def test_plain_curved_bit_exact(m, materials):
     g.close(); ref.close()
 
 
-def test_curved_cavity_keeps_its_accuracy():
+@pytest.mark.parametrize("m", CURVED, ids=["pec_n4", "mixed_bc_n5", "periodic_n7"])
+@pytest.mark.parametrize("materials", [False, True])
+def test_fused64_curved_per_step(m, materials):
+    """The curvilinear kernel of the fused FP64 form against the oracle, with
+    the Ricker source on: 1e-12 relative per step over 4 steps."""
+    eps = (lambda x, y, z: 1.0 + 0.5 * np.sin(2 * x) ** 2) if materials else None
+    mu = (lambda x, y, z: 1.0 + 0.2 * np.cos(3 * z) ** 2) if materials else None
+    ref = make_ref(m["N"], m["nel"], (0, 0, 0), (1, 1, 1), m["bc"], eps=eps, mu=mu,
+                   deform=m["deform"])
+    g = gpu_from_ref(ref, "fused64")
+    H, E = smooth_fields(ref, 6)
+    ref.set_state(H, E); g.set_state(H, E)
+    src = dict(xc=(0.4, 0.5, 0.6), sigma=0.2, amp=1.0, f0=2.0, t0=0.1)
+    ref.set_source(**src); g.set_source(**src)
+    dt = 0.2 * ref.dxmin()
+    for step in range(4):
+        ref.op_rk(step * dt, dt)
+        g.run(1, step * dt, dt)
+        gH, gE = g.get_state()
+        assert rel_err(gH, gE, ref.hn, ref.en) <= 1e-12 * (step + 1), step
+    g.close(); ref.close()
+
+
+@pytest.mark.parametrize("form", ["plain", "fused64"])
+def test_curved_cavity_keeps_its_accuracy(form):
     """TM110 cavity on a deformed 4^3, N=7 mesh (the walls stay put, so the
     analytic mode is unchanged): after 300 steps the L2 error stays small.
     It is larger than on the affine mesh (9e-10 there): the curved geometry
@@ -48,7 +73,7 @@ def test_curved_cavity_keeps_its_accuracy():
     res = {}
     for deform in (0.0, 0.04):
         ref = make_ref(7, (4, 4, 4), (0, 0, 0), (1, 1, 1), (0, 0, 0), deform=deform)
-        g = gpu_from_ref(ref, "plain")
+        g = gpu_from_ref(ref, form)
         x, y, z = (a.copy() for a in ref.coords())
         c = cases.make("cavity")
         dt = 0.5 * cases.min_gll_spacing(x, y, z, 8, 64) * 0.5
@@ -61,10 +86,19 @@ def test_curved_cavity_keeps_its_accuracy():
     assert res[0.04] < 1e-6, res
 
 
-@pytest.mark.parametrize("form", ["fused64", "mixed"])
-def test_fused_forms_refuse_curved_meshes(form):
+def test_curved_refusals():
+    """The mixed form needs affine elements; the curvilinear FP64 kernel has
+    no PML, dispersive media or adjoint."""
     ref = make_ref(4, (2, 2, 2), (0, 0, 0), (1, 1, 1), (0, 0, 0), deform=0.05)
     with pytest.raises(L.NekgpuError) as e:
-        gpu_from_ref(ref, form)
+        gpu_from_ref(ref, "mixed")
     assert e.value.status == -2
+    g = gpu_from_ref(ref, "fused64")
+    g.set_state(np.zeros((3, g.npts)), np.zeros((3, g.npts)))
+    for call in (lambda: g.set_dispersive(g.DRUDE, np.ones((2, g.npts)), np.arange(3)),
+                 lambda: g.adjoint_gradient(1, 0.0, 0.01, np.ones(g.npts))):
+        with pytest.raises(L.NekgpuError) as e:
+            call()
+        assert e.value.status == -8
+    g.close()
     ref.close()
