@@ -182,6 +182,18 @@ int nekgpu_set_source_kind(nekgpu_ctx* ctx, int kind);
 int nekgpu_set_source(nekgpu_ctx* ctx, int enabled, const double xc[3], double sigma,
                       double amp, double f0, double t0);
 
+/* ---- dealiased curl (NEKGPU_PLAIN) ------------------------------------------ */
+/* param(18) = -1: maxwell_wght_dcurl (src/cem_maxwell.F:1541-1729) on lxd GLL
+ * points per direction instead of maxwell_wght_curl.  The tables are the
+ * reference's (built on its first dcurl call): jgl(lxd,nx1) interpolation
+ * (gen_int), dxmd(lxd,lxd) derivative (gen_dgl), w3md(lxd^3) weights, and
+ * metd the nine metric cofactors interpolated to the lxd^3 points, ordered
+ * rx, ry, rz, sx, sy, sz, tx, ty, tz, each (lxd^3, nelt).  lxd = 0 switches
+ * back; NEKGPU_ERR_UNSUPPORTED for the other forms, 2-D meshes or an lxd
+ * whose element working set does not fit in shared memory (~220 KB). */
+int nekgpu_set_dealias(nekgpu_ctx* ctx, int lxd, const double* jgl, const double* dxmd,
+                       const double* w3md, const double* metd);
+
 /* ---- dispersive media ---------------------------------------------------- */
 #define NEKGPU_DRUDE 1
 #define NEKGPU_LORENTZ 2

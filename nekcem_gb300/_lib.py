@@ -73,6 +73,7 @@ SIGNATURES = [
     ("nekgpu_volume", C.c_double, [C.c_void_p]),
     ("nekgpu_set_source_kind", C.c_int, [C.c_void_p, C.c_int]),
     ("nekgpu_set_source", C.c_int, [C.c_void_p, C.c_int, dp, C.c_double, C.c_double, C.c_double, C.c_double]),
+    ("nekgpu_set_dealias", C.c_int, [C.c_void_p, C.c_int, dp, dp, dp, dp]),
     ("nekgpu_set_dispersive", C.c_int, [C.c_void_p, C.c_int, dp, C.c_long, ip, C.c_long]),
     ("nekgpu_set_current", C.c_int, [C.c_void_p, C.c_int, dp, C.c_long]),
     ("nekgpu_get_current", C.c_int, [C.c_void_p, C.c_int, dp, C.c_long]),

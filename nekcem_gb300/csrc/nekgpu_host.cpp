@@ -1482,6 +1482,40 @@ int nekgpu_set_source_kind(nekgpu_ctx* c, int kind) {
   return NEKGPU_OK;
 }
 
+// Dealiased curl of the plain form: the driver's tables as the reference
+// builds them on the first maxwell_wght_dcurl call.
+int nekgpu_set_dealias(nekgpu_ctx* c, int lxd, const double* jgl, const double* dxmd,
+                       const double* w3md, const double* metd) {
+  if (!c) return NEKGPU_ERR_ARG;
+  if (c->form != NEKGPU_PLAIN || c->ndim == 2) return NEKGPU_ERR_UNSUPPORTED;
+  if (lxd == 0) {
+    c->pargs.md = 0;
+    return NEKGPU_OK;
+  }
+  const int mx = c->nx, md = lxd;
+  if (md < mx || !jgl || !dxmd || !w3md || !metd) return NEKGPU_ERR_ARG;
+  int dev_smem = 0;
+  cudaDeviceGetAttribute(&dev_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device);
+  if (dcurl_smem(mx, md) > (size_t)std::min(dev_smem, 220 * 1024)) return NEKGPU_ERR_UNSUPPORTED;
+  const long md2 = (long)md * md, md3 = md2 * md;
+  std::vector<double> vjgl(jgl, jgl + md * mx), vjgt((size_t)md * mx), vD(dxmd, dxmd + md2),
+      vDt(md2), vw3(w3md, w3md + md3), vmet(metd, metd + 9 * md3 * c->nelt);
+  for (int j = 0; j < mx; ++j)
+    for (int i = 0; i < md; ++i) vjgt[j + (size_t)mx * i] = vjgl[i + (size_t)md * j];
+  for (int j = 0; j < md; ++j)
+    for (int i = 0; i < md; ++i) vDt[j + (size_t)md * i] = vD[i + (size_t)md * j];
+  DevAlloc A(c);
+  double *d1, *d2, *d3, *d4, *d5, *d6;
+  int st;
+  if ((st = A.put(&d1, vjgl)) || (st = A.put(&d2, vjgt)) || (st = A.put(&d3, vD)) ||
+      (st = A.put(&d4, vDt)) || (st = A.put(&d5, vw3)) || (st = A.put(&d6, vmet)))
+    return st;
+  PlainDev& a = c->pargs;
+  a.jgl = d1; a.jgt = d2; a.dxmd = d3; a.dxtmd = d4; a.w3md = d5; a.metd = d6;
+  a.md = md;
+  return NEKGPU_OK;
+}
+
 // Dispersive media: the per-node model and parameters live on the host; each
 // call rebuilds the compact per-element device arrays of all listed nodes.
 int nekgpu_set_dispersive(nekgpu_ctx* c, int model, const double* params, long ld,

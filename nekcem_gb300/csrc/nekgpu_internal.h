@@ -116,6 +116,11 @@ struct PlainDev {
   double* pmlk;            // 6*npts: their RK registers
   double* pmlres;          // 12*npts: respmlbn, respmldn, respmlhn, respmlen
   DispDev disp;
+  // dealiased curl (md > 0): md GLL points per direction, interpolation
+  // jgl (md x mx) and its transpose jgt, derivative dxmd / dxtmd on the md
+  // points, weights w3md (md^3), metrics on the md^3 points (9 x md^3 x nelt)
+  int md;
+  const double *jgl, *jgt, *dxmd, *dxtmd, *w3md, *metd;
 };
 
 // PML data of the fused forms, compact over the PML elements (slot l holds
@@ -336,6 +341,8 @@ int plain_invqmass(Context* c);
 int plain_rk_update(Context* c, double ca, double cb, double dt);
 int plain_pml_step(Context* c);                                   // pml_step
 int plain_pml_rk_update(Context* c, double ca, double cb, double dt);
+// shared memory of the dealiased curl kernel for nx1 = mx, lxd = md
+size_t dcurl_smem(int mx, int md);
 // cem_maxwell_drude / cem_maxwell_lorentz with the currents' rk4_upd
 int plain_dispersive(Context* c, double ca, double cb, double dt);
 int plain_gs(Context* c, double* d_u, int nfld);
@@ -375,7 +382,5 @@ int norms_noalloc(Context* c, const double* exact_dev, double l2[6], double linf
 int util_norms(Context* c, const double* d_exact, double l2[6], double linf[6]);
 int util_energy(Context* c, double* energy);
 int util_blowup(Context* c, int* bad);
-int util_strided_copy(Context* c, double* dst, const double* src, long n, int ncomp,
-                      long dst_ld, long src_ld);
 
 }  // namespace nekgpu

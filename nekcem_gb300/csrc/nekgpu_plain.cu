@@ -84,6 +84,110 @@ __global__ void k_curl(PlainDev a) {
   }
 }
 
+// mxm (src/nek5_mxm_std.F:173-191) on shared-memory operands by the whole
+// block: c(i,j) = sum_l a(i,l) b(l,j), l ascending, a n1 x n2, b n2 x n3
+__device__ __forceinline__ void block_mxm(const double* A, int n1, const double* B, int n2,
+                                          double* Cm, int n3) {
+  for (int t = threadIdx.x; t < n1 * n3; t += blockDim.x) {
+    const int i = t % n1, j = t / n1;
+    double s = A[i] * B[n2 * j];
+    for (int l = 1; l < n2; ++l) s = s + A[i + n1 * l] * B[l + n2 * j];
+    Cm[t] = s;
+  }
+}
+
+// maxwell_wght_dcurl (src/cem_maxwell.F:1541-1729): per element, each field
+// interpolated to md^3 points (intp_rstd forward = specmpn with jgl, jgt,
+// src/cem_common.F:418-460, 507-538), local_grad3 there with dxmd, the
+// weighted curl with the interpolated metrics, and the projection back
+// (intp_rstd backward: specmpn with jgt, jgl).  H -> resE, E -> resH
+// (negated, chsign).  One CTA per element, every array in shared memory.
+__global__ void k_dcurl(PlainDev a) {
+  extern __shared__ double sm[];
+  const int mx = a.nx, md = a.md;
+  const int mx2 = mx * mx, mx3 = mx2 * mx, md2 = md * md, md3 = md2 * md;
+  double* s_jgl = sm;                 // md x mx
+  double* s_jgt = s_jgl + md * mx;    // mx x md
+  double* s_D = s_jgt + md * mx;      // md x md
+  double* s_Dt = s_D + md2;           // md x md
+  double* s_w3 = s_Dt + md2;          // md^3
+  double* s_ju = s_w3 + md3;          // 3 md^3
+  double* s_wd = s_ju + 3 * md3;      // 3 md^3
+  double* s_t1 = s_wd + 3 * md3;      // max(md mx^2, mx md^2)
+  double* s_t2 = s_t1 + md2 * mx;     // max(md^2 mx, mx^2 md)
+  double* s_u = s_t2 + md2 * mx;      // mx^3
+  const int e = blockIdx.x;
+  const long P = a.npts;
+  for (int t = threadIdx.x; t < md * mx; t += blockDim.x) {
+    s_jgl[t] = a.jgl[t];
+    s_jgt[t] = a.jgt[t];
+  }
+  for (int t = threadIdx.x; t < md2; t += blockDim.x) {
+    s_D[t] = a.dxmd[t];
+    s_Dt[t] = a.dxtmd[t];
+  }
+  for (int t = threadIdx.x; t < md3; t += blockDim.x) s_w3[t] = a.w3md[t];
+  for (int fld = 0; fld < 2; ++fld) {
+    const int uin = fld == 0 ? 0 : 3, wout = fld == 0 ? 3 : 0;
+    // ---- forward interpolation of the three components ----------------------
+    for (int q = 0; q < 3; ++q) {
+      __syncthreads();
+      for (int t = threadIdx.x; t < mx3; t += blockDim.x)
+        s_u[t] = a.u[(long)(uin + q) * P + (long)e * mx3 + t];
+      __syncthreads();
+      block_mxm(s_jgl, md, s_u, mx, s_t1, mx2);
+      __syncthreads();
+      for (int iz = 0; iz < mx; ++iz) block_mxm(s_t1 + md * mx * iz, md, s_jgt, mx, s_t2 + md2 * iz, md);
+      __syncthreads();
+      block_mxm(s_t2, md2, s_jgt, mx, s_ju + q * md3, md);
+    }
+    __syncthreads();
+    // ---- derivatives and the weighted curl on the md^3 points -----------------
+    for (int v = threadIdx.x; v < md3; v += blockDim.x) {
+      const int i = v % md, j = (v / md) % md, k = v / md2;
+      double g[3][3];
+      for (int q = 0; q < 3; ++q) {
+        const double* u = s_ju + q * md3;
+        double s = s_D[i] * u[md * j + md2 * k];
+        for (int l = 1; l < md; ++l) s = s + s_D[i + md * l] * u[l + md * j + md2 * k];
+        g[q][0] = s;
+        s = u[i + md2 * k] * s_Dt[md * j];
+        for (int l = 1; l < md; ++l) s = s + u[i + md * l + md2 * k] * s_Dt[l + md * j];
+        g[q][1] = s;
+        s = u[i + md * j] * s_Dt[md * k];
+        for (int l = 1; l < md; ++l) s = s + u[i + md * j + md2 * l] * s_Dt[l + md * k];
+        g[q][2] = s;
+      }
+      const double w = s_w3[v];
+      const double u1rw = g[0][0] * w, u1sw = g[0][1] * w, u1tw = g[0][2] * w;
+      const double u2rw = g[1][0] * w, u2sw = g[1][1] * w, u2tw = g[1][2] * w;
+      const double u3rw = g[2][0] * w, u3sw = g[2][1] * w, u3tw = g[2][2] * w;
+      const long nm = (long)md3 * a.nelt, k0 = (long)e * md3 + v;
+      const double* M = a.metd;
+      const double rx = M[k0], ry = M[nm + k0], rz = M[2 * nm + k0];
+      const double sx = M[3 * nm + k0], sy = M[4 * nm + k0], sz = M[5 * nm + k0];
+      const double tx = M[6 * nm + k0], ty = M[7 * nm + k0], tz = M[8 * nm + k0];
+      s_wd[v] = u3rw * ry + u3sw * sy + u3tw * ty - u2rw * rz - u2sw * sz - u2tw * tz;
+      s_wd[md3 + v] = u1rw * rz + u1sw * sz + u1tw * tz - u3rw * rx - u3sw * sx - u3tw * tx;
+      s_wd[2 * md3 + v] = u2rw * rx + u2sw * sx + u2tw * tx - u1rw * ry - u1sw * sy - u1tw * ty;
+    }
+    // ---- projection back to the nx1^3 points ------------------------------------
+    for (int q = 0; q < 3; ++q) {
+      __syncthreads();
+      block_mxm(s_jgt, mx, s_wd + q * md3, md, s_t1, md2);
+      __syncthreads();
+      for (int iz = 0; iz < md; ++iz) block_mxm(s_t1 + mx * md * iz, mx, s_jgl, md, s_t2 + mx2 * iz, mx);
+      __syncthreads();
+      for (int t = threadIdx.x; t < mx3; t += blockDim.x) {
+        const int ij = t % mx2, kk = t / mx2;
+        double s = s_t2[ij] * s_jgl[md * kk];
+        for (int l = 1; l < md; ++l) s = s + s_t2[ij + mx2 * l] * s_jgl[l + md * kk];
+        a.res[(long)(wout + q) * P + (long)e * mx3 + t] = fld == 1 ? -s : s;
+      }
+    }
+  }
+}
+
 // cem_maxwell_restrict_to_face (src/cem_maxwell.F:604-623)
 __global__ void k_restrict(PlainDev a) {
   long j = blockIdx.x * (long)blockDim.x + threadIdx.x;
@@ -315,7 +419,23 @@ int plain_dispersive(Context* c, double ca, double cb, double dt) {
   return last_error();
 }
 
+size_t dcurl_smem(int mx, int md) {
+  const size_t md2 = (size_t)md * md, md3 = md2 * md;
+  return (2 * (size_t)md * mx + 2 * md2 + 7 * md3 + 2 * md2 * mx + (size_t)mx * mx * mx) *
+         sizeof(double);
+}
+
 int plain_cem_maxwell(Context* c) {
+  if (c->pargs.md) {
+    static bool dattr = false;
+    if (!dattr) {
+      cudaFuncSetAttribute(k_dcurl, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
+      dattr = true;
+    }
+    k_dcurl<<<c->nelt, kThreads, dcurl_smem(c->nx, c->pargs.md), c->stream>>>(c->pargs);
+    c->last_launches += 1;
+    return last_error();
+  }
   const int n = c->nx, n3 = n * n * n;
   size_t smem = (3 * (size_t)n3 + 2 * n * n) * sizeof(double);
   static bool attr_set = false;

@@ -165,6 +165,19 @@ class MaxwellGPU:
         L.check(L.load().nekgpu_set_source(self._h, 1 if enabled else 0, x, sigma, amp, f0, t0),
                 "nekgpu_set_source")
 
+    # ---- dealiased curl (plain form) ------------------------------------------
+    def set_dealias(self, lxd: int, jgl=None, dxmd=None, w3md=None, metd=None):
+        """maxwell_wght_dcurl on lxd points per direction with the reference's
+        tables (Fortran layouts, flattened); lxd = 0 switches it off."""
+        if lxd == 0:
+            L.check(L.load().nekgpu_set_dealias(self._h, 0, None, None, None, None),
+                    "nekgpu_set_dealias")
+            return
+        arrs = [np.ascontiguousarray(a, dtype=np.float64).ravel() for a in (jgl, dxmd, w3md, metd)]
+        self._keep.extend(arrs)
+        L.check(L.load().nekgpu_set_dealias(self._h, int(lxd), *[_dp(a) for a in arrs]),
+                "nekgpu_set_dealias")
+
     # ---- dispersive media (cem_maxwell_drude / cem_maxwell_lorentz) ----------
     DRUDE, LORENTZ = 1, 2
 

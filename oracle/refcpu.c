@@ -57,6 +57,11 @@ struct ref_ctx {
   int *drudeindex, *lorentzindex;
   double *drudeparams, *djn, *dkjn, *dresjn;
   double *lorentzparams, *ljn, *lkjn, *lresjn;
+  /* dealiased curl (ifdealias, param(18) = -1): md = lxd GLL points per
+   * direction, interpolation jgl (md x mx) / jgt, derivative dxmd / dxtmd on
+   * the md points, weights w3md and the metrics interpolated to md^3 nodes */
+  int md;
+  double *jgl, *jgt, *dxmd, *dxtmd, *w3md, *metd;
   int rkstep_now; /* stage of the op in progress (0 outside ref_rk_stage) */
   double dt_now;
   double volvm1;
@@ -617,6 +622,7 @@ void ref_destroy(ref_ctx* c) {
                  c->lorentzparams, c->ljn, c->lkjn, c->lresjn};
   for (size_t i = 0; i < sizeof(q) / sizeof(q[0]); ++i) free(q[i]);
   free(c->drudeindex); free(c->lorentzindex);
+  free(c->jgl); free(c->jgt); free(c->dxmd); free(c->dxtmd); free(c->w3md); free(c->metd);
   free(c->gs_order); free(c->gs_start);
   free(c);
 }
@@ -644,6 +650,10 @@ double* ref_darray(ref_ctx* c, const char* name, long* len) {
       {"pmlbn", c->pmlbn, c->pmlbn ? 3 * c->npts : 0},
       {"pmldn", c->pmldn, c->pmldn ? 3 * c->npts : 0},
       {"pmlinner", c->pmlinner, c->ifpml ? 6 : 0}, {"pmlouter", c->pmlouter, c->ifpml ? 6 : 0},
+      {"jgl", c->jgl, c->md ? (long)c->md * c->n : 0},
+      {"dxmd", c->dxmd, c->md ? (long)c->md * c->md : 0},
+      {"w3md", c->w3md, c->md ? (long)c->md * c->md * c->md : 0},
+      {"metd", c->metd, c->md ? 9L * c->md * c->md * c->md * c->nelt : 0},
       {"drudejn", c->djn, c->djn ? 3 * c->npts : 0},
       {"lorentzjn", c->ljn, c->ljn ? 6 * c->npts : 0},
   };
@@ -795,8 +805,13 @@ static void invqmass_2d(ref_ctx* c);
 void ref_cem_maxwell(ref_ctx* c) {
   if (c->ndim == 2) { cem_maxwell_2d(c); return; }
   long np = c->npts;
-  ref_wght_curl(c, c->resen, c->resen + np, c->resen + 2 * np, c->hn, c->hn + np, c->hn + 2 * np);
-  ref_wght_curl(c, c->reshn, c->reshn + np, c->reshn + 2 * np, c->en, c->en + np, c->en + 2 * np);
+  if (c->md) { /* ifdealias branch (src/cem_maxwell.F:519-530) */
+    ref_wght_dcurl(c, c->resen, c->resen + np, c->resen + 2 * np, c->hn, c->hn + np, c->hn + 2 * np);
+    ref_wght_dcurl(c, c->reshn, c->reshn + np, c->reshn + 2 * np, c->en, c->en + np, c->en + 2 * np);
+  } else {
+    ref_wght_curl(c, c->resen, c->resen + np, c->resen + 2 * np, c->hn, c->hn + np, c->hn + 2 * np);
+    ref_wght_curl(c, c->reshn, c->reshn + np, c->reshn + 2 * np, c->en, c->en + np, c->en + 2 * np);
+  }
 #pragma omp parallel for schedule(static) num_threads(g_threads)
   for (long i = 0; i < 3 * np; ++i) c->reshn[i] = -c->reshn[i];
 }
@@ -1682,3 +1697,135 @@ ref_ctx* ref_create_box2d(int N, int nelx, int nely, const double lo[2], const d
 
 int ref_ndim(const ref_ctx* c) { return c->ndim; }
 int ref_imode(const ref_ctx* c) { return c->imode; }
+
+/* ------------------------------------------------------------------------ */
+/* Dealiased curl (maxwell_wght_dcurl, src/cem_maxwell.F:1541-1729)          */
+/* ------------------------------------------------------------------------ */
+
+/* fd_weights_full (src/nek5_coef.F:1804-1857): Fornberg's finite-difference
+ * weights c(j,k) at xx for the points x(0:n), derivatives 0..m.  c holds
+ * (n+1)*(m+1) values, c[j + (n+1)*k]. */
+static void fd_weights(double xx, const double* x, int n, int m, double* c) {
+  int np = n + 1;
+  double c1 = 1.0, c4 = x[0] - xx;
+  for (int k = 0; k <= m; ++k)
+    for (int j = 0; j <= n; ++j) c[j + np * k] = 0.0;
+  c[0] = 1.0;
+  for (int i = 1; i <= n; ++i) {
+    int mn = i < m ? i : m;
+    double c2 = 1.0, c5 = c4;
+    c4 = x[i] - xx;
+    for (int j = 0; j < i; ++j) {
+      double c3 = x[i] - x[j];
+      c2 = c2 * c3;
+      if (j == i - 1) {
+        for (int k = mn; k >= 1; --k)
+          c[i + np * k] = c1 * ((double)k * c[i - 1 + np * (k - 1)] - c5 * c[i - 1 + np * k]) / c2;
+        c[i] = -c1 * c5 * c[i - 1] / c2;
+      }
+      for (int k = mn; k >= 1; --k)
+        c[j + np * k] = (c4 * c[j + np * k] - (double)k * c[j + np * (k - 1)]) / c3;
+      c[j] = c4 * c[j] / c3;
+    }
+    c1 = c2;
+  }
+}
+
+/* specmpn (src/cem_common.F:418-460): tensor-product interpolation from
+ * na^3 to nb^3 with ba (nb x na) and ab (na x nb) */
+static void specmpn3(double* b, int nb, const double* a, int na, const double* ba,
+                     const double* ab) {
+  double* w1 = dalloc((long)nb * na * na);
+  double* w2 = dalloc((long)nb * nb * na);
+  mxm(ba, nb, a, na, w1, na * na);
+  for (int iz = 0; iz < na; ++iz)
+    mxm(w1 + (long)nb * na * iz, nb, ab, na, w2 + (long)nb * nb * iz, nb);
+  mxm(w2, nb * nb, ab, na, b, nb);
+  free(w1); free(w2);
+}
+
+/* the tables of maxwell_wght_dcurl's first call: gen_int (src/cem_common.F:
+ * 584-617, GLL mx -> GLL md), gen_dgl (:619-674), w3md and the metrics
+ * interpolated with intp_rstd; md = 0 switches the dealiased curl off */
+int ref_set_dealias(ref_ctx* c, int md) {
+  free(c->jgl); free(c->jgt); free(c->dxmd); free(c->dxtmd); free(c->w3md); free(c->metd);
+  c->jgl = c->jgt = c->dxmd = c->dxtmd = c->w3md = c->metd = NULL;
+  c->md = 0;
+  if (md == 0) return 0;
+  int mx = c->n;
+  if (c->ndim != 3 || md < mx || md > 32) return -1;
+  double *zx = dalloc(mx), *wx = dalloc(mx), *zd = dalloc(md), *wd = dalloc(md);
+  double* cw = dalloc(2L * (md > mx ? md : mx));
+  ref_zwgll(zx, wx, mx);
+  ref_zwgll(zd, wd, md);
+  c->jgl = dalloc((long)md * mx); c->jgt = dalloc((long)md * mx);
+  for (int i = 0; i < md; ++i) {
+    fd_weights(zd[i], zx, mx - 1, 0, cw);
+    for (int j = 0; j < mx; ++j) c->jgl[i + (long)md * j] = cw[j];
+  }
+  for (int j = 0; j < mx; ++j)
+    for (int i = 0; i < md; ++i) c->jgt[j + (long)mx * i] = c->jgl[i + (long)md * j];
+  c->dxmd = dalloc((long)md * md); c->dxtmd = dalloc((long)md * md);
+  for (int i = 0; i < md; ++i) {
+    fd_weights(zd[i], zd, md - 1, 1, cw);
+    for (int j = 0; j < md; ++j) c->dxmd[i + (long)md * j] = cw[md + j];
+  }
+  for (int j = 0; j < md; ++j)
+    for (int i = 0; i < md; ++i) c->dxtmd[j + (long)md * i] = c->dxmd[i + (long)md * j];
+  long md3 = (long)md * md * md, mx3 = (long)mx * mx * mx;
+  c->w3md = dalloc(md3);
+  for (int k = 0; k < md; ++k)
+    for (int j = 0; j < md; ++j)
+      for (int i = 0; i < md; ++i) c->w3md[i + md * j + (long)md * md * k] = wd[i] * wd[j] * wd[k];
+  c->metd = dalloc(9 * md3 * c->nelt);
+  const double* mt[9] = {c->rxm1, c->rym1, c->rzm1, c->sxm1, c->sym1, c->szm1,
+                         c->txm1, c->tym1, c->tzm1};
+  for (int q = 0; q < 9; ++q)
+    for (int e = 0; e < c->nelt; ++e)
+      specmpn3(c->metd + md3 * (c->nelt * (long)q + e), md, mt[q] + mx3 * e, mx, c->jgl, c->jgt);
+  free(zx); free(wx); free(zd); free(wd); free(cw);
+  c->md = md;
+  return 0;
+}
+
+/* maxwell_wght_dcurl, ldim = 3: (w1,w2,w3) = B curl(u1,u2,u3) evaluated on
+ * the md^3 points and projected back with the transposed interpolation */
+void ref_wght_dcurl(ref_ctx* c, double* w1, double* w2, double* w3, const double* u1,
+                    const double* u2, const double* u3) {
+  int mx = c->n, md = c->md;
+  long mx3 = (long)mx * mx * mx, md3 = (long)md * md * md, md2 = (long)md * md;
+  long nm = md3 * c->nelt;
+#pragma omp parallel for schedule(static) num_threads(g_threads)
+  for (int e = 0; e < c->nelt; ++e) {
+    double *ju[3], *g[9], *wdd[3];
+    for (int q = 0; q < 3; ++q) { ju[q] = dalloc(md3); wdd[q] = dalloc(md3); }
+    for (int q = 0; q < 9; ++q) g[q] = dalloc(md3);
+    const double* u[3] = {u1 + mx3 * e, u2 + mx3 * e, u3 + mx3 * e};
+    for (int q = 0; q < 3; ++q) {
+      specmpn3(ju[q], md, u[q], mx, c->jgl, c->jgt);
+      mxm(c->dxmd, md, ju[q], md, g[3 * q], (int)md2);
+      for (int k = 0; k < md; ++k)
+        mxm(ju[q] + md2 * k, md, c->dxtmd, md, g[3 * q + 1] + md2 * k, md);
+      mxm(ju[q], (int)md2, c->dxtmd, md, g[3 * q + 2], md);
+    }
+    const double* M = c->metd;
+    for (long i = 0; i < md3; ++i) {
+      long k = i + md3 * e;
+      double w = c->w3md[i];
+      double u1rw = g[0][i] * w, u1sw = g[1][i] * w, u1tw = g[2][i] * w;
+      double u2rw = g[3][i] * w, u2sw = g[4][i] * w, u2tw = g[5][i] * w;
+      double u3rw = g[6][i] * w, u3sw = g[7][i] * w, u3tw = g[8][i] * w;
+      double rx = M[k], ry = M[nm + k], rz = M[2 * nm + k];
+      double sx = M[3 * nm + k], sy = M[4 * nm + k], sz = M[5 * nm + k];
+      double tx = M[6 * nm + k], ty = M[7 * nm + k], tz = M[8 * nm + k];
+      wdd[0][i] = u3rw * ry + u3sw * sy + u3tw * ty - u2rw * rz - u2sw * sz - u2tw * tz;
+      wdd[1][i] = u1rw * rz + u1sw * sz + u1tw * tz - u3rw * rx - u3sw * sx - u3tw * tx;
+      wdd[2][i] = u2rw * rx + u2sw * sx + u2tw * tx - u1rw * ry - u1sw * sy - u1tw * ty;
+    }
+    double* out[3] = {w1 + mx3 * e, w2 + mx3 * e, w3 + mx3 * e};
+    for (int q = 0; q < 3; ++q) specmpn3(out[q], mx, wdd[q], md, c->jgt, c->jgl);
+    for (int q = 0; q < 3; ++q) { free(ju[q]); free(wdd[q]); }
+    for (int q = 0; q < 9; ++q) free(g[q]);
+  }
+}
+

@@ -98,6 +98,14 @@ void ref_set_drude(ref_ctx* c, const double* params, const int* index, long n);
 void ref_set_lorentz(ref_ctx* c, const double* params, const int* index, long n);
 void ref_dispersive(ref_ctx* c, int rkstep, double dt);
 
+/* Dealiased curl (param(18) = -1: maxwell_wght_dcurl, src/cem_maxwell.F:
+ * 1541-1729) on md = lxd >= nx1 GLL points per direction; md = 0 returns to
+ * maxwell_wght_curl.  Returns -1 for a bad md or a 2-D mesh.  The tables
+ * are the darrays "jgl" (md x mx), "dxmd" (md x md), "w3md" and "metd". */
+int ref_set_dealias(ref_ctx* c, int md);
+void ref_wght_dcurl(ref_ctx* c, double* w1, double* w2, double* w3, const double* u1,
+                    const double* u2, const double* u3);
+
 /* ---- the reference routines on the hot path ---- */
 void ref_local_grad3(double* ur, double* us, double* ut, const double* u, int n,
                      const double* D, const double* Dt);

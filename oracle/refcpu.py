@@ -61,6 +61,8 @@ def lib():
         L.ref_set_source_kind.argtypes = [vp, ip]
         L.ref_set_pml.argtypes = [vp, ip, C.c_double, C.c_double]
         L.ref_pml_step.argtypes = [vp]
+        L.ref_set_dealias.restype = ip
+        L.ref_set_dealias.argtypes = [vp, ip]
         L.ref_create_box2d.restype = vp
         L.ref_create_box2d.argtypes = [ip, ip, ip, dp, dp, C.POINTER(C.c_int), ip]
         L.ref_set_drude.argtypes = [vp, dp, C.POINTER(C.c_int), C.c_long]
@@ -215,6 +217,12 @@ class RefBox:
     def lorentz_jn(self):
         """(6, npts) view of the Lorentz currents: J1 (3 rows) then J2"""
         return self.d("lorentzjn").reshape(6, self.npts)
+
+    def set_dealias(self, md: int):
+        """Dealiased curl on md GLL points per direction (param(18) = -1 with
+        lxd = md); 0 returns to the plain weighted curl."""
+        if lib().ref_set_dealias(self._c, int(md)) != 0:
+            raise ValueError("ref_set_dealias rejected md")
 
     def set_source_kind(self, kind: int):
         lib().ref_set_source_kind(self._c, int(kind))

@@ -16,6 +16,7 @@ import numpy as np
 import pytest
 
 from helpers import gpu_from_ref, make_ref, smooth_fields
+from nekcem_gb300 import _lib as L
 from oracle import refcpu as R
 
 
@@ -108,7 +109,7 @@ def test_plain_dcurl_bit_exact(N, md, bc, deform):
                    eps=lambda x, y, z: 1.0 + 0.5 * np.sin(2 * x) ** 2)
     ref.set_dealias(md)
     g = gpu_from_ref(ref, "plain")
-    g.set_dealias(md)
+    g.set_dealias(md, ref.d("jgl"), ref.d("dxmd"), ref.d("w3md"), ref.d("metd"))
     H, E = smooth_fields(ref, 7)
     ref.set_state(H, E); g.set_state(H, E)
     dt = 0.2 * ref.dxmin()
@@ -117,3 +118,28 @@ def test_plain_dcurl_bit_exact(N, md, bc, deform):
     np.testing.assert_array_equal(gH, ref.hn)
     np.testing.assert_array_equal(gE, ref.en)
     g.close(); ref.close()
+
+
+@pytest.mark.gpu
+def test_dealias_refusals():
+    ref = make_ref(4, (2, 2, 2), (0, 0, 0), (1, 1, 1), (0, 0, 0), deform=0.05)
+    ref.set_dealias(6)
+    tabs = (ref.d("jgl"), ref.d("dxmd"), ref.d("w3md"), ref.d("metd"))
+    g = gpu_from_ref(ref, "fused64")
+    with pytest.raises(L.NekgpuError) as e:
+        g.set_dealias(6, *tabs)
+    assert e.value.status == -8
+    g.close()
+    g = gpu_from_ref(ref, "plain")
+    with pytest.raises(L.NekgpuError) as e:
+        g.set_dealias(4, *tabs)  # fewer points than nx1
+    assert e.value.status == -1
+    g.set_dealias(6, *tabs)
+    g.set_dealias(0)  # back to the plain curl
+    H, E = smooth_fields(ref, 2)
+    ref.set_dealias(0)
+    ref.set_state(H, E); g.set_state(H, E)
+    ref.run(2, 0.0, 1e-3); g.run(2, 0.0, 1e-3)
+    np.testing.assert_array_equal(g.get_state()[1], ref.en)
+    g.close(); ref.close()
+
