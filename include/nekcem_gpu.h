@@ -182,6 +182,34 @@ int nekgpu_set_source_kind(nekgpu_ctx* ctx, int kind);
 int nekgpu_set_source(nekgpu_ctx* ctx, int enabled, const double xc[3], double sigma,
                       double amp, double f0, double t0);
 
+/* ---- incident field (userinc) ------------------------------------------------ */
+/* userinc between the restriction to faces and the flux
+ * (src/cem_maxwell.F:495-496) in the plane-wave form of the reference's
+ * cases (tests/drude/drude.usr:7-42): the face values of the n listed slots
+ * (1-based incindex) get amp[0..2] * cos(k.x - omega t) on H and amp[3..5] *
+ * cos(...) on E, x the face node, t the stage time.  n = 0 removes it.  All
+ * three 3-D forms (not on curvilinear meshes); needs node coordinates. */
+int nekgpu_set_incident(nekgpu_ctx* ctx, const int* slots, long n, const double amp[6],
+                        const double kvec[3], double omega);
+/* Sets "pmlbn" or "pmldn" (3*npts, the reference layout; a case's userini
+ * sets pmlbn = mu H, pmldn = eps E); nodes outside the PML are ignored. */
+int nekgpu_set_array(nekgpu_ctx* ctx, const char* name, const double* in);
+
+/* ---- graphene sheets (NEKGPU_PLAIN) ------------------------------------------ */
+/* cem_3d_graphene_current (src/cem_maxwell.F:2827-2931) run through userfsrc
+ * as tests/3dgraphene does: on the n listed face slots (1-based graphindex)
+ * the surface current from the face fields and the 12 parameters
+ * params(nxzfl,12) (a_d, b_d, b_cp1, a_211, a_221, b_11, b_21, b_cp2, a_212,
+ * a_222, b_12, b_22), its auxiliary currents advanced with the RK stage, and
+ * -J added to the -n x H part of the flux before the face sum.  yconduc is
+ * the reference's face array (nxzfl).  The currents start at zero; n = 0
+ * removes the sheets.  Plain form only (NEKGPU_ERR_UNSUPPORTED otherwise). */
+int nekgpu_set_graphene(nekgpu_ctx* ctx, const double* params, const int* slots, long n,
+                        const double* yconduc);
+/* The face currents fjn(ld,3,6), ld >= nxzfl: listed slots only. */
+int nekgpu_set_graphene_current(nekgpu_ctx* ctx, const double* fjn, long ld);
+int nekgpu_get_graphene_current(nekgpu_ctx* ctx, double* fjn, long ld);
+
 /* ---- dealiased curl (NEKGPU_PLAIN) ------------------------------------------ */
 /* param(18) = -1: maxwell_wght_dcurl (src/cem_maxwell.F:1541-1729) on lxd GLL
  * points per direction instead of maxwell_wght_curl.  The tables are the

@@ -73,6 +73,11 @@ SIGNATURES = [
     ("nekgpu_volume", C.c_double, [C.c_void_p]),
     ("nekgpu_set_source_kind", C.c_int, [C.c_void_p, C.c_int]),
     ("nekgpu_set_source", C.c_int, [C.c_void_p, C.c_int, dp, C.c_double, C.c_double, C.c_double, C.c_double]),
+    ("nekgpu_set_incident", C.c_int, [C.c_void_p, ip, C.c_long, dp, dp, C.c_double]),
+    ("nekgpu_set_array", C.c_int, [C.c_void_p, C.c_char_p, dp]),
+    ("nekgpu_set_graphene", C.c_int, [C.c_void_p, dp, ip, C.c_long, dp]),
+    ("nekgpu_set_graphene_current", C.c_int, [C.c_void_p, dp, C.c_long]),
+    ("nekgpu_get_graphene_current", C.c_int, [C.c_void_p, dp, C.c_long]),
     ("nekgpu_set_dealias", C.c_int, [C.c_void_p, C.c_int, dp, dp, dp, dp]),
     ("nekgpu_set_dispersive", C.c_int, [C.c_void_p, C.c_int, dp, C.c_long, ip, C.c_long]),
     ("nekgpu_set_current", C.c_int, [C.c_void_p, C.c_int, dp, C.c_long]),

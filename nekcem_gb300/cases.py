@@ -318,6 +318,197 @@ class DispersiveWave:
         return np.stack(J)
 
 
+class DrudeHalfSpace:
+    """The reference's tests/drude case (a normally incident plane wave on a
+    Drude half-space, tests/drude/drude.usr) restated in 3-D: x and z
+    periodic, 'PML' at both y ends (6 layers, order 3, error 1e-15; the
+    reference has PEC below, where the transmitted wave has decayed by
+    e^-43), vacuum above y = 0, a Drude medium below (eps_inf = 1, a = 0,
+    b = 100, so eps(omega = 5) = -3 and the wave is totally reflected).  The
+    incident field cos(-k1 y - omega t) (H_z, eta1 E_x) enters through the
+    y = 0 faces of the upper elements (userinc); above them the field is the
+    reflected wave (damped inside the PML as usersol damps it), below it the
+    evanescent transmitted wave with its Drude current."""
+
+    N, nel = 8, (2, 32, 2)
+    lo, hi = (-2.5, -5.0, -2.5), (2.5, 5.0, 2.5)
+    bc = (PERIODIC, 2, PERIODIC)
+    pml = (6, 3.0, 1e-15)
+    dt, nsteps = 0.005, 1000
+    omega, a, b = 5.0, 0.0, 100.0
+
+    def __init__(self):
+        w = self.omega
+        self.eps2 = 1.0 - self.b / (w * (w + 1j * self.a))
+        self.eta1 = 1.0
+        eta2 = np.sqrt(1.0 / self.eps2 + 0j)
+        if eta2.real == 0.0 and eta2.imag > 0.0:  # the branch drude.usr picks
+            eta2 = -eta2
+        self.eta2 = eta2
+        self.k1 = w
+        self.k2 = w * np.sqrt(self.eps2 + 0j)
+        self.refl = (self.eta1 - eta2) / (self.eta1 + eta2)
+        self.tran = 2 * self.eta1 / (self.eta1 + eta2)
+        hy = (self.hi[1] - self.lo[1]) / self.nel[1]
+        self.pml_inner = self.hi[1] - self.pml[0] * hy
+        self.pml_outer = self.hi[1]
+
+    def regions(self, y, n3):
+        """per node: upper (element centre y > 0) and inside the upper PML"""
+        yc = np.repeat(np.asarray(y).reshape(-1, n3).mean(axis=1), n3)
+        return yc > 0.0, yc > self.pml_inner
+
+    def exact(self, x, y, z, t, n3):
+        up, inpml = self.regions(y, n3)
+        d = self.pml_outer - self.pml_inner
+        order, referr = self.pml[1], self.pml[2]
+        smax = -(order + 1) * np.log(referr) / (2.0 * self.eta1 * d)
+        fac = np.where(inpml, (smax * d / (order + 1)) * np.clip((y - self.pml_inner) / d, 0, None)
+                       ** (order + 1), 0.0)
+        w = self.omega
+        usc_up = self.refl * np.exp(1j * (self.k1 * y - w * t) - self.eta1 * fac)
+        usc_lo = self.tran * np.exp(1j * (-self.k2 * y - w * t))
+        zero = np.zeros_like(y)
+        Hz = np.where(up, usc_up.real, usc_lo.real)
+        Ex = np.where(up, (-self.eta1 * usc_up).real, (self.eta2 * usc_lo).real)
+        return np.stack([zero, zero, Hz]), np.stack([Ex, zero, zero])
+
+    def drude(self, y, n3):
+        """node indices of the Drude medium, its parameters (2, n) and the
+        initial current (3, n)"""
+        up, _ = self.regions(y, n3)
+        idx = np.nonzero(~up)[0]
+        n = np.size(y)
+        params = np.stack([np.full(n, self.a), np.full(n, self.b)])
+        sig = self.b / (self.a - 1j * self.omega)
+        efac = self.tran * self.eta2 * np.exp(1j * (-self.k2 * np.asarray(y)))
+        J = np.zeros((3, n))
+        J[0, idx] = (sig * efac).real[idx]
+        return idx, params, J
+
+    def incident_slots(self, y, cemface, n3, nf):
+        """0-based face slots of the upper elements' faces that lie on y = 0"""
+        up, _ = self.regions(y, n3)
+        y = np.asarray(y)
+        cf = np.asarray(cemface).reshape(-1, nf)
+        slots = []
+        for f in range(cf.shape[0]):
+            nodes = cf[f]
+            if up[nodes[0]] and np.all(np.abs(y[nodes]) <= 1e-8):
+                slots.extend(range(f * nf, (f + 1) * nf))
+        return np.array(slots, dtype=np.int64)
+
+    def incident(self):
+        """amp (H then E), k and omega of userinc"""
+        return (0.0, 0.0, 1.0, self.eta1, 0.0, 0.0), (0.0, -self.k1, 0.0), self.omega
+
+
+class GrapheneSheet:
+    """The reference's tests/3dgraphene case: two superimposed normally
+    incident plane waves (TE: H_z, E_x; TM: E_z, H_x) from y > 0 on a
+    graphene sheet at y = 0 (Drude term plus two critical points,
+    cem_3d_graphene_current), vacuum on both sides, 'PML' at both y ends
+    (2 layers, order 3, error 1e-10), x and z periodic; 4 x 12 x 4 elements
+    on [-2.5,2.5] x [-5,5] x [-2.5,2.5], N=8, dt = 0.005, 1000 steps.  The
+    exact solution is the reflected wave above and the transmitted wave
+    below, each damped inside its PML as usersol damps it."""
+
+    N, nel = 8, (4, 12, 4)
+    lo, hi = (-2.5, -5.0, -2.5), (2.5, 5.0, 2.5)
+    bc = (PERIODIC, 2, PERIODIC)
+    pml = (2, 3.0, 1e-10)
+    dt, nsteps = 0.005, 1000
+    omega = 5.0
+    # a_d, b_d, b_cp1, a_211, a_221, b_11, b_21, b_cp2, a_212, a_222, b_12, b_22
+    params = (0.0, 1.499, -2.599e-03, 4.632e+05, 1.090e+03, -1.391, -3.125e+02,
+              -1.049e-03, 4.271e+05, 2.742e+02, -7.769e-02, 4.268e+02)
+    l2tol = (5e-4, 1e-14, 5e-4, 5e-4, 1e-14, 5e-4)
+    linftol = (5e-3, 5e-12, 5e-3, 5e-3, 5e-12, 5e-3)
+
+    def __init__(self):
+        w, CI = self.omega, 1j
+        a_d, b_d, b_cp1, a_211, a_221, b_11, b_21, b_cp2, a_212, a_222, b_12, b_22 = self.params
+        s_d = b_d / (a_d - CI * w)
+        s_cp1 = (CI / w) * ((a_211 * b_11 + CI * w * b_21) / (w ** 2 - a_211 + CI * w * a_221) + b_11) - b_cp1
+        s_cp2 = (CI / w) * ((a_212 * b_12 + CI * w * b_22) / (w ** 2 - a_212 + CI * w * a_222) + b_12) - b_cp2
+        sg = s_d + s_cp1 + s_cp2
+        z1 = z2 = 1.0
+        self.sigma = sg
+        self.reflte = (z1 - z2 + sg * z1 * z2) / (z1 + z2 + sg * z1 * z2)
+        self.trante = 2 * z1 / (z1 + z2 + sg * z1 * z2)
+        self.refltm = (z2 - z1 - z1 * z2 * sg) / (z1 + z2 + z1 * z2 * sg)
+        self.trantm = 2 * z2 / (z1 + z2 + z1 * z2 * sg)
+        hy = (self.hi[1] - self.lo[1]) / self.nel[1]
+        self.up_inner, self.up_outer = self.hi[1] - self.pml[0] * hy, self.hi[1]
+        self.lo_inner, self.lo_outer = self.lo[1] + self.pml[0] * hy, self.lo[1]
+
+    def regions(self, y, n3):
+        yc = np.repeat(np.asarray(y).reshape(-1, n3).mean(axis=1), n3)
+        return yc > 0.0, (yc > self.up_inner) | (yc < self.lo_inner)
+
+    def exact(self, x, y, z, t, n3):
+        up, inpml = self.regions(y, n3)
+        order, referr = self.pml[1], self.pml[2]
+        w, eta, ky = self.omega, 1.0, self.omega
+        d_up = self.up_outer - self.up_inner
+        d_lo = self.lo_inner - self.lo_outer
+        smax_up = -(order + 1) * np.log(referr) / (2 * eta * d_up)
+        smax_lo = -(order + 1) * np.log(referr) / (2 * eta * d_lo)
+        y = np.asarray(y)
+        fac = np.where(up, (smax_up * d_up / (order + 1)) * np.clip((y - self.up_inner) / d_up, 0, None)
+                       ** (order + 1),
+                       (smax_lo * d_lo / (order + 1)) * np.clip((self.lo_inner - y) / d_lo, 0, None)
+                       ** (order + 1))
+        fac = np.where(inpml, fac, 0.0)
+        uu_up = np.exp(1j * (ky * y - w * t) - eta * fac)
+        uu_lo = np.exp(1j * (-ky * y - w * t) - eta * fac)
+        zero = np.zeros_like(y)
+        Hz = np.where(up, (self.reflte * uu_up).real, (self.trante * uu_lo).real)
+        Ex = np.where(up, -(self.reflte * eta * uu_up).real, (self.trante * eta * uu_lo).real)
+        Ez = np.where(up, (self.refltm * uu_up).real, (self.trantm * uu_lo).real)
+        Hx = np.where(up, (self.refltm * uu_up / eta).real, -(self.trantm * uu_lo / eta).real)
+        return np.stack([Hx, zero, Hz]), np.stack([Ex, zero, Ez])
+
+    def face_slots(self, y, cemface, n3, nf, upper_only):
+        up, _ = self.regions(y, n3)
+        y = np.asarray(y)
+        cf = np.asarray(cemface).reshape(-1, nf)
+        out = []
+        for f in range(cf.shape[0]):
+            nodes = cf[f]
+            if (up[nodes[0]] or not upper_only) and np.all(np.abs(y[nodes]) <= 1e-8):
+                out.extend(range(f * nf, (f + 1) * nf))
+        return np.array(out, dtype=np.int64)
+
+    def sheet(self, y, cemface, n3, nf, nxzfl):
+        """graphene slots (both sides of y = 0), params (12, nxzfl) and the
+        initial face currents (6, 3, nxzfl) of userini"""
+        slots = self.face_slots(y, cemface, n3, nf, upper_only=False)
+        params = np.zeros((12, nxzfl))
+        params[:, slots] = np.asarray(self.params)[:, None]
+        w, CI = self.omega, 1j
+        a_d, b_d, b_cp1, a_211, a_221, b_11, b_21, b_cp2, a_212, a_222, b_12, b_22 = self.params
+        enpar = np.array([0.5 * 1.0 * (1.0 - self.reflte), 0.0, 0.5 * (1.0 + self.refltm)])
+        fjn = np.zeros((6, 3, nxzfl))
+        f2 = b_d / (a_d - CI * w)
+        f4 = (a_211 * b_11 + CI * w * b_21) / (w ** 2 - a_211 + CI * w * a_221)
+        f3 = (CI / w) * (f4 + b_11)
+        f6 = (a_212 * b_12 + CI * w * b_22) / (w ** 2 - a_212 + CI * w * a_222)
+        f5 = (CI / w) * (f6 + b_12)
+        for k, fac in ((1, f2), (3, f4), (2, f3), (5, f6), (4, f5)):
+            for m in range(3):
+                fjn[k, m, slots] = (fac * enpar[m]).real
+        return slots, params, fjn
+
+    def incident_slots(self, y, cemface, n3, nf):
+        return self.face_slots(y, cemface, n3, nf, upper_only=True)
+
+    def incident(self):
+        """amp (H then E), k, omega: incfhz += u, incfex += eta u, incfez += u,
+        incfhx -= u/eta, u = cos(-ky y - omega t)"""
+        return (-1.0, 0.0, 1.0, 1.0, 0.0, 1.0), (0.0, -self.omega, 0.0), self.omega
+
+
 def zero_fields(x, y, z):
     return np.zeros((3, x.size)), np.zeros((3, x.size))
 

@@ -322,10 +322,23 @@ __global__ void __launch_bounds__(Cfg<NX, T>::NT, Cfg<NX, T>::kMinBlocks)
         T dH[3], dE[3];
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
-          const T hm = s_uT[c * N3 + v], em = s_uT[(c + 3) * N3 + v];
+          T hm = s_uT[c * N3 + v], em = s_uT[(c + 3) * N3 + v];
+          T hp = pe >= 0 ? s_nb[c * NF + t] : T(0), ep = pe >= 0 ? s_nb[(c + 3) * NF + t] : T(0);
+          if (EXT && !C::kMixed && a.inc_elem) {
+            // userinc: the incident field on the own side of a listed face
+            // node, or on the partner's side when the partner's slot is listed
+            const int io = a.inc_elem[e];
+            if (io >= 0) {
+              const double* iv = a.inc_val + (long)io * 12 * NF + t;
+              hm += (T)iv[c * NF];
+              em += (T)iv[(3 + c) * NF];
+              hp += (T)iv[(6 + c) * NF];
+              ep += (T)iv[(9 + c) * NF];
+            }
+          }
           if (pe >= 0) {
-            dH[c] = s_nb[c * NF + t] - hm;
-            dE[c] = s_nb[(c + 3) * NF + t] - em;
+            dH[c] = hp - hm;
+            dE[c] = ep - em;
           } else {  // PEC mirror: H+ = H-, E+ = -E-
             dH[c] = T(0);
             dE[c] = T(-2) * em;
@@ -548,7 +561,8 @@ int dispatch_nx(Context* c, const FusedDev& a) {
 
 template <typename T>
 int dispatch(Context* c, const FusedDev& a) {
-  return (a.pml.slot || a.disp.slot) ? dispatch_nx<T, true>(c, a) : dispatch_nx<T, false>(c, a);
+  return (a.pml.slot || a.disp.slot || a.inc_elem) ? dispatch_nx<T, true>(c, a)
+                                                  : dispatch_nx<T, false>(c, a);
 }
 
 }  // namespace
@@ -601,6 +615,7 @@ int fused_stage(Context* c, int rkstep, double time, double dt) {
     a.src_ft = source_ft(c->src, time + dt * c->rk_c[rkstep - 1]);
     a.src_ftf = (float)a.src_ft;
   }
+  if (a.inc_elem && (st = incident_upload(c, time + dt * c->rk_c[rkstep - 1]))) return st;
   st = c->form == NEKGPU_MIXED_NAIVE ? dispatch<float>(c, a) : dispatch<double>(c, a);
   if (st) return st;
   c->cur ^= 1;

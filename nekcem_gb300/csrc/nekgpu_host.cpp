@@ -31,6 +31,29 @@ int check_cuda(cudaError_t e) {
   return NEKGPU_ERR_CUDA;
 }
 
+int incident_upload(Context* c, double rktime) {
+  const long n = (long)c->inc_slots.size();
+  if (!n) return NEKGPU_OK;
+  const long NF = 6L * c->nx * c->nx;
+  const bool plain = c->form == NEKGPU_PLAIN;
+  for (long q = 0; q < n; ++q) {
+    const long i = c->inc_nodes[q];
+    const double ph = c->inc_k[0] * c->host_x[i] + c->inc_k[1] * c->host_y[i] +
+                      c->inc_k[2] * c->host_z[i] - c->inc_omega * rktime;
+    const double u = std::cos(ph);
+    if (plain) {
+      for (int m = 0; m < 6; ++m) c->inc_host[6 * q + m] = c->inc_amp[m] * u;
+    } else {
+      for (int m = 0; m < 6; ++m) c->inc_host[c->inc_own_pos[q] + m * NF] = c->inc_amp[m] * u;
+      if (c->inc_partner_pos[q] >= 0)
+        for (int m = 0; m < 6; ++m) c->inc_host[c->inc_partner_pos[q] + m * NF] = c->inc_amp[m] * u;
+    }
+  }
+  return check_cuda(cudaMemcpyAsync(c->d_inc_val, c->inc_host.data(),
+                                    c->inc_host.size() * sizeof(double), cudaMemcpyHostToDevice,
+                                    c->stream));
+}
+
 // rk_storage, RK45 branch (src/cem_common.F:78-104): Carpenter-Kennedy
 // 5-stage 4th-order low-storage coefficients.
 void rk_coeffs(double a[5], double b[5], double c[6]) {
@@ -752,6 +775,7 @@ int upload_common(Context* c, DevAlloc& A, const std::vector<double>& bm1,
 int upload_plain(Context* c, const PlainHost& p) {
   DevAlloc A(c);
   int st;
+  c->host_cemface = p.cemface;
   if ((st = A.get(&c->d_u[0], 6 * c->npts))) return st;
   if ((st = upload_common(c, A, p.bm1, p.ebm1, p.hbm1))) return st;
   PlainDev& a = c->pargs;
@@ -889,6 +913,7 @@ int upload_fused(Context* c, const Compact& cp) {
   if ((st = upload_common(c, A, cp.bm1, cp.ebm1, cp.hbm1))) return st;
   if ((st = A.get(&c->d_coef, 2 * c->npts))) return st;
   if ((st = A.put(&c->d_nbr, cp.nbr))) return st;
+  c->host_nbr = cp.nbr;
   c->host_w3 = cp.w3;
   c->host_rx.resize(c->nelt);
   for (int e = 0; e < c->nelt; ++e) c->host_rx[e] = cp.egeom[9 * (size_t)e];
@@ -1126,7 +1151,9 @@ int plain_stage(Context* c, int rkstep, double time, double dt) {
   const double rktime = time + dt * c->rk_c[rkstep - 1];
   if ((st = plain_cem_maxwell(c))) return st;
   if ((st = plain_restrict_to_face(c))) return st;
-  if ((st = plain_flux3d(c))) return st;
+  if (c->pargs.ninc && ((st = incident_upload(c, rktime)) || (st = plain_incident(c)))) return st;
+  const double rk[3] = {c->rk_a[rkstep - 1], c->rk_b[rkstep - 1], dt};
+  if ((st = plain_flux3d(c, rk))) return st;
   if ((st = plain_add_flux_to_res(c))) return st;
   if ((st = plain_pml_step(c))) return st;
   if ((st = plain_dispersive(c, c->rk_a[rkstep - 1], c->rk_b[rkstep - 1], dt))) return st;
@@ -1480,6 +1507,175 @@ int nekgpu_set_source_kind(nekgpu_ctx* c, int kind) {
   if (!c || kind < 0 || kind > 1) return NEKGPU_ERR_ARG;
   c->src.kind = kind;
   return NEKGPU_OK;
+}
+
+// userinc as a plane wave on listed face slots.  The values depend on the
+// stage time; the host evaluates amp * cos(k.x - omega t) per listed slot
+// each stage (the reference's arithmetic, on the CPU) and uploads them.
+int nekgpu_set_incident(nekgpu_ctx* c, const int* slots, long n, const double amp[6],
+                        const double kvec[3], double omega) {
+  if (!c || n < 0 || (n > 0 && (!slots || !amp || !kvec))) return NEKGPU_ERR_ARG;
+  if (c->ndim == 2 || c->curved || c->form == NEKGPU_MIXED_NAIVE) return NEKGPU_ERR_UNSUPPORTED;
+  const long n3 = (long)c->nx * c->nx * c->nx, NF = 6L * c->nx * c->nx;
+  if (n > 0 && (long)c->host_x.size() != c->npts) return NEKGPU_ERR_STATE;  // needs coordinates
+  std::vector<int> sl(n), nodes(n);
+  std::vector<char> seen(c->nxzfl, 0);
+  for (long q = 0; q < n; ++q) {
+    const long j = (long)slots[q] - 1;
+    if (j < 0 || j >= c->nxzfl || seen[j]) return NEKGPU_ERR_ARG;
+    seen[j] = 1;
+    sl[q] = (int)j;
+    if (c->form == NEKGPU_PLAIN) {
+      nodes[q] = c->host_cemface.empty() ? -1 : c->host_cemface[j];
+      if (nodes[q] < 0) return NEKGPU_ERR_STATE;
+    } else {  // the fused forms hold the reference numbering (checked at init)
+      const long e = j / NF, t = j % NF, f = t / ((long)c->nx * c->nx), ab = t % ((long)c->nx * c->nx);
+      nodes[q] = (int)(e * n3 + face_vol((int)f, (int)(ab % c->nx), (int)(ab / c->nx), c->nx));
+    }
+  }
+  DevAlloc A(c);
+  int st;
+  c->inc_slots = sl;
+  c->inc_nodes = nodes;
+  for (int m = 0; m < 6; ++m) c->inc_amp[m] = n ? amp[m] : 0.0;
+  for (int m = 0; m < 3; ++m) c->inc_k[m] = n ? kvec[m] : 0.0;
+  c->inc_omega = omega;
+  c->pargs.ninc = 0;
+  c->fargs.inc_elem = c->margs.inc_elem = nullptr;
+  if (n == 0) return NEKGPU_OK;
+  if (c->form == NEKGPU_PLAIN) {
+    int* d;
+    if ((st = A.put(&d, sl)) || (st = A.get(&c->d_inc_val, 6 * n))) return st;
+    c->pargs.inc_slot = d;
+    c->pargs.inc_val = c->d_inc_val;
+    c->pargs.ninc = (int)n;
+    c->inc_host.assign(6 * n, 0.0);
+    return NEKGPU_OK;
+  }
+  // each listed slot adds to its own side and, across the face, to the value
+  // its partner element sees of this side (the gs sum carries the modified
+  // face value to both slots)
+  std::vector<int> rows(c->nelt, -1);
+  c->inc_elem_rows.clear();
+  auto row_of = [&](int e) {
+    if (rows[e] < 0) {
+      rows[e] = (int)c->inc_elem_rows.size();
+      c->inc_elem_rows.push_back(e);
+    }
+    return rows[e];
+  };
+  const long N2 = (long)c->nx * c->nx;
+  c->inc_own_pos.assign(n, -1);
+  c->inc_partner_pos.assign(n, -1);
+  for (long q = 0; q < n; ++q) {
+    const long j = sl[q], e = j / NF, t = j % NF, f = t / N2, ab = t % N2;
+    c->inc_own_pos[q] = (long)row_of((int)e) * 12 * NF + t;
+    const int pe = c->host_nbr[6 * e + f];
+    if (pe >= 0) {
+      const long fo = f < 4 ? (f + 2) & 3 : 9 - f;  // the opposite slot of the partner
+      c->inc_partner_pos[q] = (long)row_of(pe) * 12 * NF + 6 * NF + fo * N2 + ab;
+    }
+  }
+  const size_t nv = 12 * (size_t)NF * c->inc_elem_rows.size();
+  if ((st = A.put(&c->d_inc_elem, rows)) || (st = A.get(&c->d_inc_val, nv))) return st;
+  c->inc_host.assign(nv, 0.0);
+  c->fargs.inc_elem = c->margs.inc_elem = c->d_inc_elem;
+  c->fargs.inc_val = c->margs.inc_val = c->d_inc_val;
+  return NEKGPU_OK;
+}
+
+// Graphene sheets (plain form): the reference's graphparams(nxzfl,12),
+// graphindex (1-based) and yconduc(nxzfl); the face currents start at zero.
+int nekgpu_set_graphene(nekgpu_ctx* c, const double* params, const int* slots, long n,
+                        const double* yconduc) {
+  if (!c || n < 0 || (n > 0 && (!params || !slots || !yconduc))) return NEKGPU_ERR_ARG;
+  if (c->form != NEKGPU_PLAIN || c->ndim == 2) return NEKGPU_ERR_UNSUPPORTED;
+  const long L = c->nxzfl;
+  std::vector<int> sl(n);
+  std::vector<char> seen(L, 0);
+  std::vector<double> par(12 * (size_t)n), yc(n);
+  for (long q = 0; q < n; ++q) {
+    const long j = (long)slots[q] - 1;
+    if (j < 0 || j >= L || seen[j]) return NEKGPU_ERR_ARG;
+    seen[j] = 1;
+    sl[q] = (int)j;
+    for (int p = 0; p < 12; ++p) par[p * n + q] = params[p * L + j];
+    yc[q] = yconduc[j];
+  }
+  c->pargs.ngraph = 0;
+  c->gr_slots = sl;
+  if (n == 0) return NEKGPU_OK;
+  DevAlloc A(c);
+  int* d_sl;
+  double *d_par, *d_yc, *d_f, *d_k;
+  int st;
+  if ((st = A.put(&d_sl, sl)) || (st = A.put(&d_par, par)) || (st = A.put(&d_yc, yc)) ||
+      (st = A.get(&d_f, 18 * n)) || (st = A.get(&d_k, 18 * n)))
+    return st;
+  if (check_cuda(cudaMemset(d_f, 0, 18 * n * sizeof(double))) ||
+      check_cuda(cudaMemset(d_k, 0, 18 * n * sizeof(double))))
+    return NEKGPU_ERR_CUDA;
+  PlainDev& a = c->pargs;
+  a.gr_slot = d_sl; a.gr_par = d_par; a.gr_yc = d_yc; a.gr_f = d_f; a.gr_k = d_k;
+  a.ngraph = (int)n;
+  return NEKGPU_OK;
+}
+
+// The graphene face currents in the reference layout fjn(ld,3,6) (only the
+// listed slots are read / written; other slots read 0)
+static int graphene_copy(nekgpu_ctx* c, double* fjn, long ld, bool to_device) {
+  if (!c || !fjn || ld < c->nxzfl) return NEKGPU_ERR_ARG;
+  const long ng = c->pargs.ngraph;
+  std::vector<double> h(18 * (size_t)ng);
+  if (ng && (check_cuda(cudaStreamSynchronize(c->stream)) ||
+             check_cuda(cudaMemcpy(h.data(), c->pargs.gr_f, h.size() * sizeof(double),
+                                   cudaMemcpyDeviceToHost))))
+    return NEKGPU_ERR_CUDA;
+  if (!to_device) std::fill(fjn, fjn + 18 * ld, 0.0);
+  for (long q = 0; q < ng; ++q)
+    for (int r = 0; r < 18; ++r) {  // r = 3k + m: fjn(j, m, k)
+      if (to_device)
+        h[r * ng + q] = fjn[r * ld + c->gr_slots[q]];
+      else
+        fjn[r * ld + c->gr_slots[q]] = h[r * ng + q];
+    }
+  if (to_device && ng &&
+      check_cuda(cudaMemcpy(c->pargs.gr_f, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice)))
+    return NEKGPU_ERR_CUDA;
+  return NEKGPU_OK;
+}
+
+int nekgpu_set_graphene_current(nekgpu_ctx* c, const double* fjn, long ld) {
+  return graphene_copy(c, const_cast<double*>(fjn), ld, true);
+}
+
+int nekgpu_get_graphene_current(nekgpu_ctx* c, double* fjn, long ld) {
+  return graphene_copy(c, fjn, ld, false);
+}
+
+// PML auxiliary fields set from the reference layout (3*npts; the case's
+// userini sets pmlbn = mu H, pmldn = eps E); nodes outside the PML ignored
+int nekgpu_set_array(nekgpu_ctx* c, const char* name, const double* in) {
+  if (!c || !name || !in) return NEKGPU_ERR_ARG;
+  const std::string nm(name);
+  const bool bn = nm == "pmlbn", dn = nm == "pmldn";
+  if (!bn && !dn) return NEKGPU_ERR_ARG;
+  if (!c->npml) return NEKGPU_ERR_STATE;
+  const long P = c->npts, n3 = (long)c->nx * c->nx * c->nx;
+  if (check_cuda(cudaStreamSynchronize(c->stream))) return NEKGPU_ERR_CUDA;
+  if (c->form == NEKGPU_PLAIN)
+    return check_cuda(cudaMemcpy(c->d_pml_aux + (dn ? 3 * P : 0), in, 3 * P * sizeof(double),
+                                 cudaMemcpyHostToDevice));
+  const long nn = (long)c->npml * n3;
+  std::vector<double> h(6 * (size_t)nn);
+  if (check_cuda(cudaMemcpy(h.data(), c->d_pml_aux, h.size() * sizeof(double), cudaMemcpyDeviceToHost)))
+    return NEKGPU_ERR_CUDA;
+  for (long l = 0; l < c->npml; ++l)
+    for (long v = 0; v < n3; ++v) {
+      const long q = l * n3 + v, g = (long)c->pml_elems[l] * n3 + v;
+      for (int cc = 0; cc < 3; ++cc) h[((dn ? 3 : 0) + cc) * nn + q] = in[cc * P + g];
+    }
+  return check_cuda(cudaMemcpy(c->d_pml_aux, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice));
 }
 
 // Dealiased curl of the plain form: the driver's tables as the reference

@@ -121,6 +121,17 @@ struct PlainDev {
   // points, weights w3md (md^3), metrics on the md^3 points (9 x md^3 x nelt)
   int md;
   const double *jgl, *jgt, *dxmd, *dxtmd, *w3md, *metd;
+  // userinc: the stage's incident values (6 per listed slot) and the slots
+  int ninc;
+  const int* inc_slot;
+  const double* inc_val;
+  // graphene sheets on listed face slots, compact per listed slot q:
+  // gr_par[p*ng + q] (12 parameters), gr_yc[q] (yconduc), gr_f / gr_k
+  // [(3k + m)*ng + q] the face currents fjn(.,m,k) and their RK registers
+  int ngraph;
+  const int* gr_slot;
+  const double *gr_par, *gr_yc;
+  double *gr_f, *gr_k;
 };
 
 // PML data of the fused forms, compact over the PML elements (slot l holds
@@ -142,6 +153,9 @@ struct FusedDev {
   long npts;
   PmlDev pml;
   DispDev disp;
+  const int* inc_elem;    // nelt: row of the element in inc_val, -1 without incident faces
+  const double* inc_val;  // [row][12][6*nx^2]: the stage's incident face values, H and E
+                          // on the own side (0..5) and on the partner's side (6..11)
   const double* u_in;
   double* u_out;
   double* k;            // RK register read
@@ -186,6 +200,8 @@ struct MixedDev {
   int* status;
   PmlDev pml;
   DispDev disp;
+  const int* inc_elem;    // as in FusedDev
+  const double* inc_val;
   double dt;
 };
 
@@ -310,6 +326,20 @@ struct Context {
   double *d_disp_data = nullptr, *d_disp_aux = nullptr, *d_disp_k = nullptr;
   int *d_disp_slot = nullptr, *d_disp_elem = nullptr;
   long disp_n = 0;
+  // userinc plane wave amp * cos(k.x - omega t) on listed face slots: the
+  // slots and their nodes on the host, the values recomputed every stage
+  std::vector<int> inc_slots, inc_nodes;
+  std::vector<int> host_cemface;  // plain form: 0-based volume node of each face slot
+  double inc_amp[6] = {0, 0, 0, 0, 0, 0}, inc_k[3] = {0, 0, 0}, inc_omega = 0;
+  std::vector<int> inc_elem_rows;  // fused forms: the elements with incident faces
+  std::vector<long> inc_own_pos, inc_partner_pos;  // fused forms: table positions per slot
+  std::vector<int> host_nbr;       // fused forms: 6*nelt partner elements, -1 PEC mirror
+  std::vector<double> inc_host;    // staging of the values
+  int* d_inc_slot = nullptr;
+  int* d_inc_elem = nullptr;
+  double* d_inc_val = nullptr;
+  // graphene sheets (plain form): listed slots on the host
+  std::vector<int> gr_slots;
   // adjoint face-slot coefficients (built on first use, FP64 fused form)
   double* d_adj_slot = nullptr;
   std::vector<double> adj_jw;  // objective weights set by nekgpu_adjoint_init
@@ -334,7 +364,8 @@ void rk_coeffs(double a[5], double b[5], double c[6]);
 // kernel launchers (nekgpu_plain.cu)
 int plain_cem_maxwell(Context* c);
 int plain_restrict_to_face(Context* c);
-int plain_flux3d(Context* c);
+// rk = {ca, cb, dt} of the stage: the graphene currents run inside the flux
+int plain_flux3d(Context* c, const double* rk = nullptr);
 int plain_add_flux_to_res(Context* c);
 int plain_usersrc(Context* c, double ft);
 int plain_invqmass(Context* c);
@@ -345,6 +376,10 @@ int plain_pml_rk_update(Context* c, double ca, double cb, double dt);
 size_t dcurl_smem(int mx, int md);
 // cem_maxwell_drude / cem_maxwell_lorentz with the currents' rk4_upd
 int plain_dispersive(Context* c, double ca, double cb, double dt);
+// userinc: adds the stage's incident values to the restricted face fields
+int plain_incident(Context* c);
+// computes the incident values of the stage time and uploads them (all forms)
+int incident_upload(Context* c, double rktime);
 int plain_gs(Context* c, double* d_u, int nfld);
 
 // kernel launchers (nekgpu_fused.cu)

@@ -539,6 +539,21 @@ __global__ void __launch_bounds__(MCfg<NX>::NT, 3) k_mixed_stage(const MixedDev 
             dH[c] = 0.0f;
             dE[c] = -2.0f * (ev.x + ev.y);
           }
+          if (EXT && a.inc_elem) {
+            // userinc: the incident field on the own side of a listed face
+            // node, or on the partner's side when the partner's slot is listed
+            const int io = a.inc_elem[e];
+            if (io >= 0) {
+              const double* iv = a.inc_val + (long)io * 12 * NF + t;
+              const float ih = d2f_hi(iv[c * NF]), ie = d2f_hi(iv[(3 + c) * NF]);
+              if (pe >= 0) {
+                dH[c] += d2f_hi(iv[(6 + c) * NF]) - ih;
+                dE[c] += d2f_hi(iv[(9 + c) * NF]) - ie;
+              } else {
+                dE[c] -= 2.0f * ie;
+              }
+            }
+          }
         }
         float Y02 = -0.5f, C02Y = 0.5f * a.C0f, Z02 = 0.5f, C02Z = 0.5f * a.C0f;
         if (a.fcoef) {
@@ -726,7 +741,8 @@ int mixed_stage(Context* c, int rkstep, double time, double dt) {
   a.b = c->rk_b[rkstep - 1];
   a.dt = dt;
   if (c->src.enabled) a.src_ftf = (float)source_ft(c->src, time + dt * c->rk_c[rkstep - 1]);
-  const bool ext = a.pml.slot || a.disp.slot;
+  const bool ext = a.pml.slot || a.disp.slot || a.inc_elem;
+  if (a.inc_elem && (st = incident_upload(c, time + dt * c->rk_c[rkstep - 1]))) return st;
   switch (c->nx) {
     case 3: st = ext ? launch_mixed<3, true>(c, a) : launch_mixed<3, false>(c, a); break;
     case 4: st = ext ? launch_mixed<4, true>(c, a) : launch_mixed<4, false>(c, a); break;

@@ -407,9 +407,74 @@ __global__ void k_dispersive(PlainDev a, int n3, double ca, double cb, double dt
   }
 }
 
+// userinc (src/cem_maxwell.F:495-496): the listed slots' face values get the
+// stage's incident field, H into fhn and E into fen
+__global__ void k_incident(PlainDev a) {
+  const long q = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (q >= a.ninc) return;
+  const long j = a.inc_slot[q], L = a.nxzfl;
+  for (int m = 0; m < 6; ++m) a.fface[m * L + j] = a.fface[m * L + j] + a.inc_val[6 * q + m];
+}
+
+// cem_3d_graphene_current (src/cem_maxwell.F:2827-2931) at one listed face
+// slot: the surface current from the face fields, the residuals of its Drude
+// and critical-point currents and their rk4_upd, then userfsrc's -J on the
+// -n x H part of srflx (tests/3dgraphene/3dgraphene.usr:236-264)
+__global__ void k_graphene(PlainDev a, double ca, double cb, double dt) {
+  const long q = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  const long ng = a.ngraph;
+  if (q >= ng) return;
+  const long j = a.gr_slot[q], L = a.nxzfl;
+  double p[12];
+  for (int i = 0; i < 12; ++i) p[i] = a.gr_par[i * ng + q];
+  const double a_d = p[0], b_d = p[1], b_cp1 = p[2], a_211 = p[3], a_221 = p[4], b_11 = p[5];
+  const double b_21 = p[6], b_cp2 = p[7], a_212 = p[8], a_222 = p[9], b_12 = p[10], b_22 = p[11];
+  const double ux = a.unx[j], uy = a.uny[j], uz = a.unz[j];
+  const double* fh = a.fface;
+  const double* fe = a.fface + 3 * L;
+  double nH[3], nEn[3];
+  nH[0] = -uy * fh[2 * L + j] + uz * fh[L + j];
+  nH[1] = ux * fh[2 * L + j] - uz * fh[j];
+  nH[2] = -ux * fh[L + j] + uy * fh[j];
+  const double ndotE = ux * fe[j] + uy * fe[L + j] + uz * fe[2 * L + j];
+  nEn[0] = fe[j] - ux * ndotE;
+  nEn[1] = fe[L + j] - uy * ndotE;
+  nEn[2] = fe[2 * L + j] - uz * ndotE;
+  const double Yfac = 0.5 / a.Y0[j];
+  const double cpfac = b_cp1 + b_cp2;
+  const double jnfac = 1.0 - cpfac * Yfac;
+  for (int m = 0; m < 3; ++m) {
+    double F[6], R[6];
+    for (int k = 1; k < 6; ++k) F[k] = a.gr_f[(3 * k + m) * ng + q];
+    const double tmp = Yfac * (nH[m] + a.gr_yc[q] * nEn[m]);
+    F[0] = (F[1] + F[2] + F[4] - cpfac * tmp) / jnfac;
+    const double f = tmp - Yfac * F[0];
+    R[1] = -a_d * F[1] + b_d * f;
+    R[2] = F[3] + b_11 * f;
+    R[3] = -a_211 * F[2] - a_221 * F[3] + b_21 * f;
+    R[4] = F[5] + b_12 * f;
+    R[5] = -a_212 * F[4] - a_222 * F[5] + b_22 * f;
+    a.gr_f[m * ng + q] = F[0];
+    for (int k = 1; k < 6; ++k) {
+      const long o = (3 * k + m) * ng + q;
+      const double kh = ca * a.gr_k[o] + dt * R[k];
+      a.gr_k[o] = kh;
+      a.gr_f[o] = F[k] + cb * kh;
+    }
+    a.srflx[(3 + m) * L + j] = a.srflx[(3 + m) * L + j] - F[0];
+  }
+}
+
 int last_error() { return check_cuda(cudaGetLastError()); }
 
 }  // namespace
+
+int plain_incident(Context* c) {
+  if (!c->pargs.ninc) return NEKGPU_OK;
+  k_incident<<<blocks_for(c->pargs.ninc), kThreads, 0, c->stream>>>(c->pargs);
+  c->last_launches += 1;
+  return last_error();
+}
 
 int plain_dispersive(Context* c, double ca, double cb, double dt) {
   if (!c->pargs.disp.n) return NEKGPU_OK;
@@ -462,8 +527,12 @@ int plain_gs(Context* c, double* d_u, int nfld) {
   return last_error();
 }
 
-int plain_flux3d(Context* c) {
+int plain_flux3d(Context* c, const double* rk) {
   k_flux_pre<<<blocks_for(c->nxzfl), kThreads, 0, c->stream>>>(c->pargs);
+  if (rk && c->pargs.ngraph) {
+    c->last_launches += 1;
+    k_graphene<<<blocks_for(c->pargs.ngraph), kThreads, 0, c->stream>>>(c->pargs, rk[0], rk[1], rk[2]);
+  }
   int st = plain_gs(c, c->pargs.srflx, 6);
   if (st) return st;
   c->last_launches += 1;

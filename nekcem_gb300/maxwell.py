@@ -165,6 +165,44 @@ class MaxwellGPU:
         L.check(L.load().nekgpu_set_source(self._h, 1 if enabled else 0, x, sigma, amp, f0, t0),
                 "nekgpu_set_source")
 
+    # ---- incident field (userinc) and PML auxiliary fields ---------------------
+    def set_incident(self, slots, amp, k, omega):
+        """userinc plane wave amp * cos(k.x - omega t) on the 0-based face
+        slots (amp: H then E)."""
+        sl = np.ascontiguousarray(np.asarray(slots) + 1, dtype=np.int32)
+        a = (C.c_double * 6)(*amp)
+        kk = (C.c_double * 3)(*k)
+        self._keep.append(sl)
+        L.check(L.load().nekgpu_set_incident(self._h, sl.ctypes.data_as(L.ip), int(sl.size), a, kk,
+                                             float(omega)), "nekgpu_set_incident")
+
+    def set_array(self, name: str, values: np.ndarray):
+        """"pmlbn" / "pmldn" (3, npts)"""
+        v = np.ascontiguousarray(values, dtype=np.float64).reshape(-1)
+        L.check(L.load().nekgpu_set_array(self._h, name.encode(), _dp(v)), "nekgpu_set_array")
+
+    # ---- graphene sheets (plain form) -----------------------------------------
+    def set_graphene(self, params, slots, yconduc):
+        """sheets on the 0-based face slots: params (12, nxzfl), yconduc (nxzfl)"""
+        p = np.ascontiguousarray(params, dtype=np.float64).reshape(-1)
+        yc = np.ascontiguousarray(yconduc, dtype=np.float64).reshape(-1)
+        sl = np.ascontiguousarray(np.asarray(slots) + 1, dtype=np.int32)
+        self._keep.extend([p, yc, sl])
+        L.check(L.load().nekgpu_set_graphene(self._h, _dp(p), sl.ctypes.data_as(L.ip), int(sl.size),
+                                             _dp(yc)), "nekgpu_set_graphene")
+
+    def set_graphene_current(self, fjn):
+        """(6, 3, nxzfl) face currents"""
+        f = np.ascontiguousarray(fjn, dtype=np.float64).reshape(-1)
+        L.check(L.load().nekgpu_set_graphene_current(self._h, _dp(f), self.nxzfl),
+                "nekgpu_set_graphene_current")
+
+    def get_graphene_current(self) -> np.ndarray:
+        f = np.empty(18 * self.nxzfl)
+        L.check(L.load().nekgpu_get_graphene_current(self._h, _dp(f), self.nxzfl),
+                "nekgpu_get_graphene_current")
+        return f.reshape(6, 3, self.nxzfl)
+
     # ---- dealiased curl (plain form) ------------------------------------------
     def set_dealias(self, lxd: int, jgl=None, dxmd=None, w3md=None, metd=None):
         """maxwell_wght_dcurl on lxd points per direction with the reference's

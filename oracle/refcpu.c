@@ -62,6 +62,16 @@ struct ref_ctx {
    * the md points, weights w3md and the metrics interpolated to md^3 nodes */
   int md;
   double *jgl, *jgt, *dxmd, *dxtmd, *w3md, *metd;
+  /* graphene sheets (the /usergraph/ block of tests/3dgraphene): 12
+   * parameters per face slot (nxzfl,12), the listed slots, the face currents
+   * fjn(nxzfl,3,6) with registers and residuals */
+  long ngraph;
+  int* graphindex;
+  double *graphparams, *fjn, *kfjn, *resfjn;
+  /* userinc plane wave: amp (H then E) * cos(k.x - omega t) on listed slots */
+  long ninc;
+  int* incslot;
+  double incamp[6], inck[3], incomega;
   int rkstep_now; /* stage of the op in progress (0 outside ref_rk_stage) */
   double dt_now;
   double volvm1;
@@ -623,6 +633,8 @@ void ref_destroy(ref_ctx* c) {
   for (size_t i = 0; i < sizeof(q) / sizeof(q[0]); ++i) free(q[i]);
   free(c->drudeindex); free(c->lorentzindex);
   free(c->jgl); free(c->jgt); free(c->dxmd); free(c->dxtmd); free(c->w3md); free(c->metd);
+  free(c->incslot);
+  free(c->graphindex); free(c->graphparams); free(c->fjn); free(c->kfjn); free(c->resfjn);
   free(c->gs_order); free(c->gs_start);
   free(c);
 }
@@ -650,6 +662,8 @@ double* ref_darray(ref_ctx* c, const char* name, long* len) {
       {"pmlbn", c->pmlbn, c->pmlbn ? 3 * c->npts : 0},
       {"pmldn", c->pmldn, c->pmldn ? 3 * c->npts : 0},
       {"pmlinner", c->pmlinner, c->ifpml ? 6 : 0}, {"pmlouter", c->pmlouter, c->ifpml ? 6 : 0},
+      {"fjn", c->fjn, c->fjn ? 18 * c->nxzfl : 0},
+      {"yconduc", c->yconduc, c->nxzfl},
       {"jgl", c->jgl, c->md ? (long)c->md * c->n : 0},
       {"dxmd", c->dxmd, c->md ? (long)c->md * c->md : 0},
       {"w3md", c->w3md, c->md ? (long)c->md * c->md * c->md : 0},
@@ -906,10 +920,12 @@ void ref_flux_upwind(ref_ctx* c) {
   }
 }
 
-/* cem_maxwell_flux3d (src/cem_maxwell.F:922-1002); userfsrc is a no-op */
+/* cem_maxwell_flux3d (src/cem_maxwell.F:922-1002); userfsrc carries the
+ * graphene currents when sheets are set (a no-op otherwise) */
 void ref_flux3d(ref_ctx* c) {
   if (c->ndim == 2) { flux2d(c); return; }
   ref_flux_pre(c);
+  if (c->ngraph && c->rkstep_now > 0) ref_graphene(c, c->rkstep_now, c->dt_now);
   ref_gs_op_fields(c, c->srflx, c->nxzfl, 6);
   if (c->ncempec > 0) ref_flux_pec(c);
   ref_flux_upwind(c);
@@ -1209,10 +1225,41 @@ void ref_pml_step(ref_ctx* c) {
   }
 }
 
-/* cem_maxwell_op (src/cem_maxwell.F:484-508); userinc/userfsrc no-ops */
+/* userinc (called by cem_maxwell_op between the restriction and the flux,
+ * src/cem_maxwell.F:495-496) in the plane-wave form the reference's cases
+ * use (tests/drude/drude.usr:7-42, tests/3dgraphene/3dgraphene.usr:7-50):
+ * the face values of the listed slots get amp * cos(k.x - omega t). */
+void ref_set_incident(ref_ctx* c, const int* slots, long n, const double amp[6],
+                      const double k[3], double omega) {
+  free(c->incslot);
+  c->incslot = ialloc(n);
+  memcpy(c->incslot, slots, (size_t)n * sizeof(int));
+  c->ninc = n;
+  for (int m = 0; m < 6; ++m) c->incamp[m] = amp[m];
+  for (int m = 0; m < 3; ++m) c->inck[m] = k[m];
+  c->incomega = omega;
+}
+
+void ref_userinc(ref_ctx* c, double rktime) {
+  long nf = c->nxzfl;
+  for (long q = 0; q < c->ninc; ++q) {
+    long j = c->incslot[q];
+    long i = c->cemface[j];
+    double ph = c->inck[0] * c->xm1[i] + c->inck[1] * c->ym1[i] + c->inck[2] * c->zm1[i] -
+                c->incomega * rktime;
+    double u = cos(ph);
+    for (int m = 0; m < 3; ++m) {
+      c->fhn[j + m * nf] = c->fhn[j + m * nf] + c->incamp[m] * u;
+      c->fen[j + m * nf] = c->fen[j + m * nf] + c->incamp[3 + m] * u;
+    }
+  }
+}
+
+/* cem_maxwell_op (src/cem_maxwell.F:484-508); userfsrc is a no-op */
 void ref_maxwell_op(ref_ctx* c, double rktime) {
   ref_cem_maxwell(c);
   ref_restrict_to_face(c);
+  if (c->ninc) ref_userinc(c, rktime);
   ref_flux3d(c);
   ref_add_flux_to_res(c);
   if (c->ifpml) ref_pml_step(c);
@@ -1827,5 +1874,73 @@ void ref_wght_dcurl(ref_ctx* c, double* w1, double* w2, double* w3, const double
     for (int q = 0; q < 3; ++q) { free(ju[q]); free(wdd[q]); }
     for (int q = 0; q < 9; ++q) free(g[q]);
   }
+}
+
+/* ------------------------------------------------------------------------ */
+/* Graphene sheets (cem_3d_graphene_current, src/cem_maxwell.F:2827-2931,   */
+/* called through userfsrc, tests/3dgraphene/3dgraphene.usr:236-264)        */
+/* ------------------------------------------------------------------------ */
+
+void ref_set_graphene(ref_ctx* c, const double* params, const int* slots, long n) {
+  long nf = c->nxzfl;
+  free(c->graphindex); free(c->graphparams); free(c->fjn); free(c->kfjn); free(c->resfjn);
+  c->graphindex = ialloc(n);
+  memcpy(c->graphindex, slots, (size_t)n * sizeof(int));
+  c->graphparams = dalloc(12 * nf);
+  memcpy(c->graphparams, params, 12 * nf * sizeof(double));
+  c->fjn = dalloc(18 * nf); c->kfjn = dalloc(18 * nf); c->resfjn = dalloc(18 * nf);
+  c->ngraph = n;
+}
+
+/* the surface current of the listed face nodes from the face fields, the
+ * residuals of its auxiliary (Drude and two critical-point) currents, their
+ * rk4_upd, and userfsrc's -J on the -n x H part of srflx (before the gs sum) */
+void ref_graphene(ref_ctx* c, int rkstep, double dt) {
+  long nf = c->nxzfl;
+#define FJ(arr, j, comp, k) arr[(j) + nf * ((comp) + 3 * (k))]
+  const double *fh = c->fhn, *fe = c->fen;
+  for (long q = 0; q < c->ngraph; ++q) {
+    long j = c->graphindex[q];
+    const double* p = c->graphparams;
+    double a_d = p[j], b_d = p[nf + j], b_cp1 = p[2 * nf + j], a_211 = p[3 * nf + j];
+    double a_221 = p[4 * nf + j], b_11 = p[5 * nf + j], b_21 = p[6 * nf + j];
+    double b_cp2 = p[7 * nf + j], a_212 = p[8 * nf + j], a_222 = p[9 * nf + j];
+    double b_12 = p[10 * nf + j], b_22 = p[11 * nf + j];
+    double ux = c->unx[j], uy = c->uny[j], uz = c->unz[j];
+    double nH[3], nEn[3];
+    nH[0] = -uy * fh[2 * nf + j] + uz * fh[nf + j];
+    nH[1] = ux * fh[2 * nf + j] - uz * fh[j];
+    nH[2] = -ux * fh[nf + j] + uy * fh[j];
+    double ndotE = ux * fe[j] + uy * fe[nf + j] + uz * fe[2 * nf + j];
+    nEn[0] = fe[j] - ux * ndotE;
+    nEn[1] = fe[nf + j] - uy * ndotE;
+    nEn[2] = fe[2 * nf + j] - uz * ndotE;
+    double Yfac = 0.5 / c->Y_0[j];
+    double cpfac = b_cp1 + b_cp2;
+    double jnfac = 1.0 - cpfac * Yfac;
+    for (int m = 0; m < 3; ++m) {
+      double tmp = Yfac * (nH[m] + c->yconduc[j] * nEn[m]);
+      FJ(c->fjn, j, m, 0) = (FJ(c->fjn, j, m, 1) + FJ(c->fjn, j, m, 2) + FJ(c->fjn, j, m, 4) -
+                             cpfac * tmp) / jnfac;
+      double f = tmp - Yfac * FJ(c->fjn, j, m, 0);
+      FJ(c->resfjn, j, m, 1) = -a_d * FJ(c->fjn, j, m, 1) + b_d * f;
+      FJ(c->resfjn, j, m, 2) = FJ(c->fjn, j, m, 3) + b_11 * f;
+      FJ(c->resfjn, j, m, 3) = -a_211 * FJ(c->fjn, j, m, 2) - a_221 * FJ(c->fjn, j, m, 3) + b_21 * f;
+      FJ(c->resfjn, j, m, 4) = FJ(c->fjn, j, m, 5) + b_12 * f;
+      FJ(c->resfjn, j, m, 5) = -a_212 * FJ(c->fjn, j, m, 4) - a_222 * FJ(c->fjn, j, m, 5) + b_22 * f;
+    }
+  }
+  double ra[5], rb[5], rc[6];
+  ref_rk_coeffs(ra, rb, rc);
+  for (int k = 1; k < 6; ++k)
+    for (int m = 0; m < 3; ++m)
+      ref_rk4_upd(&FJ(c->fjn, 0, m, k), &FJ(c->kfjn, 0, m, k), &FJ(c->resfjn, 0, m, k),
+                  rb[rkstep - 1], ra[rkstep - 1], dt, nf);
+  double* s = c->srflx;
+  for (long q = 0; q < c->ngraph; ++q) {
+    long j = c->graphindex[q];
+    for (int m = 0; m < 3; ++m) s[(3 + m) * nf + j] = s[(3 + m) * nf + j] - FJ(c->fjn, j, m, 0);
+  }
+#undef FJ
 }
 

@@ -98,6 +98,21 @@ void ref_set_drude(ref_ctx* c, const double* params, const int* index, long n);
 void ref_set_lorentz(ref_ctx* c, const double* params, const int* index, long n);
 void ref_dispersive(ref_ctx* c, int rkstep, double dt);
 
+/* userinc as a plane wave on listed face slots (0-based): the face values
+ * get amp[0..2] (H) and amp[3..5] (E) times cos(k.x - omega t) between the
+ * restriction and the flux; n = 0 switches it off. */
+void ref_set_incident(ref_ctx* c, const int* slots, long n, const double amp[6],
+                      const double k[3], double omega);
+void ref_userinc(ref_ctx* c, double rktime);
+
+/* Graphene sheets (cem_3d_graphene_current, src/cem_maxwell.F:2827-2931,
+ * through userfsrc as tests/3dgraphene does): params (nxzfl,12) per face
+ * slot, n listed 0-based slots; inside ref_rk_stage the face currents are
+ * computed after the flux's first loop and subtracted from -n x H before the
+ * gs sum.  The currents are the darray "fjn" (nxzfl,3,6), zero after this. */
+void ref_set_graphene(ref_ctx* c, const double* params, const int* slots, long n);
+void ref_graphene(ref_ctx* c, int rkstep, double dt);
+
 /* Dealiased curl (param(18) = -1: maxwell_wght_dcurl, src/cem_maxwell.F:
  * 1541-1729) on md = lxd >= nx1 GLL points per direction; md = 0 returns to
  * maxwell_wght_curl.  Returns -1 for a bad md or a 2-D mesh.  The tables

@@ -61,6 +61,8 @@ def lib():
         L.ref_set_source_kind.argtypes = [vp, ip]
         L.ref_set_pml.argtypes = [vp, ip, C.c_double, C.c_double]
         L.ref_pml_step.argtypes = [vp]
+        L.ref_set_incident.argtypes = [vp, C.POINTER(C.c_int), C.c_long, dp, dp, C.c_double]
+        L.ref_set_graphene.argtypes = [vp, dp, C.POINTER(C.c_int), C.c_long]
         L.ref_set_dealias.restype = ip
         L.ref_set_dealias.argtypes = [vp, ip]
         L.ref_create_box2d.restype = vp
@@ -217,6 +219,29 @@ class RefBox:
     def lorentz_jn(self):
         """(6, npts) view of the Lorentz currents: J1 (3 rows) then J2"""
         return self.d("lorentzjn").reshape(6, self.npts)
+
+    def set_incident(self, slots, amp, k, omega):
+        """userinc plane wave amp * cos(k.x - omega t) on the 0-based face
+        slots (amp: H then E, 6 values)."""
+        slots = np.ascontiguousarray(slots, dtype=np.int32)
+        a = (C.c_double * 6)(*amp)
+        kk = (C.c_double * 3)(*k)
+        lib().ref_set_incident(self._c, slots.ctypes.data_as(C.POINTER(C.c_int)), int(slots.size),
+                               a, kk, float(omega))
+
+    def set_graphene(self, params, slots):
+        """graphene sheets on the 0-based face slots: params (12, nxzfl) in the
+        reference's graphparams column order"""
+        params = np.ascontiguousarray(params, dtype=np.float64).reshape(-1)
+        assert params.size == 12 * self.nxzfl
+        slots = np.ascontiguousarray(slots, dtype=np.int32)
+        lib().ref_set_graphene(self._c, _dp(params), slots.ctypes.data_as(C.POINTER(C.c_int)),
+                               int(slots.size))
+
+    @property
+    def fjn(self):
+        """(6, 3, nxzfl) view of the face currents fjn(nxzfl,3,6)"""
+        return self.d("fjn").reshape(6, 3, self.nxzfl)
 
     def set_dealias(self, md: int):
         """Dealiased curl on md GLL points per direction (param(18) = -1 with

@@ -1,0 +1,109 @@
+"""Graphene sheets (cem_3d_graphene_current, src/cem_maxwell.F:2827-2931,
+through userfsrc as tests/3dgraphene/3dgraphene.usr does) with the incident
+field (userinc) and the PML: the reference's tests/3dgraphene case
+(cases.GrapheneSheet: two normally incident plane waves on a sheet with a
+Drude term and two critical points).
+
+CPU: the oracle passes the case's own userchk tolerances after 1000 steps
+(L2 <= 5e-4, Linf <= 5e-3 on H_x, H_z, E_x, E_z; L2 <= 1e-14, Linf <= 5e-12
+on H_y, E_y).  GPU: the plain form matches the oracle bit for bit (fields
+and face currents) and passes the same tolerances; the fused forms refuse
+graphene.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from helpers import gpu_from_box, gpu_from_ref, make_ref
+from nekcem_gb300 import cases
+from nekcem_gb300 import _lib as L
+
+CS = cases.GrapheneSheet()
+
+
+def setup(ref, g, N):
+    x, y, z = (a.copy() for a in ref.coords())
+    n3, nf = (N + 1) ** 3, (N + 1) ** 2
+    H, E = CS.exact(x, y, z, 0.0, n3)
+    slots, params, fjn = CS.sheet(y, ref.i("cemface"), n3, nf, ref.nxzfl)
+    inc = CS.incident_slots(y, ref.i("cemface"), n3, nf)
+    amp, k, om = CS.incident()
+    if g is None:
+        ref.set_state(H, E)
+        ref.d("pmlbn")[:] = H.ravel()
+        ref.d("pmldn")[:] = E.ravel()
+        ref.set_graphene(params, slots)
+        ref.fjn[:] = fjn
+        ref.set_incident(inc, amp, k, om)
+    else:
+        g.set_state(H, E)
+        g.set_array("pmlbn", H)
+        g.set_array("pmldn", E)
+        g.set_graphene(params, slots, ref.d("yconduc"))
+        g.set_graphene_current(fjn)
+        g.set_incident(inc, amp, k, om)
+    return (x, y, z), n3
+
+
+def check(H, E, xyz, t, n3, ref):
+    He, Ee = CS.exact(*xyz, t, n3)
+    got = [H[0], H[1], H[2], E[0], E[1], E[2]]
+    want = [He[0], He[1], He[2], Ee[0], Ee[1], Ee[2]]
+    for q in range(6):
+        l2, li = ref.cem_error(got[q], want[q])
+        assert l2 <= CS.l2tol[q] and li <= CS.linftol[q], (q, l2, li)
+
+
+def make_case(N):
+    return make_ref(N, CS.nel, CS.lo, CS.hi, CS.bc, pml=CS.pml, threads=8)
+
+
+def test_oracle_graphene_known_answer():
+    ref = make_case(CS.N)
+    xyz, n3 = setup(ref, None, CS.N)
+    t = ref.run(CS.nsteps, 0.0, CS.dt)
+    check(ref.hn, ref.en, xyz, t, n3, ref)
+    ref.close()
+
+
+@pytest.mark.gpu
+def test_plain_graphene_bit_exact():
+    N = 4
+    ref = make_case(N)
+    g = gpu_from_ref(ref, "plain")
+    setup(ref, None, N)
+    setup(ref, g, N)
+    ref.run(20, 0.0, CS.dt)
+    g.run(20, 0.0, CS.dt)
+    H, E = g.get_state()
+    np.testing.assert_array_equal(H, ref.hn)
+    np.testing.assert_array_equal(E, ref.en)
+    np.testing.assert_array_equal(g.get_graphene_current(), ref.fjn)
+    g.close(); ref.close()
+
+
+@pytest.mark.gpu
+def test_graphene_known_answer_gpu():
+    ref = make_case(CS.N)
+    g = gpu_from_box(ref, "plain")
+    xyz, n3 = setup(ref, g, CS.N)
+    t = g.run(CS.nsteps, 0.0, CS.dt)
+    H, E = g.get_state()
+    check(H, E, xyz, t, n3, ref)
+    g.close(); ref.close()
+
+
+@pytest.mark.gpu
+def test_graphene_refusals():
+    ref = make_ref(3, (2, 2, 2), (0, 0, 0), (1, 1, 1), (0, 0, 0))
+    g = gpu_from_box(ref, "fused64")
+    with pytest.raises(L.NekgpuError) as e:
+        g.set_graphene(np.zeros((12, g.nxzfl)), np.arange(3), np.ones(g.nxzfl))
+    assert e.value.status == -8
+    g.close()
+    g = gpu_from_ref(ref, "plain")
+    with pytest.raises(L.NekgpuError) as e:
+        g.set_graphene(np.zeros((12, g.nxzfl)), np.array([1, 1]), np.ones(g.nxzfl))
+    assert e.value.status == -1
+    g.close(); ref.close()

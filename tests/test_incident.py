@@ -1,0 +1,139 @@
+"""userinc (incident fields on listed faces, src/cem_maxwell.F:495-496) with
+the PML and a Drude medium: the reference's tests/drude case restated in 3-D
+(cases.DrudeHalfSpace: a plane wave totally reflected by a Drude half-space,
+the reflected wave absorbed in the PML).
+
+CPU: the oracle passes the case's own tolerances (userchk: L2 <= 1e-7 and
+Linf <= 5e-6 on H_z and E_x after 1000 steps of dt = 0.005 at N=8).
+GPU: the plain form matches the oracle bit for bit with the incident field,
+PML and currents on; fused FP64 at 1e-12 per step; mixed at its per-step
+tolerance; every form passes the case's tolerances.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from helpers import gpu_from_box, gpu_from_ref, make_ref, rel_err
+from nekcem_gb300 import MaxwellGPU, cases
+from nekcem_gb300 import _lib as L
+from oracle import refcpu as R
+
+CS = cases.DrudeHalfSpace()
+
+
+def setup(obj, ref, N):
+    """initial state, PML auxiliary fields, Drude current and incident field
+    on the oracle (obj is ref) or a GPU context"""
+    x, y, z = (a.copy() for a in ref.coords())
+    n3 = (N + 1) ** 3
+    idx, params, J = CS.drude(y, n3)
+    H, E = CS.exact(x, y, z, 0.0, n3)
+    slots = CS.incident_slots(y, ref.i("cemface"), n3, (N + 1) ** 2)
+    amp, k, om = CS.incident()
+    if obj is ref:
+        ref.set_drude(params[0], params[1], idx)
+        ref.drude_jn[:] = J
+        ref.set_state(H, E)
+        ref.d("pmlbn")[:] = H.ravel()
+        ref.d("pmldn")[:] = E.ravel()
+        ref.set_incident(slots, amp, k, om)
+    else:
+        obj.set_dispersive(obj.DRUDE, params, idx)
+        obj.set_current(obj.DRUDE, J)
+        obj.set_state(H, E)
+        obj.set_array("pmlbn", H)
+        obj.set_array("pmldn", E)
+        obj.set_incident(slots, amp, k, om)
+    return (x, y, z), n3
+
+
+def check_known_answer(H, E, xyz, t, n3, ref, quiet=1e-12):
+    """userchk's tolerances on H_z and E_x; the other components, zero in the
+    exact solution, stay at rounding level (quiet: the L2 bound; the mixed
+    form's FP32 contractions leave ~1e-10 there)"""
+    He, Ee = CS.exact(*xyz, t, n3)
+    for q in range(3):
+        for got, want, active in ((H[q], He[q], q == 2), (E[q], Ee[q], q == 0)):
+            l2, li = ref.cem_error(got, want)
+            if active:
+                assert l2 <= 1e-7 and li <= 5e-6, (q, l2, li)
+            else:
+                assert l2 <= quiet and li <= 100 * quiet, (q, l2, li)
+
+
+def make_case(N):
+    return make_ref(N, CS.nel, CS.lo, CS.hi, CS.bc, pml=CS.pml, threads=8)
+
+
+def test_oracle_drude_known_answer():
+    ref = make_case(CS.N)
+    xyz, n3 = setup(ref, ref, CS.N)
+    t = ref.run(CS.nsteps, 0.0, CS.dt)
+    check_known_answer(ref.hn, ref.en, xyz, t, n3, ref)
+    ref.close()
+
+
+@pytest.mark.gpu
+def test_plain_incident_bit_exact():
+    N = 5
+    ref = make_case(N)
+    g = gpu_from_ref(ref, "plain")
+    setup(ref, ref, N)
+    setup(g, ref, N)
+    ref.run(20, 0.0, CS.dt)
+    g.run(20, 0.0, CS.dt)
+    H, E = g.get_state()
+    np.testing.assert_array_equal(H, ref.hn)
+    np.testing.assert_array_equal(E, ref.en)
+    np.testing.assert_array_equal(g.array("pmldn"), ref.d("pmldn"))
+    np.testing.assert_array_equal(g.get_current(g.DRUDE), ref.drude_jn)
+    g.close(); ref.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("form,tol", [("fused64", 1e-12), ("mixed", 2e-6)])
+def test_fused_incident_per_step(form, tol):
+    N = 5
+    ref = make_case(N)
+    g = gpu_from_box(ref, form)
+    setup(ref, ref, N)
+    setup(g, ref, N)
+    for step in range(3):
+        ref.op_rk(step * CS.dt, CS.dt)
+        g.run(1, step * CS.dt, CS.dt)
+        H, E = g.get_state()
+        assert rel_err(H, E, ref.hn, ref.en) <= tol * (step + 1), step
+    g.close(); ref.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("form", ["plain", "fused64", "mixed"])
+def test_drude_known_answer_gpu(form):
+    ref = make_case(CS.N)
+    g = gpu_from_box(ref, form)
+    xyz, n3 = setup(g, ref, CS.N)
+    t = g.run(CS.nsteps, 0.0, CS.dt)
+    H, E = g.get_state()
+    check_known_answer(H, E, xyz, t, n3, ref, quiet=1e-8 if form == "mixed" else 1e-12)
+    g.close(); ref.close()
+
+
+@pytest.mark.gpu
+def test_incident_refusals():
+    ref = make_ref(3, (2, 2, 2), (0, 0, 0), (1, 1, 1), (0, 0, 0))
+    g = gpu_from_box(ref, "fused64")
+    amp, k = (0, 0, 1, 1, 0, 0), (0, 1, 0)
+    for bad in ([-1], [g.nxzfl], [3, 3]):
+        with pytest.raises(L.NekgpuError) as e:
+            g.set_incident(np.array(bad), amp, k, 1.0)
+        assert e.value.status == -1
+    g.set_incident(np.arange(4), amp, k, 1.0)
+    g.set_state(np.zeros((3, g.npts)), np.zeros((3, g.npts)))
+    with pytest.raises(L.NekgpuError) as e:  # no adjoint through userinc
+        g.adjoint_gradient(1, 0.0, 0.01, np.ones(g.npts))
+    assert e.value.status == -8
+    with pytest.raises(L.NekgpuError) as e:  # no PML on this mesh
+        g.set_array("pmlbn", np.zeros((3, g.npts)))
+    assert e.value.status == -5
+    g.close(); ref.close()
