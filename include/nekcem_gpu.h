@@ -356,6 +356,9 @@ int nekgpu_checkpoint_load(nekgpu_ctx* ctx, const char* path, double* time, long
 /* Runs nsteps steps between CUDA events on the context stream and returns the
  * elapsed device milliseconds (state advances; *time += nsteps*dt). */
 int nekgpu_time_steps(nekgpu_ctx* ctx, int nsteps, double* time, double dt, double* ms);
+/* device memory held by the context, bytes (a set_* call that replaces
+ * earlier data frees the earlier device arrays) */
+long nekgpu_device_bytes(const nekgpu_ctx* ctx);
 /* kernel launches issued by the last nekgpu_step / nekgpu_time_steps call */
 long nekgpu_last_launches(const nekgpu_ctx* ctx);
 /* synchronise the context stream */

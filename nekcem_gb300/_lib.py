@@ -113,6 +113,7 @@ SIGNATURES = [
     ("nekgpu_checkpoint_load", C.c_int, [C.c_void_p, C.c_char_p, dp, C.POINTER(C.c_long)]),
     ("nekgpu_time_steps", C.c_int, [C.c_void_p, C.c_int, dp, C.c_double, dp]),
     ("nekgpu_last_launches", C.c_long, [C.c_void_p]),
+    ("nekgpu_device_bytes", C.c_long, [C.c_void_p]),
     ("nekgpu_sync", C.c_int, [C.c_void_p]),
 ]
 

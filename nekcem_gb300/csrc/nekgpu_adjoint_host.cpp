@@ -167,6 +167,7 @@ int build_adjoint_data(Context* c) {
     return NEKGPU_ERR_NOMEM;
   }
   c->allocs.push_back(pd);
+  c->alloc_bytes.push_back(k.size() * 8);
   c->dev_bytes += k.size() * 8;
   c->d_adj_slot = (double*)pd;
   if (check_cuda(cudaMemcpy(pd, k.data(), k.size() * 8, cudaMemcpyHostToDevice))) return NEKGPU_ERR_CUDA;

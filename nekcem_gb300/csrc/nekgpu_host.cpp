@@ -31,6 +31,18 @@ int check_cuda(cudaError_t e) {
   return NEKGPU_ERR_CUDA;
 }
 
+void release_dev(Context* c, const void* p) {
+  if (!p) return;
+  for (size_t i = 0; i < c->allocs.size(); ++i)
+    if (c->allocs[i] == p) {
+      cudaFree(c->allocs[i]);  // synchronises: no launch still reads it
+      c->dev_bytes -= c->alloc_bytes[i];
+      c->allocs.erase(c->allocs.begin() + i);
+      c->alloc_bytes.erase(c->alloc_bytes.begin() + i);
+      return;
+    }
+}
+
 int incident_upload(Context* c, double rktime) {
   const long n = (long)c->inc_slots.size();
   if (!n) return NEKGPU_OK;
@@ -197,6 +209,7 @@ struct DevAlloc {
     used += bytes;
     c->dev_bytes += bytes;
     c->allocs.push_back(q);
+    c->alloc_bytes.push_back(bytes);
     *p = (T*)q;
     return NEKGPU_OK;
   }
@@ -213,6 +226,7 @@ struct DevAlloc {
 void free_all(Context* c) {
   for (void* p : c->allocs) cudaFree(p);
   c->allocs.clear();
+  c->alloc_bytes.clear();
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
   if (c->stream) cudaStreamDestroy(c->stream);
@@ -1503,6 +1517,8 @@ int nekgpu_get_array(nekgpu_ctx* c, const char* name, double* out) {
   return NEKGPU_OK;
 }
 
+long nekgpu_device_bytes(const nekgpu_ctx* c) { return c ? (long)c->dev_bytes : 0; }
+
 int nekgpu_set_source_kind(nekgpu_ctx* c, int kind) {
   if (!c || kind < 0 || kind > 1) return NEKGPU_ERR_ARG;
   c->src.kind = kind;
@@ -1533,6 +1549,13 @@ int nekgpu_set_incident(nekgpu_ctx* c, const int* slots, long n, const double am
       nodes[q] = (int)(e * n3 + face_vol((int)f, (int)(ab % c->nx), (int)(ab / c->nx), c->nx));
     }
   }
+  for (const void* q : {(const void*)c->d_inc_slot, (const void*)c->d_inc_elem,
+                        (const void*)c->d_inc_val, (const void*)c->pargs.inc_slot})
+    release_dev(c, q);
+  c->d_inc_slot = nullptr;
+  c->d_inc_elem = nullptr;
+  c->d_inc_val = nullptr;
+  c->pargs.inc_slot = nullptr;
   DevAlloc A(c);
   int st;
   c->inc_slots = sl;
@@ -1602,7 +1625,14 @@ int nekgpu_set_graphene(nekgpu_ctx* c, const double* params, const int* slots, l
     for (int p = 0; p < 12; ++p) par[p * n + q] = params[p * L + j];
     yc[q] = yconduc[j];
   }
-  c->pargs.ngraph = 0;
+  PlainDev& pa = c->pargs;
+  for (const void* q : {(const void*)pa.gr_slot, (const void*)pa.gr_par, (const void*)pa.gr_yc,
+                        (const void*)pa.gr_f, (const void*)pa.gr_k})
+    release_dev(c, q);
+  pa.gr_slot = nullptr;
+  pa.gr_par = pa.gr_yc = nullptr;
+  pa.gr_f = pa.gr_k = nullptr;
+  pa.ngraph = 0;
   c->gr_slots = sl;
   if (n == 0) return NEKGPU_OK;
   DevAlloc A(c);
@@ -1684,10 +1714,15 @@ int nekgpu_set_dealias(nekgpu_ctx* c, int lxd, const double* jgl, const double* 
                        const double* w3md, const double* metd) {
   if (!c) return NEKGPU_ERR_ARG;
   if (c->form != NEKGPU_PLAIN || c->ndim == 2) return NEKGPU_ERR_UNSUPPORTED;
-  if (lxd == 0) {
-    c->pargs.md = 0;
-    return NEKGPU_OK;
+  {
+    PlainDev& pa = c->pargs;
+    for (const void* q : {(const void*)pa.jgl, (const void*)pa.jgt, (const void*)pa.dxmd,
+                          (const void*)pa.dxtmd, (const void*)pa.w3md, (const void*)pa.metd})
+      release_dev(c, q);
+    pa.jgl = pa.jgt = pa.dxmd = pa.dxtmd = pa.w3md = pa.metd = nullptr;
+    pa.md = 0;
   }
+  if (lxd == 0) return NEKGPU_OK;
   const int mx = c->nx, md = lxd;
   if (md < mx || !jgl || !dxmd || !w3md || !metd) return NEKGPU_ERR_ARG;
   int dev_smem = 0;
@@ -1746,6 +1781,12 @@ int nekgpu_set_dispersive(nekgpu_ctx* c, int model, const double* params, long l
         break;
       }
   const long nn = (long)elems.size() * n3;
+  for (const void* q : {(const void*)c->d_disp_slot, (const void*)c->d_disp_elem,
+                        (const void*)c->d_disp_data, (const void*)c->d_disp_aux,
+                        (const void*)c->d_disp_k})
+    release_dev(c, q);
+  c->d_disp_slot = c->d_disp_elem = nullptr;
+  c->d_disp_data = c->d_disp_aux = c->d_disp_k = nullptr;
   DispDev d{};
   if (nn) {
     std::vector<double> data((size_t)kDispData * nn, 0.0);
@@ -1857,6 +1898,10 @@ int nekgpu_set_source(nekgpu_ctx* c, int enabled, const double xc[3], double sig
       return NEKGPU_ERR_CUDA;
     c->pargs.src_w = c->d_src_w_plain;
   } else {
+    release_dev(c, c->d_src_elem);  // a previous source's arrays
+    release_dev(c, c->d_src_w);
+    c->d_src_elem = nullptr;
+    c->d_src_w = nullptr;
     // elements whose weights are all below 1e-30 of the peak carry no source
     const long n3 = (long)c->nx * c->nx * c->nx;
     std::vector<int> off(c->nelt, -1);

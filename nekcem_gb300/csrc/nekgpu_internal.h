@@ -289,6 +289,7 @@ struct Context {
   double* d_red = nullptr;     // reduction scratch
   int* d_status = nullptr;
   std::vector<void*> allocs;
+  std::vector<size_t> alloc_bytes;  // size of each entry of allocs
   size_t dev_bytes = 0;  // device bytes held in allocs
 
   // fused form
@@ -359,6 +360,8 @@ struct Context {
 
 // host helpers (nekgpu_host.cpp)
 int check_cuda(cudaError_t e);
+// frees a device allocation of the context (null or foreign pointers ignored)
+void release_dev(Context* c, const void* p);
 void rk_coeffs(double a[5], double b[5], double c[6]);
 
 // kernel launchers (nekgpu_plain.cu)

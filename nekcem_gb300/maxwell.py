@@ -293,6 +293,9 @@ class MaxwellGPU:
                                            C.byref(ms)), "nekgpu_time_steps")
         return t.value, ms.value
 
+    def device_bytes(self) -> int:
+        return int(L.load().nekgpu_device_bytes(self._h))
+
     def last_launches(self) -> int:
         return int(L.load().nekgpu_last_launches(self._h))
 

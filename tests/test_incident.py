@@ -137,3 +137,31 @@ def test_incident_refusals():
         g.set_array("pmlbn", np.zeros((3, g.npts)))
     assert e.value.status == -5
     g.close(); ref.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("form", ["plain", "fused64", "mixed"])
+def test_repeated_set_calls_do_not_grow_device_memory(form):
+    """Replacing currents, incident faces, sources (and the plain form's
+    graphene sheets and dealiasing tables) frees the earlier device arrays."""
+    ref = make_ref(4, (2, 2, 2), (0, 0, 0), (1, 1, 1), (0, 0, 0), deform=0.0)
+    g = gpu_from_ref(ref, form) if form == "plain" else gpu_from_box(ref, form)
+    n, nf = g.npts, g.nxzfl
+    amp, k = (0, 0, 1, 1, 0, 0), (0, 1, 0)
+
+    def set_all(i):
+        g.set_dispersive(g.DRUDE, np.ones((2, n)), np.arange(10 + i))
+        g.set_incident(np.arange(4 + i), amp, k, 1.0)
+        g.set_source((0.5, 0.5, 0.5), 0.2 + 0.01 * i, 1.0, 1.0, 0.0)
+        if form == "plain":
+            g.set_graphene(np.zeros((12, nf)), np.arange(3 + i), np.ones(nf))
+            ref.set_dealias(6)
+            g.set_dealias(6, ref.d("jgl"), ref.d("dxmd"), ref.d("w3md"), ref.d("metd"))
+
+    set_all(0)
+    base = g.device_bytes()
+    for i in range(1, 4):
+        set_all(i)
+    grown = g.device_bytes() - base
+    assert grown <= 2048, grown  # the lists grew by a few entries only
+    g.close(); ref.close()
