@@ -195,7 +195,7 @@ int nekgpu_set_incident(nekgpu_ctx* ctx, const int* slots, long n, const double 
  * sets pmlbn = mu H, pmldn = eps E); nodes outside the PML are ignored. */
 int nekgpu_set_array(nekgpu_ctx* ctx, const char* name, const double* in);
 
-/* ---- graphene sheets (NEKGPU_PLAIN) ------------------------------------------ */
+/* ---- graphene sheets ------------------------------------------------------------ */
 /* cem_3d_graphene_current (src/cem_maxwell.F:2827-2931) run through userfsrc
  * as tests/3dgraphene does: on the n listed face slots (1-based graphindex)
  * the surface current from the face fields and the 12 parameters
@@ -203,7 +203,9 @@ int nekgpu_set_array(nekgpu_ctx* ctx, const char* name, const double* in);
  * a_222, b_12, b_22), its auxiliary currents advanced with the RK stage, and
  * -J added to the -n x H part of the flux before the face sum.  yconduc is
  * the reference's face array (nxzfl).  The currents start at zero; n = 0
- * removes the sheets.  Plain form only (NEKGPU_ERR_UNSUPPORTED otherwise). */
+ * removes the sheets.  Plain form: any listed slot; fused FP64 and mixed
+ * forms: slots on interior faces (NEKGPU_ERR_UNSUPPORTED for wall slots,
+ * curvilinear and 2-D meshes). */
 int nekgpu_set_graphene(nekgpu_ctx* ctx, const double* params, const int* slots, long n,
                         const double* yconduc);
 /* The face currents fjn(ld,3,6), ld >= nxzfl: listed slots only. */

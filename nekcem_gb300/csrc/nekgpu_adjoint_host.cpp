@@ -380,7 +380,7 @@ extern "C" int nekgpu_adjoint_gradient(nekgpu_ctx* c, int nsteps, double t0, dou
   if (!c || !jw || !J || !dJdeps || nsteps < 1) return NEKGPU_ERR_ARG;
   // no adjoint through PML or dispersive currents
   if (c->form != NEKGPU_FUSED64 || c->npml || c->disp_n || c->ndim == 2 || c->curved ||
-      !c->inc_slots.empty())
+      !c->inc_slots.empty() || c->grdev.ng)
     return NEKGPU_ERR_UNSUPPORTED;
   if (!c->have_state) return NEKGPU_ERR_STATE;
   int st = build_adjoint_data(c);

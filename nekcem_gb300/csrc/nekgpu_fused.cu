@@ -319,7 +319,7 @@ __global__ void __launch_bounds__(Cfg<NX, T>::NT, Cfg<NX, T>::kMinBlocks)
         const int fa = ab % NX, fb = ab / NX;
         const int v = face_vol<NX>(f, fa, fb);
         const int pe = nbr[f];
-        T dH[3], dE[3];
+        T dH[3], dE[3], hmv[3], emv[3], hpv[3], epv[3];
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
           T hm = s_uT[c * N3 + v], em = s_uT[(c + 3) * N3 + v];
@@ -336,12 +336,37 @@ __global__ void __launch_bounds__(Cfg<NX, T>::NT, Cfg<NX, T>::kMinBlocks)
               ep += (T)iv[(9 + c) * NF];
             }
           }
+          hmv[c] = hm; emv[c] = em; hpv[c] = hp; epv[c] = ep;
           if (pe >= 0) {
             dH[c] = hp - hm;
             dE[c] = ep - em;
           } else {  // PEC mirror: H+ = H-, E+ = -E-
             dH[c] = T(0);
             dE[c] = T(-2) * em;
+          }
+        }
+        if (EXT && !C::kMixed && a.gr.elem) {
+          // graphene (userfsrc): the sheet's currents on both sides of the
+          // face node enter as n x [H] - J, i.e. [H] + n x J
+          const int gr = a.gr.elem[e];
+          const int go = gr >= 0 ? a.gr.own[(long)gr * NF + t] : -1;
+          const int gp = gr >= 0 ? a.gr.part[(long)gr * NF + t] : -1;
+          if (go >= 0 || gp >= 0) {
+            double nv[3] = {0.0, 0.0, 0.0}, nm[3];
+            nv[slot_axis(f)] = (double)slot_side(f);
+            for (int c = 0; c < 3; ++c) nm[c] = -nv[c];
+            const double fhm[3] = {(double)hmv[0], (double)hmv[1], (double)hmv[2]};
+            const double fem[3] = {(double)emv[0], (double)emv[1], (double)emv[2]};
+            const double fhp[3] = {(double)hpv[0], (double)hpv[1], (double)hpv[2]};
+            const double fep[3] = {(double)epv[0], (double)epv[1], (double)epv[2]};
+            double J[3] = {0.0, 0.0, 0.0};
+            if (go >= 0) graphene_slot(a.gr, go, nv, fhm, fem, true, first_stage, a.a, a.b, a.dt, J);
+            if (gp >= 0 && pe >= 0) graphene_slot(a.gr, gp, nm, fhp, fep, false, first_stage, a.a, a.b, a.dt, J);
+            if (pe >= 0) {  // a PEC face keeps its mirror flux
+              dH[0] += (T)(nv[1] * J[2] - nv[2] * J[1]);
+              dH[1] += (T)(nv[2] * J[0] - nv[0] * J[2]);
+              dH[2] += (T)(nv[0] * J[1] - nv[1] * J[0]);
+            }
           }
         }
         T Y02 = T(-0.5), C02Y = T(0.5) * C0, Z02 = T(0.5), C02Z = T(0.5) * C0;
@@ -561,8 +586,8 @@ int dispatch_nx(Context* c, const FusedDev& a) {
 
 template <typename T>
 int dispatch(Context* c, const FusedDev& a) {
-  return (a.pml.slot || a.disp.slot || a.inc_elem) ? dispatch_nx<T, true>(c, a)
-                                                  : dispatch_nx<T, false>(c, a);
+  return (a.pml.slot || a.disp.slot || a.inc_elem || a.gr.elem) ? dispatch_nx<T, true>(c, a)
+                                                               : dispatch_nx<T, false>(c, a);
 }
 
 }  // namespace
@@ -616,8 +641,13 @@ int fused_stage(Context* c, int rkstep, double time, double dt) {
     a.src_ftf = (float)a.src_ft;
   }
   if (a.inc_elem && (st = incident_upload(c, time + dt * c->rk_c[rkstep - 1]))) return st;
+  if (a.gr.elem) {
+    a.gr.f_in = c->d_gr_f[c->gr_cur];
+    a.gr.f_out = c->d_gr_f[c->gr_cur ^ 1];
+  }
   st = c->form == NEKGPU_MIXED_NAIVE ? dispatch<float>(c, a) : dispatch<double>(c, a);
   if (st) return st;
+  if (a.gr.elem) c->gr_cur ^= 1;
   c->cur ^= 1;
   return NEKGPU_OK;
 }

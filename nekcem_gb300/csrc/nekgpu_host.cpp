@@ -1607,12 +1607,78 @@ int nekgpu_set_incident(nekgpu_ctx* c, const int* slots, long n, const double am
   return NEKGPU_OK;
 }
 
+// Graphene sheets in the fused FP64 and mixed forms: interior face slots of
+// the affine mesh; Y_0 = (yconduc + partner's yconduc) / 2 as
+// cem_maxwell_materials forms it for an interior face node.
+static int set_graphene_fused(nekgpu_ctx* c, const double* params, const int* slots, long n,
+                              const double* yconduc) {
+  const long L = c->nxzfl, N2 = (long)c->nx * c->nx, NF = 6 * N2;
+  std::vector<int> sl(n);
+  std::vector<char> seen(L, 0);
+  std::vector<double> par(12 * (size_t)n), y0(n), yc(n);
+  std::vector<int> rows(c->nelt, -1), relem;
+  auto row_of = [&](int e) {
+    if (rows[e] < 0) {
+      rows[e] = (int)relem.size();
+      relem.push_back(e);
+    }
+    return rows[e];
+  };
+  std::vector<std::pair<long, int>> own, part;  // (row*NF + t, g)
+  for (long q = 0; q < n; ++q) {
+    const long j = (long)slots[q] - 1;
+    if (j < 0 || j >= L || seen[j]) return NEKGPU_ERR_ARG;
+    seen[j] = 1;
+    sl[q] = (int)j;
+    const long e = j / NF, t = j % NF, f = t / N2, ab = t % N2;
+    const int pe = c->host_nbr[6 * e + f];
+    if (pe < 0) return NEKGPU_ERR_UNSUPPORTED;  // sheets on interior faces only
+    const long fo = f < 4 ? (f + 2) & 3 : 9 - f, tp = fo * N2 + ab;
+    for (int p = 0; p < 12; ++p) par[p * n + q] = params[p * L + j];
+    yc[q] = yconduc[j];
+    y0[q] = 0.5 * (yconduc[j] + yconduc[(long)pe * NF + tp]);
+    own.push_back({(long)row_of((int)e) * NF + t, (int)q});
+    part.push_back({(long)row_of(pe) * NF + tp, (int)q});
+  }
+  GrapheneDev& G = c->grdev;
+  for (const void* q : {(const void*)G.elem, (const void*)G.own, (const void*)G.part,
+                        (const void*)G.par, (const void*)G.y0, (const void*)G.yc, (const void*)G.k,
+                        (const void*)c->d_gr_f[0], (const void*)c->d_gr_f[1]})
+    release_dev(c, q);
+  G = GrapheneDev{};
+  c->d_gr_f[0] = c->d_gr_f[1] = nullptr;
+  c->gr_cur = 0;
+  c->gr_slots = sl;
+  c->fargs.gr = c->margs.gr = G;
+  if (n == 0) return NEKGPU_OK;
+  std::vector<int> vown(relem.size() * NF, -1), vpart(relem.size() * NF, -1);
+  for (auto& o : own) vown[o.first] = o.second;
+  for (auto& o : part) vpart[o.first] = o.second;
+  DevAlloc A(c);
+  int *d_elem, *d_own, *d_part;
+  double *d_par, *d_y0, *d_yc, *d_k;
+  int st;
+  if ((st = A.put(&d_elem, rows)) || (st = A.put(&d_own, vown)) || (st = A.put(&d_part, vpart)) ||
+      (st = A.put(&d_par, par)) || (st = A.put(&d_y0, y0)) || (st = A.put(&d_yc, yc)) ||
+      (st = A.get(&d_k, 18 * n)) || (st = A.get(&c->d_gr_f[0], 18 * n)) ||
+      (st = A.get(&c->d_gr_f[1], 18 * n)))
+    return st;
+  for (void* d : {(void*)d_k, (void*)c->d_gr_f[0], (void*)c->d_gr_f[1]})
+    if (check_cuda(cudaMemset(d, 0, 18 * n * sizeof(double)))) return NEKGPU_ERR_CUDA;
+  G.elem = d_elem; G.own = d_own; G.part = d_part;
+  G.par = d_par; G.y0 = d_y0; G.yc = d_yc; G.k = d_k;
+  G.ng = n;
+  c->fargs.gr = c->margs.gr = G;
+  return NEKGPU_OK;
+}
+
 // Graphene sheets (plain form): the reference's graphparams(nxzfl,12),
 // graphindex (1-based) and yconduc(nxzfl); the face currents start at zero.
 int nekgpu_set_graphene(nekgpu_ctx* c, const double* params, const int* slots, long n,
                         const double* yconduc) {
   if (!c || n < 0 || (n > 0 && (!params || !slots || !yconduc))) return NEKGPU_ERR_ARG;
-  if (c->form != NEKGPU_PLAIN || c->ndim == 2) return NEKGPU_ERR_UNSUPPORTED;
+  if (c->ndim == 2 || c->curved || c->form == NEKGPU_MIXED_NAIVE) return NEKGPU_ERR_UNSUPPORTED;
+  if (c->form != NEKGPU_PLAIN) return set_graphene_fused(c, params, slots, n, yconduc);
   const long L = c->nxzfl;
   std::vector<int> sl(n);
   std::vector<char> seen(L, 0);
@@ -1655,10 +1721,12 @@ int nekgpu_set_graphene(nekgpu_ctx* c, const double* params, const int* slots, l
 // listed slots are read / written; other slots read 0)
 static int graphene_copy(nekgpu_ctx* c, double* fjn, long ld, bool to_device) {
   if (!c || !fjn || ld < c->nxzfl) return NEKGPU_ERR_ARG;
-  const long ng = c->pargs.ngraph;
+  const bool plain = c->form == NEKGPU_PLAIN;
+  const long ng = plain ? c->pargs.ngraph : c->grdev.ng;
+  double* dptr = plain ? c->pargs.gr_f : c->d_gr_f[c->gr_cur];
   std::vector<double> h(18 * (size_t)ng);
   if (ng && (check_cuda(cudaStreamSynchronize(c->stream)) ||
-             check_cuda(cudaMemcpy(h.data(), c->pargs.gr_f, h.size() * sizeof(double),
+             check_cuda(cudaMemcpy(h.data(), dptr, h.size() * sizeof(double),
                                    cudaMemcpyDeviceToHost))))
     return NEKGPU_ERR_CUDA;
   if (!to_device) std::fill(fjn, fjn + 18 * ld, 0.0);
@@ -1670,7 +1738,7 @@ static int graphene_copy(nekgpu_ctx* c, double* fjn, long ld, bool to_device) {
         fjn[r * ld + c->gr_slots[q]] = h[r * ng + q];
     }
   if (to_device && ng &&
-      check_cuda(cudaMemcpy(c->pargs.gr_f, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice)))
+      check_cuda(cudaMemcpy(dptr, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice)))
     return NEKGPU_ERR_CUDA;
   return NEKGPU_OK;
 }

@@ -148,11 +148,72 @@ struct PmlDev {
   long n;                 // npml * N3
 };
 
+// Graphene sheets in the fused forms: per element row (elements with a listed
+// slot or the partner of one), per face node the compact index of the own
+// slot and of the partner's slot when listed (-1 otherwise); per listed slot
+// g the 12 parameters, Y_0, yconduc, and the face currents fjn(.,m,k) at
+// [(3k+m)*ng + g], read from f_in and written to f_out (swapped every stage:
+// a face node's two sides read each other's currents), RK registers in k.
+struct GrapheneDev {
+  const int* elem;
+  const int* own;
+  const int* part;
+  const double *par, *y0, *yc;
+  const double* f_in;
+  double* f_out;
+  double* k;
+  long ng;
+};
+
+#ifdef __CUDACC__
+// cem_3d_graphene_current (src/cem_maxwell.F:2827-2931) at listed slot g with
+// unit normal n and face fields fh, fe: adds the surface current J to Jacc;
+// with update, also the residuals of the auxiliary currents and their RK
+// update (FP64, fused low-storage form).
+__device__ inline void graphene_slot(const GrapheneDev& G, long g, const double n[3],
+                                     const double fh[3], const double fe[3], bool update,
+                                     bool first_stage, double ra, double rb, double dt,
+                                     double Jacc[3]) {
+  const long ng = G.ng;
+  double p[12];
+  for (int i = 0; i < 12; ++i) p[i] = G.par[i * ng + g];
+  const double nH[3] = {-n[1] * fh[2] + n[2] * fh[1], n[0] * fh[2] - n[2] * fh[0],
+                        -n[0] * fh[1] + n[1] * fh[0]};
+  const double ndotE = n[0] * fe[0] + n[1] * fe[1] + n[2] * fe[2];
+  const double Yfac = 0.5 / G.y0[g];
+  const double cpfac = p[2] + p[7];
+  const double jnfac = 1.0 - cpfac * Yfac;
+  for (int m = 0; m < 3; ++m) {
+    double F[6];
+    for (int k = 1; k < 6; ++k) F[k] = G.f_in[(3 * k + m) * ng + g];
+    const double tmp = Yfac * (nH[m] + G.yc[g] * (fe[m] - n[m] * ndotE));
+    const double J0 = (F[1] + F[2] + F[4] - cpfac * tmp) / jnfac;
+    Jacc[m] += J0;
+    if (!update) continue;
+    const double f = tmp - Yfac * J0;
+    double R[6];
+    R[1] = -p[0] * F[1] + p[1] * f;
+    R[2] = F[3] + p[5] * f;
+    R[3] = -p[3] * F[2] - p[4] * F[3] + p[6] * f;
+    R[4] = F[5] + p[10] * f;
+    R[5] = -p[8] * F[4] - p[9] * F[5] + p[11] * f;
+    G.f_out[m * ng + g] = J0;
+    for (int k = 1; k < 6; ++k) {
+      const long o = (3 * k + m) * ng + g;
+      const double kh = first_stage ? dt * R[k] : fma(ra, G.k[o], dt * R[k]);
+      G.k[o] = kh;
+      G.f_out[o] = fma(rb, kh, F[k]);
+    }
+  }
+}
+#endif
+
 struct FusedDev {
   int nelt;
   long npts;
   PmlDev pml;
   DispDev disp;
+  GrapheneDev gr;
   const int* inc_elem;    // nelt: row of the element in inc_val, -1 without incident faces
   const double* inc_val;  // [row][12][6*nx^2]: the stage's incident face values, H and E
                           // on the own side (0..5) and on the partner's side (6..11)
@@ -202,6 +263,7 @@ struct MixedDev {
   DispDev disp;
   const int* inc_elem;    // as in FusedDev
   const double* inc_val;
+  GrapheneDev gr;
   double dt;
 };
 
@@ -339,8 +401,12 @@ struct Context {
   int* d_inc_slot = nullptr;
   int* d_inc_elem = nullptr;
   double* d_inc_val = nullptr;
-  // graphene sheets (plain form): listed slots on the host
+  // graphene sheets: listed slots on the host; the fused forms' current
+  // buffers (two, swapped every stage) and the elements' rows
   std::vector<int> gr_slots;
+  double* d_gr_f[2] = {nullptr, nullptr};
+  int gr_cur = 0;
+  GrapheneDev grdev{};
   // adjoint face-slot coefficients (built on first use, FP64 fused form)
   double* d_adj_slot = nullptr;
   std::vector<double> adj_jw;  // objective weights set by nekgpu_adjoint_init

@@ -555,6 +555,46 @@ __global__ void __launch_bounds__(MCfg<NX>::NT, 3) k_mixed_stage(const MixedDev 
             }
           }
         }
+        if (EXT && a.gr.elem) {
+          // graphene (userfsrc): the sheet's currents on both sides of the
+          // face node enter as n x [H] - J, i.e. [H] + n x J (FP64)
+          const int gr = a.gr.elem[e];
+          const int go = gr >= 0 ? a.gr.own[(long)gr * NF + t] : -1;
+          const int gp = gr >= 0 ? a.gr.part[(long)gr * NF + t] : -1;
+          if (go >= 0 || gp >= 0) {
+            double nv[3] = {0.0, 0.0, 0.0}, nm[3];
+            nv[slot_axis(f)] = (double)slot_side(f);
+            double fhm[3], fem[3], fhp[3], fep[3];
+            const int io = a.inc_elem ? a.inc_elem[e] : -1;
+            for (int c = 0; c < 3; ++c) {
+              nm[c] = -nv[c];
+              const float2 h = s_u2[c * N3P + pv], ev = s_u2[(c + 3) * N3P + pv];
+              fhm[c] = f2d(h.x) + f2d(h.y);
+              fem[c] = f2d(ev.x) + f2d(ev.y);
+              fhp[c] = fep[c] = 0.0;
+              if (pe >= 0) {
+                const float2 ph = s_nb2[c * NF + t], pE = s_nb2[(c + 3) * NF + t];
+                fhp[c] = f2d(ph.x) + f2d(ph.y);
+                fep[c] = f2d(pE.x) + f2d(pE.y);
+              }
+              if (io >= 0) {
+                const double* iv = a.inc_val + (long)io * 12 * NF + t;
+                fhm[c] += iv[c * NF];
+                fem[c] += iv[(3 + c) * NF];
+                fhp[c] += iv[(6 + c) * NF];
+                fep[c] += iv[(9 + c) * NF];
+              }
+            }
+            double J[3] = {0.0, 0.0, 0.0};
+            if (go >= 0) graphene_slot(a.gr, go, nv, fhm, fem, true, first_stage, a.a, a.b, a.dt, J);
+            if (gp >= 0 && pe >= 0) graphene_slot(a.gr, gp, nm, fhp, fep, false, first_stage, a.a, a.b, a.dt, J);
+            if (pe >= 0) {  // a PEC face keeps its mirror flux
+              dH[0] += d2f_hi(nv[1] * J[2] - nv[2] * J[1]);
+              dH[1] += d2f_hi(nv[2] * J[0] - nv[0] * J[2]);
+              dH[2] += d2f_hi(nv[0] * J[1] - nv[1] * J[0]);
+            }
+          }
+        }
         float Y02 = -0.5f, C02Y = 0.5f * a.C0f, Z02 = 0.5f, C02Z = 0.5f * a.C0f;
         if (a.fcoef) {
           const float4 fc = reinterpret_cast<const float4*>(a.fcoef)[(long)e * NF + t];
@@ -741,8 +781,12 @@ int mixed_stage(Context* c, int rkstep, double time, double dt) {
   a.b = c->rk_b[rkstep - 1];
   a.dt = dt;
   if (c->src.enabled) a.src_ftf = (float)source_ft(c->src, time + dt * c->rk_c[rkstep - 1]);
-  const bool ext = a.pml.slot || a.disp.slot || a.inc_elem;
+  const bool ext = a.pml.slot || a.disp.slot || a.inc_elem || a.gr.elem;
   if (a.inc_elem && (st = incident_upload(c, time + dt * c->rk_c[rkstep - 1]))) return st;
+  if (a.gr.elem) {
+    a.gr.f_in = c->d_gr_f[c->gr_cur];
+    a.gr.f_out = c->d_gr_f[c->gr_cur ^ 1];
+  }
   switch (c->nx) {
     case 3: st = ext ? launch_mixed<3, true>(c, a) : launch_mixed<3, false>(c, a); break;
     case 4: st = ext ? launch_mixed<4, true>(c, a) : launch_mixed<4, false>(c, a); break;
@@ -755,6 +799,7 @@ int mixed_stage(Context* c, int rkstep, double time, double dt) {
   }
   if (st) return st;
   c->cur ^= 1;
+  if (a.gr.elem) c->gr_cur ^= 1;
   return NEKGPU_OK;
 }
 

@@ -7,8 +7,9 @@ Drude term and two critical points).
 CPU: the oracle passes the case's own userchk tolerances after 1000 steps
 (L2 <= 5e-4, Linf <= 5e-3 on H_x, H_z, E_x, E_z; L2 <= 1e-14, Linf <= 5e-12
 on H_y, E_y).  GPU: the plain form matches the oracle bit for bit (fields
-and face currents) and passes the same tolerances; the fused forms refuse
-graphene.
+and face currents); the fused FP64 form to 1e-12 per step and the mixed form
+to its per-step tolerance; all three pass the case's tolerances on the
+active components.
 """
 from __future__ import annotations
 
@@ -46,13 +47,19 @@ def setup(ref, g, N):
     return (x, y, z), n3
 
 
-def check(H, E, xyz, t, n3, ref):
+def check(H, E, xyz, t, n3, ref, quiet=None):
+    """userchk's tolerances; quiet replaces the tolerance of the two
+    components that are zero in the exact solution (the mixed form's FP32
+    contractions leave ~1e-10 there)"""
     He, Ee = CS.exact(*xyz, t, n3)
     got = [H[0], H[1], H[2], E[0], E[1], E[2]]
     want = [He[0], He[1], He[2], Ee[0], Ee[1], Ee[2]]
     for q in range(6):
         l2, li = ref.cem_error(got[q], want[q])
-        assert l2 <= CS.l2tol[q] and li <= CS.linftol[q], (q, l2, li)
+        l2t, lit = CS.l2tol[q], CS.linftol[q]
+        if quiet is not None and q in (1, 4):
+            l2t, lit = quiet, 100 * quiet
+        assert l2 <= l2t and li <= lit, (q, l2, li)
 
 
 def make_case(N):
@@ -84,13 +91,34 @@ def test_plain_graphene_bit_exact():
 
 
 @pytest.mark.gpu
-def test_graphene_known_answer_gpu():
+@pytest.mark.parametrize("form,tol", [("fused64", 1e-12), ("mixed", 2e-6)])
+def test_fused_graphene_per_step(form, tol):
+    N = 4
+    ref = make_case(N)
+    g = gpu_from_box(ref, form)
+    setup(ref, None, N)
+    setup(ref, g, N)
+    for step in range(3):
+        ref.op_rk(step * CS.dt, CS.dt)
+        g.run(1, step * CS.dt, CS.dt)
+        H, E = g.get_state()
+        scale = max(np.abs(ref.hn).max(), np.abs(ref.en).max())
+        assert np.abs(np.concatenate([H, E]) - np.concatenate([ref.hn, ref.en])).max() <= \
+            tol * (step + 1) * scale, step
+    f = g.get_graphene_current()
+    assert np.abs(f - ref.fjn).max() <= 100 * tol * np.abs(ref.fjn).max()
+    g.close(); ref.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("form", ["plain", "fused64", "mixed"])
+def test_graphene_known_answer_gpu(form):
     ref = make_case(CS.N)
-    g = gpu_from_box(ref, "plain")
+    g = gpu_from_box(ref, form)
     xyz, n3 = setup(ref, g, CS.N)
     t = g.run(CS.nsteps, 0.0, CS.dt)
     H, E = g.get_state()
-    check(H, E, xyz, t, n3, ref)
+    check(H, E, xyz, t, n3, ref, quiet=1e-8 if form == "mixed" else None)
     g.close(); ref.close()
 
 
@@ -98,6 +126,11 @@ def test_graphene_known_answer_gpu():
 def test_graphene_refusals():
     ref = make_ref(3, (2, 2, 2), (0, 0, 0), (1, 1, 1), (0, 0, 0))
     g = gpu_from_box(ref, "fused64")
+    with pytest.raises(L.NekgpuError) as e:  # a wall slot: sheets on interior faces only
+        g.set_graphene(np.zeros((12, g.nxzfl)), np.arange(3), np.ones(g.nxzfl))
+    assert e.value.status == -8
+    g.close()
+    g = gpu_from_box(ref, "mixed_naive")
     with pytest.raises(L.NekgpuError) as e:
         g.set_graphene(np.zeros((12, g.nxzfl)), np.arange(3), np.ones(g.nxzfl))
     assert e.value.status == -8
