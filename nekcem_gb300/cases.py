@@ -328,18 +328,31 @@ class DrudeHalfSpace:
     incident field cos(-k1 y - omega t) (H_z, eta1 E_x) enters through the
     y = 0 faces of the upper elements (userinc); above them the field is the
     reflected wave (damped inside the PML as usersol damps it), below it the
-    evanescent transmitted wave with its Drude current."""
+    evanescent transmitted wave with its Drude current.
+
+    model="lorentz" restates tests/lorentz/lorentz.usr the same way: a
+    Lorentz half-space with a = 0, b = 0.9 omega^2, c = b (eps = -8), its
+    two currents initialised as the case's userini does; userchk's
+    tolerances there are L2 5e-6 and Linf 5e-5 on H_z and E_x."""
 
     N, nel = 8, (2, 32, 2)
     lo, hi = (-2.5, -5.0, -2.5), (2.5, 5.0, 2.5)
     bc = (PERIODIC, 2, PERIODIC)
     pml = (6, 3.0, 1e-15)
     dt, nsteps = 0.005, 1000
-    omega, a, b = 5.0, 0.0, 100.0
+    omega, a, b, c = 5.0, 0.0, 100.0, 0.0
 
-    def __init__(self):
+    def __init__(self, model: str = "drude"):
+        self.model = model
         w = self.omega
-        self.eps2 = 1.0 - self.b / (w * (w + 1j * self.a))
+        if model == "lorentz":
+            self.a, self.b = 0.0, 0.9 * w * w
+            self.c = self.b
+            self.eps2 = 1.0 + self.c / (self.b - 1j * self.a * w - w * w)
+            self.l2tol, self.linftol = 5e-6, 5e-5
+        else:
+            self.eps2 = 1.0 - self.b / (w * (w + 1j * self.a))
+            self.l2tol, self.linftol = 1e-7, 5e-6
         self.eta1 = 1.0
         eta2 = np.sqrt(1.0 / self.eps2 + 0j)
         if eta2.real == 0.0 and eta2.imag > 0.0:  # the branch drude.usr picks
@@ -374,14 +387,23 @@ class DrudeHalfSpace:
         return np.stack([zero, zero, Hz]), np.stack([Ex, zero, zero])
 
     def drude(self, y, n3):
-        """node indices of the Drude medium, its parameters (2, n) and the
-        initial current (3, n)"""
+        """node indices of the dispersive medium, its parameters ((2, n)
+        Drude, (3, n) Lorentz) and the initial currents ((3, n) Drude J;
+        (6, n) Lorentz J1 then J2), as the cases' userini set them"""
         up, _ = self.regions(y, n3)
         idx = np.nonzero(~up)[0]
         n = np.size(y)
-        params = np.stack([np.full(n, self.a), np.full(n, self.b)])
-        sig = self.b / (self.a - 1j * self.omega)
+        w = self.omega
         efac = self.tran * self.eta2 * np.exp(1j * (-self.k2 * np.asarray(y)))
+        if self.model == "lorentz":
+            params = np.stack([np.full(n, self.a), np.full(n, self.b), np.full(n, self.c)])
+            sig = 1j * self.c * w / (w * w + 1j * self.a * w - self.b)
+            J = np.zeros((6, n))
+            J[0, idx] = (sig * efac).real[idx]
+            J[3, idx] = ((1j / w) * sig * efac).real[idx]
+            return idx, params, J
+        params = np.stack([np.full(n, self.a), np.full(n, self.b)])
+        sig = self.b / (self.a - 1j * w)
         J = np.zeros((3, n))
         J[0, idx] = (sig * efac).real[idx]
         return idx, params, J
@@ -401,6 +423,88 @@ class DrudeHalfSpace:
     def incident(self):
         """amp (H then E), k and omega of userinc"""
         return (0.0, 0.0, 1.0, self.eta1, 0.0, 0.0), (0.0, -self.k1, 0.0), self.omega
+
+
+class DielectricHalfSpace:
+    """The reference's tests/2ddielectric case (twomat: a normally incident
+    plane wave on a dielectric half-space eps2 = 2) restated in 3-D like
+    DrudeHalfSpace: 2 x 32 x 2 elements on [-2.5,2.5] x [-5,5] x
+    [-2.5,2.5], N=8, x and z periodic, 'PML' at both y ends (10 layers,
+    order 3, error 1e-30, params 77-79 of 2ddielectric.rea: both the
+    reflected and the transmitted wave leave
+    through a PML, and usersol damps each inside its own), dt = 0.005, 1000
+    steps; TE (H_z, E_x) or TM (E_z, H_x).  userchk's tolerances: L2 5e-7,
+    Linf 5e-6 on the two active components."""
+
+    N, nel = 8, (2, 32, 2)
+    lo, hi = (-2.5, -5.0, -2.5), (2.5, 5.0, 2.5)
+    bc = (PERIODIC, 2, PERIODIC)
+    pml = (10, 3.0, 1e-30)
+    dt, nsteps = 0.005, 1000
+    omega, eps1, eps2 = 5.0, 1.0, 2.0
+    l2tol, linftol = 5e-7, 5e-6
+
+    def __init__(self, mode: int = TE):
+        self.mode = mode
+        z1, z2 = np.sqrt(1.0 / self.eps1), np.sqrt(1.0 / self.eps2)
+        self.z1, self.z2 = z1, z2
+        if mode == TE:
+            self.refl, self.tran = (z1 - z2) / (z1 + z2), 2 * z1 / (z1 + z2)
+        else:
+            self.refl, self.tran = (z2 - z1) / (z1 + z2), 2 * z2 / (z1 + z2)
+        hy = (self.hi[1] - self.lo[1]) / self.nel[1]
+        self.up_inner, self.up_outer = self.hi[1] - self.pml[0] * hy, self.hi[1]
+        self.lo_inner, self.lo_outer = self.lo[1] + self.pml[0] * hy, self.lo[1]
+
+    def regions(self, y, n3):
+        yc = np.repeat(np.asarray(y).reshape(-1, n3).mean(axis=1), n3)
+        return yc > 0.0, (yc > self.up_inner) | (yc < self.lo_inner)
+
+    def eps(self, y, n3):
+        up, _ = self.regions(y, n3)
+        return np.where(up, self.eps1, self.eps2)
+
+    def exact(self, x, y, z, t, n3):
+        up, inpml = self.regions(y, n3)
+        y = np.asarray(y)
+        eps = np.where(up, self.eps1, self.eps2)
+        eta, ky = np.sqrt(1.0 / eps), self.omega * np.sqrt(eps)
+        order, referr = self.pml[1], self.pml[2]
+        d_up = self.up_outer - self.up_inner
+        d_lo = self.lo_inner - self.lo_outer
+        with np.errstate(divide="ignore", invalid="ignore"):
+            f_up = (-(order + 1) * np.log(referr) / (2 * eta * d_up) * d_up / (order + 1)) * \
+                np.clip((y - self.up_inner) / d_up, 0, None) ** (order + 1)
+            f_lo = (-(order + 1) * np.log(referr) / (2 * eta * d_lo) * d_lo / (order + 1)) * \
+                np.clip((self.lo_inner - y) / d_lo, 0, None) ** (order + 1)
+        fac = np.where(inpml, np.where(up, f_up, f_lo), 0.0)
+        uu = np.where(up, self.refl * np.exp(-eta * fac) * np.cos(ky * y - self.omega * t),
+                      self.tran * np.exp(-eta * fac) * np.cos(-ky * y - self.omega * t))
+        zero = np.zeros_like(y)
+        if self.mode == TE:
+            H = np.stack([zero, zero, uu])
+            E = np.stack([np.where(up, -eta * uu, eta * uu), zero, zero])
+        else:
+            H = np.stack([np.where(up, uu / eta, -uu / eta), zero, zero])
+            E = np.stack([zero, zero, uu])
+        return H, E
+
+    def incident_slots(self, y, cemface, n3, nf):
+        up, _ = self.regions(y, n3)
+        y = np.asarray(y)
+        cf = np.asarray(cemface).reshape(-1, nf)
+        out = []
+        for f in range(cf.shape[0]):
+            nodes = cf[f]
+            if up[nodes[0]] and np.all(np.abs(y[nodes]) <= 1e-8):
+                out.extend(range(f * nf, (f + 1) * nf))
+        return np.array(out, dtype=np.int64)
+
+    def incident(self):
+        eta, ky = np.sqrt(1.0 / self.eps1), self.omega * np.sqrt(self.eps1)
+        if self.mode == TE:  # incfhz += u, incfex += eta u
+            return (0.0, 0.0, 1.0, eta, 0.0, 0.0), (0.0, -ky, 0.0), self.omega
+        return (-1.0 / eta, 0.0, 0.0, 0.0, 0.0, 1.0), (0.0, -ky, 0.0), self.omega
 
 
 class GrapheneSheet:
