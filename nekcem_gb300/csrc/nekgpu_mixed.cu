@@ -176,9 +176,13 @@ constexpr int round32(int a) { return (a + 31) / 32 * 32; }
 template <int NX>
 struct MCfg {
   static constexpr int N2 = NX * NX, N3 = N2 * NX;
-  // padded node layout i + RS*j + SZ*k: with NX=8 (RS=9, SZ=72) the warp's
-  // accesses along r- and s-lines hit 32 distinct banks
-  static constexpr int RS = NX + 1;
+  // Node layout of the FP32 pair arrays.  NX = 8: unpadded, node
+  // v = i + 8j + 64k stored at v ^ ((v >> 3) & 15) (low three bits i^j, bit 3
+  // j0^k0), so the 16 lanes of a half warp -- 8 lines or nodes of two
+  // neighbouring rows -- hit 16 distinct 8-byte bank pairs along r-, s- and
+  // t-lines, on every face and in node order.  Other NX: rows padded to NX+1.
+  static constexpr bool kSwz = (NX == 8);
+  static constexpr int RS = kSwz ? NX : NX + 1;
   static constexpr int SZ = RS * NX;
   static constexpr int N3P = NX * SZ;
   static constexpr int NF = 6 * N2;
@@ -189,13 +193,14 @@ struct MCfg {
   static constexpr int FPT = (NF + NT - 1) / NT;
   static constexpr int TPT = (NTASK + NT - 1) / NT;
   static constexpr bool kTma = (N3 % 2) == 0;
-  // the staged FP64 state is dead once split, so the residual pairs reuse
-  // its space: 74 KB at NX=8, three blocks per SM
+  // One area holds, in turn, the staged FP64 state (until the split), the
+  // partner face values parked for the flux (FP64) and the residual pairs:
+  // 54 KB in all at NX=8, four blocks per SM
   static constexpr size_t off_u64 = 0;
   static constexpr size_t off_R2 = 0;                       // float2 residual (hi, lo)
-  static constexpr size_t off_u2 = cmax(6 * N3 * 8, 6 * N3P * 8);  // float2 (uh, ul)
-  static constexpr size_t off_nb2 = off_u2 + 6 * N3P * 8;   // float2 partner (hi, lo); then flux in .x
-  static constexpr size_t off_wmax = off_nb2 + 6 * NF * 8;
+  static constexpr size_t off_u2 = cmax(cmax(6 * N3 * 8, 6 * N3P * 8), 6 * NF * 8);  // float2 (uh, ul)
+  static constexpr size_t off_F = off_u2 + 6 * N3P * 8;     // float flux [face][line slot][N2]
+  static constexpr size_t off_wmax = off_F + 24 * N2 * 4;
   static constexpr size_t off_E = off_wmax + NW * 6 * 4;
   static constexpr size_t off_bar = (off_E + 8 * 4 + 15) / 16 * 16;
   static constexpr size_t smem = off_bar + 16;
@@ -214,18 +219,28 @@ __constant__ const int kLineInit[3][4] = {{1, 1, 1, 1}, {0, 1, 0, 1}, {0, 0, 0, 
 template <int NX, int DIR>
 __device__ __forceinline__ int line_node(int a, int b, int l) {
   constexpr int RS = MCfg<NX>::RS, SZ = MCfg<NX>::SZ;
+  if constexpr (MCfg<NX>::kSwz) {
+    // node (l,a,b), (a,l,b) or (a,b,l) under the NX = 8 swizzle
+    if constexpr (DIR == 0) return (((a << 3) | (b << 6)) ^ ((b & 1) << 3)) | (l ^ a);
+    if constexpr (DIR == 1) return (a ^ l) | ((l ^ (b & 1)) << 3) | (b << 6);
+    return (a ^ b) | ((b ^ (l & 1)) << 3) | (l << 6);
+  }
   return DIR == 0 ? l + RS * a + SZ * b : (DIR == 1 ? a + RS * l + SZ * b : a + RS * b + SZ * l);
 }
 template <int NX>
-__device__ __forceinline__ int pnode(int v) {  // padded index of node v = i + NX*j + NX^2*k
+__device__ __forceinline__ int pnode(int v) {  // stored index of node v = i + NX*j + NX^2*k
+  if constexpr (MCfg<NX>::kSwz) return v ^ ((v >> 3) & 15);
   return (v % NX) + MCfg<NX>::RS * ((v / NX) % NX) + MCfg<NX>::SZ * (v / (NX * NX));
 }
 
 // One direction of the contraction: tasks (component, line) accumulate the
-// signed derivative pair into the residual pair arrays.
+// signed derivative pair into the residual pair arrays.  The line's two end
+// nodes lie on the faces normal to DIR; the lifted flux of those faces in the
+// task's residual component (s_F, stored in this direction's slot order) is
+// added to their low parts.
 template <int NX, int DIR>
-__device__ __forceinline__ void line_phase(const float2* s_u2, float2* s_R2, bool cubic, float rh,
-                                           float rl) {
+__device__ __forceinline__ void line_phase(const float2* s_u2, float2* s_R2, const float* s_F,
+                                           bool cubic, float rh, float rl) {
   using C = MCfg<NX>;
   const int tid = opaque_tid();
 #pragma unroll
@@ -238,6 +253,11 @@ __device__ __forceinline__ void line_phase(const float2* s_u2, float2* s_R2, boo
       const float sg = kLineSign[DIR][slot];
       const bool init = kLineInit[DIR][slot] != 0;
       const float2* pu = s_u2 + comp * C::N3P;
+      // lifted flux at the line's ends: faces 3|1 (r), 0|2 (s), 4|5 (t)
+      constexpr int FM = DIR == 0 ? 3 : (DIR == 1 ? 0 : 4);
+      constexpr int FP = DIR == 0 ? 1 : (DIR == 1 ? 2 : 5);
+      const float flux_m = s_F[(FM * 4 + slot) * C::N2 + lam];
+      const float flux_p = s_F[(FP * 4 + slot) * C::N2 + lam];
       float2 u[NX];
 #pragma unroll
       for (int l = 0; l < NX; ++l) u[l] = pu[line_node<NX, DIR>(la, lb, l)];
@@ -278,6 +298,8 @@ __device__ __forceinline__ void line_phase(const float2* s_u2, float2* s_R2, boo
         }
         h *= sg;
         r *= sg;
+        if (i == 0) r += flux_m;
+        if (i == NX - 1) r += flux_p;
         float2* Rp = R0 + line_node<NX, DIR>(la, lb, i);
         if (init) {
           *Rp = make_float2(h, r);
@@ -374,9 +396,16 @@ __device__ __forceinline__ void disp_node(const MixedDev& a, int l, int v, long 
   }
 }
 
-// EXT: the variant with the PML and dispersive-current branches
+// Blocks per SM the launch is built for: four of the unpadded NX = 8 layout
+// (54 KB, 64 registers), three otherwise and with the extension branches.
 template <int NX, bool EXT>
-__global__ void __launch_bounds__(MCfg<NX>::NT, 3) k_mixed_stage(const MixedDev a) {
+constexpr int mixed_min_blocks() { return (MCfg<NX>::kSwz && !EXT) ? 4 : 3; }
+
+// EXT: the variant with the PML, dispersive-current, incident-field and
+// graphene branches
+template <int NX, bool EXT>
+__global__ void __launch_bounds__(MCfg<NX>::NT, mixed_min_blocks<NX, EXT>())
+    k_mixed_stage(const MixedDev a) {
   using C = MCfg<NX>;
   constexpr int N2 = C::N2, N3 = C::N3, NT = C::NT, NF = C::NF, N3P = C::N3P;
   constexpr int NPT = C::NPT, FPT = C::FPT;
@@ -384,7 +413,7 @@ __global__ void __launch_bounds__(MCfg<NX>::NT, 3) k_mixed_stage(const MixedDev 
   double* s_u64 = reinterpret_cast<double*>(smem + C::off_u64);
   float2* s_u2 = reinterpret_cast<float2*>(smem + C::off_u2);
   float2* s_R2 = reinterpret_cast<float2*>(smem + C::off_R2);
-  float2* s_nb2 = reinterpret_cast<float2*>(smem + C::off_nb2);  // partner (hi, lo); then flux
+  float* s_F = reinterpret_cast<float*>(smem + C::off_F);
   unsigned* s_wmax = reinterpret_cast<unsigned*>(smem + C::off_wmax);
   unsigned* s_E = reinterpret_cast<unsigned*>(smem + C::off_E);
   uint64_t* bar = reinterpret_cast<uint64_t*>(smem + C::off_bar);
@@ -420,7 +449,7 @@ __global__ void __launch_bounds__(MCfg<NX>::NT, 3) k_mixed_stage(const MixedDev 
     int tid = opaque_tid();
     const int* nbr = a.nbr + 6 * e;
     const float* eg = a.egm + 12 * e;
-    // ---- early loads: partner face nodes, RK register and coefficients ----
+    // ---- early loads: partner face nodes (kept in registers until the flux)
     double nbv[FPT][6];
 #pragma unroll
     for (int q = 0; q < FPT; ++q) {
@@ -496,29 +525,20 @@ __global__ void __launch_bounds__(MCfg<NX>::NT, 3) k_mixed_stage(const MixedDev 
           }
         }
       }
-#pragma unroll
-      for (int q = 0; q < FPT; ++q) {
-        const int t = tid + q * NT;
-        if (t < NF && nbr[t / N2] >= 0) {
-#pragma unroll
-          for (int c = 0; c < 6; ++c)
-            s_nb2[c * NF + t] = make_float2(d2f_hi(nbv[q][c]), d2f_lo(nbv[q][c]));
-        }
-      }
     }
     __syncthreads();
-    // ---- contractions: r, s, t lines ----------------------------------------
-    {
-      const bool cubic = eg[10] != 0.0f;
-      const float r1h = eg[0], r1l = eg[1], r2h = eg[2], r2l = eg[3];
-      line_phase<NX, 0>(s_u2, s_R2, cubic, 0.0f, 0.0f);
-      __syncthreads();
-      line_phase<NX, 1>(s_u2, s_R2, cubic, r1h, r1l);
-      __syncthreads();
-      line_phase<NX, 2>(s_u2, s_R2, cubic, r2h, r2l);
-    }
-    // ---- upwind flux per face node (same interval: reads uh/ul, writes nbh) -
+    // ---- upwind flux per face node, lifted, into s_F ------------------------
+    // The partner values are parked in the dead FP64 staging area (each thread
+    // reads back only what it wrote) to keep the flux's registers free.
     tid = opaque_tid();
+    double* s_nbv = s_u64;
+#pragma unroll
+    for (int q = 0; q < FPT; ++q) {
+      const int t = tid + q * NT;
+      if (t < NF && nbr[t / N2] >= 0)
+#pragma unroll
+        for (int c = 0; c < 6; ++c) s_nbv[c * NF + t] = nbv[q][c];
+    }
 #pragma unroll
     for (int q = 0; q < FPT; ++q) {
       const int t = tid + q * NT;
@@ -532,9 +552,9 @@ __global__ void __launch_bounds__(MCfg<NX>::NT, 3) k_mixed_stage(const MixedDev 
         for (int c = 0; c < 3; ++c) {
           const float2 h = s_u2[c * N3P + pv], ev = s_u2[(c + 3) * N3P + pv];
           if (pe >= 0) {  // jump = (partner_hi - own_hi) + (partner_lo - own_lo)
-            const float2 ph = s_nb2[c * NF + t], pE = s_nb2[(c + 3) * NF + t];
-            dH[c] = (ph.x - h.x) + (ph.y - h.y);
-            dE[c] = (pE.x - ev.x) + (pE.y - ev.y);
+            const double ph = s_nbv[c * NF + t], pE = s_nbv[(c + 3) * NF + t];
+            dH[c] = (d2f_hi(ph) - h.x) + (d2f_lo(ph) - h.y);
+            dE[c] = (d2f_hi(pE) - ev.x) + (d2f_lo(pE) - ev.y);
           } else {  // PEC mirror: H+ = H-, E+ = -E-
             dH[c] = 0.0f;
             dE[c] = -2.0f * (ev.x + ev.y);
@@ -571,12 +591,8 @@ __global__ void __launch_bounds__(MCfg<NX>::NT, 3) k_mixed_stage(const MixedDev 
               const float2 h = s_u2[c * N3P + pv], ev = s_u2[(c + 3) * N3P + pv];
               fhm[c] = f2d(h.x) + f2d(h.y);
               fem[c] = f2d(ev.x) + f2d(ev.y);
-              fhp[c] = fep[c] = 0.0;
-              if (pe >= 0) {
-                const float2 ph = s_nb2[c * NF + t], pE = s_nb2[(c + 3) * NF + t];
-                fhp[c] = f2d(ph.x) + f2d(ph.y);
-                fep[c] = f2d(pE.x) + f2d(pE.y);
-              }
+              fhp[c] = pe >= 0 ? s_nbv[c * NF + t] : 0.0;
+              fep[c] = pe >= 0 ? s_nbv[(c + 3) * NF + t] : 0.0;
               if (io >= 0) {
                 const double* iv = a.inc_val + (long)io * 12 * NF + t;
                 fhm[c] += iv[c * NF];
@@ -603,63 +619,55 @@ __global__ void __launch_bounds__(MCfg<NX>::NT, 3) k_mixed_stage(const MixedDev 
         const float sg = (float)slot_side(f);
         const float lf = eg[4 + f];  // area / (bm1 * 2/hx) at this face
         const float sY = sg * Y02, sZ = sg * Z02;
-        float fH[3], fE[3];
+        // the four tangential components, in the line slot order of the
+        // face's direction (residuals 5,4,2,1 | 5,3,2,0 | 4,3,1,0)
+        float F0, F1, F2, F3;
         switch (slot_axis(f)) {
           case 0:
-            fH[0] = 0.0f;
-            fH[1] = fmaf(-sY, dE[2], C02Y * dH[1]);
-            fH[2] = fmaf(sY, dE[1], C02Y * dH[2]);
-            fE[0] = 0.0f;
-            fE[1] = fmaf(-sZ, dH[2], C02Z * dE[1]);
-            fE[2] = fmaf(sZ, dH[1], C02Z * dE[2]);
+            F0 = fmaf(sZ, dH[1], C02Z * dE[2]);   // E3
+            F1 = fmaf(-sZ, dH[2], C02Z * dE[1]);  // E2
+            F2 = fmaf(sY, dE[1], C02Y * dH[2]);   // H3
+            F3 = fmaf(-sY, dE[2], C02Y * dH[1]);  // H2
             break;
           case 1:
-            fH[0] = fmaf(sY, dE[2], C02Y * dH[0]);
-            fH[1] = 0.0f;
-            fH[2] = fmaf(-sY, dE[0], C02Y * dH[2]);
-            fE[0] = fmaf(sZ, dH[2], C02Z * dE[0]);
-            fE[1] = 0.0f;
-            fE[2] = fmaf(-sZ, dH[0], C02Z * dE[2]);
+            F0 = fmaf(-sZ, dH[0], C02Z * dE[2]);  // E3
+            F1 = fmaf(sZ, dH[2], C02Z * dE[0]);   // E1
+            F2 = fmaf(-sY, dE[0], C02Y * dH[2]);  // H3
+            F3 = fmaf(sY, dE[2], C02Y * dH[0]);   // H1
             break;
           default:
-            fH[0] = fmaf(-sY, dE[1], C02Y * dH[0]);
-            fH[1] = fmaf(sY, dE[0], C02Y * dH[1]);
-            fH[2] = 0.0f;
-            fE[0] = fmaf(-sZ, dH[1], C02Z * dE[0]);
-            fE[1] = fmaf(sZ, dH[0], C02Z * dE[1]);
-            fE[2] = 0.0f;
+            F0 = fmaf(sZ, dH[0], C02Z * dE[1]);   // E2
+            F1 = fmaf(-sZ, dH[1], C02Z * dE[0]);  // E1
+            F2 = fmaf(sY, dE[0], C02Y * dH[1]);   // H2
+            F3 = fmaf(-sY, dE[1], C02Y * dH[0]);  // H1
             break;
         }
-#pragma unroll
-        for (int c = 0; c < 3; ++c) {
-          s_nb2[c * NF + t].x = lf * fH[c];
-          s_nb2[(c + 3) * NF + t].x = lf * fE[c];
-        }
-      }
-    }
-    // RK register and coefficients, loaded late to keep registers free above
-    tid = opaque_tid();
-    double kv[NPT][6];
-    float2 cv[NPT][2];
-#pragma unroll
-    for (int q = 0; q < NPT; ++q) {
-      const int v = tid + q * NT;
-      if (v < N3) {
-        const long g = (long)e * N3 + v;
-        if (!first_stage) {
-#pragma unroll
-          for (int c = 0; c < 6; ++c) kv[q][c] = a.k[c * P + g];
-        }
-        cv[q][0] = a.coef[g];
-        cv[q][1] = a.coef[P + g];
+        float* Fp = s_F + f * 4 * N2 + ab;
+        Fp[0] = lf * F0;
+        Fp[N2] = lf * F1;
+        Fp[2 * N2] = lf * F2;
+        Fp[3 * N2] = lf * F3;
       }
     }
     __syncthreads();
-    // ---- lift, source, inverse mass, RK update --------------------------------
+    // ---- contractions (and lift): r, s, t lines --------------------------------
+    {
+      const bool cubic = eg[10] != 0.0f;
+      const float r1h = eg[0], r1l = eg[1], r2h = eg[2], r2l = eg[3];
+      line_phase<NX, 0>(s_u2, s_R2, s_F, cubic, 0.0f, 0.0f);
+      __syncthreads();
+      line_phase<NX, 1>(s_u2, s_R2, s_F, cubic, r1h, r1l);
+      __syncthreads();
+      line_phase<NX, 2>(s_u2, s_R2, s_F, cubic, r2h, r2l);
+    }
+    tid = opaque_tid();
+    __syncthreads();
+    // ---- source, inverse mass, RK update ----------------------------------------
     // The state is read again from global memory (an L2 hit: this element's
-    // block was copied in at the start of its turn).  Every read of the
-    // residual pairs happens before the barrier that lets the next element's
-    // TMA overwrite them.
+    // block was copied in at the start of its turn), the RK register and the
+    // coefficients (prefetched into L2 with the TMA) node by node.  Every read
+    // of the residual pairs happens before the barrier that lets the next
+    // element's TMA overwrite them.
     const int so = a.src_elem ? a.src_elem[e] : -1;
     const int pml_l = (EXT && a.pml.slot) ? a.pml.slot[e] : -1;
     const int disp_l = (EXT && a.disp.slot) ? a.disp.slot[e] : -1;
@@ -667,7 +675,6 @@ __global__ void __launch_bounds__(MCfg<NX>::NT, 3) k_mixed_stage(const MixedDev 
     for (int q = 0; q < NPT; ++q) {
       const int v = tid + q * NT;
       if (v >= N3) continue;
-      const int i = v % NX, j = (v / NX) % NX, k = v / N2;
       const int pv = pnode<NX>(v);
       float Rh[6], Rl[6];
 #pragma unroll
@@ -676,22 +683,17 @@ __global__ void __launch_bounds__(MCfg<NX>::NT, 3) k_mixed_stage(const MixedDev 
         Rh[c] = rr.x;
         Rl[c] = rr.y;
       }
-      auto add = [&](int f, int ab) {
-#pragma unroll
-        for (int c = 0; c < 6; ++c) Rl[c] += s_nb2[c * NF + f * N2 + ab].x;
-      };
-      if (j == 0) add(0, i + NX * k);
-      if (i == NX - 1) add(1, j + NX * k);
-      if (j == NX - 1) add(2, i + NX * k);
-      if (i == 0) add(3, j + NX * k);
-      if (k == 0) add(4, i + NX * j);
-      if (k == NX - 1) add(5, i + NX * j);
       if (EXT && pml_l >= 0) pml_node<N3>(a, pml_l, v, (long)e * N3 + v, first_stage, Rh, Rl);
       if (EXT && disp_l >= 0) disp_node<N3>(a, disp_l, v, (long)e * N3 + v, first_stage, Rh, Rl);
       if (so >= 0) Rl[5] = fmaf(a.src_w[(long)so * N3 + v], a.src_ftf, Rl[5]);
-      const float chh = cv[q][0].x, chl = cv[q][0].y;
-      const float ceh = cv[q][1].x, cel = cv[q][1].y;
       const long g = (long)e * N3 + v;
+      double kv[6];
+      if (!first_stage)
+#pragma unroll
+        for (int c = 0; c < 6; ++c) kv[c] = a.k[c * P + g];
+      const float2 cvh = a.coef[g], cve = a.coef[P + g];
+      const float chh = cvh.x, chl = cvh.y;
+      const float ceh = cve.x, cel = cve.y;
 #pragma unroll
       for (int c = 0; c < 6; ++c) {
         const float ch = c < 3 ? chh : ceh, cl = c < 3 ? chl : cel;
@@ -700,7 +702,7 @@ __global__ void __launch_bounds__(MCfg<NX>::NT, 3) k_mixed_stage(const MixedDev 
         ee = fmaf(ch, Rl[c], ee);
         ee = fmaf(cl, Rh[c], ee);
         const double r = f2d(p) + f2d(ee);
-        const double kn = first_stage ? r : fma(a.a, kv[q][c], r);
+        const double kn = first_stage ? r : fma(a.a, kv[c], r);
         a.k[c * P + g] = kn;
         a.u_out[c * P + g] = fma(a.b, kn, __ldg(a.u_in + c * P + g));
       }
