@@ -193,6 +193,13 @@ struct MCfg {
   static constexpr int FPT = (NF + NT - 1) / NT;
   static constexpr int TPT = (NTASK + NT - 1) / NT;
   static constexpr bool kTma = (N3 % 2) == 0;
+  // Where the components finish (inverse mass, RK update) without the
+  // extension terms: true = the t-line tasks finish H1, H2, E1, E2 on their
+  // lines and H3, E3 (no t-derivative) finish beside them, with no barrier and
+  // no residual round trip; false = node by node after the t-lines (NX = 8:
+  // at 64 registers the t-line tasks cannot cover the loads of eight finishes;
+  // measured 3 % slower there, 20 % faster at NX = 6).
+  static constexpr bool kFin = !kSwz;
   // One area holds, in turn, the staged FP64 state (until the split), the
   // partner face values parked for the flux (FP64) and the residual pairs:
   // 54 KB in all at NX=8, four blocks per SM
@@ -233,14 +240,38 @@ __device__ __forceinline__ int pnode(int v) {  // stored index of node v = i + N
   return (v % NX) + MCfg<NX>::RS * ((v / NX) % NX) + MCfg<NX>::SZ * (v / (NX * NX));
 }
 
+// Inverse mass and RK update of one component c at global node g, in FP64,
+// from the normalised residual pair (Rh, Rl): the pair times the dt-scaled
+// FP64 coefficient as a float-float product, rounded to FP64 once (DADD),
+// then k = a k + r and u = u + b k (two DFMA; one at stage 1).  The state is
+// read again from global memory (an L2 hit: the element's block was copied in
+// at the start of its turn), the RK register and the coefficients were
+// prefetched into L2 with that copy.
+__device__ __forceinline__ void rk_finish(const MixedDev& a, int c, long g, float Rh, float Rl,
+                                          bool first_stage) {
+  const long P = a.npts;
+  const float2 cf = a.coef[(c < 3 ? 0 : P) + g];
+  const float p = cf.x * Rh;
+  float ee = fmaf(cf.x, Rh, -p);
+  ee = fmaf(cf.x, Rl, ee);
+  ee = fmaf(cf.y, Rh, ee);
+  const double r = f2d(p) + f2d(ee);
+  const double kn = first_stage ? r : fma(a.a, a.k[c * P + g], r);
+  a.k[c * P + g] = kn;
+  a.u_out[c * P + g] = fma(a.b, kn, __ldg(a.u_in + c * P + g));
+}
+
 // One direction of the contraction: tasks (component, line) accumulate the
 // signed derivative pair into the residual pair arrays.  The line's two end
 // nodes lie on the faces normal to DIR; the lifted flux of those faces in the
 // task's residual component (s_F, stored in this direction's slot order) is
-// added to their low parts.
-template <int NX, int DIR>
+// added to their low parts.  FIN (last direction): the residual of the
+// task's component is complete at the line's nodes, so the task finishes
+// them (inverse mass, RK update) instead of storing the pairs.
+template <int NX, int DIR, bool FIN>
 __device__ __forceinline__ void line_phase(const float2* s_u2, float2* s_R2, const float* s_F,
-                                           bool cubic, float rh, float rl) {
+                                           bool cubic, float rh, float rl, const MixedDev& a,
+                                           int e, bool first_stage) {
   using C = MCfg<NX>;
   const int tid = opaque_tid();
 #pragma unroll
@@ -301,7 +332,14 @@ __device__ __forceinline__ void line_phase(const float2* s_u2, float2* s_R2, con
         if (i == 0) r += flux_m;
         if (i == NX - 1) r += flux_p;
         float2* Rp = R0 + line_node<NX, DIR>(la, lb, i);
-        if (init) {
+        if (FIN) {
+          const float2 old = *Rp;
+          float sum, err;
+          two_sum(old.x, h, sum, err);
+          const int vol = DIR == 0 ? i + NX * la + C::N2 * lb
+                                   : (DIR == 1 ? la + NX * i + C::N2 * lb : la + NX * lb + C::N2 * i);
+          rk_finish(a, rt, (long)e * C::N3 + vol, sum, (old.y + r) + err, first_stage);
+        } else if (init) {
           *Rp = make_float2(h, r);
         } else {
           const float2 old = *Rp;
@@ -409,6 +447,7 @@ __global__ void __launch_bounds__(MCfg<NX>::NT, mixed_min_blocks<NX, EXT>())
   using C = MCfg<NX>;
   constexpr int N2 = C::N2, N3 = C::N3, NT = C::NT, NF = C::NF, N3P = C::N3P;
   constexpr int NPT = C::NPT, FPT = C::FPT;
+  constexpr bool FIN = !EXT && C::kFin;  // the extension terms need all six at a node
   extern __shared__ __align__(16) unsigned char smem[];
   double* s_u64 = reinterpret_cast<double*>(smem + C::off_u64);
   float2* s_u2 = reinterpret_cast<float2*>(smem + C::off_u2);
@@ -654,57 +693,57 @@ __global__ void __launch_bounds__(MCfg<NX>::NT, mixed_min_blocks<NX, EXT>())
     {
       const bool cubic = eg[10] != 0.0f;
       const float r1h = eg[0], r1l = eg[1], r2h = eg[2], r2l = eg[3];
-      line_phase<NX, 0>(s_u2, s_R2, s_F, cubic, 0.0f, 0.0f);
+      line_phase<NX, 0, false>(s_u2, s_R2, s_F, cubic, 0.0f, 0.0f, a, e, first_stage);
       __syncthreads();
-      line_phase<NX, 1>(s_u2, s_R2, s_F, cubic, r1h, r1l);
+      line_phase<NX, 1, false>(s_u2, s_R2, s_F, cubic, r1h, r1l, a, e, first_stage);
       __syncthreads();
-      line_phase<NX, 2>(s_u2, s_R2, s_F, cubic, r2h, r2l);
+      // without the extension terms each component can finish on its own
+      // (MCfg::kFin): H3, E3 (no t-derivative) are complete since the s-lines
+      line_phase<NX, 2, FIN>(s_u2, s_R2, s_F, cubic, r2h, r2l, a, e, first_stage);
     }
-    tid = opaque_tid();
-    __syncthreads();
-    // ---- source, inverse mass, RK update ----------------------------------------
-    // The state is read again from global memory (an L2 hit: this element's
-    // block was copied in at the start of its turn), the RK register and the
-    // coefficients (prefetched into L2 with the TMA) node by node.  Every read
-    // of the residual pairs happens before the barrier that lets the next
-    // element's TMA overwrite them.
-    const int so = a.src_elem ? a.src_elem[e] : -1;
-    const int pml_l = (EXT && a.pml.slot) ? a.pml.slot[e] : -1;
-    const int disp_l = (EXT && a.disp.slot) ? a.disp.slot[e] : -1;
+    if constexpr (FIN) {
+      tid = opaque_tid();
+      const int so = a.src_elem ? a.src_elem[e] : -1;
+      constexpr int NPT2 = (2 * N3 + NT - 1) / NT;
 #pragma unroll
-    for (int q = 0; q < NPT; ++q) {
-      const int v = tid + q * NT;
-      if (v >= N3) continue;
-      const int pv = pnode<NX>(v);
-      float Rh[6], Rl[6];
-#pragma unroll
-      for (int c = 0; c < 6; ++c) {
-        const float2 rr = s_R2[c * N3P + pv];
-        Rh[c] = rr.x;
-        Rl[c] = rr.y;
+      for (int q = 0; q < NPT2; ++q) {
+        const int w = tid + q * NT;
+        if (w < 2 * N3) {
+          const int c = w < N3 ? 2 : 5;
+          const int v = w < N3 ? w : w - N3;
+          const float2 rr = s_R2[c * N3P + pnode<NX>(v)];
+          float Rl = rr.y;
+          if (c == 5 && so >= 0) Rl = fmaf(a.src_w[(long)so * N3 + v], a.src_ftf, Rl);
+          rk_finish(a, c, (long)e * N3 + v, rr.x, Rl, first_stage);
+        }
       }
-      if (EXT && pml_l >= 0) pml_node<N3>(a, pml_l, v, (long)e * N3 + v, first_stage, Rh, Rl);
-      if (EXT && disp_l >= 0) disp_node<N3>(a, disp_l, v, (long)e * N3 + v, first_stage, Rh, Rl);
-      if (so >= 0) Rl[5] = fmaf(a.src_w[(long)so * N3 + v], a.src_ftf, Rl[5]);
-      const long g = (long)e * N3 + v;
-      double kv[6];
-      if (!first_stage)
+    }
+    if constexpr (!FIN) {
+      tid = opaque_tid();
+      __syncthreads();
+      // ---- source, inverse mass, RK update ----------------------------------------
+      // All six components of a node at once (the PML and dispersive terms
+      // couple them to the node's auxiliary fields).
+      const int so = a.src_elem ? a.src_elem[e] : -1;
+      const int pml_l = (EXT && a.pml.slot) ? a.pml.slot[e] : -1;
+      const int disp_l = (EXT && a.disp.slot) ? a.disp.slot[e] : -1;
 #pragma unroll
-        for (int c = 0; c < 6; ++c) kv[c] = a.k[c * P + g];
-      const float2 cvh = a.coef[g], cve = a.coef[P + g];
-      const float chh = cvh.x, chl = cvh.y;
-      const float ceh = cve.x, cel = cve.y;
+      for (int q = 0; q < NPT; ++q) {
+        const int v = tid + q * NT;
+        if (v >= N3) continue;
+        const int pv = pnode<NX>(v);
+        float Rh[6], Rl[6];
 #pragma unroll
-      for (int c = 0; c < 6; ++c) {
-        const float ch = c < 3 ? chh : ceh, cl = c < 3 ? chl : cel;
-        const float p = ch * Rh[c];
-        float ee = fmaf(ch, Rh[c], -p);
-        ee = fmaf(ch, Rl[c], ee);
-        ee = fmaf(cl, Rh[c], ee);
-        const double r = f2d(p) + f2d(ee);
-        const double kn = first_stage ? r : fma(a.a, kv[c], r);
-        a.k[c * P + g] = kn;
-        a.u_out[c * P + g] = fma(a.b, kn, __ldg(a.u_in + c * P + g));
+        for (int c = 0; c < 6; ++c) {
+          const float2 rr = s_R2[c * N3P + pv];
+          Rh[c] = rr.x;
+          Rl[c] = rr.y;
+        }
+        if (EXT && pml_l >= 0) pml_node<N3>(a, pml_l, v, (long)e * N3 + v, first_stage, Rh, Rl);
+        if (EXT && disp_l >= 0) disp_node<N3>(a, disp_l, v, (long)e * N3 + v, first_stage, Rh, Rl);
+        if (so >= 0) Rl[5] = fmaf(a.src_w[(long)so * N3 + v], a.src_ftf, Rl[5]);
+#pragma unroll
+        for (int c = 0; c < 6; ++c) rk_finish(a, c, (long)e * N3 + v, Rh[c], Rl[c], first_stage);
       }
     }
     __syncthreads();  // staged u consumed: the next element may land
