@@ -200,13 +200,14 @@ struct MCfg {
   // at 64 registers the t-line tasks cannot cover the loads of eight finishes;
   // measured 3 % slower there, 20 % faster at NX = 6).
   static constexpr bool kFin = !kSwz;
-  // One area holds, in turn, the staged FP64 state (until the split), the
-  // partner face values parked for the flux (FP64) and the residual pairs:
-  // 54 KB in all at NX=8, four blocks per SM
-  static constexpr size_t off_u64 = 0;
-  static constexpr size_t off_R2 = 0;                       // float2 residual (hi, lo)
-  static constexpr size_t off_u2 = cmax(cmax(6 * N3 * 8, 6 * N3P * 8), 6 * NF * 8);  // float2 (uh, ul)
-  static constexpr size_t off_F = off_u2 + 6 * N3P * 8;     // float flux [face][line slot][N2]
+  // Two areas of SA bytes swap roles from one element to the next.  One holds,
+  // in turn, the staged FP64 state (until the split), the partner face values
+  // parked for the flux (FP64) and the residual pairs (hi, lo); the other the
+  // split pairs (uh, ul), dead after the t-lines, so the next element's state
+  // can land there while this one is finished.  54 KB in all at NX=8, four
+  // blocks per SM.
+  static constexpr size_t SA = cmax(cmax(6 * N3 * 8, 6 * N3P * 8), 6 * NF * 8);
+  static constexpr size_t off_F = 2 * SA;                   // float flux [face][line slot][N2]
   static constexpr size_t off_wmax = off_F + 24 * N2 * 4;
   static constexpr size_t off_E = off_wmax + NW * 6 * 4;
   static constexpr size_t off_bar = (off_E + 8 * 4 + 15) / 16 * 16;
@@ -449,9 +450,6 @@ __global__ void __launch_bounds__(MCfg<NX>::NT, mixed_min_blocks<NX, EXT>())
   constexpr int NPT = C::NPT, FPT = C::FPT;
   constexpr bool FIN = !EXT && C::kFin;  // the extension terms need all six at a node
   extern __shared__ __align__(16) unsigned char smem[];
-  double* s_u64 = reinterpret_cast<double*>(smem + C::off_u64);
-  float2* s_u2 = reinterpret_cast<float2*>(smem + C::off_u2);
-  float2* s_R2 = reinterpret_cast<float2*>(smem + C::off_R2);
   float* s_F = reinterpret_cast<float*>(smem + C::off_F);
   unsigned* s_wmax = reinterpret_cast<unsigned*>(smem + C::off_wmax);
   unsigned* s_E = reinterpret_cast<unsigned*>(smem + C::off_E);
@@ -471,10 +469,12 @@ __global__ void __launch_bounds__(MCfg<NX>::NT, mixed_min_blocks<NX, EXT>())
     }
   }
   __syncthreads();
-  auto issue_tma = [&](int e) {
+  // element e's state into area `into`
+  auto issue_tma = [&](int e, int into) {
     const unsigned bytes = N3 * 8;
+    double* dst = reinterpret_cast<double*>(smem + into * C::SA);
     mbar_expect_tx(bar, 6u * bytes);
-    for (int c = 0; c < 6; ++c) tma_load_1d(s_u64 + c * N3, a.u_in + c * P + (long)e * N3, bytes, bar);
+    for (int c = 0; c < 6; ++c) tma_load_1d(dst + c * N3, a.u_in + c * P + (long)e * N3, bytes, bar);
     // the RK register and the coefficients are read at the end of the
     // element's turn: start bringing them into L2 now
     if (!first_stage)
@@ -482,10 +482,15 @@ __global__ void __launch_bounds__(MCfg<NX>::NT, mixed_min_blocks<NX, EXT>())
     for (int c = 0; c < 2; ++c) prefetch_l2(a.coef + c * P + (long)e * N3, N3 * 8u);
   };
   unsigned parity = 0;
-  if (C::kTma && tid == 0 && blockIdx.x < a.nelt) issue_tma(blockIdx.x);
+  int buf = 0;  // area of the element's staged state and residual pairs
+  if (C::kTma && tid == 0 && blockIdx.x < a.nelt) issue_tma(blockIdx.x, 0);
 
-  for (int e = blockIdx.x; e < a.nelt; e += gridDim.x) {
+  for (int e = blockIdx.x; e < a.nelt; e += gridDim.x, buf ^= 1) {
     int tid = opaque_tid();
+    double* s_u64 = reinterpret_cast<double*>(smem + buf * C::SA);
+    float2* s_R2 = reinterpret_cast<float2*>(smem + buf * C::SA);
+    float2* s_u2 = reinterpret_cast<float2*>(smem + (buf ^ 1) * C::SA);
+    const int en = e + gridDim.x;
     const int* nbr = a.nbr + 6 * e;
     const float* eg = a.egm + 12 * e;
     // ---- early loads: partner face nodes (kept in registers until the flux)
@@ -717,10 +722,21 @@ __global__ void __launch_bounds__(MCfg<NX>::NT, mixed_min_blocks<NX, EXT>())
           rk_finish(a, c, (long)e * N3 + v, rr.x, Rl, first_stage);
         }
       }
-    }
-    if constexpr (!FIN) {
+      __syncthreads();  // the split pairs are consumed: the next element may land
+      if (C::kTma && tid == 0 && en < a.nelt) {
+        fence_proxy_async_smem();
+        issue_tma(en, buf ^ 1);
+      }
+    } else {
       tid = opaque_tid();
       __syncthreads();
+      // the split pairs are consumed: the next element's state lands in their
+      // area while this one finishes (the next element's own barriers order
+      // these reads of the residual pairs before its split overwrites them)
+      if (C::kTma && tid == 0 && en < a.nelt) {
+        fence_proxy_async_smem();
+        issue_tma(en, buf ^ 1);
+      }
       // ---- source, inverse mass, RK update ----------------------------------------
       // All six components of a node at once (the PML and dispersive terms
       // couple them to the node's auxiliary fields).
@@ -745,12 +761,6 @@ __global__ void __launch_bounds__(MCfg<NX>::NT, mixed_min_blocks<NX, EXT>())
 #pragma unroll
         for (int c = 0; c < 6; ++c) rk_finish(a, c, (long)e * N3 + v, Rh[c], Rl[c], first_stage);
       }
-    }
-    __syncthreads();  // staged u consumed: the next element may land
-    const int en = e + gridDim.x;
-    if (C::kTma && tid == 0 && en < a.nelt) {
-      fence_proxy_async_smem();
-      issue_tma(en);
     }
   }
 }
