@@ -553,19 +553,25 @@ __global__ void __launch_bounds__(MCfg<NX>::NT, mixed_min_blocks<NX, EXT>())
     tid = opaque_tid();
     {
       const float M = 12582912.0f;  // 1.5 * 2^23: float rounding to integers
+      unsigned Ec[6];
 #pragma unroll
-      for (int c = 0; c < 6; ++c) {
-        const int E = (int)s_E[c];
-        const float qv = __int_as_float((E - 905) << 23);    // 2^(E-1032)
-        const float qi = __int_as_float((1159 - E) << 23);   // 2^(1032-E)
+      for (int c = 0; c < 6; ++c) Ec[c] = s_E[c];
 #pragma unroll
-        for (int q = 0; q < NPT; ++q) {
-          const int v = tid + q * NT;
-          if (v < N3) {
-            const double u = s_u64[c * N3 + v];
-            const float uf = d2f_hi(u), ulo = d2f_lo(u);
+      for (int q = 0; q < NPT; ++q) {
+        const int v = tid + q * NT;
+        if (v < N3) {
+          double u[6];  // loaded before any store (which they could not pass)
+#pragma unroll
+          for (int c = 0; c < 6; ++c) u[c] = s_u64[c * N3 + v];
+          const int pv = pnode<NX>(v);
+#pragma unroll
+          for (int c = 0; c < 6; ++c) {
+            const int E = (int)Ec[c];
+            const float qv = __int_as_float((E - 905) << 23);    // 2^(E-1032)
+            const float qi = __int_as_float((1159 - E) << 23);   // 2^(1032-E)
+            const float uf = d2f_hi(u[c]), ulo = d2f_lo(u[c]);
             const float uh = (__fadd_rn(__fmaf_rn(uf, qi, M), -M)) * qv;
-            s_u2[c * N3P + pnode<NX>(v)] = make_float2(uh, __fadd_rn(__fsub_rn(uf, uh), ulo));
+            s_u2[c * N3P + pv] = make_float2(uh, __fadd_rn(__fsub_rn(uf, uh), ulo));
           }
         }
       }
