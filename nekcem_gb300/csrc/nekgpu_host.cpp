@@ -229,9 +229,18 @@ void free_all(Context* c) {
   c->alloc_bytes.clear();
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
+  for (cudaEvent_t e : c->chunk_in)
+    if (e) cudaEventDestroy(e);
+  for (cudaEvent_t e : c->chunk_done)
+    if (e) cudaEventDestroy(e);
+  for (cudaEvent_t& e : c->chunk_fence)
+    if (e) cudaEventDestroy(e), e = nullptr;
+  if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
   if (c->stream) cudaStreamDestroy(c->stream);
+  c->chunk_in.clear();
+  c->chunk_done.clear();
   c->ev0 = c->ev1 = nullptr;
-  c->stream = nullptr;
+  c->copy_stream = c->stream = nullptr;
 }
 
 // ---------------------------------------------------------------------------
@@ -1177,6 +1186,111 @@ int plain_stage(Context* c, int rkstep, double time, double dt) {
   return plain_pml_rk_update(c, c->rk_a[rkstep - 1], c->rk_b[rkstep - 1], dt);
 }
 
+// ---------------------------------------------------------------------------
+// One RK step on host fields with the copies overlapped (mixed form).
+// The elements are cut into up to eight contiguous chunks of whole waves of
+// the stage kernel's blocks.  The state is copied in chunk by chunk on a copy
+// stream; stage 1 of a chunk waits only for the copies of the chunks holding
+// its elements' face partners (periodic wrap-around included), stage 5 runs
+// chunk by chunk and each chunk is copied back as soon as it is done.  The
+// kernels, their inputs and so the results are those of the plain sequence
+// copy in, five stages, copy out.
+// ---------------------------------------------------------------------------
+bool chunked_step_applies(Context* c) {
+  if (c->form != NEKGPU_MIXED || c->ndim != 3 || c->curved || c->host_nbr.empty()) return false;
+  const MixedDev& m = c->margs;
+  if (m.pml.slot || m.disp.slot || m.inc_elem || m.gr.elem) return false;
+  if (c->chunk_begin.empty()) {
+    // chunks of whole waves of the stage kernel's persistent grid (known
+    // after a first launch), so that no chunk launch ends in a partial wave
+    // but the last
+    const int wave = c->fused_grid > 0 ? c->fused_grid : 0;
+    if (wave <= 0) return false;
+    const int waves = (c->nelt + wave - 1) / wave;
+    const int per = (waves + 7) / 8;  // waves per chunk: at most eight chunks
+    const int nch = (waves + per - 1) / per;
+    if (nch < 2) return false;
+    c->chunk_begin.resize(nch + 1);
+    for (int k = 0; k <= nch; ++k) c->chunk_begin[k] = (int)std::min<long>(c->nelt, (long)k * per * wave);
+    std::vector<int> owner(c->nelt);
+    for (int k = 0; k < nch; ++k)
+      for (int e = c->chunk_begin[k]; e < c->chunk_begin[k + 1]; ++e) owner[e] = k;
+    c->chunk_wait.assign(nch, 0);
+    for (int k = 0; k < nch; ++k) {
+      int w = k;
+      for (int e = c->chunk_begin[k]; e < c->chunk_begin[k + 1]; ++e)
+        for (int f = 0; f < 6; ++f) {
+          const int p = c->host_nbr[6 * (long)e + f];
+          if (p >= 0) w = std::max(w, owner[p]);
+        }
+      c->chunk_wait[k] = w;
+    }
+    c->chunk_order.resize(nch);
+    for (int k = 0; k < nch; ++k) c->chunk_order[k] = k;
+    std::stable_sort(c->chunk_order.begin(), c->chunk_order.end(),
+                     [&](int x, int y) { return c->chunk_wait[x] < c->chunk_wait[y]; });
+    c->chunk_in.assign(nch, nullptr);
+    c->chunk_done.assign(nch, nullptr);
+    for (int k = 0; k < nch; ++k)
+      if (check_cuda(cudaEventCreateWithFlags(&c->chunk_in[k], cudaEventDisableTiming)) ||
+          check_cuda(cudaEventCreateWithFlags(&c->chunk_done[k], cudaEventDisableTiming)))
+        return false;
+    for (cudaEvent_t& e : c->chunk_fence)
+      if (check_cuda(cudaEventCreateWithFlags(&e, cudaEventDisableTiming))) return false;
+    if (check_cuda(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking))) return false;
+  }
+  return c->copy_stream != nullptr;
+}
+
+int chunked_step(Context* c, double* hn, double* en, long ld, double time, double dt) {
+  const int nch = (int)c->chunk_begin.size() - 1;
+  const long N3 = (long)c->nx * c->nx * c->nx;
+  const size_t pitch = ld * sizeof(double), w = c->npts * sizeof(double);
+  // the copy stream must not overwrite the state before earlier work on it is done
+  if (check_cuda(cudaEventRecord(c->chunk_fence[0], c->stream)) ||
+      check_cuda(cudaStreamWaitEvent(c->copy_stream, c->chunk_fence[0], 0)))
+    return NEKGPU_ERR_CUDA;
+  double* u = state(c);
+  for (int k = 0; k < nch; ++k) {
+    const long off = c->chunk_begin[k] * N3;
+    const size_t bytes = (c->chunk_begin[k + 1] - c->chunk_begin[k]) * N3 * sizeof(double);
+    if (check_cuda(cudaMemcpy2DAsync(u + off, w, hn + off, pitch, bytes, 3, cudaMemcpyHostToDevice,
+                                     c->copy_stream)) ||
+        check_cuda(cudaMemcpy2DAsync(u + 3 * c->npts + off, w, en + off, pitch, bytes, 3,
+                                     cudaMemcpyHostToDevice, c->copy_stream)) ||
+        check_cuda(cudaEventRecord(c->chunk_in[k], c->copy_stream)))
+      return NEKGPU_ERR_CUDA;
+  }
+  int st;
+  for (int k : c->chunk_order) {
+    if (check_cuda(cudaStreamWaitEvent(c->stream, c->chunk_in[c->chunk_wait[k]], 0))) return NEKGPU_ERR_CUDA;
+    if ((st = mixed_stage_range(c, 1, time, dt, c->chunk_begin[k], c->chunk_begin[k + 1]))) return st;
+  }
+  c->cur ^= 1;
+  for (int r = 2; r <= 4; ++r)
+    if ((st = mixed_stage(c, r, time, dt))) return st;
+  double* out = c->d_u[c->cur ^ 1];
+  for (int k = 0; k < nch; ++k) {
+    if ((st = mixed_stage_range(c, 5, time, dt, c->chunk_begin[k], c->chunk_begin[k + 1]))) return st;
+    if (check_cuda(cudaEventRecord(c->chunk_done[k], c->stream)) ||
+        check_cuda(cudaStreamWaitEvent(c->copy_stream, c->chunk_done[k], 0)))
+      return NEKGPU_ERR_CUDA;
+    const long off = c->chunk_begin[k] * N3;
+    const size_t bytes = (c->chunk_begin[k + 1] - c->chunk_begin[k]) * N3 * sizeof(double);
+    if (check_cuda(cudaMemcpy2DAsync(hn + off, pitch, out + off, w, bytes, 3, cudaMemcpyDeviceToHost,
+                                     c->copy_stream)) ||
+        check_cuda(cudaMemcpy2DAsync(en + off, pitch, out + 3 * c->npts + off, w, bytes, 3,
+                                     cudaMemcpyDeviceToHost, c->copy_stream)))
+      return NEKGPU_ERR_CUDA;
+  }
+  c->cur ^= 1;
+  // later work on the context stream follows the copies back
+  if (check_cuda(cudaEventRecord(c->chunk_fence[1], c->copy_stream)) ||
+      check_cuda(cudaStreamWaitEvent(c->stream, c->chunk_fence[1], 0)))
+    return NEKGPU_ERR_CUDA;
+  return NEKGPU_OK;
+}
+
 int do_stage(Context* c, int rkstep, double time, double dt) {
   if (rkstep < 1 || rkstep > 5) return NEKGPU_ERR_ARG;
   if (c->ndim == 2) return stage2d(c, rkstep, time, dt);
@@ -2077,7 +2191,13 @@ int nekgpu_step(nekgpu_ctx* c, int nsteps, double* time, double dt) {
 int nekgpu_op_rk_host(nekgpu_ctx* c, double* hn, double* en, long ld, double time, double dt) {
   if (!c || !hn || !en || ld < c->npts) return NEKGPU_ERR_ARG;
   c->last_launches = 0;
-  int st = copy_fields_in(c, state(c), hn, en, ld);
+  int st = NEKGPU_OK;
+  if (chunked_step_applies(c)) {
+    if ((st = chunked_step(c, hn, en, ld, time, dt))) return st;
+    c->have_state = true;
+    return sync_status(c);
+  }
+  st = copy_fields_in(c, state(c), hn, en, ld);
   if (st) return st;
   c->have_state = true;
   for (int r = 1; r <= 5 && !st; ++r) st = do_stage(c, r, time, dt);

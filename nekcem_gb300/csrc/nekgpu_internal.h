@@ -265,6 +265,7 @@ struct MixedDev {
   const double* inc_val;
   GrapheneDev gr;
   double dt;
+  int e_begin, e_end;  // elements of this launch
 };
 
 // Reverse of one FP64 stage (nekgpu_adjoint.cu)
@@ -341,6 +342,14 @@ struct Context {
   double volume = 0;
   cudaStream_t stream = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  // host-field step in element chunks (nekgpu_op_rk_host, mixed form): copies
+  // on their own stream, one event per chunk copied in / finished
+  cudaStream_t copy_stream = nullptr;
+  std::vector<cudaEvent_t> chunk_in, chunk_done;
+  cudaEvent_t chunk_fence[2] = {nullptr, nullptr};  // stream hand-overs before / after
+  std::vector<int> chunk_begin;  // nchunk + 1 element offsets
+  std::vector<int> chunk_order;  // stage-1 launch order of the chunks
+  std::vector<int> chunk_wait;   // per chunk: the last copy its stage-1 launch needs
 
   // device memory
   double* d_u[2] = {nullptr, nullptr};  // state (plain uses d_u[0] only)
@@ -461,6 +470,9 @@ int scale_coef(Context* c, double dt);
 
 // nekgpu_mixed.cu
 int mixed_stage(Context* c, int rkstep, double time, double dt);
+// one mixed stage over elements [e0, e1) of the current state, writing the
+// other state buffer without switching to it
+int mixed_stage_range(Context* c, int rkstep, double time, double dt, int e0, int e1);
 // the mixed form keeps dt-scaled coefficients as (hi, lo) float pairs in d_coef
 int scale_coef_pairs(Context* c, double dt);
 // D(i,j) in three FP32 pieces: Dh on a 10-bit grid per row (exact products

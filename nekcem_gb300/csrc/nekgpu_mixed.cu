@@ -483,9 +483,9 @@ __global__ void __launch_bounds__(MCfg<NX>::NT, mixed_min_blocks<NX, EXT>())
   };
   unsigned parity = 0;
   int buf = 0;  // area of the element's staged state and residual pairs
-  if (C::kTma && tid == 0 && blockIdx.x < a.nelt) issue_tma(blockIdx.x, 0);
+  if (C::kTma && tid == 0 && a.e_begin + (int)blockIdx.x < a.e_end) issue_tma(a.e_begin + blockIdx.x, 0);
 
-  for (int e = blockIdx.x; e < a.nelt; e += gridDim.x, buf ^= 1) {
+  for (int e = a.e_begin + blockIdx.x; e < a.e_end; e += gridDim.x, buf ^= 1) {
     int tid = opaque_tid();
     double* s_u64 = reinterpret_cast<double*>(smem + buf * C::SA);
     float2* s_R2 = reinterpret_cast<float2*>(smem + buf * C::SA);
@@ -729,7 +729,7 @@ __global__ void __launch_bounds__(MCfg<NX>::NT, mixed_min_blocks<NX, EXT>())
         }
       }
       __syncthreads();  // the split pairs are consumed: the next element may land
-      if (C::kTma && tid == 0 && en < a.nelt) {
+      if (C::kTma && tid == 0 && en < a.e_end) {
         fence_proxy_async_smem();
         issue_tma(en, buf ^ 1);
       }
@@ -739,7 +739,7 @@ __global__ void __launch_bounds__(MCfg<NX>::NT, mixed_min_blocks<NX, EXT>())
       // the split pairs are consumed: the next element's state lands in their
       // area while this one finishes (the next element's own barriers order
       // these reads of the residual pairs before its split overwrites them)
-      if (C::kTma && tid == 0 && en < a.nelt) {
+      if (C::kTma && tid == 0 && en < a.e_end) {
         fence_proxy_async_smem();
         issue_tma(en, buf ^ 1);
       }
@@ -798,7 +798,9 @@ int launch_mixed(Context* c, const MixedDev& a) {
     grid = per_sm * sms;
     ready = true;
   }
-  const int g = c->nelt < grid ? c->nelt : grid;
+  const int n = a.e_end - a.e_begin;
+  if (n <= 0) return NEKGPU_OK;
+  const int g = n < grid ? n : grid;
   c->fused_grid = g;
   kern<<<g, C::NT, C::smem, c->stream>>>(a);
   c->last_launches += 1;
@@ -828,10 +830,12 @@ int scale_coef_pairs(Context* c, double dt) {
   return check_cuda(cudaGetLastError());
 }
 
-int mixed_stage(Context* c, int rkstep, double time, double dt) {
+int mixed_stage_range(Context* c, int rkstep, double time, double dt, int e0, int e1) {
   int st = scale_coef_pairs(c, dt);
   if (st) return st;
   MixedDev a = c->margs;
+  a.e_begin = e0;
+  a.e_end = e1;
   a.u_in = c->d_u[c->cur];
   a.u_out = c->d_u[c->cur ^ 1];
   a.a = c->rk_a[rkstep - 1];
@@ -854,9 +858,14 @@ int mixed_stage(Context* c, int rkstep, double time, double dt) {
     case 9: st = ext ? launch_mixed<9, true>(c, a) : launch_mixed<9, false>(c, a); break;
     default: return NEKGPU_ERR_UNSUPPORTED;
   }
+  return st;
+}
+
+int mixed_stage(Context* c, int rkstep, double time, double dt) {
+  const int st = mixed_stage_range(c, rkstep, time, dt, 0, c->nelt);
   if (st) return st;
   c->cur ^= 1;
-  if (a.gr.elem) c->gr_cur ^= 1;
+  if (c->margs.gr.elem) c->gr_cur ^= 1;
   return NEKGPU_OK;
 }
 
