@@ -144,6 +144,9 @@ class ClockSampler:
 
 
 def dist_setup(n):
+    """One process per GPU under torchrun: NCCL where there are GPUs, gloo on
+    a host without them (the host-side logic of the N > 1 path: replicas,
+    barriers and the max over ranks)."""
     if n <= 1 or "RANK" not in os.environ:
         return None, 0, 1
     import torch
@@ -151,8 +154,11 @@ def dist_setup(n):
     rank = int(os.environ["RANK"])
     world = int(os.environ["WORLD_SIZE"])
     local = int(os.environ.get("LOCAL_RANK", rank))
-    torch.cuda.set_device(local)
-    dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    if torch.cuda.is_available():
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    else:
+        dist.init_process_group("gloo")
     return dist, rank, world
 
 
@@ -160,7 +166,8 @@ def reduce_max(dist, x: float) -> float:
     if dist is None:
         return x
     import torch
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
 
