@@ -152,6 +152,7 @@ def sol_planewave(x, y, z, t):
 # ---- materials and sources -----------------------------------------------------
 
 TE, TM = 1, 2
+BOTH = 3  # TE and TM superposed (3-D cases only)
 
 
 def sol_2dboxpec(mode: int):
@@ -434,7 +435,8 @@ class DielectricHalfSpace:
     reflected and the transmitted wave leave
     through a PML, and usersol damps each inside its own), dt = 0.005, 1000
     steps; TE (H_z, E_x) or TM (E_z, H_x).  userchk's tolerances: L2 5e-7,
-    Linf 5e-6 on the two active components."""
+    Linf 5e-6 on the two active components.  mode BOTH runs TE and TM
+    superposed (their components are disjoint), as tests/3ddielectric does."""
 
     N, nel = 8, (2, 32, 2)
     lo, hi = (-2.5, -5.0, -2.5), (2.5, 5.0, 2.5)
@@ -448,13 +450,20 @@ class DielectricHalfSpace:
         self.mode = mode
         z1, z2 = np.sqrt(1.0 / self.eps1), np.sqrt(1.0 / self.eps2)
         self.z1, self.z2 = z1, z2
-        if mode == TE:
-            self.refl, self.tran = (z1 - z2) / (z1 + z2), 2 * z1 / (z1 + z2)
+        # uservp of the reference's dielectric cases
+        self.reflte, self.trante = (z1 - z2) / (z1 + z2), 2 * z1 / (z1 + z2)
+        self.refltm, self.trantm = (z2 - z1) / (z1 + z2), 2 * z2 / (z1 + z2)
+        if mode == TM:
+            self.refl, self.tran = self.refltm, self.trantm
         else:
-            self.refl, self.tran = (z2 - z1) / (z1 + z2), 2 * z2 / (z1 + z2)
+            self.refl, self.tran = self.reflte, self.trante
         hy = (self.hi[1] - self.lo[1]) / self.nel[1]
         self.up_inner, self.up_outer = self.hi[1] - self.pml[0] * hy, self.hi[1]
         self.lo_inner, self.lo_outer = self.lo[1] + self.pml[0] * hy, self.lo[1]
+
+    def active(self):
+        """component indices (H1..H3, E1..E3 = 0..5) the wave lives in"""
+        return {TE: (2, 3), TM: (0, 5)}.get(self.mode, (0, 2, 3, 5))
 
     def regions(self, y, n3):
         yc = np.repeat(np.asarray(y).reshape(-1, n3).mean(axis=1), n3)
@@ -465,6 +474,8 @@ class DielectricHalfSpace:
         return np.where(up, self.eps1, self.eps2)
 
     def exact(self, x, y, z, t, n3):
+        """usersol: the reflected wave above y = 0, the transmitted one below,
+        each damped inside its PML"""
         up, inpml = self.regions(y, n3)
         y = np.asarray(y)
         eps = np.where(up, self.eps1, self.eps2)
@@ -478,16 +489,20 @@ class DielectricHalfSpace:
             f_lo = (-(order + 1) * np.log(referr) / (2 * eta * d_lo) * d_lo / (order + 1)) * \
                 np.clip((self.lo_inner - y) / d_lo, 0, None) ** (order + 1)
         fac = np.where(inpml, np.where(up, f_up, f_lo), 0.0)
-        uu = np.where(up, self.refl * np.exp(-eta * fac) * np.cos(ky * y - self.omega * t),
-                      self.tran * np.exp(-eta * fac) * np.cos(-ky * y - self.omega * t))
+        wave = np.where(up, np.exp(-eta * fac) * np.cos(ky * y - self.omega * t),
+                        np.exp(-eta * fac) * np.cos(-ky * y - self.omega * t))
         zero = np.zeros_like(y)
-        if self.mode == TE:
-            H = np.stack([zero, zero, uu])
-            E = np.stack([np.where(up, -eta * uu, eta * uu), zero, zero])
-        else:
-            H = np.stack([np.where(up, uu / eta, -uu / eta), zero, zero])
-            E = np.stack([zero, zero, uu])
-        return H, E
+        H = [zero, zero, zero]
+        E = [zero, zero, zero]
+        if self.mode in (TE, BOTH):
+            uu = np.where(up, self.reflte, self.trante) * wave
+            H[2] = uu
+            E[0] = np.where(up, -eta * uu, eta * uu)
+        if self.mode in (TM, BOTH):
+            uu = np.where(up, self.refltm, self.trantm) * wave
+            H[0] = np.where(up, uu / eta, -uu / eta)
+            E[2] = uu
+        return np.stack(H), np.stack(E)
 
     def incident_slots(self, y, cemface, n3, nf):
         up, _ = self.regions(y, n3)
@@ -501,10 +516,40 @@ class DielectricHalfSpace:
         return np.array(out, dtype=np.int64)
 
     def incident(self):
+        """userinc: amplitudes (H1..H3, E1..E3) of cos(-ky y - omega t)"""
         eta, ky = np.sqrt(1.0 / self.eps1), self.omega * np.sqrt(self.eps1)
-        if self.mode == TE:  # incfhz += u, incfex += eta u
-            return (0.0, 0.0, 1.0, eta, 0.0, 0.0), (0.0, -ky, 0.0), self.omega
-        return (-1.0 / eta, 0.0, 0.0, 0.0, 0.0, 1.0), (0.0, -ky, 0.0), self.omega
+        te = (0.0, 0.0, 1.0, eta, 0.0, 0.0)   # incfhz += u, incfex += eta u
+        tm = (-1.0 / eta, 0.0, 0.0, 0.0, 0.0, 1.0)  # incfhx -= u/eta, incfez += u
+        if self.mode == TE:
+            amp = te
+        elif self.mode == TM:
+            amp = tm
+        else:
+            amp = tuple(a + b for a, b in zip(te, tm))
+        return amp, (0.0, -ky, 0.0), self.omega
+
+
+class Dielectric3D(DielectricHalfSpace):
+    """The reference's tests/3ddielectric case (maxwell-3ddielectric-1mat and
+    -2mat, param(70) = 0 | 1): TE and TM plane waves together, normally
+    incident from y > 0 on eps2 = 1 or 2, omega = 2; 4 x 8 x 4 elements on
+    [-2.5,2.5] x [-5,5] x [-2.5,2.5] (usrdat2 scales the [-1,1]^3 box), N=8
+    (SIZE lxi = 8), x and z periodic, 'PML' at both y ends (2 layers, order 3,
+    error 1e-10: params 77-79), dt = 0.005, 1000 steps.  userchk's
+    tolerances per component H1..H3, E1..E3: L2 5e-4, 5e-14, 5e-4, 5e-4,
+    5e-14, 5e-4; Linf 5e-3 on the active components and 1e-12 (2mat) or
+    5e-12 (1mat) on H2 and E2."""
+
+    nel = (4, 8, 4)
+    pml = (2, 3.0, 1e-10)
+    omega = 2.0
+
+    def __init__(self, twomat: bool):
+        self.eps2 = 2.0 if twomat else 1.0
+        super().__init__(BOTH)
+        q = 1e-12 if twomat else 5e-12
+        self.l2tol = (5e-4, 5e-14, 5e-4, 5e-4, 5e-14, 5e-4)
+        self.linftol = (5e-3, q, 5e-3, 5e-3, q, 5e-3)
 
 
 class GrapheneSheet:

@@ -2,7 +2,8 @@
 the PML and a dispersive or dielectric half-space: the reference's
 tests/drude, tests/lorentz and tests/2ddielectric cases restated in 3-D
 (cases.DrudeHalfSpace, cases.DielectricHalfSpace: a plane wave reflected at
-y = 0, the waves leaving through the PML).
+y = 0, the waves leaving through the PML) and its 3-D tests/3ddielectric
+(cases.Dielectric3D, TE and TM together, eps2 = 1 or 2).
 
 CPU: the oracle passes the case's own tolerances (userchk: L2 <= 1e-7 and
 Linf <= 5e-6 on H_z and E_x after 1000 steps of dt = 0.005 at N=8).
@@ -147,8 +148,8 @@ def test_lorentz_known_answer_gpu(form):
     g.close(); ref.close()
 
 
-def dielectric_run(mode, form):
-    cs = cases.DielectricHalfSpace(mode)
+def dielectric_run(cs, form):
+    """cs: a cases.DielectricHalfSpace; form None runs the oracle"""
     ref = make_ref(cs.N, cs.nel, cs.lo, cs.hi, cs.bc, pml=cs.pml, threads=8,
                    eps=lambda x, y, z: cs.eps(y, (cs.N + 1) ** 3))
     x, y, z = (a.copy() for a in ref.coords())
@@ -174,28 +175,49 @@ def dielectric_run(mode, form):
         Hg, Eg = g.get_state()
         g.close()
     He, Ee = cs.exact(x, y, z, t, n3)
-    active = (2, 3) if mode == cases.TE else (0, 5)
+    per_comp = isinstance(cs.l2tol, tuple)
+    l2t = cs.l2tol if per_comp else (cs.l2tol,) * 6
+    lit = cs.linftol if per_comp else (cs.linftol,) * 6
     quiet = 1e-8 if form == "mixed" else 1e-12
     got = [Hg[0], Hg[1], Hg[2], Eg[0], Eg[1], Eg[2]]
     want = [He[0], He[1], He[2], Ee[0], Ee[1], Ee[2]]
     for q in range(6):
         l2, li = ref.cem_error(got[q], want[q])
-        if q in active:
-            assert l2 <= cs.l2tol and li <= cs.linftol, (q, l2, li)
+        if q in cs.active():
+            assert l2 <= l2t[q] and li <= lit[q], (q, l2, li)
+        elif per_comp and form != "mixed":
+            # the case's own tolerances on the components the wave leaves at zero
+            assert l2 <= l2t[q] and li <= lit[q], (q, l2, li)
         else:
+            # FP32 contractions leave ~1e-9 there (the reference's 5e-14 is
+            # FP64 round-off)
             assert l2 <= quiet and li <= 100 * quiet, (q, l2, li)
     ref.close()
 
 
 def test_oracle_dielectric_known_answer():
-    dielectric_run(cases.TE, None)
+    dielectric_run(cases.DielectricHalfSpace(cases.TE), None)
 
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("mode", [cases.TE, cases.TM])
 @pytest.mark.parametrize("form", ["plain", "fused64", "mixed"])
 def test_dielectric_known_answer_gpu(mode, form):
-    dielectric_run(mode, form)
+    dielectric_run(cases.DielectricHalfSpace(mode), form)
+
+
+@pytest.mark.parametrize("twomat", [False, True], ids=["1mat", "2mat"])
+def test_oracle_3ddielectric_known_answer(twomat):
+    """the reference's maxwell-3ddielectric-1mat / -2mat at userchk's
+    tolerances (TE and TM together, 4 x 8 x 4 elements, N=8, PML in y)"""
+    dielectric_run(cases.Dielectric3D(twomat), None)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("twomat", [False, True], ids=["1mat", "2mat"])
+@pytest.mark.parametrize("form", ["plain", "fused64", "mixed"])
+def test_3ddielectric_known_answer_gpu(twomat, form):
+    dielectric_run(cases.Dielectric3D(twomat), form)
 
 
 @pytest.mark.gpu
