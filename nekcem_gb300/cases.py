@@ -435,8 +435,10 @@ class DielectricHalfSpace:
     reflected and the transmitted wave leave
     through a PML, and usersol damps each inside its own), dt = 0.005, 1000
     steps; TE (H_z, E_x) or TM (E_z, H_x).  userchk's tolerances: L2 5e-7,
-    Linf 5e-6 on the two active components.  mode BOTH runs TE and TM
-    superposed (their components are disjoint), as tests/3ddielectric does."""
+    Linf 5e-6 on the two active components; with one material (param(70) =
+    0: eps2 = 1, the wave passes y = 0 unreflected) L2 5e-8, Linf 1e-6 (TE)
+    or 5e-6 (TM).  mode BOTH runs TE and TM superposed (their components are
+    disjoint), as tests/3ddielectric does."""
 
     N, nel = 8, (2, 32, 2)
     lo, hi = (-2.5, -5.0, -2.5), (2.5, 5.0, 2.5)
@@ -446,8 +448,11 @@ class DielectricHalfSpace:
     omega, eps1, eps2 = 5.0, 1.0, 2.0
     l2tol, linftol = 5e-7, 5e-6
 
-    def __init__(self, mode: int = TE):
+    def __init__(self, mode: int = TE, twomat: bool = True):
         self.mode = mode
+        if not twomat:
+            self.eps2 = 1.0
+            self.l2tol, self.linftol = 5e-8, (1e-6 if mode == TE else 5e-6)
         z1, z2 = np.sqrt(1.0 / self.eps1), np.sqrt(1.0 / self.eps2)
         self.z1, self.z2 = z1, z2
         # uservp of the reference's dielectric cases

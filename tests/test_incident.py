@@ -195,15 +195,17 @@ def dielectric_run(cs, form):
     ref.close()
 
 
-def test_oracle_dielectric_known_answer():
-    dielectric_run(cases.DielectricHalfSpace(cases.TE), None)
+@pytest.mark.parametrize("twomat", [True, False], ids=["2mat", "1mat"])
+def test_oracle_dielectric_known_answer(twomat):
+    dielectric_run(cases.DielectricHalfSpace(cases.TE, twomat), None)
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("twomat", [True, False], ids=["2mat", "1mat"])
 @pytest.mark.parametrize("mode", [cases.TE, cases.TM])
 @pytest.mark.parametrize("form", ["plain", "fused64", "mixed"])
-def test_dielectric_known_answer_gpu(mode, form):
-    dielectric_run(cases.DielectricHalfSpace(mode), form)
+def test_dielectric_known_answer_gpu(mode, form, twomat):
+    dielectric_run(cases.DielectricHalfSpace(mode, twomat), form)
 
 
 @pytest.mark.parametrize("twomat", [False, True], ids=["1mat", "2mat"])
