@@ -484,6 +484,8 @@ __global__ void __launch_bounds__(MCfg<NX>::NT, mixed_min_blocks<NX, EXT>())
     if (!first_stage)
       for (int c = 0; c < 6; ++c) prefetch_l2(a.k + c * P + (long)e * N3, bytes);
     for (int c = 0; c < 2; ++c) prefetch_l2(a.coef + c * P + (long)e * N3, N3 * 8u);
+    // and the face impedance coefficients the flux reads (float4 per face node)
+    if (a.fcoef) prefetch_l2(reinterpret_cast<const float4*>(a.fcoef) + (long)e * NF, NF * 16u);
   };
   unsigned parity = 0;
   int buf = 0;  // area of the element's staged state and residual pairs
