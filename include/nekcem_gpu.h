@@ -265,7 +265,11 @@ int nekgpu_stage(nekgpu_ctx* ctx, int rkstep, double time, double dt);
  * *time += dt after each step as time_advancing_pde does (src/cem_drive.F:639). */
 int nekgpu_step(nekgpu_ctx* ctx, int nsteps, double* time, double dt);
 /* Drop-in for one cem_maxwell_op_rk call on host arrays: copies hn/en in,
- * runs the 5 stages, copies hn/en back.  The RK register stays on the GPU. */
+ * runs the 5 stages, copies hn/en back; returns when hn/en hold the new
+ * state.  The RK register stays on the GPU.  In the mixed form on meshes of
+ * several waves of blocks the copies overlap stages 1 and 5 chunk by chunk
+ * (same results bit for bit); hn/en page-locked with nekgpu_register_host
+ * let the copies run at the link's rate. */
 int nekgpu_op_rk_host(nekgpu_ctx* ctx, double* hn, double* en, long ld, double time,
                       double dt);
 
