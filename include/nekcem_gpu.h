@@ -307,6 +307,11 @@ int nekgpu_norms(nekgpu_ctx* ctx, const double* exact_h, const double* exact_e, 
 int nekgpu_norms_noalloc(nekgpu_ctx* ctx, const double* exact_dev, double l2[6], double linf[6]);
 /* field energy 0.5*sum bm1*(eps|E|^2 + mu|H|^2), FP64 on device */
 int nekgpu_energy(nekgpu_ctx* ctx, double* energy);
+/* Failure-detection self-test: one kernel polls an mbarrier that nothing
+ * arrives at `polls` times (1..2^22), as the stage kernels poll for their
+ * copies, and gives up; returns NEKGPU_ERR_TIMEOUT (the status word the stage
+ * kernels set when a wait runs out) and leaves the context usable. */
+int nekgpu_selftest_wait(nekgpu_ctx* ctx, int polls);
 /* chk_blowup (src/cem_common.F:1150-1165): NEKGPU_ERR_BLOWUP if any state
  * value is non-finite or above 1e20 in magnitude */
 int nekgpu_check_blowup(nekgpu_ctx* ctx);

@@ -2299,6 +2299,18 @@ int nekgpu_energy(nekgpu_ctx* c, double* energy) {
   return util_energy(c, energy);
 }
 
+int nekgpu_selftest_wait(nekgpu_ctx* c, int polls) {
+  if (!c || polls < 1 || polls > (1 << 22)) return NEKGPU_ERR_ARG;
+  c->last_launches = 0;
+  if (check_cuda(cudaMemsetAsync(c->d_status, 0, sizeof(int), c->stream))) return NEKGPU_ERR_CUDA;
+  int st = wait_selftest(c, polls);
+  if (st) return st;
+  st = sync_status(c);
+  // the context stays usable: clear the word the wait set
+  if (check_cuda(cudaMemset(c->d_status, 0, sizeof(int)))) return NEKGPU_ERR_CUDA;
+  return st;
+}
+
 int nekgpu_check_blowup(nekgpu_ctx* c) {
   if (!c) return NEKGPU_ERR_ARG;
   int bad = 0;

@@ -470,6 +470,8 @@ int scale_coef(Context* c, double dt);
 
 // nekgpu_mixed.cu
 int mixed_stage(Context* c, int rkstep, double time, double dt);
+// launches a kernel whose bounded mbarrier wait runs out (sets the status word)
+int wait_selftest(Context* c, int polls);
 // one mixed stage over elements [e0, e1) of the current state, writing the
 // other state buffer without switching to it
 int mixed_stage_range(Context* c, int rkstep, double time, double dt, int e0, int e1);

@@ -813,7 +813,28 @@ int launch_mixed(Context* c, const MixedDev& a) {
   return check_cuda(cudaGetLastError());
 }
 
+// The bounded wait run out on purpose: an mbarrier that nothing arrives at,
+// polled `polls` times, then the status word is set as a stage kernel sets it
+// when its copy never lands.  No fault, no trap, no endless loop.
+__global__ void k_wait_selftest(int polls, int* status) {
+  __shared__ uint64_t bar;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  bool done = false;
+  for (int it = 0; it < polls && !done; ++it) done = mbar_try_wait(&bar, 0);
+  if (!done && threadIdx.x == 0) atomicExch(status, 1);
+}
+
 }  // namespace
+
+int wait_selftest(Context* c, int polls) {
+  k_wait_selftest<<<1, 32, 0, c->stream>>>(polls, c->d_status);
+  c->last_launches += 1;
+  return check_cuda(cudaGetLastError());
+}
 
 int mixed_upload_D(int nx, const float* tab, size_t count) {
   static bool done[kMaxMixed + 1] = {false};

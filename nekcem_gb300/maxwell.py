@@ -341,6 +341,11 @@ class MaxwellGPU:
         L.check(L.load().nekgpu_energy(self._h, C.byref(e)), "nekgpu_energy")
         return e.value
 
+    def selftest_wait(self, polls: int = 1000) -> int:
+        """status of a kernel whose bounded mbarrier wait runs out on purpose
+        (NEKGPU_ERR_TIMEOUT); the context stays usable"""
+        return int(L.load().nekgpu_selftest_wait(self._h, int(polls)))
+
     def check_blowup(self):
         L.check(L.load().nekgpu_check_blowup(self._h), "nekgpu_check_blowup")
 

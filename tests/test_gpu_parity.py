@@ -408,6 +408,28 @@ def test_blowup_detection():
     g.close(); ref.close()
 
 
+def test_bounded_wait_runs_out_and_context_survives():
+    """A device wait that nothing ends (an mbarrier no one arrives at) gives
+    up after its poll budget and reports NEKGPU_ERR_TIMEOUT through the
+    status word, without a fault; the same context then steps normally and
+    matches a fresh one bit for bit."""
+    ref = ref_for("pec_n5")
+    g = gpu_from_box(ref, "mixed")
+    assert g.selftest_wait(1000) == -7
+    assert g.selftest_wait(1) == -7
+    H, E = smooth_fields(ref, 31)
+    dt = 0.2 * ref.dxmin()
+    g.set_state(H, E)
+    g.run(3, 0.0, dt)
+    g2 = gpu_from_box(ref, "mixed")
+    g2.set_state(H, E)
+    g2.run(3, 0.0, dt)
+    a, b = g.get_state(), g2.get_state()
+    np.testing.assert_array_equal(a[0], b[0])
+    np.testing.assert_array_equal(a[1], b[1])
+    g.close(); g2.close(); ref.close()
+
+
 @pytest.mark.parametrize("form", ["fused64", "mixed"])
 def test_energy_central_vs_upwind(form):
     """Central flux (C0=0) on a periodic box: the semi-discrete operator
