@@ -178,7 +178,9 @@ int nekgpu_set_source_kind(nekgpu_ctx* ctx, int kind);
 /* Gaussian-in-space, Ricker-in-time E_z volume source in mass-weighted form,
  * added before the inverse mass like usersrc (src/cem_maxwell.F:503):
  * resEz += bm1 * amp * exp(-|x-xc|^2/(2 sigma^2)) * ricker(t; f0, t0),
- * ricker(t) = (1 - 2 a^2) exp(-a^2), a = pi f0 (t - t0).  enabled=0 clears. */
+ * ricker(t) = (1 - 2 a^2) exp(-a^2), a = pi f0 (t - t0).  enabled=0 clears.
+ * 2-D TM context: a line current along z on E3 = E_z (z ignored: give
+ * xc[2] = 0); a TE context has no E_z (NEKGPU_ERR_UNSUPPORTED). */
 int nekgpu_set_source(nekgpu_ctx* ctx, int enabled, const double xc[3], double sigma,
                       double amp, double f0, double t0);
 

@@ -155,6 +155,9 @@ __global__ void k_stage2d(const Stage2dDev a) {
   if (j == n - 1) add(2, i);
   if (i == 0) add(3, j);
   const long g = (long)e * n2 + v;
+  // usersrc after the lift, before the inverse mass (src/cem_maxwell.F:503):
+  // the TM form's E3 += bm1-weighted Gaussian x time factor
+  if (a.src_w) r[2] = r[2] + a.src_w[g] * a.src_ft;
   const double hb = a.hbm1[g], eb = a.ebm1[g];
   r[0] = r[0] * (tm ? hb : eb);
   r[1] = r[1] * (tm ? hb : eb);
@@ -174,8 +177,8 @@ __global__ void k_stage2d(const Stage2dDev a) {
 }  // namespace
 
 int stage2d(Context* c, int rkstep, double time, double dt) {
-  (void)time;  // no time-dependent terms in the 2-D form
   Stage2dDev a = c->s2;
+  if (a.src_w) a.src_ft = source_ft(c->src, time + dt * c->rk_c[rkstep - 1]);
   a.u_in = c->d_u[c->cur];
   a.u_out = c->d_u[c->cur ^ 1];
   a.k = c->d_k;

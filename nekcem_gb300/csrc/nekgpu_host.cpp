@@ -2053,6 +2053,7 @@ int nekgpu_set_source(nekgpu_ctx* c, int enabled, const double xc[3], double sig
   if (!c) return NEKGPU_ERR_ARG;
   if (!enabled) {
     c->src.enabled = false;
+    c->s2.src_w = nullptr;
     c->pargs.src_w = nullptr;
     c->fargs.src_elem = nullptr;
     c->fargs.src_w = nullptr;
@@ -2061,7 +2062,8 @@ int nekgpu_set_source(nekgpu_ctx* c, int enabled, const double xc[3], double sig
     return NEKGPU_OK;
   }
   if (!xc || !(sigma > 0)) return NEKGPU_ERR_ARG;
-  if (c->ndim == 2) return NEKGPU_ERR_UNSUPPORTED;  // 3-D volume source only
+  // 2-D: the TM form's E3 is E_z (a line source along z); TE has no E_z
+  if (c->ndim == 2 && c->imode != 2) return NEKGPU_ERR_UNSUPPORTED;
   if ((long)c->host_x.size() != c->npts) return NEKGPU_ERR_STATE;  // needs coordinates
   const double s2 = 2.0 * sigma * sigma;
   std::vector<double> g(c->npts);
@@ -2073,12 +2075,15 @@ int nekgpu_set_source(nekgpu_ctx* c, int enabled, const double xc[3], double sig
   }
   DevAlloc A(c);
   int st;
-  if (c->form == NEKGPU_PLAIN) {
+  if (c->form == NEKGPU_PLAIN || c->ndim == 2) {
     if (!c->d_src_w_plain && (st = A.get(&c->d_src_w_plain, c->npts))) return st;
     if (check_cuda(cudaMemcpy(c->d_src_w_plain, g.data(), c->npts * sizeof(double),
                               cudaMemcpyHostToDevice)))
       return NEKGPU_ERR_CUDA;
-    c->pargs.src_w = c->d_src_w_plain;
+    if (c->ndim == 2)
+      c->s2.src_w = c->d_src_w_plain;
+    else
+      c->pargs.src_w = c->d_src_w_plain;
   } else {
     release_dev(c, c->d_src_elem);  // a previous source's arrays
     release_dev(c, c->d_src_w);

@@ -328,6 +328,8 @@ struct Stage2dDev {
   double* u_out;
   double* k;
   double ca, cb, dt;
+  const double* src_w;  // npts or null: TM volume source on E3 (usersrc)
+  double src_ft;        // its time factor at the stage time
 };
 
 struct Context {

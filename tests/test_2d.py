@@ -117,6 +117,37 @@ def test_2d_bit_exact(name, mode, materials):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("name", list(MESHES_2D))
+@pytest.mark.parametrize("kind", [0, 1])
+def test_2d_tm_source_bit_exact(name, kind):
+    """usersrc in the TM form: a Gaussian line current on E_z (z ignored),
+    added after the lift and before the inverse mass, as the reference's 2-D
+    cases do (tests/2dboxpml/2dboxpml.usr: srcez -= norm exp(..) sin(-omega t)
+    bm1); Ricker (kind 0) or sin(f0 t) (kind 1) in time; bit-identical to the
+    oracle over 5 steps from rest."""
+    b = MESHES_2D[name]
+    ref = R.RefBox2D(b["N"], b["nel"], b["lo"], b["hi"], b["bc"], TM)
+    x, y, z = ref.coords()
+    g = MaxwellGPU.from_arrays2d(oracle_arrays(ref), ref.n, ref.nelt, TM)
+    xc = (0.5 * (b["lo"][0] + b["hi"][0]), 0.5 * (b["lo"][1] + b["hi"][1]), 0.0)
+    src = dict(xc=xc, sigma=0.15, amp=2.0, f0=2.0, t0=0.05)
+    for obj in (ref, g):
+        obj.set_source_kind(kind)
+        obj.set_source(**src)
+    zero = np.zeros((3, ref.npts))
+    ref.set_state(zero, zero)
+    g.set_state(zero, zero)
+    dt = 0.2 * ref.dxmin()
+    ref.run(5, 0.0, dt)
+    g.run(5, 0.0, dt)
+    Hg, Eg = g.get_state()
+    assert np.abs(ref.en[2]).max() > 1e-6  # the source drove the field
+    np.testing.assert_array_equal(Hg, ref.hn)
+    np.testing.assert_array_equal(Eg, ref.en)
+    g.close(); ref.close()
+
+
+@pytest.mark.gpu
 @pytest.mark.parametrize("name", list(cases.CASES_2D))
 @pytest.mark.parametrize("mode", [TE, TM])
 def test_2d_known_answers_gpu(name, mode):
@@ -129,8 +160,10 @@ def test_2d_refusals(tmp_path):
     arrays = oracle_arrays(ref)
     g = MaxwellGPU.from_arrays2d(arrays, ref.n, ref.nelt, TM)
     g.set_state(np.zeros((3, g.npts)), np.zeros((3, g.npts)))
+    te = MaxwellGPU.from_arrays2d(arrays, ref.n, ref.nelt, TE)  # TE has no E_z
+    te.set_state(np.zeros((3, g.npts)), np.zeros((3, g.npts)))
     calls = [
-        lambda: g.set_source((0.5, 0.5, 0.0), 0.1, 1.0, 1.0, 0.0),
+        lambda: te.set_source((0.5, 0.5, 0.0), 0.1, 1.0, 1.0, 0.0),
         lambda: g.set_dispersive(g.DRUDE, np.ones((2, g.npts)), np.arange(3)),
         lambda: g.adjoint_gradient(1, 0.0, 0.01, np.ones(g.npts)),
         lambda: g.write_vtk(str(tmp_path / "x.vtk")),
@@ -139,7 +172,7 @@ def test_2d_refusals(tmp_path):
         with pytest.raises(L.NekgpuError) as e:
             call()
         assert e.value.status == -8
-    g.close()
+    g.close(); te.close()
     bad = dict(arrays)
     cf = bad["cemface"].copy()
     cf[[0, 1]] = cf[[1, 0]]  # not the reference's face numbering
