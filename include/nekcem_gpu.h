@@ -147,8 +147,11 @@ int nekgpu_init_box(nekgpu_ctx** ctx, const nekgpu_box* box, int form);
  * nxzfl = 4 nx1 nelt slots in the reference's 2-D face numbering; the z
  * metrics, unzm and zmn are not read.  One kernel per RK stage in the
  * reference's FP64 arithmetic (bit-identical to the CPU path); fields keep
- * the (ld,3) layout with the inactive components left as set.  No source,
- * dispersive media, PML, adjoint or VTK output in 2-D. */
+ * the (ld,3) layout with the inactive components left as set.  PML: the
+ * mesh's pmlsigma (3*npts), pmlptr and materials as in 3-D (pml_step on the
+ * active components, their pmlbn/pmldn through nekgpu_set_array /
+ * nekgpu_get_array).  Volume source: TM only (a line current on E_z).  No
+ * dispersive media, adjoint or VTK output in 2-D. */
 int nekgpu_init2d(nekgpu_ctx** ctx, const nekgpu_mesh* mesh, int imode);
 int nekgpu_finalize(nekgpu_ctx* ctx);
 

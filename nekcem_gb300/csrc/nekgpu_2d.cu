@@ -155,6 +155,33 @@ __global__ void k_stage2d(const Stage2dDev a) {
   if (j == n - 1) add(2, i);
   if (i == 0) add(3, j);
   const long g = (long)e * n2 + v;
+  // pml_step after the lift (src/cem_maxwell_pml.F:508-590) on the active
+  // components, in the reference's expression order: the auxiliary residual
+  // res/bm1 - A aux and the PML term (-A aux + B aux - C u) bm1 added to res.
+  // (A, B, C) per component: x (sy, sx, sz), y (sz, sy, sx), z (sx, sz, sy),
+  // sigma/eps everywhere except C on E, which is sigma itself.
+  const bool pml = a.pml_elem && a.pml_elem[e];
+  double pres[3] = {0.0, 0.0, 0.0};
+  if (pml) {
+    const double bm = a.bm1[g];
+    const double bm1inv = 1.0 / bm;
+    const double sig[3] = {a.pml_sigma[g], a.pml_sigma[g + P], a.pml_sigma[g + 2 * P]};
+    const double ep = a.eps[g];
+    const double sp[3] = {sig[0] / ep, sig[1] / ep, sig[2] / ep};
+    const double permeab = a.mu[g];
+    for (int q = 0; q < 3; ++q) {
+      const int c = comp[q], x = c % 3;  // x: the component's axis
+      const int ia = x == 0 ? 1 : (x == 1 ? 2 : 0), ib = x, ic = x == 0 ? 2 : (x == 1 ? 0 : 1);
+      const double aux = a.pml_aux[(long)c * P + g];
+      pres[q] = r[q] * bm1inv - sp[ia] * aux;
+      double t;
+      if (c < 3)
+        t = -sp[ia] * aux + sp[ib] * aux - sp[ic] * permeab * s_u[q * n2 + v];
+      else
+        t = -sp[ia] * aux + sp[ib] * aux - sig[ic] * s_u[q * n2 + v];
+      r[q] = r[q] + t * bm;
+    }
+  }
   // usersrc after the lift, before the inverse mass (src/cem_maxwell.F:503):
   // the TM form's E3 += bm1-weighted Gaussian x time factor
   if (a.src_w) r[2] = r[2] + a.src_w[g] * a.src_ft;
@@ -172,6 +199,13 @@ __global__ void k_stage2d(const Stage2dDev a) {
   }
   for (int c = 0; c < 6; ++c)  // the inactive components carry over
     if (!active[c]) a.u_out[c * P + g] = a.u_in[c * P + g];
+  if (pml)  // rk4_upd of the active auxiliary fields (src/cem_maxwell.F:1942-1955)
+    for (int q = 0; q < 3; ++q) {
+      const long o = comp[q] * P + g;
+      const double kk = a.ca * a.pml_k[o] + a.dt * pres[q];
+      a.pml_k[o] = kk;
+      a.pml_aux[o] = a.pml_aux[o] + a.cb * kk;
+    }
 }
 
 }  // namespace

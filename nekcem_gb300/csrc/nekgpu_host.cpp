@@ -1469,6 +1469,37 @@ int nekgpu_init2d(nekgpu_ctx** ctx, const nekgpu_mesh* m, int imode) {
     if (!st && !(st = A.put(&di, cemface))) a.cemface = di;
     if (!st && !(st = A.put(&di, partner))) a.partner = di;
     if (!st && !(st = A.put(&di, pec))) a.pec = di;
+    if (!st && m->pmlsigma && m->npml > 0) {
+      // PML: the reference's full-size arrays, stepped by the stage kernel
+      if (!m->pmlptr || !m->permittivity || !m->permeability) st = NEKGPU_ERR_ARG;
+      std::vector<int> flag(m->nelt, 0);
+      for (int l = 0; l < m->npml && !st; ++l) {
+        const int e = m->pmlptr[l] - 1;
+        if (e < 0 || e >= m->nelt || (l > 0 && e <= c->pml_elems.back())) st = NEKGPU_ERR_ARG;
+        else { c->pml_elems.push_back(e); flag[e] = 1; }
+      }
+      if (!st) {
+        c->npml = m->npml;
+        int* dflag;
+        if ((st = A.put(&dflag, flag)) ||
+            (st = A.put(&c->d_pml_sigma, std::vector<double>(m->pmlsigma, m->pmlsigma + 3 * npts))) ||
+            (st = A.put(&c->d_eps, std::vector<double>(m->permittivity, m->permittivity + npts))) ||
+            (st = A.put(&c->d_mu, std::vector<double>(m->permeability, m->permeability + npts))) ||
+            (st = A.get(&c->d_pml_aux, 6 * npts)) || (st = A.get(&c->d_pml_k, 6 * npts))) {
+        } else if (check_cuda(cudaMemset(c->d_pml_aux, 0, 6 * npts * sizeof(double))) ||
+                   check_cuda(cudaMemset(c->d_pml_k, 0, 6 * npts * sizeof(double)))) {
+          st = NEKGPU_ERR_CUDA;
+        } else {
+          a.pml_elem = dflag;
+          a.pml_sigma = c->d_pml_sigma;
+          a.eps = c->d_eps;
+          a.mu = c->d_mu;
+          a.bm1 = c->d_bm1;
+          a.pml_aux = c->d_pml_aux;
+          a.pml_k = c->d_pml_k;
+        }
+      }
+    }
     if (!st && m->xmn && m->ymn) {
       c->host_x.assign(m->xmn, m->xmn + npts);
       c->host_y.assign(m->ymn, m->ymn + npts);
@@ -1609,7 +1640,7 @@ int nekgpu_get_array(nekgpu_ctx* c, const char* name, double* out) {
   const long P = c->npts, n3 = (long)c->nx * c->nx * c->nx;
   std::fill(out, out + 3 * P, 0.0);
   if (!c->npml) return NEKGPU_OK;
-  if (c->form == NEKGPU_PLAIN) {
+  if (c->form == NEKGPU_PLAIN || c->ndim == 2) {  // full-size arrays
     const double* src = sg ? c->d_pml_sigma : c->d_pml_aux + (dn ? 3 * P : 0);
     return check_cuda(cudaMemcpy(out, src, 3 * P * sizeof(double), cudaMemcpyDeviceToHost));
   }
@@ -1875,7 +1906,7 @@ int nekgpu_set_array(nekgpu_ctx* c, const char* name, const double* in) {
   if (!c->npml) return NEKGPU_ERR_STATE;
   const long P = c->npts, n3 = (long)c->nx * c->nx * c->nx;
   if (check_cuda(cudaStreamSynchronize(c->stream))) return NEKGPU_ERR_CUDA;
-  if (c->form == NEKGPU_PLAIN)
+  if (c->form == NEKGPU_PLAIN || c->ndim == 2)  // full-size arrays
     return check_cuda(cudaMemcpy(c->d_pml_aux + (dn ? 3 * P : 0), in, 3 * P * sizeof(double),
                                  cudaMemcpyHostToDevice));
   const long nn = (long)c->npml * n3;

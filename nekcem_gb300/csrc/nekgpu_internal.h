@@ -330,6 +330,11 @@ struct Stage2dDev {
   double ca, cb, dt;
   const double* src_w;  // npts or null: TM volume source on E3 (usersrc)
   double src_ft;        // its time factor at the stage time
+  // PML (pml_step, the reference's full-size arrays); pml_elem null without
+  const int* pml_elem;          // nelt: 1 on PML elements
+  const double *pml_sigma;      // 3*npts sigma x, y, z
+  const double *eps, *mu, *bm1;  // npts
+  double *pml_aux, *pml_k;      // 6*npts pmlbn(3), pmldn(3) and their RK registers
 };
 
 struct Context {

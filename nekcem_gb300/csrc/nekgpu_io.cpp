@@ -142,7 +142,8 @@ namespace {
 const double* state_ptr(Context* c) { return c->form == NEKGPU_PLAIN ? c->d_u[0] : c->d_u[c->cur]; }
 long aux_len(const Context* c) {
   if (!c->npml) return 0;
-  return c->form == NEKGPU_PLAIN ? 6 * c->npts : 6L * c->npml * c->nx * c->nx * c->nx;
+  return (c->form == NEKGPU_PLAIN || c->ndim == 2) ? 6 * c->npts
+                                                    : 6L * c->npml * c->nx * c->nx * c->nx;
 }
 
 }  // namespace

@@ -1077,10 +1077,11 @@ static void gs_max(ref_ctx* c, double* v) {
 /* march_faces (src/cem_maxwell_pml.F:85-137) */
 static void march_faces(ref_ctx* c, double* far) {
   long n2 = c->nxzf;
+  const int nfc = c->nfaces;
   for (int e = 0; e < c->nelt; ++e)
-    for (int ax = 0; ax < 3; ++ax) {
-      double* pf = far + n2 * (pos_slot[ax] + 6L * e);
-      double* nf = far + n2 * (neg_slot[ax] + 6L * e);
+    for (int ax = 0; ax < c->ndim; ++ax) {
+      double* pf = far + n2 * (pos_slot[ax] + (long)nfc * e);
+      double* nf = far + n2 * (neg_slot[ax] + (long)nfc * e);
       for (long i = 0; i < n2; ++i) {
         double sum = pf[i] + nf[i];
         if (sum != 0) { pf[i] = pf[i] + 1; nf[i] = nf[i] + 1; }
@@ -1090,16 +1091,22 @@ static void march_faces(ref_ctx* c, double* far) {
 }
 
 void ref_set_pml(ref_ctx* c, int thick, double order, double referr) {
-  const int n = c->n;
-  const long n2 = c->nxzf, n3 = (long)n * n * n, np = c->npts;
-  /* pml_fill_faceary (:139-190): ones at the interior nodes of 'PML' faces,
-   * then `thick` marches */
+  const int n = c->n, nd = c->ndim, nfc = c->nfaces;
+  const long n2 = c->nxzf, np = c->npts;
+  const long n3 = nd == 3 ? (long)n * n * n : (long)n * n;  /* nodes per element */
+  /* pml_fill_faceary (:139-190): ones at the interior nodes of 'PML' faces
+   * (2-D: face nodes 2..lx1-1), then `thick` marches */
   double* far = dalloc(c->nxzfl);
   for (int e = 0; e < c->nelt; ++e)
-    for (int f = 0; f < 6; ++f)
-      if (c->cbc[6 * e + f] == 3)
-        for (int b = 1; b < n - 1; ++b)
-          for (int a = 1; a < n - 1; ++a) far[a + (long)n * b + n2 * (f + 6L * e)] = 1;
+    for (int f = 0; f < nfc; ++f)
+      if (c->cbc[nfc * e + f] == 3) {
+        if (nd == 3) {
+          for (int b = 1; b < n - 1; ++b)
+            for (int a = 1; a < n - 1; ++a) far[a + (long)n * b + n2 * (f + 6L * e)] = 1;
+        } else {
+          for (int a = 1; a < n - 1; ++a) far[a + n2 * (f + 4L * e)] = 1;
+        }
+      }
   for (int i = 0; i < thick; ++i) march_faces(c, far);
 
   /* pml_extent_and_tags (:261-431); extents in sym order (x-, x+, y-, ...) */
@@ -1112,14 +1119,15 @@ void ref_set_pml(ref_ctx* c, int thick, double order, double referr) {
   }
   free(c->pmltag);
   c->pmltag = ialloc(c->nelt);
-  const long ind = 1 + (long)n;  /* face node (1,1): a face interior point */
+  /* a face interior point: node (1,1) of the face in 3-D, node 2 (1-based) in 2-D */
+  const long ind = nd == 3 ? 1 + (long)n : 1;
   const double* coord[3] = {c->xm1, c->ym1, c->zm1};
   const double* met[3][3] = {{c->rxm1, c->sxm1, c->txm1}, {c->rym1, c->sym1, c->tym1},
                              {c->rzm1, c->szm1, c->tzm1}};
   for (int e = 0; e < c->nelt; ++e)
-    for (int ax = 0; ax < 3; ++ax) {
-      double here = far[ind + n2 * (neg_slot[ax] + 6L * e)];
-      double opp = far[ind + n2 * (pos_slot[ax] + 6L * e)];
+    for (int ax = 0; ax < nd; ++ax) {
+      double here = far[ind + n2 * (neg_slot[ax] + (long)nfc * e)];
+      double opp = far[ind + n2 * (pos_slot[ax] + (long)nfc * e)];
       if (here == 0 || opp == 0) continue;
       /* dir_local_to_global (:192-259) of the local -ax direction */
       double loc[3] = {0, 0, 0}, glob[3];
@@ -1169,7 +1177,7 @@ void ref_set_pml(ref_ctx* c, int thick, double order, double referr) {
   }
   for (int l = 0; l < c->maxpml; ++l) {
     int e = c->pmlptr[l];
-    for (int face = 0; face < 6; ++face) {
+    for (int face = 0; face < 2 * nd; ++face) {
       int ax = face / 2;
       double width = fabs(c->pmlouter[face] - c->pmlinner[face]);
       if (!(c->pmltag[e] & (1 << face))) continue;
@@ -1188,7 +1196,8 @@ void ref_set_pml(ref_ctx* c, int thick, double order, double referr) {
 
 /* pml_step (src/cem_maxwell_pml.F:508-590) */
 void ref_pml_step(ref_ctx* c) {
-  const long n3 = (long)c->n * c->n * c->n, np = c->npts;
+  const long n3 = c->ndim == 3 ? (long)c->n * c->n * c->n : (long)c->n * c->n;
+  const long np = c->npts;
   double *sg = c->pmlsigma, *bn = c->pmlbn, *dn = c->pmldn;
   double *rb = c->respmlbn, *rd = c->respmldn, *rh = c->respmlhn, *re = c->respmlen;
   double *hn = c->hn, *en = c->en, *rsh = c->reshn, *rse = c->resen;
@@ -1318,14 +1327,14 @@ void ref_rk_stage(ref_ctx* c, int rkstep, double time, double dt) {
     r[2] = (tm ? c->resen : c->reshn) + 2 * np;
     for (int q = 0; q < 3; ++q)
       ref_rk4_upd(u[q], k[q], r[q], b[rkstep - 1], a[rkstep - 1], dt, np);
-    return;
+  } else {
+    for (int q = 0; q < 3; ++q)
+      ref_rk4_upd(c->hn + q * np, c->khn + q * np, c->reshn + q * np, b[rkstep - 1],
+                  a[rkstep - 1], dt, np);
+    for (int q = 0; q < 3; ++q)
+      ref_rk4_upd(c->en + q * np, c->ken + q * np, c->resen + q * np, b[rkstep - 1],
+                  a[rkstep - 1], dt, np);
   }
-  for (int q = 0; q < 3; ++q)
-    ref_rk4_upd(c->hn + q * np, c->khn + q * np, c->reshn + q * np, b[rkstep - 1], a[rkstep - 1],
-                dt, np);
-  for (int q = 0; q < 3; ++q)
-    ref_rk4_upd(c->en + q * np, c->ken + q * np, c->resen + q * np, b[rkstep - 1], a[rkstep - 1],
-                dt, np);
   if (c->ifpml) { /* src/cem_maxwell.F:1942-1955 */
     for (int q = 0; q < 3; ++q)
       ref_rk4_upd(c->pmlbn + q * np, c->kpmlbn + q * np, c->respmlbn + q * np, b[rkstep - 1],
@@ -1591,7 +1600,6 @@ static void invqmass_2d(ref_ctx* c) {
 ref_ctx* ref_create_box2d(int N, int nelx, int nely, const double lo[2], const double hi[2],
                           const int bc[2], int imode) {
   if (N < 1 || N > 15 || nelx < 1 || nely < 1 || (imode != 1 && imode != 2)) return NULL;
-  if (bc[0] == REF_BC_PML || bc[1] == REF_BC_PML) return NULL;
   ref_ctx* c = (ref_ctx*)calloc(1, sizeof(ref_ctx));
   int n = N + 1;
   c->N = N; c->n = n;
@@ -1704,7 +1712,8 @@ ref_ctx* ref_create_box2d(int N, int nelx, int nely, const double lo[2], const d
       int ax = slot_axis[f], sd = slot_side[f];
       int plane = ec[ax] + (sd > 0 ? 1 : 0);
       int boundary = (plane == 0 || plane == c->nel[ax]);
-      if (boundary) c->cbc[4 * e + f] = c->bc[ax] == REF_BC_PERIODIC ? 2 : 1;
+      if (boundary)
+        c->cbc[4 * e + f] = c->bc[ax] == REF_BC_PERIODIC ? 2 : (c->bc[ax] == REF_BC_PML ? 3 : 1);
       if (boundary && c->bc[ax] == REF_BC_PERIODIC) plane = plane % c->nel[ax];
       long long fid = ax == 0 ? (long long)plane * nely + ec[1]
                               : yoff + (long long)plane * nelx + ec[0];
@@ -1718,9 +1727,9 @@ ref_ctx* ref_create_box2d(int N, int nelx, int nely, const double lo[2], const d
   gs_setup_local(c);
   c->cempec = ialloc(nxzfl);
   long l = 0;
-  for (int e = 0; e < c->nelt; ++e)
+  for (int e = 0; e < c->nelt; ++e)  /* 'PEC' and 'PML' faces (cem_maxwell_pec_init) */
     for (int f = 0; f < 4; ++f)
-      if (c->cbc[4 * e + f] == 1)
+      if (c->cbc[4 * e + f] == 1 || c->cbc[4 * e + f] == 3)
         for (long j = 0; j < n; ++j) c->cempec[l++] = (int)(j + (long)n * (f + 4L * e));
   c->ncempec = l;
 

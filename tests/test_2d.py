@@ -147,6 +147,88 @@ def test_2d_tm_source_bit_exact(name, kind):
     g.close(); ref.close()
 
 
+PML2D = 2  # REF_BC_PML / NEKGPU_BC_PML
+
+
+def boxpml2d(gpu: bool):
+    """The reference's maxwell-2dboxpml-tm (tests/2dboxpml, param(4) = 2):
+    8 x 8 elements on [-1,1]^2 (usrdat2 scales the box), N=8, 'PML' on all
+    four sides (2 layers, order 3, error 1e-8: params 77-79), a Gaussian line
+    current I0 delta(x) delta(y) sin(omega t) on E_z (width 0.1, omega = 2,
+    norm 1/(2 pi width^2)), zero initial fields, dt = 0.1 dxmin (CFL 0.1),
+    4000 steps; usersol is zero and userchk asks L2 and Linf <= 1 on H_x, H_y
+    and E_z (the waves must leave through the PML)."""
+    ref = R.RefBox2D(8, (8, 8), (-1.0, -1.0), (1.0, 1.0), (PML2D, PML2D), TM)
+    ref.set_pml(2, 3.0, 1e-8)
+    ref.pml = (2, 3.0, 1e-8)
+    src = dict(xc=(0.0, 0.0, 0.0), sigma=0.1, amp=1.0 / (2 * np.pi * 0.01), f0=2.0, t0=0.0)
+    obj = ref
+    if gpu:
+        obj = MaxwellGPU.from_arrays2d(oracle_arrays(ref), ref.n, ref.nelt, TM)
+    obj.set_source_kind(1)
+    obj.set_source(**src)
+    zero = np.zeros((3, ref.npts))
+    obj.set_state(zero, zero)
+    dt = 0.1 * ref.dxmin()
+    obj.run(4000, 0.0, dt)
+    if gpu:
+        H, E = obj.get_state()
+        obj.close()
+    else:
+        H, E = ref.hn.copy(), ref.en.copy()
+    for comp in (H[0], H[1], E[2]):
+        l2, li = ref.cem_error(comp, np.zeros_like(comp))
+        assert l2 <= 1.0 and li <= 1.0, (l2, li)
+        assert li > 1e-3  # the source did drive the field
+    ref.close()
+
+
+def test_oracle_2dboxpml_known_answer():
+    boxpml2d(gpu=False)
+
+
+@pytest.mark.gpu
+def test_2dboxpml_known_answer_gpu():
+    boxpml2d(gpu=True)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("mode", [TE, TM])
+@pytest.mark.parametrize("materials", [False, True])
+def test_2d_pml_bit_exact(mode, materials):
+    """pml_step and the auxiliary fields' RK update in the 2-D form: state and
+    pmlbn / pmldn bit-identical to the oracle over 5 steps ('PML' on x, PEC
+    or periodic on y, random fields, the auxiliary fields started at mu H and
+    eps E as the reference's userini sets them)."""
+    bc = (PML2D, PEC if mode == TE else PER)
+    ref = R.RefBox2D(5, (6, 4), (0.0, 0.0), (1.5, 1.0), bc, mode)
+    x, y, z = ref.coords()
+    if materials:
+        ref.set_materials(1.0 + 0.5 * np.sin(3 * x) ** 2, 1.0 + 0.3 * np.cos(2 * y) ** 2)
+    ref.set_pml(2, 3.0, 1e-6)
+    ref.pml = (2, 3.0, 1e-6)
+    g = MaxwellGPU.from_arrays2d(oracle_arrays(ref), ref.n, ref.nelt, mode)
+    rng = np.random.default_rng(7 + mode)
+    H = np.zeros((3, ref.npts)); E = np.zeros((3, ref.npts))
+    Hact, Eact = ((0, 1), (2,)) if mode == TM else ((2,), (0, 1))
+    for q in Hact: H[q] = rng.standard_normal(ref.npts)
+    for q in Eact: E[q] = rng.standard_normal(ref.npts)
+    eps, mu = ref.d("permittivity"), ref.d("permeability")
+    ref.set_state(H, E); g.set_state(H, E)
+    ref.d("pmlbn")[:] = (mu * H).ravel(); ref.d("pmldn")[:] = (eps * E).ravel()
+    g.set_array("pmlbn", mu * H); g.set_array("pmldn", eps * E)
+    dt = 0.2 * ref.dxmin()
+    ref.run(5, 0.0, dt)
+    g.run(5, 0.0, dt)
+    Hg, Eg = g.get_state()
+    np.testing.assert_array_equal(Hg, ref.hn)
+    np.testing.assert_array_equal(Eg, ref.en)
+    np.testing.assert_array_equal(g.array("pmlbn"), ref.d("pmlbn"))
+    np.testing.assert_array_equal(g.array("pmldn"), ref.d("pmldn"))
+    assert np.abs(ref.d("pmldn")).max() > 0
+    g.close(); ref.close()
+
+
 @pytest.mark.gpu
 @pytest.mark.parametrize("name", list(cases.CASES_2D))
 @pytest.mark.parametrize("mode", [TE, TM])
