@@ -150,7 +150,7 @@ int nekgpu_init_box(nekgpu_ctx** ctx, const nekgpu_box* box, int form);
  * the (ld,3) layout with the inactive components left as set.  PML: the
  * mesh's pmlsigma (3*npts), pmlptr and materials as in 3-D (pml_step on the
  * active components, their pmlbn/pmldn through nekgpu_set_array /
- * nekgpu_get_array).  Volume source: TM only (a line current on E_z).  No
+ * nekgpu_get_array).  Volume source: a line source on E_z (TM) or H_z (TE).  No
  * dispersive media, adjoint or VTK output in 2-D. */
 int nekgpu_init2d(nekgpu_ctx** ctx, const nekgpu_mesh* mesh, int imode);
 int nekgpu_finalize(nekgpu_ctx* ctx);
@@ -182,8 +182,9 @@ int nekgpu_set_source_kind(nekgpu_ctx* ctx, int kind);
  * added before the inverse mass like usersrc (src/cem_maxwell.F:503):
  * resEz += bm1 * amp * exp(-|x-xc|^2/(2 sigma^2)) * ricker(t; f0, t0),
  * ricker(t) = (1 - 2 a^2) exp(-a^2), a = pi f0 (t - t0).  enabled=0 clears.
- * 2-D TM context: a line current along z on E3 = E_z (z ignored: give
- * xc[2] = 0); a TE context has no E_z (NEKGPU_ERR_UNSUPPORTED). */
+ * 2-D context: a line source along z (z ignored: give xc[2] = 0) on the
+ * out-of-plane field, E3 = E_z in TM and H3 = H_z in TE, as the reference's
+ * 2-D cases drive it (tests/2dboxpml/2dboxpml.usr). */
 int nekgpu_set_source(nekgpu_ctx* ctx, int enabled, const double xc[3], double sigma,
                       double amp, double f0, double t0);
 

@@ -183,7 +183,8 @@ __global__ void k_stage2d(const Stage2dDev a) {
     }
   }
   // usersrc after the lift, before the inverse mass (src/cem_maxwell.F:503):
-  // the TM form's E3 += bm1-weighted Gaussian x time factor
+  // the out-of-plane field (E3 in TM, H3 in TE) += bm1-weighted Gaussian x
+  // time factor
   if (a.src_w) r[2] = r[2] + a.src_w[g] * a.src_ft;
   const double hb = a.hbm1[g], eb = a.ebm1[g];
   r[0] = r[0] * (tm ? hb : eb);

@@ -2093,8 +2093,8 @@ int nekgpu_set_source(nekgpu_ctx* c, int enabled, const double xc[3], double sig
     return NEKGPU_OK;
   }
   if (!xc || !(sigma > 0)) return NEKGPU_ERR_ARG;
-  // 2-D: the TM form's E3 is E_z (a line source along z); TE has no E_z
-  if (c->ndim == 2 && c->imode != 2) return NEKGPU_ERR_UNSUPPORTED;
+  // 2-D: a line source along z on the out-of-plane field, E3 = E_z in TM and
+  // H3 = H_z in TE, as the reference's 2-D cases drive them
   if ((long)c->host_x.size() != c->npts) return NEKGPU_ERR_STATE;  // needs coordinates
   const double s2 = 2.0 * sigma * sigma;
   std::vector<double> g(c->npts);

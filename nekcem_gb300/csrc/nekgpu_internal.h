@@ -328,7 +328,7 @@ struct Stage2dDev {
   double* u_out;
   double* k;
   double ca, cb, dt;
-  const double* src_w;  // npts or null: TM volume source on E3 (usersrc)
+  const double* src_w;  // npts or null: volume source on E3 (TM) or H3 (TE) (usersrc)
   double src_ft;        // its time factor at the stage time
   // PML (pml_step, the reference's full-size arrays); pml_elem null without
   const int* pml_elem;          // nelt: 1 on PML elements

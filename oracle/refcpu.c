@@ -1031,13 +1031,15 @@ void ref_dispersive(ref_ctx* c, int rkstep, double dt) {
   if (c->ljn) lorentz_step(c, rkstep, dt);
 }
 
-/* usersrc (src/cem_maxwell.F:503): mass-weighted E_z source */
+/* usersrc (src/cem_maxwell.F:503): mass-weighted E_z source; in the 2-D TE
+ * form the out-of-plane H_z instead (tests/2dboxpml/2dboxpml.usr:28-100:
+ * srchz in TE, srcez in TM) */
 void ref_usersrc(ref_ctx* c, double rktime) {
   if (!c->src_w) return;
   /* kind 1: tests/3dboxpml/3dboxpml.usr:72-82, srcez - exp(..) * sin(-omega t) * bm1 */
   double ft = c->src_kind == 1 ? -c->src_amp * sin(-c->src_f0 * rktime)
                                : c->src_amp * ref_source_time(rktime, c->src_f0, c->src_t0);
-  double* rez = c->resen + 2 * c->npts;
+  double* rez = (c->ndim == 2 && c->imode == 1 ? c->reshn : c->resen) + 2 * c->npts;
   for (long i = 0; i < c->npts; ++i) rez[i] = rez[i] + c->src_w[i] * ft;
 }
 

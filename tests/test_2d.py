@@ -119,16 +119,18 @@ def test_2d_bit_exact(name, mode, materials):
 @pytest.mark.gpu
 @pytest.mark.parametrize("name", list(MESHES_2D))
 @pytest.mark.parametrize("kind", [0, 1])
-def test_2d_tm_source_bit_exact(name, kind):
-    """usersrc in the TM form: a Gaussian line current on E_z (z ignored),
-    added after the lift and before the inverse mass, as the reference's 2-D
-    cases do (tests/2dboxpml/2dboxpml.usr: srcez -= norm exp(..) sin(-omega t)
-    bm1); Ricker (kind 0) or sin(f0 t) (kind 1) in time; bit-identical to the
-    oracle over 5 steps from rest."""
+@pytest.mark.parametrize("mode", [TE, TM])
+def test_2d_source_bit_exact(name, kind, mode):
+    """usersrc in the 2-D forms: a Gaussian line source on the out-of-plane
+    field (E_z in TM, H_z in TE; z ignored), added after the lift and before
+    the inverse mass, as the reference's 2-D cases do
+    (tests/2dboxpml/2dboxpml.usr: srcez or srchz -= norm exp(..)
+    sin(-omega t) bm1); Ricker (kind 0) or sin(f0 t) (kind 1) in time;
+    bit-identical to the oracle over 5 steps from rest."""
     b = MESHES_2D[name]
-    ref = R.RefBox2D(b["N"], b["nel"], b["lo"], b["hi"], b["bc"], TM)
+    ref = R.RefBox2D(b["N"], b["nel"], b["lo"], b["hi"], b["bc"], mode)
     x, y, z = ref.coords()
-    g = MaxwellGPU.from_arrays2d(oracle_arrays(ref), ref.n, ref.nelt, TM)
+    g = MaxwellGPU.from_arrays2d(oracle_arrays(ref), ref.n, ref.nelt, mode)
     xc = (0.5 * (b["lo"][0] + b["hi"][0]), 0.5 * (b["lo"][1] + b["hi"][1]), 0.0)
     src = dict(xc=xc, sigma=0.15, amp=2.0, f0=2.0, t0=0.05)
     for obj in (ref, g):
@@ -141,7 +143,8 @@ def test_2d_tm_source_bit_exact(name, kind):
     ref.run(5, 0.0, dt)
     g.run(5, 0.0, dt)
     Hg, Eg = g.get_state()
-    assert np.abs(ref.en[2]).max() > 1e-6  # the source drove the field
+    out_of_plane = ref.en[2] if mode == TM else ref.hn[2]
+    assert np.abs(out_of_plane).max() > 1e-6  # the source drove the field
     np.testing.assert_array_equal(Hg, ref.hn)
     np.testing.assert_array_equal(Eg, ref.en)
     g.close(); ref.close()
@@ -150,21 +153,22 @@ def test_2d_tm_source_bit_exact(name, kind):
 PML2D = 2  # REF_BC_PML / NEKGPU_BC_PML
 
 
-def boxpml2d(gpu: bool):
-    """The reference's maxwell-2dboxpml-tm (tests/2dboxpml, param(4) = 2):
-    8 x 8 elements on [-1,1]^2 (usrdat2 scales the box), N=8, 'PML' on all
-    four sides (2 layers, order 3, error 1e-8: params 77-79), a Gaussian line
-    current I0 delta(x) delta(y) sin(omega t) on E_z (width 0.1, omega = 2,
-    norm 1/(2 pi width^2)), zero initial fields, dt = 0.1 dxmin (CFL 0.1),
-    4000 steps; usersol is zero and userchk asks L2 and Linf <= 1 on H_x, H_y
-    and E_z (the waves must leave through the PML)."""
-    ref = R.RefBox2D(8, (8, 8), (-1.0, -1.0), (1.0, 1.0), (PML2D, PML2D), TM)
+def boxpml2d(gpu: bool, mode: int):
+    """The reference's maxwell-2dboxpml-te / -tm (tests/2dboxpml, param(4) =
+    1 | 2): 8 x 8 elements on [-1,1]^2 (usrdat2 scales the box), N=8, 'PML'
+    on all four sides (2 layers, order 3, error 1e-8: params 77-79), a
+    Gaussian line current I0 delta(x) delta(y) sin(omega t) on the
+    out-of-plane field (E_z in TM, H_z in TE; width 0.1, omega = 2, norm
+    1/(2 pi width^2)), zero initial fields, dt = 0.1 dxmin (CFL 0.1), 4000
+    steps; usersol is zero and userchk asks L2 and Linf <= 1 on the mode's
+    three components (the waves must leave through the PML)."""
+    ref = R.RefBox2D(8, (8, 8), (-1.0, -1.0), (1.0, 1.0), (PML2D, PML2D), mode)
     ref.set_pml(2, 3.0, 1e-8)
     ref.pml = (2, 3.0, 1e-8)
     src = dict(xc=(0.0, 0.0, 0.0), sigma=0.1, amp=1.0 / (2 * np.pi * 0.01), f0=2.0, t0=0.0)
     obj = ref
     if gpu:
-        obj = MaxwellGPU.from_arrays2d(oracle_arrays(ref), ref.n, ref.nelt, TM)
+        obj = MaxwellGPU.from_arrays2d(oracle_arrays(ref), ref.n, ref.nelt, mode)
     obj.set_source_kind(1)
     obj.set_source(**src)
     zero = np.zeros((3, ref.npts))
@@ -176,20 +180,22 @@ def boxpml2d(gpu: bool):
         obj.close()
     else:
         H, E = ref.hn.copy(), ref.en.copy()
-    for comp in (H[0], H[1], E[2]):
+    for comp in ((H[0], H[1], E[2]) if mode == TM else (E[0], E[1], H[2])):
         l2, li = ref.cem_error(comp, np.zeros_like(comp))
         assert l2 <= 1.0 and li <= 1.0, (l2, li)
         assert li > 1e-3  # the source did drive the field
     ref.close()
 
 
-def test_oracle_2dboxpml_known_answer():
-    boxpml2d(gpu=False)
+@pytest.mark.parametrize("mode", [TE, TM])
+def test_oracle_2dboxpml_known_answer(mode):
+    boxpml2d(False, mode)
 
 
 @pytest.mark.gpu
-def test_2dboxpml_known_answer_gpu():
-    boxpml2d(gpu=True)
+@pytest.mark.parametrize("mode", [TE, TM])
+def test_2dboxpml_known_answer_gpu(mode):
+    boxpml2d(True, mode)
 
 
 @pytest.mark.gpu
@@ -242,10 +248,7 @@ def test_2d_refusals(tmp_path):
     arrays = oracle_arrays(ref)
     g = MaxwellGPU.from_arrays2d(arrays, ref.n, ref.nelt, TM)
     g.set_state(np.zeros((3, g.npts)), np.zeros((3, g.npts)))
-    te = MaxwellGPU.from_arrays2d(arrays, ref.n, ref.nelt, TE)  # TE has no E_z
-    te.set_state(np.zeros((3, g.npts)), np.zeros((3, g.npts)))
     calls = [
-        lambda: te.set_source((0.5, 0.5, 0.0), 0.1, 1.0, 1.0, 0.0),
         lambda: g.set_dispersive(g.DRUDE, np.ones((2, g.npts)), np.arange(3)),
         lambda: g.adjoint_gradient(1, 0.0, 0.01, np.ones(g.npts)),
         lambda: g.write_vtk(str(tmp_path / "x.vtk")),
@@ -254,7 +257,7 @@ def test_2d_refusals(tmp_path):
         with pytest.raises(L.NekgpuError) as e:
             call()
         assert e.value.status == -8
-    g.close(); te.close()
+    g.close()
     bad = dict(arrays)
     cf = bad["cemface"].copy()
     cf[[0, 1]] = cf[[1, 0]]  # not the reference's face numbering
