@@ -663,6 +663,59 @@ class GrapheneSheet:
         return (-1.0, 0.0, 1.0, 1.0, 0.0, 1.0), (0.0, -self.omega, 0.0), self.omega
 
 
+class Graphene2D(GrapheneSheet):
+    """The reference's tests/2dgraphene (maxwell-2dgraphene-te / -tm) restated
+    in 3-D like the other 2-D cases: one mode, TE (H_z, E_x) or TM (E_z, H_x),
+    the same sheet model as tests/3dgraphene; 4 x 32 elements on [-2.5,2.5] x
+    [-5,5] (usrdat2: sx = 5, sy = 10), two periodic elements along z on
+    [-2.5,2.5] (no coarser than y, so dxmin is the 2-D one), N=8, 'PML' at
+    both y ends (6 layers, order 3, error 1e-15: params 77-79), dt = 0.2
+    dxmin (CFL 0.2), 1000 steps.  userchk's tolerances: L2 1e-7, Linf 5e-6 on
+    the mode's two components.  The 2-D case also bounds E_y (TE) or H_y (TM),
+    zero in the exact solution, by its 2-D round-off (L2 1e-14, Linf 5e-13);
+    the 3-D operator's round-off there is larger (Linf 6.9e-13), so all
+    components that are zero get the FP64 round-off bound of the tests."""
+
+    nel = (4, 32, 2)
+    pml = (6, 3.0, 1e-15)
+    cfl = 0.2
+
+    def __init__(self, mode: int):
+        super().__init__()
+        self.mode = mode
+        act = (2, 3) if mode == TE else (0, 5)
+        self.l2tol = tuple(1e-7 if q in act else None for q in range(6))
+        self.linftol = tuple(5e-6 if q in act else None for q in range(6))
+
+    def exact(self, x, y, z, t, n3):
+        H, E = super().exact(x, y, z, t, n3)
+        if self.mode == TE:  # H_z, E_x
+            H[0] = 0.0; E[2] = 0.0
+        else:  # E_z, H_x
+            H[2] = 0.0; E[0] = 0.0
+        return H, E
+
+    def sheet(self, y, cemface, n3, nf, nxzfl):
+        # userini's enpar for the one mode (tests/2dgraphene/2dgraphene.usr)
+        keep = self.refltm, self.reflte
+        if self.mode == TE:
+            self.refltm = -1.0  # 0.5 (1 + refl) = 0 on z
+        else:
+            self.reflte = 1.0   # 0.5 z1 (1 - refl) = 0 on x
+        try:
+            return super().sheet(y, cemface, n3, nf, nxzfl)
+        finally:
+            self.refltm, self.reflte = keep
+
+    def incident(self):
+        amp, k, om = super().incident()
+        if self.mode == TE:  # incfhz += u, incfex += eta u
+            amp = (0.0, 0.0, 1.0, 1.0, 0.0, 0.0)
+        else:  # incfez += u, incfhx -= u/eta
+            amp = (-1.0, 0.0, 0.0, 0.0, 0.0, 1.0)
+        return amp, k, om
+
+
 def zero_fields(x, y, z):
     return np.zeros((3, x.size)), np.zeros((3, x.size))
 
