@@ -437,11 +437,13 @@ __device__ __forceinline__ void disp_node(const MixedDev& a, int l, int v, long 
 
 // Blocks per SM the launch is built for: four of the unpadded NX = 8 layout
 // (54 KB, 64 registers), six at NX = 6 (160 threads, 28 KB, 64 registers:
-// 2 % faster than five at 72; seven spill and lose 12 %), three otherwise
-// and with the extension branches.
+// 2 % faster than five at 72; seven spill and lose 12 %), two at NX = 9
+// (384 threads, 85 KB: shared memory allows no third, and 80 registers
+// instead of 56 remove the spills: 4.5 % faster), three otherwise and with
+// the extension branches.
 template <int NX, bool EXT>
 constexpr int mixed_min_blocks() {
-  return EXT ? 3 : (MCfg<NX>::kSwz ? 4 : (NX == 6 ? 6 : 3));
+  return NX == 9 ? 2 : (EXT ? 3 : (MCfg<NX>::kSwz ? 4 : (NX == 6 ? 6 : 3)));
 }
 
 // EXT: the variant with the PML, dispersive-current, incident-field and
