@@ -6,8 +6,9 @@
  * element-major COMMON arrays; under a NEKGPU build, cem_maxwell_op_rk
  * (src/cem_maxwell.F:327-345) calls nekgpu_step / nekgpu_op_rk_host instead of
  * its five CPU stages, after cem_maxwell_init (src/cem_maxwell.F:65-191) has
- * handed the static arrays to nekgpu_init.  The Fortran binding
- * (iso_c_binding interfaces) is shown in INTEGRATION.md.
+ * handed the static arrays to nekgpu_init.  The Fortran side binds these
+ * entry points with iso_c_binding interfaces (bind(c), scalars by value
+ * where declared so here, arrays as assumed-size dummies).
  *
  * Conventions
  *   - Plain C types only; all arrays are caller-owned host memory in the
@@ -267,12 +268,19 @@ int nekgpu_unregister_host(nekgpu_ctx* ctx, void* ptr);
 /* One RK stage rkstep=1..5 at time `time` (rk_c + cem_maxwell_op +
  * rk_maxwell_ab; src/cem_maxwell.F:336-340). */
 int nekgpu_stage(nekgpu_ctx* ctx, int rkstep, double time, double dt);
-/* nsteps full steps (cem_maxwell_op_rk each), device-resident state;
- * *time += dt after each step as time_advancing_pde does (src/cem_drive.F:639). */
+/* nsteps full steps (cem_maxwell_op_rk each) on the device-resident state,
+ * step s running its stages at *time + c_i dt.  On return *time has been
+ * advanced by the library: dt is added after every step, in the same
+ * floating-point order as time_advancing_pde's `time = time + dt`
+ * (src/cem_drive.F:639), so *time ends at the time of the new state.
+ * A driver whose own loop advances time after the call (time_advancing_pde
+ * does) must therefore pass a copy, `tloc = time; nekgpu_step(ctx, 1, &tloc,
+ * dt);` -- passing its own time variable would advance it twice per step. */
 int nekgpu_step(nekgpu_ctx* ctx, int nsteps, double* time, double dt);
 /* Drop-in for one cem_maxwell_op_rk call on host arrays: copies hn/en in,
- * runs the 5 stages, copies hn/en back; returns when hn/en hold the new
- * state.  The RK register stays on the GPU.  In the mixed form on meshes of
+ * runs the 5 stages at time + c_i dt, copies hn/en back; returns when hn/en
+ * hold the new state.  time is taken by value and not advanced: the caller's
+ * loop adds dt itself, as time_advancing_pde does.  The RK register stays on the GPU.  In the mixed form on meshes of
  * several waves of blocks the copies overlap stages 1 and 5 chunk by chunk
  * (same results bit for bit); hn/en page-locked with nekgpu_register_host
  * let the copies run at the link's rate. */

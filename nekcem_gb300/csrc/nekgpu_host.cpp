@@ -2136,19 +2136,25 @@ int nekgpu_set_source(nekgpu_ctx* c, int enabled, const double xc[3], double sig
     int* d_off;
     if ((st = A.put(&d_off, off))) return st;
     if (c->form == NEKGPU_MIXED) {
-      // normalised like the residual: weight / (bm1 * 2/hx) = weight / (w3 * rx)
-      std::vector<float> wf(wd.size());
+      // normalised like the residual: weight / (bm1 * 2/hx) = weight / (w3 * rx),
+      // as a (hi, lo) float pair (~2^-48 of the weight)
+      std::vector<float> wf(2 * wd.size());
       for (int e = 0, s0 = 0; e < c->nelt; ++e) {
         if (off[e] < 0) continue;
-        for (long v = 0; v < n3; ++v)
-          wf[(size_t)s0 * n3 + v] = (float)(wd[(size_t)s0 * n3 + v] / (c->host_w3[v] * c->host_rx[e]));
+        for (long v = 0; v < n3; ++v) {
+          const size_t i = (size_t)s0 * n3 + v;
+          const double w = wd[i] / (c->host_w3[v] * c->host_rx[e]);
+          const float hi = (float)w;
+          wf[2 * i] = hi;
+          wf[2 * i + 1] = (float)(w - (double)hi);
+        }
         ++s0;
       }
       float* d;
       if ((st = A.put(&d, wf))) return st;
       c->d_src_w = d;
       c->margs.src_elem = d_off;
-      c->margs.src_w = d;
+      c->margs.src_w = reinterpret_cast<const float2*>(d);
     } else if (c->form == NEKGPU_MIXED_NAIVE) {
       std::vector<float> wf(wd.begin(), wd.end());
       float* d;

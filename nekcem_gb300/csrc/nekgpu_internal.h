@@ -254,8 +254,8 @@ struct MixedDev {
   const float* egm;     // 12*nelt: rho_y (hi,lo), rho_z (hi,lo), lift factor per slot, cubic
   const void* fcoef;    // float4 per face node, null when uniform
   const int* src_elem;  // nelt or null
-  const float* src_w;   // normalised source weights, nx^3 per source element
-  float src_ftf;
+  const float2* src_w;  // normalised source weights as (hi, lo) pairs, nx^3 per source element
+  float2 src_ft2;       // time factor of the stage as a (hi, lo) pair
   double a, b;
   float C0f;
   int* status;

@@ -87,6 +87,20 @@ __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
   e = (a - (s - bb)) + (b - bb);
 }
 
+// (Rh, Rl) += w * f for float pairs w = (wh, wl), f = (fh, fl): the product's
+// rounding error and cross terms go to the low part (~2^-46 of |w f|), so a
+// volume source enters the residual pair at the pair's own precision
+__device__ __forceinline__ void add_pair_product(float& Rh, float& Rl, float2 w, float2 f) {
+  const float p = w.x * f.x;
+  float e = fmaf(w.x, f.x, -p);
+  e = fmaf(w.x, f.y, e);
+  e = fmaf(w.y, f.x, e);
+  float s, t;
+  two_sum(Rh, p, s, t);
+  Rh = s;
+  Rl = (Rl + e) + t;
+}
+
 // ---------------------------------------------------------------------------
 // mbarrier + 1-D TMA bulk copy (PTX)
 // ---------------------------------------------------------------------------
@@ -731,9 +745,9 @@ __global__ void __launch_bounds__(MCfg<NX>::NT, mixed_min_blocks<NX, EXT>())
           const int c = w < N3 ? 2 : 5;
           const int v = w < N3 ? w : w - N3;
           const float2 rr = s_R2[c * N3P + pnode<NX>(v)];
-          float Rl = rr.y;
-          if (c == 5 && so >= 0) Rl = fmaf(a.src_w[(long)so * N3 + v], a.src_ftf, Rl);
-          rk_finish(a, c, (long)e * N3 + v, rr.x, Rl, first_stage);
+          float Rh = rr.x, Rl = rr.y;
+          if (c == 5 && so >= 0) add_pair_product(Rh, Rl, a.src_w[(long)so * N3 + v], a.src_ft2);
+          rk_finish(a, c, (long)e * N3 + v, Rh, Rl, first_stage);
         }
       }
       __syncthreads();  // the split pairs are consumed: the next element may land
@@ -771,7 +785,7 @@ __global__ void __launch_bounds__(MCfg<NX>::NT, mixed_min_blocks<NX, EXT>())
         }
         if (EXT && pml_l >= 0) pml_node<N3>(a, pml_l, v, (long)e * N3 + v, first_stage, Rh, Rl);
         if (EXT && disp_l >= 0) disp_node<N3>(a, disp_l, v, (long)e * N3 + v, first_stage, Rh, Rl);
-        if (so >= 0) Rl[5] = fmaf(a.src_w[(long)so * N3 + v], a.src_ftf, Rl[5]);
+        if (so >= 0) add_pair_product(Rh[5], Rl[5], a.src_w[(long)so * N3 + v], a.src_ft2);
 #pragma unroll
         for (int c = 0; c < 6; ++c) rk_finish(a, c, (long)e * N3 + v, Rh[c], Rl[c], first_stage);
       }
@@ -870,7 +884,11 @@ int mixed_stage_range(Context* c, int rkstep, double time, double dt, int e0, in
   a.a = c->rk_a[rkstep - 1];
   a.b = c->rk_b[rkstep - 1];
   a.dt = dt;
-  if (c->src.enabled) a.src_ftf = (float)source_ft(c->src, time + dt * c->rk_c[rkstep - 1]);
+  if (c->src.enabled) {
+    const double ft = source_ft(c->src, time + dt * c->rk_c[rkstep - 1]);
+    const float hi = (float)ft;
+    a.src_ft2 = make_float2(hi, (float)(ft - (double)hi));
+  }
   const bool ext = a.pml.slot || a.disp.slot || a.inc_elem || a.gr.elem;
   if (a.inc_elem && (st = incident_upload(c, time + dt * c->rk_c[rkstep - 1]))) return st;
   if (a.gr.elem) {

@@ -18,7 +18,10 @@
 //    race and give wrong results; serialise them;
 //  * the first call on a device looks up the array's device address with
 //    cudaGetSymbolAddress (once per device, with that device current); make
-//    that first call before any stream capture.
+//    that first call before any stream capture;
+//  * the call works on the context's own device: when another device is
+//    current it makes the context's device current for the call and puts the
+//    caller's device back before returning.
 // Nothing in the array has to start at zero: each call writes every partial
 // it later reads.
 #include <cuda_runtime.h>
@@ -88,12 +91,11 @@ __global__ void k_norm_final(int nblocks, double* __restrict__ part) {
 
 }  // namespace
 
-// Set-up (first call per device) and the reduction; allocates nothing.
-int norms_noalloc(Context* c, const double* exact_dev, double l2[6], double linf[6]) {
-  if (c->npts > (long)kMaxBlocks * kPointsPerBlock) return NEKGPU_ERR_TOO_LARGE;
-  int dev = 0;
-  if (check_cuda(cudaGetDevice(&dev))) return NEKGPU_ERR_CUDA;
-  if (dev < 0 || dev >= kMaxDevices) return NEKGPU_ERR_UNSUPPORTED;
+namespace {
+
+// Set-up (first call per device) and the reduction on the current device,
+// which is the context's; allocates nothing.
+int norms_on_device(Context* c, int dev, const double* exact_dev, double l2[6], double linf[6]) {
   if (!g_scratch_ptr[dev]) {
     double* p = nullptr;
     if (check_cuda(cudaGetSymbolAddress((void**)&p, g_norm_scratch))) return NEKGPU_ERR_CUDA;
@@ -117,6 +119,20 @@ int norms_noalloc(Context* c, const double* exact_dev, double l2[6], double linf
     linf[q] = fin[6 + q];
   }
   return NEKGPU_OK;
+}
+
+}  // namespace
+
+int norms_noalloc(Context* c, const double* exact_dev, double l2[6], double linf[6]) {
+  if (c->npts > (long)kMaxBlocks * kPointsPerBlock) return NEKGPU_ERR_TOO_LARGE;
+  const int dev = c->device;
+  if (dev < 0 || dev >= kMaxDevices) return NEKGPU_ERR_UNSUPPORTED;
+  int prev = 0;
+  if (check_cuda(cudaGetDevice(&prev))) return NEKGPU_ERR_CUDA;
+  if (prev != dev && check_cuda(cudaSetDevice(dev))) return NEKGPU_ERR_CUDA;
+  const int st = norms_on_device(c, dev, exact_dev, l2, linf);
+  if (prev != dev && check_cuda(cudaSetDevice(prev)) && st == NEKGPU_OK) return NEKGPU_ERR_CUDA;
+  return st;
 }
 
 }  // namespace nekgpu

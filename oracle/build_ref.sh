@@ -5,15 +5,18 @@
 # serial branch.  Only the sources the gs path needs are compiled.  Test
 # infrastructure only; outputs go to oracle/_ref/ (git-ignored).
 #
-# usage: oracle/build_ref.sh [REFERENCE_ROOT]   (default /root/reference)
+# usage: oracle/build_ref.sh [REFERENCE_ROOT]
+#   REFERENCE_ROOT defaults to $NEKCEM_REFERENCE_ROOT, else /root/reference.
+#   Exit status 3 (nothing built) when the reference tree is not there: the
+#   GPU machines carry the built library in oracle/_ref/ instead.
 set -euo pipefail
-REF="${1:-/root/reference}"
+REF="${1:-${NEKCEM_REFERENCE_ROOT:-/root/reference}}"
 JL="$REF/src/jl"
 HERE="$(cd "$(dirname "$0")" && pwd)"
 OUT="$HERE/_ref"
 if [ ! -f "$JL/gs.c" ]; then
-  echo "reference jl sources not found under $JL" >&2
-  exit 2
+  echo "reference jl sources not found under $JL: nothing built" >&2
+  exit 3
 fi
 mkdir -p "$OUT"
 OBJ="$(mktemp -d)"

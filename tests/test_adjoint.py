@@ -217,3 +217,39 @@ def test_memory_budget_selects_the_binomial_schedule(monkeypatch):
     with pytest.raises(L.NekgpuError) as e:
         pb.gradient(eps)
     assert e.value.status == -4
+
+
+@pytest.mark.gpu
+def test_adjoint_workload_matches_central_differences_at_full_length():
+    """The adjoint configuration at its own size and length: unit PEC box,
+    8^3 elements, N=7, eps = 1 + 3 sigmoid(Gaussian random field, length
+    0.15, seed 4), the Gaussian E_z source (sigma 0.05 at 0.3 (1,1,1),
+    Ricker), zero initial fields, 2000 RK45 steps, J = sum bm1 |E|^2 over the
+    probe cube [0.7, 0.9]^3 at the final time.  dJ/deps from the adjoint with
+    sqrt(steps) checkpointing against central differences of the FP64
+    forward, h = 1e-6, 20 directions v ~ N(0,1) per node from seeds
+    1000..1019, 1e-6 relative."""
+    from adjoint_autograd import BoxProblem
+    c = cases.make("adjoint")
+    g = MaxwellGPU.from_box(c.N, c.nel, c.lo, c.hi, c.bc, form="fused64")
+    x, y, z = g.coords()
+    bm1 = g.array("bmn")
+    g.close()
+    eps = c.eps(x, y, z)
+    (p0, p1), (q0, q1), (r0, r1) = c.extra["probe"]
+    inside = (x > p0) & (x < p1) & (y > q0) & (y < q1) & (z > r0) & (z < r1)
+    jw = np.where(inside, bm1, 0.0)
+    H0, E0 = c.init_fields(x, y, z)
+    dt = c.timestep(x, y, z)
+    pb = BoxProblem(c.N, c.nel, c.lo, c.hi, c.bc, H0, E0, jw, c.nsteps, dt, source=c.source)
+    J, grad = pb.gradient(eps)
+    assert c.nsteps == 2000
+    assert J == pytest.approx(pb.objective(eps), rel=1e-14)
+    h = 1e-6
+    worst = 0.0
+    for seed in range(1000, 1020):
+        d = np.random.default_rng(seed).standard_normal(eps.size)
+        fd = (pb.objective(eps + h * d) - pb.objective(eps - h * d)) / (2 * h)
+        ad = float(grad @ d)
+        worst = max(worst, abs(fd - ad) / abs(ad))
+    assert worst <= 1e-6, worst

@@ -5,7 +5,9 @@ not acceptable between steps).  It takes the exact fields already on the
 device and keeps its scratch in a fixed device array of the library, so it
 must agree with nekgpu_norms -- which copies the exact fields to a fresh
 device buffer -- on two calls in a row (the second reuses the array the first
-left behind), and it must refuse meshes larger than that array allows.
+left behind), leave the context's device memory and the device's free
+memory unchanged across a call, and refuse meshes larger than that array
+allows.
 
 This file is collected last on purpose (pytest runs files in name order).
 """
@@ -46,11 +48,17 @@ def test_norms_noalloc_matches_norms_twice(form):
     Hx, Ex = c.exact(x, y, z, t)
     l2_ref, li_ref = g.cem_error(Hx, Ex)
     exact_dev = _device_copy(np.concatenate([Hx.ravel(), Ex.ravel()]))
+    import torch
     for call in range(2):
+        # the first call also loads the kernels; the second must allocate nothing
+        before = (g.device_bytes(), torch.cuda.mem_get_info()[0])
         st, l2, li = _noalloc(g, exact_dev.data_ptr())
+        after = (g.device_bytes(), torch.cuda.mem_get_info()[0])
         assert st == 0, L.load().nekgpu_error_string(st).decode()
         np.testing.assert_allclose(l2, l2_ref, rtol=1e-12, atol=0, err_msg=f"call {call}")
         np.testing.assert_allclose(li, li_ref, rtol=1e-12, atol=0, err_msg=f"call {call}")
+        if call == 1:
+            assert after == before, (before, after)
     g.close()
 
 
