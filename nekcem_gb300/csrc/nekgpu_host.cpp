@@ -961,6 +961,18 @@ int upload_fused(Context* c, const Compact& cp) {
       c->d_fcoef = d;
     } else {
       std::vector<float> f(cp.fcoef.begin(), cp.fcoef.end());
+      if (c->form == NEKGPU_MIXED) {
+        // float pairs: per face node the hi parts (Y02, C02Y, Z02, C02Z), then
+        // the lo parts
+        const size_t nf = cp.fcoef.size() / 4;
+        f.assign(8 * nf, 0.0f);
+        for (size_t j = 0; j < nf; ++j)
+          for (int q = 0; q < 4; ++q) {
+            const double v = cp.fcoef[4 * j + q];
+            f[8 * j + q] = (float)v;
+            f[8 * j + 4 + q] = (float)(v - (double)f[8 * j + q]);
+          }
+      }
       float* d;
       if ((st = A.put(&d, f))) return st;
       c->d_fcoef = d;
@@ -969,20 +981,34 @@ int upload_fused(Context* c, const Compact& cp) {
   if ((st = fused_setup(c))) return st;
   c->coef_dt = std::nan("");
   if (c->form == NEKGPU_MIXED) {
-    // per element: rho_y = sy/rx and rho_z = tz/rx as float pairs, the lift
-    // factor area/(bm1*2/hx) = A_f/(w_end*rx) per slot, and a cubic flag
+    // per element (16 floats): rho_y = sy/rx and rho_z = tz/rx as float
+    // pairs (1, 0 both on cubic elements), then the lift factor
+    // area/(bm1*2/hx) = A_f/(w_end*rx) per slot, hi parts then lo parts
     const double wend = cp.w[0];
-    std::vector<float> egm(12 * (size_t)c->nelt, 0.0f);
+    std::vector<float> egm(16 * (size_t)c->nelt, 0.0f);
     for (int e = 0; e < c->nelt; ++e) {
       const double* g = &cp.egeom[9 * (size_t)e];
       const double ry = g[1] / g[0], rz = g[2] / g[0];
-      float* o = &egm[12 * (size_t)e];
+      float* o = &egm[16 * (size_t)e];
       o[0] = (float)ry; o[1] = (float)(ry - (double)o[0]);
       o[2] = (float)rz; o[3] = (float)(rz - (double)o[2]);
-      for (int f = 0; f < 6; ++f) o[4 + f] = (float)(g[3 + f] / (wend * g[0]));
-      o[10] = (ry == 1.0 && rz == 1.0) ? 1.0f : 0.0f;
+      for (int f = 0; f < 6; ++f) {
+        const double lf = g[3 + f] / (wend * g[0]);
+        o[4 + f] = (float)lf;
+        o[10 + f] = (float)(lf - (double)o[4 + f]);
+      }
     }
     if ((st = A.put(&c->d_egm, egm))) return st;
+    c->mixed_pec = false;
+    for (int v : cp.nbr) c->mixed_pec = c->mixed_pec || v < 0;
+    // the warp-specialised kernel's residual ring: two slots of six
+    // components per block, for up to four blocks per SM
+    if (c->nx == 8 || c->nx == 6) {
+      int sms = 0;
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
+      c->ring_floats2 = (size_t)4 * std::max(sms, 1) * 2 * 6 * (size_t)c->nx * c->nx * c->nx;
+      if ((st = A.get(&c->d_ring, c->ring_floats2))) return st;
+    }
     MixedDev& m = c->margs;
     m = MixedDev{};
     m.nelt = c->nelt;
@@ -994,6 +1020,7 @@ int upload_fused(Context* c, const Compact& cp) {
     m.fcoef = c->d_fcoef;
     m.C0f = (float)cp.C0;
     m.status = c->d_status;
+    m.ring = c->d_ring;
     if (c->nx > kMaxMixed) return NEKGPU_ERR_UNSUPPORTED;
     // the mixed form uses the library's own GLL D of this order (exactly
     // centro-antisymmetric, computed once per order); a caller's D must agree

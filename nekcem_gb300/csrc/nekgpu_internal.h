@@ -251,8 +251,8 @@ struct MixedDev {
   double* k;
   const float2* coef;   // 2*npts (hi, lo) pairs of dt*hbm1*w3*rx | dt*ebm1*w3*rx
   const int* nbr;       // 6*nelt
-  const float* egm;     // 12*nelt: rho_y (hi,lo), rho_z (hi,lo), lift factor per slot, cubic
-  const void* fcoef;    // float4 per face node, null when uniform
+  const float* egm;     // 16*nelt: rho_y (hi,lo), rho_z (hi,lo), lift factor per slot (6 hi, 6 lo)
+  const void* fcoef;    // per face node Y02, C02Y, Z02, C02Z: float4 hi, float4 lo; null when uniform
   const int* src_elem;  // nelt or null
   const float2* src_w;  // normalised source weights as (hi, lo) pairs, nx^3 per source element
   float2 src_ft2;       // time factor of the stage as a (hi, lo) pair
@@ -266,6 +266,7 @@ struct MixedDev {
   GrapheneDev gr;
   double dt;
   int e_begin, e_end;  // elements of this launch
+  float2* ring;        // warp-specialised kernel: residual pairs, 2 slots x 6 x nx^3 per block
 };
 
 // Reverse of one FP64 stage (nekgpu_adjoint.cu)
@@ -344,6 +345,9 @@ struct Context {
   bool curved = false;      // fused FP64 form on a curvilinear mesh (nekgpu_curved.cu)
   CurvedDev cargs{};
   int device = 0;
+  bool mixed_pec = false;    // the mixed form's mesh has PEC / PML walls (nbr < 0)
+  float2* d_ring = nullptr;  // residual ring of the warp-specialised mixed kernel
+  size_t ring_floats2 = 0;   // its size in float2
   int nx = 0, nelt = 0;
   long npts = 0, nxzfl = 0;
   double volume = 0;
