@@ -999,16 +999,6 @@ int upload_fused(Context* c, const Compact& cp) {
       }
     }
     if ((st = A.put(&c->d_egm, egm))) return st;
-    c->mixed_pec = false;
-    for (int v : cp.nbr) c->mixed_pec = c->mixed_pec || v < 0;
-    // the warp-specialised kernel's residual ring: two slots of six
-    // components per block, for up to four blocks per SM
-    if (c->nx == 8 || c->nx == 6) {
-      int sms = 0;
-      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
-      c->ring_floats2 = (size_t)4 * std::max(sms, 1) * 2 * 6 * (size_t)c->nx * c->nx * c->nx;
-      if ((st = A.get(&c->d_ring, c->ring_floats2))) return st;
-    }
     MixedDev& m = c->margs;
     m = MixedDev{};
     m.nelt = c->nelt;
@@ -1020,7 +1010,6 @@ int upload_fused(Context* c, const Compact& cp) {
     m.fcoef = c->d_fcoef;
     m.C0f = (float)cp.C0;
     m.status = c->d_status;
-    m.ring = c->d_ring;
     if (c->nx > kMaxMixed) return NEKGPU_ERR_UNSUPPORTED;
     // the mixed form uses the library's own GLL D of this order (exactly
     // centro-antisymmetric, computed once per order); a caller's D must agree

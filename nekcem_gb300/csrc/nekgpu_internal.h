@@ -266,7 +266,6 @@ struct MixedDev {
   GrapheneDev gr;
   double dt;
   int e_begin, e_end;  // elements of this launch
-  float2* ring;        // warp-specialised kernel: residual pairs, 2 slots x 6 x nx^3 per block
 };
 
 // Reverse of one FP64 stage (nekgpu_adjoint.cu)
@@ -345,9 +344,6 @@ struct Context {
   bool curved = false;      // fused FP64 form on a curvilinear mesh (nekgpu_curved.cu)
   CurvedDev cargs{};
   int device = 0;
-  bool mixed_pec = false;    // the mixed form's mesh has PEC / PML walls (nbr < 0)
-  float2* d_ring = nullptr;  // residual ring of the warp-specialised mixed kernel
-  size_t ring_floats2 = 0;   // its size in float2
   int nx = 0, nelt = 0;
   long npts = 0, nxzfl = 0;
   double volume = 0;

@@ -101,15 +101,6 @@ __device__ __forceinline__ void add_pair_product(float& Rh, float& Rl, float2 w,
   Rl = (Rl + e) + t;
 }
 
-// (kh, kl) = (ah, al) * (bh, bl) as a float pair (~2^-46 of |a b|)
-__device__ __forceinline__ void pair_mul(float ah, float al, float bh, float bl, float& kh,
-                                         float& kl) {
-  kh = ah * bh;
-  float e = fmaf(ah, bh, -kh);
-  e = fmaf(ah, bl, e);
-  kl = fmaf(al, bh, e);
-}
-
 // ---------------------------------------------------------------------------
 // mbarrier + 1-D TMA bulk copy (PTX)
 // ---------------------------------------------------------------------------
@@ -230,8 +221,8 @@ struct MCfg {
   // can land there while this one is finished.  54 KB in all at NX=8, four
   // blocks per SM.
   static constexpr size_t SA = cmax(cmax(6 * N3 * 8, 6 * N3P * 8), 6 * NF * 8);
-  static constexpr size_t off_F = 2 * SA;                   // float flux [face][line slot][N2]
-  static constexpr size_t off_wmax = off_F + 24 * N2 * 4;
+  static constexpr size_t off_F = 2 * SA;  // float2 flux pairs [face][line slot][N2]
+  static constexpr size_t off_wmax = off_F + 24 * N2 * 8;
   static constexpr size_t off_E = off_wmax + NW * 6 * 4;
   static constexpr size_t off_bar = (off_E + 8 * 4 + 15) / 16 * 16;
   static constexpr size_t smem = off_bar + 16;
@@ -246,14 +237,6 @@ __constant__ const int kLineComp[3][4] = {{1, 2, 4, 5}, {0, 2, 3, 5}, {0, 1, 3, 
 __constant__ const int kLineRes[3][4] = {{5, 4, 2, 1}, {5, 3, 2, 0}, {4, 3, 1, 0}};
 __constant__ const float kLineSign[3][4] = {{1, -1, -1, 1}, {-1, 1, 1, -1}, {1, -1, -1, 1}};
 __constant__ const int kLineInit[3][4] = {{1, 1, 1, 1}, {0, 1, 0, 1}, {0, 0, 0, 0}};
-// PEC mirror flux (E+ = -E-, H+ = H-: [E] = -2E, [H] = 0) on a face normal to
-// DIR, in the residual of line slot `slot`: lf * coef * E_ec with
-//   coef = -2 C02Z                  (kPecY = 0: the E residuals)
-//   coef = kPecY * 2 * side * Y02   (kPecY = +-1: the H residuals)
-// the upwind terms of src/cem_maxwell.F:976-996 with the jumps of
-// src/cem_maxwell.F:1399-1404.
-__constant__ const int kPecEc[3][4] = {{2, 1, 1, 2}, {2, 0, 0, 2}, {1, 0, 0, 1}};
-__constant__ const int kPecY[3][4] = {{0, 0, -1, 1}, {0, 0, 1, -1}, {0, 0, -1, 1}};
 
 template <int NX, int DIR>
 __device__ __forceinline__ int line_node(int a, int b, int l) {
@@ -293,76 +276,48 @@ __device__ __forceinline__ void rk_finish(const MixedDev& a, int c, long g, floa
   a.u_out[c * P + g] = fma(a.b, kn, __ldg(a.u_in + c * P + g));
 }
 
-// The PEC mirror flux of face f (normal along DIR) in the residual of line
-// slot `slot` at the face node `node` (in-face index lam), added to the
-// output pair (h, r) in float-pair arithmetic: (lift factor pair) x
-// (coefficient pair) x (split pair of the tangential E component).  The jump
-// of a PEC face is the full field (-2E), so an FP32 flux would carry 2^-24 of
-// the field; this keeps it at the pair's precision.  Face coefficients: the
-// constants of eps = mu = 1, or the face node's (Y02, C02Z) pairs (the hi
-// parts in the node's first float4, the lo parts in its second).
-template <int NX, int DIR>
-__device__ __forceinline__ void pec_add(const float2* s_u2, const MixedDev& a, const float* eg,
-                                        int e, int f, int slot, int lam, int node, float& h,
-                                        float& r) {
-  using C = MCfg<NX>;
-  const int ec = kPecEc[DIR][slot], ys = kPecY[DIR][slot];
-  const float side = (float)slot_side(f);
-  float ch, cl;
-  if (a.fcoef) {
-    const float4* fc = reinterpret_cast<const float4*>(a.fcoef) + 2 * ((long)e * C::NF + f * C::N2 + lam);
-    const float4 hi = fc[0], lo = fc[1];
-    if (ys == 0) {
-      ch = -2.0f * hi.w;
-      cl = -2.0f * lo.w;
-    } else {
-      const float s2 = 2.0f * (float)ys * side;
-      ch = s2 * hi.x;
-      cl = s2 * lo.x;
-    }
-  } else {  // C02Z = C0/2, Y02 = -1/2
-    ch = ys == 0 ? -a.C0f : -(float)ys * side;
-    cl = 0.0f;
-  }
-  float kh, kl;
-  pair_mul(ch, cl, eg[4 + f], eg[10 + f], kh, kl);
-  const float2 ev = s_u2[(3 + ec) * C::N3P + node];
-  float p, q;
-  pair_mul(kh, kl, ev.x, ev.y, p, q);
-  float sm, t;
-  two_sum(h, p, sm, t);
-  h = sm;
-  r = (r + q) + t;
+// c1*J1 + c2*J2 times the lift factor lf, all float pairs, as a float pair.
+// A jump J = (A, B) is an unevaluated pair (jump_pair); the coefficients are
+// (hi, lo) pairs.  Absolute error ~2^-24 of |c B| and of |lf (c1 A1 + c2 A2)|
+// 2^-24, i.e. ~2^-34 of the field: the flux keeps the residual pair's
+// precision whatever the size of the jump.
+__device__ __forceinline__ float2 flux_pair(float2 c1, float2 J1, float2 c2, float2 J2, float2 lf) {
+  const float p1 = c1.x * J1.x;
+  float e1 = fmaf(c1.x, J1.x, -p1);
+  e1 = fmaf(c1.x, J1.y, e1);
+  e1 = fmaf(c1.y, J1.x, e1);
+  const float p2 = c2.x * J2.x;
+  float e2 = fmaf(c2.x, J2.x, -p2);
+  e2 = fmaf(c2.x, J2.y, e2);
+  e2 = fmaf(c2.y, J2.x, e2);
+  float s, t;
+  two_sum(p1, p2, s, t);
+  const float lo = (e1 + e2) + t;
+  const float fh = lf.x * s;
+  float fl = fmaf(lf.x, s, -fh);
+  fl = fmaf(lf.x, lo, fl);
+  fl = fmaf(lf.y, s, fl);
+  return make_float2(fh, fl);
 }
 
-// The PEC mirror flux of the element's PEC faces normal to AX, added to the
-// residual pairs: task (slot, lam) takes face node lam of the faces at both
-// ends of its line (no node lies on both).  m, p: the faces at the -|+ end
-// are PEC.
-template <int NX, int AX>
-__device__ __forceinline__ void pec_axis(const float2* s_u2, float2* s_R2, const MixedDev& a,
-                                         const float* eg, int e, bool m, bool p) {
-  using C = MCfg<NX>;
-  constexpr int FM = AX == 0 ? 3 : (AX == 1 ? 0 : 4);
-  constexpr int FP = AX == 0 ? 1 : (AX == 1 ? 2 : 5);
-  const int tid = opaque_tid();
-#pragma unroll
-  for (int q = 0; q < C::TPT; ++q) {
-    const int task = tid + q * C::NT;
-    if (task < C::NTASK) {
-      const int slot = task / C::N2, lam = task - slot * C::N2;
-      const int la = lam % NX, lb = lam / NX;
-      float2* R0 = s_R2 + kLineRes[AX][slot] * C::N3P;
-#pragma unroll
-      for (int side = 0; side < 2; ++side) {
-        if (side == 0 ? !m : !p) continue;
-        const int node = line_node<NX, AX>(la, lb, side == 0 ? 0 : NX - 1);
-        float2 R = R0[node];
-        pec_add<NX, AX>(s_u2, a, eg, e, side == 0 ? FM : FP, slot, lam, node, R.x, R.y);
-        R0[node] = R;
-      }
-    }
-  }
+__device__ __forceinline__ float2 neg2(float2 v) { return make_float2(-v.x, -v.y); }
+
+// J += d for an FP64 term d (incident fields, sheet currents), in pair
+// arithmetic
+__device__ __forceinline__ void add_jump(float2& J, double d) {
+  float s, t;
+  two_sum(J.x, d2f_hi(d), s, t);
+  J = make_float2(s, (J.y + d2f_lo(d)) + t);
+}
+
+// The jump p - (uh + ul) of a partner value p (FP64) against the own split
+// pair, as an unevaluated pair: the hi difference with its rounding error
+// (two-sum: a jump as large as the field needs 25 bits), the lo parts beside
+// it (their difference is below 2^-10 of the element's largest value).
+__device__ __forceinline__ float2 jump_pair(double p, float2 own) {
+  float s, t;
+  two_sum(d2f_hi(p), -own.x, s, t);
+  return make_float2(s, (d2f_lo(p) - own.y) + t);
 }
 
 // One direction of the contraction: tasks (component, line) accumulate the
@@ -373,7 +328,7 @@ __device__ __forceinline__ void pec_axis(const float2* s_u2, float2* s_R2, const
 // task's component is complete at the line's nodes, so the task finishes
 // them (inverse mass, RK update) instead of storing the pairs.
 template <int NX, int DIR, bool FIN>
-__device__ __forceinline__ void line_phase(const float2* s_u2, float2* s_R2, const float* s_F,
+__device__ __forceinline__ void line_phase(const float2* s_u2, float2* s_R2, const float2* s_F,
                                            bool cubic, float rh, float rl, const MixedDev& a,
                                            int e, bool first_stage) {
   using C = MCfg<NX>;
@@ -391,8 +346,8 @@ __device__ __forceinline__ void line_phase(const float2* s_u2, float2* s_R2, con
       // lifted flux at the line's ends: faces 3|1 (r), 0|2 (s), 4|5 (t)
       constexpr int FM = DIR == 0 ? 3 : (DIR == 1 ? 0 : 4);
       constexpr int FP = DIR == 0 ? 1 : (DIR == 1 ? 2 : 5);
-      const float flux_m = s_F[(FM * 4 + slot) * C::N2 + lam];
-      const float flux_p = s_F[(FP * 4 + slot) * C::N2 + lam];
+      const float2 flux_m = s_F[(FM * 4 + slot) * C::N2 + lam];
+      const float2 flux_p = s_F[(FP * 4 + slot) * C::N2 + lam];
       float2 u[NX];
 #pragma unroll
       for (int l = 0; l < NX; ++l) u[l] = pu[line_node<NX, DIR>(la, lb, l)];
@@ -433,8 +388,13 @@ __device__ __forceinline__ void line_phase(const float2* s_u2, float2* s_R2, con
         }
         h *= sg;
         r *= sg;
-        if (i == 0) r += flux_m;
-        if (i == NX - 1) r += flux_p;
+        if (i == 0 || i == NX - 1) {  // the lifted flux pair of the end's face
+          const float2 F = i == 0 ? flux_m : flux_p;
+          float s, t;
+          two_sum(h, F.x, s, t);
+          h = s;
+          r = (r + F.y) + t;
+        }
         float2* Rp = R0 + line_node<NX, DIR>(la, lb, i);
         if (FIN) {
           const float2 old = *Rp;
@@ -538,22 +498,18 @@ __device__ __forceinline__ void disp_node(const MixedDev& a, int l, int v, long 
   }
 }
 
-// Blocks per SM the launch is built for: four of the unpadded NX = 8 layout
-// (54 KB, 64 registers), six at NX = 6 (160 threads, 28 KB, 64 registers:
-// 2 % faster than five at 72; seven spill and lose 12 %), two at NX = 9
-// (384 threads, 85 KB: shared memory allows no third, and 80 registers
-// instead of 56 remove the spills: 4.5 % faster), three otherwise and with
-// the extension branches.
+// Blocks per SM the launch is built for: three at NX = 8 (62 KB of shared
+// memory with the face flux as float pairs: a fourth does not fit; up to 80
+// registers), six at NX = 6 (160 threads, 32 KB, 64 registers), two at NX = 9
+// (384 threads, 94 KB), three otherwise and with the extension branches.
 template <int NX, bool EXT>
 constexpr int mixed_min_blocks() {
-  return NX == 9 ? 2 : (EXT ? 3 : (MCfg<NX>::kSwz ? 4 : (NX == 6 ? 6 : 3)));
+  return NX == 9 ? 2 : (EXT ? 3 : (NX == 6 ? 6 : 3));
 }
 
 // EXT: the variant with the PML, dispersive-current, incident-field and
-// graphene branches.  PEC: the variant for meshes with PEC (or PML) walls,
-// which adds their mirror flux in pair arithmetic (pec_axis); meshes without
-// walls run the kernel without that code, at the register allocation it had.
-template <int NX, bool EXT, bool PEC>
+// graphene branches
+template <int NX, bool EXT>
 __global__ void __launch_bounds__(MCfg<NX>::NT, mixed_min_blocks<NX, EXT>())
     k_mixed_stage(const MixedDev a) {
   using C = MCfg<NX>;
@@ -561,7 +517,7 @@ __global__ void __launch_bounds__(MCfg<NX>::NT, mixed_min_blocks<NX, EXT>())
   constexpr int NPT = C::NPT, FPT = C::FPT;
   constexpr bool FIN = !EXT && C::kFin;  // the extension terms need all six at a node
   extern __shared__ __align__(16) unsigned char smem[];
-  float* s_F = reinterpret_cast<float*>(smem + C::off_F);
+  float2* s_F = reinterpret_cast<float2*>(smem + C::off_F);
   unsigned* s_wmax = reinterpret_cast<unsigned*>(smem + C::off_wmax);
   unsigned* s_E = reinterpret_cast<unsigned*>(smem + C::off_E);
   uint64_t* bar = reinterpret_cast<uint64_t*>(smem + C::off_bar);
@@ -710,30 +666,28 @@ __global__ void __launch_bounds__(MCfg<NX>::NT, mixed_min_blocks<NX, EXT>())
         const int fa = ab % NX, fb = ab / NX;
         const int pv = pnode<NX>(face_vol<NX>(f, fa, fb));
         const int pe = nbr[f];
-        float dH[3], dE[3];
+        float2 JH[3], JE[3];  // jumps partner - own as unevaluated pairs
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
           const float2 h = s_u2[c * N3P + pv], ev = s_u2[(c + 3) * N3P + pv];
-          if (pe >= 0) {  // jump = (partner_hi - own_hi) + (partner_lo - own_lo)
-            const double ph = s_nbv[c * NF + t], pE = s_nbv[(c + 3) * NF + t];
-            dH[c] = (d2f_hi(ph) - h.x) + (d2f_lo(ph) - h.y);
-            dE[c] = (d2f_hi(pE) - ev.x) + (d2f_lo(pE) - ev.y);
-          } else {  // PEC mirror H+ = H-, E+ = -E-: its flux is added in
-            dH[c] = 0.0f;  // pair arithmetic after the s-lines (pec_axis)
-            dE[c] = 0.0f;
+          if (pe >= 0) {
+            JH[c] = jump_pair(s_nbv[c * NF + t], h);
+            JE[c] = jump_pair(s_nbv[(c + 3) * NF + t], ev);
+          } else {  // PEC mirror H+ = H-, E+ = -E-: [H] = 0, [E] = -2E exactly
+            JH[c] = make_float2(0.0f, 0.0f);
+            JE[c] = make_float2(-2.0f * ev.x, -2.0f * ev.y);
           }
           if (EXT && a.inc_elem) {
             // userinc: the incident field on the own side of a listed face
             // node, or on the partner's side when the partner's slot is listed
             const int io = a.inc_elem[e];
-            if (io >= 0) {
+            if (io >= 0) {  // (FP64 differences: listed elements only)
               const double* iv = a.inc_val + (long)io * 12 * NF + t;
-              const float ih = d2f_hi(iv[c * NF]), ie = d2f_hi(iv[(3 + c) * NF]);
               if (pe >= 0) {
-                dH[c] += d2f_hi(iv[(6 + c) * NF]) - ih;
-                dE[c] += d2f_hi(iv[(9 + c) * NF]) - ie;
+                add_jump(JH[c], iv[(6 + c) * NF] - iv[c * NF]);
+                add_jump(JE[c], iv[(9 + c) * NF] - iv[(3 + c) * NF]);
               } else {
-                dE[c] -= 2.0f * ie;
+                add_jump(JE[c], -2.0 * iv[(3 + c) * NF]);
               }
             }
           }
@@ -768,48 +722,56 @@ __global__ void __launch_bounds__(MCfg<NX>::NT, mixed_min_blocks<NX, EXT>())
             if (go >= 0) graphene_slot(a.gr, go, nv, fhm, fem, true, first_stage, a.a, a.b, a.dt, J);
             if (gp >= 0 && pe >= 0) graphene_slot(a.gr, gp, nm, fhp, fep, false, first_stage, a.a, a.b, a.dt, J);
             if (pe >= 0) {  // a PEC face keeps its mirror flux
-              dH[0] += d2f_hi(nv[1] * J[2] - nv[2] * J[1]);
-              dH[1] += d2f_hi(nv[2] * J[0] - nv[0] * J[2]);
-              dH[2] += d2f_hi(nv[0] * J[1] - nv[1] * J[0]);
+              add_jump(JH[0], nv[1] * J[2] - nv[2] * J[1]);
+              add_jump(JH[1], nv[2] * J[0] - nv[0] * J[2]);
+              add_jump(JH[2], nv[0] * J[1] - nv[1] * J[0]);
             }
           }
         }
-        float Y02 = -0.5f, C02Y = 0.5f * a.C0f, Z02 = 0.5f, C02Z = 0.5f * a.C0f;
+        // coefficient pairs Y02, C02Y, Z02, C02Z (hi in the first float4 of
+        // the face node, lo in the second)
+        float2 Y02 = make_float2(-0.5f, 0.0f), C02Y = make_float2(0.5f * a.C0f, 0.0f);
+        float2 Z02 = make_float2(0.5f, 0.0f), C02Z = C02Y;
         if (a.fcoef) {
-          const float4 fc = reinterpret_cast<const float4*>(a.fcoef)[2 * ((long)e * NF + t)];
-          Y02 = fc.x; C02Y = fc.y; Z02 = fc.z; C02Z = fc.w;
+          const float4* fc = reinterpret_cast<const float4*>(a.fcoef) + 2 * ((long)e * NF + t);
+          const float4 hi = fc[0], lo = fc[1];
+          Y02 = make_float2(hi.x, lo.x);
+          C02Y = make_float2(hi.y, lo.y);
+          Z02 = make_float2(hi.z, lo.z);
+          C02Z = make_float2(hi.w, lo.w);
         }
         const float sg = (float)slot_side(f);
-        const float lf = eg[4 + f];  // area / (bm1 * 2/hx) at this face
-        const float sY = sg * Y02, sZ = sg * Z02;
+        const float2 sY = make_float2(sg * Y02.x, sg * Y02.y), sZ = make_float2(sg * Z02.x, sg * Z02.y);
+        // lift factor area / (bm1 * 2/hx) at this face, as a pair
+        const float2 lf = make_float2(eg[4 + f], eg[10 + f]);
         // the four tangential components, in the line slot order of the
         // face's direction (residuals 5,4,2,1 | 5,3,2,0 | 4,3,1,0)
-        float F0, F1, F2, F3;
+        float2 F0, F1, F2, F3;
         switch (slot_axis(f)) {
           case 0:
-            F0 = fmaf(sZ, dH[1], C02Z * dE[2]);   // E3
-            F1 = fmaf(-sZ, dH[2], C02Z * dE[1]);  // E2
-            F2 = fmaf(sY, dE[1], C02Y * dH[2]);   // H3
-            F3 = fmaf(-sY, dE[2], C02Y * dH[1]);  // H2
+            F0 = flux_pair(sZ, JH[1], C02Z, JE[2], lf);        // E3
+            F1 = flux_pair(neg2(sZ), JH[2], C02Z, JE[1], lf);  // E2
+            F2 = flux_pair(sY, JE[1], C02Y, JH[2], lf);        // H3
+            F3 = flux_pair(neg2(sY), JE[2], C02Y, JH[1], lf);  // H2
             break;
           case 1:
-            F0 = fmaf(-sZ, dH[0], C02Z * dE[2]);  // E3
-            F1 = fmaf(sZ, dH[2], C02Z * dE[0]);   // E1
-            F2 = fmaf(-sY, dE[0], C02Y * dH[2]);  // H3
-            F3 = fmaf(sY, dE[2], C02Y * dH[0]);   // H1
+            F0 = flux_pair(neg2(sZ), JH[0], C02Z, JE[2], lf);  // E3
+            F1 = flux_pair(sZ, JH[2], C02Z, JE[0], lf);        // E1
+            F2 = flux_pair(neg2(sY), JE[0], C02Y, JH[2], lf);  // H3
+            F3 = flux_pair(sY, JE[2], C02Y, JH[0], lf);        // H1
             break;
           default:
-            F0 = fmaf(sZ, dH[0], C02Z * dE[1]);   // E2
-            F1 = fmaf(-sZ, dH[1], C02Z * dE[0]);  // E1
-            F2 = fmaf(sY, dE[0], C02Y * dH[1]);   // H2
-            F3 = fmaf(-sY, dE[1], C02Y * dH[0]);  // H1
+            F0 = flux_pair(sZ, JH[0], C02Z, JE[1], lf);        // E2
+            F1 = flux_pair(neg2(sZ), JH[1], C02Z, JE[0], lf);  // E1
+            F2 = flux_pair(sY, JE[0], C02Y, JH[1], lf);        // H2
+            F3 = flux_pair(neg2(sY), JE[1], C02Y, JH[0], lf);  // H1
             break;
         }
-        float* Fp = s_F + f * 4 * N2 + ab;
-        Fp[0] = lf * F0;
-        Fp[N2] = lf * F1;
-        Fp[2 * N2] = lf * F2;
-        Fp[3 * N2] = lf * F3;
+        float2* Fp = s_F + f * 4 * N2 + ab;
+        Fp[0] = F0;
+        Fp[N2] = F1;
+        Fp[2 * N2] = F2;
+        Fp[3 * N2] = F3;
       }
     }
     __syncthreads();
@@ -821,29 +783,6 @@ __global__ void __launch_bounds__(MCfg<NX>::NT, mixed_min_blocks<NX, EXT>())
       __syncthreads();
       line_phase<NX, 1, false>(s_u2, s_R2, s_F, cubic, r1h, r1l, a, e, first_stage);
       __syncthreads();
-      // PEC faces: the mirror flux in pair arithmetic, once every residual
-      // has been started (after the s-lines) and before the t-lines read or
-      // finish them; axis by axis, as edge and corner nodes lie on faces of
-      // two or three axes
-      unsigned pecmask = 0;  // bit f: face f is a PEC mirror
-      if constexpr (PEC || EXT) {
-#pragma unroll
-        for (int f = 0; f < 6; ++f) pecmask |= (__ldg(a.nbr + 6 * e + f) < 0 ? 1u : 0u) << f;
-      }
-      if (pecmask) {
-        if (pecmask & 0x0Au) {  // faces 3, 1
-          pec_axis<NX, 0>(s_u2, s_R2, a, eg, e, pecmask & 0x08u, pecmask & 0x02u);
-          __syncthreads();
-        }
-        if (pecmask & 0x05u) {  // faces 0, 2
-          pec_axis<NX, 1>(s_u2, s_R2, a, eg, e, pecmask & 0x01u, pecmask & 0x04u);
-          __syncthreads();
-        }
-        if (pecmask & 0x30u) {  // faces 4, 5
-          pec_axis<NX, 2>(s_u2, s_R2, a, eg, e, pecmask & 0x10u, pecmask & 0x20u);
-          __syncthreads();
-        }
-      }
       // without the extension terms each component can finish on its own
       // (MCfg::kFin): H3, E3 (no t-derivative) are complete since the s-lines
       line_phase<NX, 2, FIN>(s_u2, s_R2, s_F, cubic, r2h, r2l, a, e, first_stage);
@@ -916,10 +855,10 @@ __global__ void k_scale_coef_pairs(float2* coef, const double* base, long n2, do
   coef[i] = make_float2(d2f_hi(v), d2f_lo(v));
 }
 
-template <int NX, bool EXT, bool PEC>
+template <int NX, bool EXT>
 int launch_mixed(Context* c, const MixedDev& a) {
   using C = MCfg<NX>;
-  auto kern = k_mixed_stage<NX, EXT, PEC>;
+  auto kern = k_mixed_stage<NX, EXT>;
   static bool ready = false;
   static int grid = 0;
   if (!ready) {
@@ -939,520 +878,6 @@ int launch_mixed(Context* c, const MixedDev& a) {
   const int g = n < grid ? n : grid;
   c->fused_grid = g;
   kern<<<g, C::NT, C::smem, c->stream>>>(a);
-  c->last_launches += 1;
-  return check_cuda(cudaGetLastError());
-}
-
-// ===========================================================================
-// Warp-specialised stage kernel (meshes without the extension terms)
-// ===========================================================================
-// The same stage as k_mixed_stage, with the work split between two kinds of
-// warps of one block, so that the FP64 inverse mass and RK update of element
-// e overlaps the FP32 phases of element e+1 instead of following them:
-//  * compute warps (MCfg::NT threads): state copy, exponent scan, split, face
-//    flux and the r/s/t line contractions; each residual component goes,
-//    once complete, to a two-slot ring of this block in global memory (it is
-//    written once and read once per element and stays in L2);
-//  * finisher warps (kFinThreads): for each element the compute warps hand
-//    over, the residual pair times the dt-scaled coefficient, then
-//    k = a k + r and u = u + b k in FP64, node by node, coalesced.
-// mbarriers hand the ring slots over (full: every compute thread arrives
-// after its last write; free: every finisher thread after its last read);
-// every wait is bounded and a timed-out wait sets the status word and stops
-// the warps that waited.  The compute warps synchronise among themselves with
-// a named barrier, so the finisher warps never wait on their phases.
-//
-// The face flux is kept as float pairs: each jump is an unevaluated pair
-// (partner_hi - own_hi with its rounding error, partner_lo - own_lo),
-// multiplied by the coefficient pairs and the lift-factor pair in float-float
-// arithmetic and added to the line outputs with a two-sum.  The flux then
-// carries ~2^-34 of the field whatever the size of the jump: a PEC wall, whose
-// mirror jump is the whole field (-2E), is an ordinary case of it.
-constexpr int kFinThreads = 64;
-// whether the stage routes meshes without the extension terms to it
-constexpr bool kRouteWs = false;
-
-template <int NX>
-struct WCfg {
-  using C = MCfg<NX>;
-  static constexpr int NTC = C::NT;
-  static constexpr int NTOT = NTC + kFinThreads;
-  static constexpr size_t off_F = 2 * C::SA;  // float2 flux pairs [face][line slot][N2]
-  static constexpr size_t off_wmax = off_F + 24 * (size_t)C::N2 * 8;
-  static constexpr size_t off_E = off_wmax + C::NW * 6 * 4;
-  // mbarriers: [0] state copy, [1..2] ring slot full, [3..4] ring slot free
-  static constexpr size_t off_bar = (off_E + 8 * 4 + 15) / 16 * 16;
-  static constexpr size_t smem = off_bar + 5 * 8;
-  static constexpr size_t ring_floats2 = 2 * 6 * (size_t)C::N3;  // float2 per block
-};
-
-template <int NX>
-constexpr int mixed_ws_min_blocks() {
-  return NX == 9 ? 2 : (NX == 8 ? 3 : 4);
-}
-
-__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
-  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
-}
-
-// the compute warps' barrier (named barrier 1; the finisher warps never join)
-template <int NTC>
-__device__ __forceinline__ void compute_bar() {
-  asm volatile("bar.sync 1, %0;" ::"n"(NTC) : "memory");
-}
-
-// c1*J1 + c2*J2 times the lift factor lf, all float pairs; a jump J = (A, B)
-// is an unevaluated pair
-__device__ __forceinline__ float2 flux_pair(float2 c1, float2 J1, float2 c2, float2 J2, float2 lf) {
-  const float p1 = c1.x * J1.x;
-  float e1 = fmaf(c1.x, J1.x, -p1);
-  e1 = fmaf(c1.x, J1.y, e1);
-  e1 = fmaf(c1.y, J1.x, e1);
-  const float p2 = c2.x * J2.x;
-  float e2 = fmaf(c2.x, J2.x, -p2);
-  e2 = fmaf(c2.x, J2.y, e2);
-  e2 = fmaf(c2.y, J2.x, e2);
-  float s, t;
-  two_sum(p1, p2, s, t);
-  const float lo = (e1 + e2) + t;
-  const float fh = lf.x * s;
-  float fl = fmaf(lf.x, s, -fh);
-  fl = fmaf(lf.x, lo, fl);
-  fl = fmaf(lf.y, s, fl);
-  return make_float2(fh, fl);
-}
-
-__device__ __forceinline__ float2 neg2(float2 v) { return make_float2(-v.x, -v.y); }
-
-// The jump p - (uh + ul) of a partner value p (FP64) against the own split
-// pair, as an unevaluated pair: the hi difference with its rounding error
-// (two-sum: a jump as large as the field needs 25 bits), the lo parts
-// beside it.
-__device__ __forceinline__ float2 jump_pair(double p, float2 own) {
-  float s, t;
-  two_sum(d2f_hi(p), -own.x, s, t);
-  return make_float2(s, (d2f_lo(p) - own.y) + t);
-}
-
-// One direction of the contraction for the warp-specialised kernel: as
-// line_phase, with the flux pairs added by two-sums, and the residual
-// components that are complete after this direction (E3, H3 after the
-// s-lines; the other four after the t-lines) written to the ring at natural
-// node order instead of back to shared memory.
-template <int NX, int DIR>
-__device__ __forceinline__ void line_phase_ws(const float2* s_u2, float2* s_R2, const float2* s_F,
-                                              bool cubic, float rh, float rl, float2* ringslot) {
-  using C = MCfg<NX>;
-  const int tid = opaque_tid();
-  constexpr int FM = DIR == 0 ? 3 : (DIR == 1 ? 0 : 4);
-  constexpr int FP = DIR == 0 ? 1 : (DIR == 1 ? 2 : 5);
-#pragma unroll
-  for (int q = 0; q < C::TPT; ++q) {
-    const int task = tid + q * C::NT;
-    if (task < C::NTASK) {
-      const int slot = task / C::N2, lam = task - slot * C::N2;
-      const int la = lam % NX, lb = lam / NX;
-      const int comp = kLineComp[DIR][slot], rt = kLineRes[DIR][slot];
-      const float sg = kLineSign[DIR][slot];
-      const bool init = kLineInit[DIR][slot] != 0;
-      // complete after this direction: written to the ring
-      const bool last = DIR == 2 || (DIR == 1 && !init);
-      const float2* pu = s_u2 + comp * C::N3P;
-      const float2 flux_m = s_F[(FM * 4 + slot) * C::N2 + lam];
-      const float2 flux_p = s_F[(FP * 4 + slot) * C::N2 + lam];
-      float2 u[NX];
-#pragma unroll
-      for (int l = 0; l < NX; ++l) u[l] = pu[line_node<NX, DIR>(la, lb, l)];
-      constexpr int H = (NX + 1) / 2;
-      float2 x[NX], y[H];
-#pragma unroll
-      for (int i = 0; i < NX; ++i) x[i] = __fmul2_rn(c_mixD[NX][0][i], u[0]);
-#pragma unroll
-      for (int i = 0; i < H; ++i) y[i] = __fmul2_rn(c_mixD[NX][1][i], make_float2(u[0].x, u[0].x));
-#pragma unroll
-      for (int l = 1; l < NX; ++l) {
-        const float2 uu = make_float2(u[l].x, u[l].x);
-#pragma unroll
-        for (int i = 0; i < NX; ++i) x[i] = __ffma2_rn(c_mixD[NX][0][i + NX * l], u[l], x[i]);
-#pragma unroll
-        for (int i = 0; i < H; ++i) y[i] = __ffma2_rn(c_mixD[NX][1][i + H * l], uu, y[i]);
-      }
-      float2* R0 = s_R2 + rt * C::N3P;
-      float2* Rg = ringslot + rt * C::N3;
-#pragma unroll
-      for (int i = 0; i < NX; ++i) {
-        float h = x[i].x, r = x[i].y + ((i & 1) ? y[i / 2].y : y[i / 2].x);
-        if (DIR != 0 && !cubic) {  // times rho = g_dir/g_x as a float pair
-          const float p = rh * h;
-          float e = fmaf(rh, h, -p);
-          e = fmaf(rh, r, e);
-          e = fmaf(rl, h, e);
-          h = p;
-          r = e;
-        }
-        h *= sg;
-        r *= sg;
-        if (i == 0 || i == NX - 1) {
-          const float2 F = i == 0 ? flux_m : flux_p;
-          float s, t;
-          two_sum(h, F.x, s, t);
-          h = s;
-          r = (r + F.y) + t;
-        }
-        float2* Rp = R0 + line_node<NX, DIR>(la, lb, i);
-        if (init) {
-          *Rp = make_float2(h, r);
-        } else {
-          const float2 old = *Rp;
-          float sum, err;
-          two_sum(old.x, h, sum, err);
-          const float2 v = make_float2(sum, (old.y + r) + err);
-          if (last) {
-            const int vol = DIR == 0 ? i + NX * la + C::N2 * lb
-                                     : (DIR == 1 ? la + NX * i + C::N2 * lb : la + NX * lb + C::N2 * i);
-            __stcg(Rg + vol, v);
-          } else {
-            *Rp = v;
-          }
-        }
-      }
-    }
-  }
-}
-
-// The finisher warps' part of one element: inverse mass and RK update of the
-// six components from the residual pairs in the ring slot R, node by node
-// (thread f takes nodes f, f + kFinThreads, ...), NB nodes' loads in flight
-// at a time.
-template <int NX>
-__device__ __forceinline__ void finish_element(const MixedDev& a, const float2* R, int e, int f,
-                                               bool first_stage) {
-  constexpr int N3 = NX * NX * NX;
-  constexpr int NJ = (N3 + kFinThreads - 1) / kFinThreads;
-  constexpr int NB = 4;
-  const long P = a.npts, g0 = (long)e * N3;
-  const int so = a.src_elem ? a.src_elem[e] : -1;
-  for (int c = 0; c < 6; ++c) {
-    const long co = c < 3 ? 0 : P;
-    for (int j0 = 0; j0 < NJ; j0 += NB) {
-      float2 rr[NB], cf[NB];
-      double kk[NB], uu[NB];
-#pragma unroll
-      for (int b = 0; b < NB; ++b) {
-        const int v = f + kFinThreads * (j0 + b);
-        if (j0 + b < NJ && v < N3) {
-          const long g = g0 + v;
-          rr[b] = __ldcg(R + c * N3 + v);
-          cf[b] = a.coef[co + g];
-          kk[b] = first_stage ? 0.0 : __ldcg(a.k + c * P + g);
-          uu[b] = __ldg(a.u_in + c * P + g);
-        }
-      }
-#pragma unroll
-      for (int b = 0; b < NB; ++b) {
-        const int v = f + kFinThreads * (j0 + b);
-        if (j0 + b < NJ && v < N3) {
-          const long g = g0 + v;
-          float Rh = rr[b].x, Rl = rr[b].y;
-          if (c == 5 && so >= 0) add_pair_product(Rh, Rl, a.src_w[(long)so * N3 + v], a.src_ft2);
-          const float p = cf[b].x * Rh;
-          float ee = fmaf(cf[b].x, Rh, -p);
-          ee = fmaf(cf[b].x, Rl, ee);
-          ee = fmaf(cf[b].y, Rh, ee);
-          const double r = f2d(p) + f2d(ee);
-          const double kn = first_stage ? r : fma(a.a, kk[b], r);
-          a.k[c * P + g] = kn;
-          a.u_out[c * P + g] = fma(a.b, kn, uu[b]);
-        }
-      }
-    }
-  }
-}
-
-template <int NX>
-__global__ void __launch_bounds__(WCfg<NX>::NTOT, mixed_ws_min_blocks<NX>())
-    k_mixed_ws(const MixedDev a) {
-  using C = MCfg<NX>;
-  using W = WCfg<NX>;
-  constexpr int N2 = C::N2, N3 = C::N3, NT = C::NT, NF = C::NF, N3P = C::N3P;
-  constexpr int NPT = C::NPT, FPT = C::FPT;
-  extern __shared__ __align__(16) unsigned char smem[];
-  float2* s_F = reinterpret_cast<float2*>(smem + W::off_F);
-  unsigned* s_wmax = reinterpret_cast<unsigned*>(smem + W::off_wmax);
-  unsigned* s_E = reinterpret_cast<unsigned*>(smem + W::off_E);
-  uint64_t* bar = reinterpret_cast<uint64_t*>(smem + W::off_bar);
-  __shared__ volatile int s_abort;  // set and read by the compute warps only, around their barriers
-
-  const long P = a.npts;
-  const bool first_stage = (a.a == 0.0);
-  if (threadIdx.x == 0) {
-    s_abort = 0;
-    mbar_init(bar + 0, 1);
-    mbar_init(bar + 1, NT);
-    mbar_init(bar + 2, NT);
-    mbar_init(bar + 3, kFinThreads);
-    mbar_init(bar + 4, kFinThreads);
-    fence_mbar_init();
-  }
-  __syncthreads();
-  float2* ring = a.ring + (long)blockIdx.x * W::ring_floats2;
-
-  if (threadIdx.x >= NT) {
-    // ---- finisher warps -------------------------------------------------------
-    const int f = threadIdx.x - NT;
-    auto pf = [&](int e) {  // the finish's inputs of element e into L2
-      if (f == 0 && e < a.e_end) {
-        const unsigned bytes = N3 * 8;
-        for (int c = 0; c < 6; ++c) prefetch_l2(a.u_in + c * P + (long)e * N3, bytes);
-        if (!first_stage)
-          for (int c = 0; c < 6; ++c) prefetch_l2(a.k + c * P + (long)e * N3, bytes);
-        for (int c = 0; c < 2; ++c) prefetch_l2(a.coef + c * P + (long)e * N3, bytes);
-      }
-    };
-    pf(a.e_begin + blockIdx.x);
-    int it = 0;
-    for (int e = a.e_begin + blockIdx.x; e < a.e_end; e += gridDim.x, ++it) {
-      const int slot = it & 1;
-      pf(e + gridDim.x);
-      // a timed-out wait has set the status word; the compute warps, which
-      // only react to their own flag, time out on the ring-free wait in turn
-      if (!mbar_wait_bounded(bar + 1 + slot, (it >> 1) & 1, a.status)) return;
-      finish_element<NX>(a, ring + slot * 6 * N3, e, f, first_stage);
-      mbar_arrive(bar + 3 + slot);
-    }
-    return;
-  }
-
-  // ---- compute warps ----------------------------------------------------------
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  int tid = threadIdx.x;
-  auto issue_tma = [&](int e, int into) {
-    const unsigned bytes = N3 * 8;
-    double* dst = reinterpret_cast<double*>(smem + into * C::SA);
-    mbar_expect_tx(bar, 6u * bytes);
-    for (int c = 0; c < 6; ++c) tma_load_1d(dst + c * N3, a.u_in + c * P + (long)e * N3, bytes, bar);
-    if (a.fcoef) prefetch_l2(reinterpret_cast<const float4*>(a.fcoef) + 2L * e * NF, NF * 32u);
-  };
-  unsigned parity = 0;
-  int buf = 0;
-  if (C::kTma && tid == 0 && a.e_begin + (int)blockIdx.x < a.e_end) issue_tma(a.e_begin + blockIdx.x, 0);
-
-  int it = 0;
-  for (int e = a.e_begin + blockIdx.x; e < a.e_end; e += gridDim.x, buf ^= 1, ++it) {
-    int tid = opaque_tid();
-    const int slot = it & 1;
-    double* s_u64 = reinterpret_cast<double*>(smem + buf * C::SA);
-    float2* s_R2 = reinterpret_cast<float2*>(smem + buf * C::SA);
-    float2* s_u2 = reinterpret_cast<float2*>(smem + (buf ^ 1) * C::SA);
-    const int en = e + gridDim.x;
-    const int* nbr = a.nbr + 6 * e;
-    const float* eg = a.egm + 16 * e;
-    // ---- early loads: partner face nodes ------------------------------------
-    double nbv[FPT][6];
-#pragma unroll
-    for (int q = 0; q < FPT; ++q) {
-      const int t = tid + q * NT;
-      if (t < NF) {
-        const int f = t / N2, ab = t - f * N2;
-        const int pe = nbr[f];
-        if (pe >= 0) {
-          const long pv = (long)pe * N3 + face_vol<NX>(slot_opp(f), ab % NX, ab / NX);
-#pragma unroll
-          for (int c = 0; c < 6; ++c) nbv[q][c] = __ldg(a.u_in + c * P + pv);
-        }
-      }
-    }
-    // ---- own element state ------------------------------------------------------
-    if (C::kTma) {
-      if (!mbar_wait_bounded(bar, parity, a.status)) s_abort = 1;
-      parity ^= 1u;
-    } else {
-#pragma unroll
-      for (int q = 0; q < NPT; ++q) {
-        const int v = tid + q * NT;
-        if (v < N3)
-#pragma unroll
-          for (int c = 0; c < 6; ++c) s_u64[c * N3 + v] = a.u_in[c * P + (long)e * N3 + v];
-      }
-    }
-    compute_bar<NT>();
-    if (s_abort) return;
-    // ---- per-component largest exponent -> 10-bit grid --------------------------
-    {
-      unsigned em[6] = {0, 0, 0, 0, 0, 0};
-#pragma unroll
-      for (int q = 0; q < NPT; ++q) {
-        const int v = tid + q * NT;
-        if (v < N3)
-#pragma unroll
-          for (int c = 0; c < 6; ++c) {
-            const unsigned hw = (unsigned)__double2hiint(s_u64[c * N3 + v]);
-            em[c] = max(em[c], (hw >> 20) & 0x7FFu);
-          }
-      }
-#pragma unroll
-      for (int c = 0; c < 6; ++c) em[c] = __reduce_max_sync(0xffffffffu, em[c]);
-      if (lane == 0)
-#pragma unroll
-        for (int c = 0; c < 6; ++c) s_wmax[warp * 6 + c] = em[c];
-    }
-    compute_bar<NT>();
-    if (tid < 6) {
-      unsigned m = 0;
-      for (int w = 0; w < C::NW; ++w) m = max(m, s_wmax[w * 6 + tid]);
-      s_E[tid] = min(max(m, 906u), 1158u);
-    }
-    compute_bar<NT>();
-    // ---- split: uh on the grid q = 2^(E-1032), ul = u - uh ----------------------
-    tid = opaque_tid();
-    {
-      const float M = 12582912.0f;
-      unsigned Ec[6];
-#pragma unroll
-      for (int c = 0; c < 6; ++c) Ec[c] = s_E[c];
-#pragma unroll
-      for (int q = 0; q < NPT; ++q) {
-        const int v = tid + q * NT;
-        if (v < N3) {
-          double u[6];
-#pragma unroll
-          for (int c = 0; c < 6; ++c) u[c] = s_u64[c * N3 + v];
-          const int pv = pnode<NX>(v);
-#pragma unroll
-          for (int c = 0; c < 6; ++c) {
-            const int E = (int)Ec[c];
-            const float qv = __int_as_float((E - 905) << 23);
-            const float qi = __int_as_float((1159 - E) << 23);
-            const float uf = d2f_hi(u[c]), ulo = d2f_lo(u[c]);
-            const float uh = (__fadd_rn(__fmaf_rn(uf, qi, M), -M)) * qv;
-            s_u2[c * N3P + pv] = make_float2(uh, __fadd_rn(__fsub_rn(uf, uh), ulo));
-          }
-        }
-      }
-    }
-    compute_bar<NT>();
-    // ---- upwind flux per face node as float pairs, lifted, into s_F -------------
-    tid = opaque_tid();
-    double* s_nbv = s_u64;
-#pragma unroll
-    for (int q = 0; q < FPT; ++q) {
-      const int t = tid + q * NT;
-      if (t < NF && nbr[t / N2] >= 0)
-#pragma unroll
-        for (int c = 0; c < 6; ++c) s_nbv[c * NF + t] = nbv[q][c];
-    }
-#pragma unroll
-    for (int q = 0; q < FPT; ++q) {
-      const int t = tid + q * NT;
-      if (t < NF) {
-        const int f = t / N2, ab = t - f * N2;
-        const int pv = pnode<NX>(face_vol<NX>(f, ab % NX, ab / NX));
-        const int pe = nbr[f];
-        float2 JH[3], JE[3];  // jumps partner - own as unevaluated pairs
-#pragma unroll
-        for (int c = 0; c < 3; ++c) {
-          const float2 h = s_u2[c * N3P + pv], ev = s_u2[(c + 3) * N3P + pv];
-          if (pe >= 0) {
-            JH[c] = jump_pair(s_nbv[c * NF + t], h);
-            JE[c] = jump_pair(s_nbv[(c + 3) * NF + t], ev);
-          } else {  // PEC mirror: H+ = H-, E+ = -E-
-            JH[c] = make_float2(0.0f, 0.0f);
-            JE[c] = make_float2(-2.0f * ev.x, -2.0f * ev.y);
-          }
-        }
-        // coefficient pairs Y02, C02Y, Z02, C02Z (hi in the first float4 of
-        // the face node, lo in the second)
-        float2 Y02 = make_float2(-0.5f, 0.0f), C02Y = make_float2(0.5f * a.C0f, 0.0f);
-        float2 Z02 = make_float2(0.5f, 0.0f), C02Z = C02Y;
-        if (a.fcoef) {
-          const float4* fc = reinterpret_cast<const float4*>(a.fcoef) + 2 * ((long)e * NF + t);
-          const float4 hi = fc[0], lo = fc[1];
-          Y02 = make_float2(hi.x, lo.x);
-          C02Y = make_float2(hi.y, lo.y);
-          Z02 = make_float2(hi.z, lo.z);
-          C02Z = make_float2(hi.w, lo.w);
-        }
-        const float sg = (float)slot_side(f);
-        const float2 sY = make_float2(sg * Y02.x, sg * Y02.y), sZ = make_float2(sg * Z02.x, sg * Z02.y);
-        const float2 lf = make_float2(eg[4 + f], eg[10 + f]);
-        float2 F0, F1, F2, F3;
-        switch (slot_axis(f)) {
-          case 0:
-            F0 = flux_pair(sZ, JH[1], C02Z, JE[2], lf);        // E3
-            F1 = flux_pair(neg2(sZ), JH[2], C02Z, JE[1], lf);  // E2
-            F2 = flux_pair(sY, JE[1], C02Y, JH[2], lf);        // H3
-            F3 = flux_pair(neg2(sY), JE[2], C02Y, JH[1], lf);  // H2
-            break;
-          case 1:
-            F0 = flux_pair(neg2(sZ), JH[0], C02Z, JE[2], lf);  // E3
-            F1 = flux_pair(sZ, JH[2], C02Z, JE[0], lf);        // E1
-            F2 = flux_pair(neg2(sY), JE[0], C02Y, JH[2], lf);  // H3
-            F3 = flux_pair(sY, JE[2], C02Y, JH[0], lf);        // H1
-            break;
-          default:
-            F0 = flux_pair(sZ, JH[0], C02Z, JE[1], lf);        // E2
-            F1 = flux_pair(neg2(sZ), JH[1], C02Z, JE[0], lf);  // E1
-            F2 = flux_pair(sY, JE[0], C02Y, JH[1], lf);        // H2
-            F3 = flux_pair(neg2(sY), JE[1], C02Y, JH[0], lf);  // H1
-            break;
-        }
-        float2* Fp = s_F + f * 4 * N2 + ab;
-        Fp[0] = F0;
-        Fp[N2] = F1;
-        Fp[2 * N2] = F2;
-        Fp[3 * N2] = F3;
-      }
-    }
-    compute_bar<NT>();
-    // ---- contractions (with the lifted flux): r, s, t lines ---------------------
-    {
-      const bool cubic = eg[0] == 1.0f && eg[1] == 0.0f && eg[2] == 1.0f && eg[3] == 0.0f;
-      const float r1h = eg[0], r1l = eg[1], r2h = eg[2], r2l = eg[3];
-      float2* rs = ring + slot * 6 * N3;
-      line_phase_ws<NX, 0>(s_u2, s_R2, s_F, cubic, 0.0f, 0.0f, rs);
-      // the ring slot of element it-2 must have been read by the finishers
-      // before this element's first ring write (in the s-lines)
-      if (it >= 2 && threadIdx.x == 0 && !mbar_wait_bounded(bar + 3 + slot, ((it >> 1) - 1) & 1, a.status))
-        s_abort = 1;
-      compute_bar<NT>();
-      if (s_abort) return;
-      line_phase_ws<NX, 1>(s_u2, s_R2, s_F, cubic, r1h, r1l, rs);
-      compute_bar<NT>();
-      line_phase_ws<NX, 2>(s_u2, s_R2, s_F, cubic, r2h, r2l, rs);
-    }
-    mbar_arrive(bar + 1 + slot);  // this thread's ring writes are done
-    compute_bar<NT>();
-    // the split pairs are consumed: the next element's state lands in their area
-    if (C::kTma && threadIdx.x == 0 && en < a.e_end) {
-      fence_proxy_async_smem();
-      issue_tma(en, buf ^ 1);
-    }
-  }
-}
-
-template <int NX>
-int launch_mixed_ws(Context* c, const MixedDev& a) {
-  using W = WCfg<NX>;
-  auto kern = k_mixed_ws<NX>;
-  static bool ready = false;
-  static int grid = 0;
-  if (!ready) {
-    if (check_cuda(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)W::smem)))
-      return NEKGPU_ERR_CUDA;
-    int per_sm = 0, sms = 0;
-    if (check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, W::NTOT, W::smem)))
-      return NEKGPU_ERR_CUDA;
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
-    if (per_sm < 1) return NEKGPU_ERR_UNSUPPORTED;
-    grid = per_sm * sms;
-    ready = true;
-  }
-  const int n = a.e_end - a.e_begin;
-  if (n <= 0) return NEKGPU_OK;
-  const int g = n < grid ? n : grid;
-  if ((size_t)g * W::ring_floats2 > c->ring_floats2) return NEKGPU_ERR_UNSUPPORTED;
-  c->fused_grid = g;
-  kern<<<g, W::NTOT, W::smem, c->stream>>>(a);
   c->last_launches += 1;
   return check_cuda(cudaGetLastError());
 }
@@ -1523,28 +948,14 @@ int mixed_stage_range(Context* c, int rkstep, double time, double dt, int e0, in
     a.gr.f_in = c->d_gr_f[c->gr_cur];
     a.gr.f_out = c->d_gr_f[c->gr_cur ^ 1];
   }
-  // meshes without the extension terms: the warp-specialised kernel where it
-  // is built for the order
-  if (!ext && c->d_ring && kRouteWs) {
-    if (c->nx == 8) return launch_mixed_ws<8>(c, a);
-    if (c->nx == 6) return launch_mixed_ws<6>(c, a);
-  }
-  // the extension variant handles walls itself; otherwise walls pick the PEC variant
-  const int v = ext ? 2 : (c->mixed_pec ? 1 : 0);
-#define NEKGPU_MIXED_CASE(NXV)                                                                 \
-  case NXV:                                                                                    \
-    st = v == 2 ? launch_mixed<NXV, true, true>(c, a)                                          \
-                : (v == 1 ? launch_mixed<NXV, false, true>(c, a) : launch_mixed<NXV, false, false>(c, a)); \
-    break;
   switch (c->nx) {
-    NEKGPU_MIXED_CASE(3)
-    NEKGPU_MIXED_CASE(4)
-    NEKGPU_MIXED_CASE(5)
-    NEKGPU_MIXED_CASE(6)
-    NEKGPU_MIXED_CASE(7)
-    NEKGPU_MIXED_CASE(8)
-    NEKGPU_MIXED_CASE(9)
-#undef NEKGPU_MIXED_CASE
+    case 3: st = ext ? launch_mixed<3, true>(c, a) : launch_mixed<3, false>(c, a); break;
+    case 4: st = ext ? launch_mixed<4, true>(c, a) : launch_mixed<4, false>(c, a); break;
+    case 5: st = ext ? launch_mixed<5, true>(c, a) : launch_mixed<5, false>(c, a); break;
+    case 6: st = ext ? launch_mixed<6, true>(c, a) : launch_mixed<6, false>(c, a); break;
+    case 7: st = ext ? launch_mixed<7, true>(c, a) : launch_mixed<7, false>(c, a); break;
+    case 8: st = ext ? launch_mixed<8, true>(c, a) : launch_mixed<8, false>(c, a); break;
+    case 9: st = ext ? launch_mixed<9, true>(c, a) : launch_mixed<9, false>(c, a); break;
     default: return NEKGPU_ERR_UNSUPPORTED;
   }
   return st;

@@ -6,9 +6,12 @@ Bars (the tolerance of each assertion is written beside it):
   * fused FP64 form: <= 1e-12 relative per step (max-norm over the 6
     components, relative to the field's max), both from the reference's
     arrays (drop-in init) and from the library's own box builder;
-  * mixed form: per step <= 2e-6 relative (FP32 contractions), and the L2
-    error against the analytic solution within 1.5x of the FP64 one.
+  * mixed form: per step <= 1e-9 relative (MIXED_TOL: the exact-hi FP32
+    contractions carry ~2^-34 of sum|D||u|; a contraction that lost the low
+    part of a split would sit near 2^-24 ~ 6e-8 and fail), and the L2 error
+    against the analytic solution within 1.5x of the FP64 one.
 """
+MIXED_TOL = 1e-9
 import numpy as np
 import pytest
 
@@ -129,7 +132,7 @@ def test_plain_steps_bit_exact(mesh):
 
 
 # ---------------------------------------------------------------------------
-# fused forms: 1e-12 per step (FP64), 2e-6 per step (mixed)
+# fused forms: 1e-12 per step (FP64), MIXED_TOL per step (mixed)
 # ---------------------------------------------------------------------------
 FUSED_MESHES = ["pec_n5", "mixed_bc", "periodic_n8", "odd_n9", "n3", "single_periodic",
                 "single_pec"]
@@ -156,19 +159,24 @@ def test_fused64_per_step(mesh, init, materials):
     g.close(); ref.close()
 
 
-@pytest.mark.parametrize("mesh", ["pec_n5", "mixed_bc", "periodic_n8", "odd_n9"])
+@pytest.mark.parametrize("mesh", list(MESHES))
 @pytest.mark.parametrize("materials", [False, True])
 def test_mixed_per_step(mesh, materials):
+    """Four steps along the oracle's path, each from the oracle's state."""
     ref = ref_for(mesh, materials)
     g = gpu_from_box(ref, "mixed")
     H, E = smooth_fields(ref, 11)
     dt = 0.2 * ref.dxmin()
-    ref.set_state(H, E); g.set_state(H, E)
-    ref.op_rk(0.0, dt)
-    g.run(1, 0.0, dt)
-    gH, gE = g.get_state()
-    err = rel_err(gH, gE, ref.hn, ref.en)
-    assert err <= 2e-6, f"relative error {err:.3e} > 2e-6"
+    t = 0.0
+    for step in range(4):
+        ref.set_state(H, E); g.set_state(H, E)
+        ref.op_rk(t, dt)
+        g.run(1, t, dt)
+        gH, gE = g.get_state()
+        err = rel_err(gH, gE, ref.hn, ref.en)
+        assert err <= MIXED_TOL, f"step {step}: relative error {err:.3e} > {MIXED_TOL:g}"
+        H, E = ref.hn.copy(), ref.en.copy()
+        t += dt
     g.close(); ref.close()
 
 
@@ -247,16 +255,34 @@ def test_cavity_fp64_matches_oracle_l2():
 # ---------------------------------------------------------------------------
 # source term, host entry points, errors
 # ---------------------------------------------------------------------------
-@pytest.mark.parametrize("form", ["plain", "fused64"])
+@pytest.mark.parametrize("form", ["plain", "fused64", "mixed"])
 def test_source_parity(form):
+    """Gaussian/Ricker E_z source from a zero state: the fields are the
+    source's alone.  Plain: bit-identical over 10 steps; fused FP64: 1e-11
+    after 10 steps; mixed: each of the 10 steps from the oracle's state
+    within MIXED_TOL."""
     ref = make_ref(5, (3, 3, 3), (0, 0, 0), (1, 1, 1), (PEC,) * 3, eps=eps_bumpy)
     src = dict(xc=(0.3, 0.45, 0.5), sigma=0.08, amp=2.0, f0=2.0, t0=0.1)
     ref.set_source(**src)
-    g = gpu_from_ref(ref, form)
+    g = gpu_from_box(ref, form) if form == "mixed" else gpu_from_ref(ref, form)
     g.set_source(**src)
     z = np.zeros((3, ref.npts))
     ref.set_state(z, z); g.set_state(z, z)
     dt = 0.2 * ref.dxmin()
+    if form == "mixed":
+        t = 0.0
+        for step in range(10):
+            H, E = ref.hn.copy(), ref.en.copy()
+            g.set_state(H, E)
+            ref.op_rk(t, dt)
+            g.run(1, t, dt)
+            gH, gE = g.get_state()
+            if step > 0:  # step 0 starts from zero: the source alone
+                err = rel_err(gH, gE, ref.hn, ref.en)
+                assert err <= MIXED_TOL, f"step {step}: relative error {err:.3e}"
+            t += dt
+        g.close(); ref.close()
+        return
     ref.run(10, 0.0, dt)
     g.run(10, 0.0, dt)
     gH, gE = g.get_state()
