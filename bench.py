@@ -200,7 +200,11 @@ def build_gpu_case(form, device_note=None):
     return c, g, (x, y, z), dt, H, E
 
 
-def time_form(form, steps, warmup, dist=None, clocks=None):
+def time_form(form, steps, warmup, dist=None, clocks=None, min_sec=1.0, min_windows=3):
+    """Windows of exactly `steps` steps, each bracketed by a barrier and a
+    device sync and timed with CUDA events on the context's stream (max over
+    ranks), repeated until they add up to `min_sec` (and at least
+    `min_windows` of them); the median window is reported."""
     c, g, xyz, dt, H, E = build_gpu_case(form)
     g.set_state(H, E)
     t = 0.0
@@ -211,16 +215,21 @@ def time_form(form, steps, warmup, dist=None, clocks=None):
     if clocks is not None:
         clocks.__enter__()
         time.sleep(0.15)  # let the sampler start before the timed region
+    win = []
     try:
-        t, ms = g.time_steps(steps, t, dt)
+        while len(win) < min_windows or sum(win) < 1e3 * min_sec:
+            barrier(dist)
+            g.sync()
+            t, ms = g.time_steps(steps, t, dt)
+            win.append(reduce_max(dist, ms))
     finally:
         if clocks is not None:
             clocks.__exit__(None, None, None)
     launches = g.last_launches()
-    ms = reduce_max(dist, ms)
     npts = g.npts
     g.close()
-    return dict(ms=ms, steps=steps, npts=npts, launches=launches, dt=dt, case=c)
+    return dict(ms=float(np.median(win)), steps=steps, windows=len(win), npts=npts,
+                launches=launches, dt=dt, case=c)
 
 
 def accuracy(form, nsteps=None):
@@ -249,27 +258,47 @@ def l2_between(a, b):
     return float(np.sqrt(d / r))
 
 
-def e2e(steps, warmup, dist=None):
+def e2e(steps, warmup, dist=None, min_sec=1.0, min_windows=3):
     """Through the C ABI with host buffers: every step copies the host fields
     in (H2D), runs the 5 stages and copies them back (D2H) -- the drop-in for
-    one cem_maxwell_op_rk call (nekgpu_op_rk_host), pinned host memory."""
+    one cem_maxwell_op_rk call (nekgpu_op_rk_host), pinned host memory.
+    Windows of `steps` steps (wall clock, barrier on both sides) until they
+    add up to `min_sec`; the median window is reported."""
     c, g, xyz, dt, H, E = build_gpu_case("mixed")
     H = np.ascontiguousarray(H); E = np.ascontiguousarray(E)
     g.register_host(H); g.register_host(E)
     t = 0.0
     for _ in range(warmup):
         g.op_rk_host(H, E, t, dt); t += dt
-    barrier(dist)
-    t0 = time.perf_counter()
-    for _ in range(steps):
-        g.op_rk_host(H, E, t, dt); t += dt
-    sec = time.perf_counter() - t0
-    sec = reduce_max(dist, sec)
+    win = []
+    while len(win) < min_windows or sum(win) < min_sec:
+        barrier(dist)
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            g.op_rk_host(H, E, t, dt); t += dt
+        win.append(reduce_max(dist, time.perf_counter() - t0))
+    # the host link alone: the whole state in (nekgpu_set_state) and out
+    # (nekgpu_get_state) between the same page-locked arrays, best of five
+    from nekcem_gb300 import _lib as L
+    lib, dp = L.load(), (lambda a: a.ctypes.data_as(L.dp))
+
+    def best_of(fn, reps=5):
+        best = 1e30
+        for _ in range(reps):
+            g.sync()
+            t0 = time.perf_counter()
+            fn()
+            g.sync()
+            best = min(best, time.perf_counter() - t0)
+        return best
+    t_in = best_of(lambda: lib.nekgpu_set_state(g._h, dp(H), dp(E), g.npts))
+    t_out = best_of(lambda: lib.nekgpu_get_state(g._h, dp(H), dp(E), g.npts))
     g.unregister_host(H); g.unregister_host(E)
     bytes_io = 6 * g.npts * 8
     npts = g.npts
     g.close()
-    return dict(sec=sec, npts=npts, h2d=bytes_io, d2h=bytes_io)
+    return dict(sec=float(np.median(win)), steps=steps, windows=len(win), npts=npts, h2d=bytes_io,
+                d2h=bytes_io, link_h2d_gbs=bytes_io / t_in / 1e9, link_d2h_gbs=bytes_io / t_out / 1e9)
 
 
 def adjoint_ratio(nsteps=0, case="adjoint", budget_mb=None):
@@ -324,9 +353,9 @@ def adjoint_ratio(nsteps=0, case="adjoint", budget_mb=None):
     return out
 
 
-def cpu_sample(steps):
+def cpu_sample(min_sec=10.0):
     """The CPU oracle (FP64 restatement of the reference's routines, all host
-    threads) on the same mesh, `steps` RK steps."""
+    threads) on the same mesh: RK steps until `min_sec` of wall time."""
     from nekcem_gb300 import cases
     from oracle import refcpu as R
     threads = os.cpu_count() or 1
@@ -338,13 +367,16 @@ def cpu_sample(steps):
         ref.set_materials(c.eps(x, y, z), np.ones(ref.npts))
     dt = c.timestep(x, y, z)
     ref.set_state(*c.init_fields(x, y, z))
-    ref.run(1, 0.0, dt)  # warm caches / threads
+    t = ref.run(1, 0.0, dt)  # warm caches / threads
+    steps, sec = 0, 0.0
     t0 = time.perf_counter()
-    ref.run(steps, dt, dt)
-    sec = time.perf_counter() - t0
+    while sec < min_sec:
+        t = ref.run(1, t, dt)
+        steps += 1
+        sec = time.perf_counter() - t0
     npts = ref.npts
     ref.close()
-    return dict(value=6 * npts * 5 * steps / sec, sec=sec, threads=threads, npts=npts)
+    return dict(value=6 * npts * 5 * steps / sec, sec=sec, steps=steps, threads=threads, npts=npts)
 
 
 def run_reference(args):
@@ -396,7 +428,8 @@ def main():
     device = int(os.environ.get("LOCAL_RANK", 0))
     peak, peak_kind = measured_peaks()
 
-    # headline: mixed form, device-resident inputs, CUDA-event timed
+    # headline: mixed form, device-resident inputs, CUDA-event timed windows
+    # of exactly --steps steps (median window)
     clk = ClockSampler(device)
     mixed = time_form("mixed", args.steps, max(3, args.warmup), dist, clocks=clk)
     clocks = clk.summary()
@@ -407,13 +440,13 @@ def main():
     launch_ms = mixed["ms"] / mixed["launches"]
     achieved = BYTES_PER_NODE_STAGE * npts / (launch_ms * 1e-3) / 1e9
 
-    e = e2e(max(3, args.steps // 10), 2, dist)
-    e2e_value = world * dof_stage_per_step * max(3, args.steps // 10) / e["sec"]
+    e = e2e(args.steps, 2, dist)
+    e2e_value = world * dof_stage_per_step * e["steps"] / e["sec"]
 
     if rank != 0:
         return
-    fp64 = time_form("fused64", max(5, args.steps // 10), 3)
-    plain = time_form("plain", max(3, args.steps // 50), 2)
+    fp64 = time_form("fused64", max(5, args.steps // 4), 3)
+    plain = time_form("plain", max(3, args.steps // 10), 2)
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": max(3, args.warmup), "ms_per_step": ms_step, "higher_is_better": True,
@@ -422,11 +455,17 @@ def main():
         "config": {"workload": WORKLOADS[CASE],
                    "elements": mixed["case"].nelt, "N": mixed["case"].N, "form": "mixed",
                    "dt": mixed["dt"],
+                   "timing": f"median of {mixed['windows']} CUDA-event windows of {args.steps} "
+                             f"steps (>= 1 s in all)",
                    "l2_policy": f"inputs larger than L2: u in/out + k + inverse mass = "
                                 f"{(6 * 8 * 3 + 16) * npts / 1e6:.0f} MB per stage",
                    "parallelism": "replicas" if world > 1 else "1 GPU"},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": e["h2d"],
-                "d2h_bytes_per_step": e["d2h"], "path": "nekgpu_op_rk_host, pinned host fields"},
+                "d2h_bytes_per_step": e["d2h"], "path": "nekgpu_op_rk_host, pinned host fields",
+                "timing": f"median of {e['windows']} windows of {e['steps']} steps",
+                "link_gbs": {"h2d": e["link_h2d_gbs"], "d2h": e["link_d2h_gbs"],
+                             "how": "whole state through nekgpu_set_state / nekgpu_get_state, "
+                                    "page-locked arrays, best of 5"}},
         "gpu_launches": mixed["launches"],
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak,
@@ -437,9 +476,11 @@ def main():
         "clocks": clocks,
         "forms": {
             "fused64": {"value": dof_stage_per_step * fp64["steps"] / (fp64["ms"] * 1e-3),
-                        "ms_per_step": fp64["ms"] / fp64["steps"]},
+                        "ms_per_step": fp64["ms"] / fp64["steps"],
+                        "timing": f"median of {fp64['windows']} windows of {fp64['steps']} steps"},
             "plain64": {"value": dof_stage_per_step * plain["steps"] / (plain["ms"] * 1e-3),
-                        "ms_per_step": plain["ms"] / plain["steps"]},
+                        "ms_per_step": plain["ms"] / plain["steps"],
+                        "timing": f"median of {plain['windows']} windows of {plain['steps']} steps"},
         },
     }
     out["forms"]["mixed_over_fused64"] = value / world / out["forms"]["fused64"]["value"]
@@ -458,10 +499,10 @@ def main():
         # 180 GB (171,661 MiB) for the context and the gradient together
         out["adjoint"] = adjoint_ratio(args.adjoint_steps or 10, case="large", budget_mb=171661)
     if not args.no_cpu and world == 1 and npts <= 10_000_000:
-        cpu = cpu_sample(max(2, min(20, args.steps // 10)))
+        cpu = cpu_sample()
         out["cpu_baseline"] = {"value": cpu["value"], "unit": UNIT, "cores": cpu["threads"],
-                               "kind": "port", "sample": f"{max(2, min(20, args.steps // 10))} RK "
-                               f"steps of the full mesh, {cpu['sec']:.1f} s"}
+                               "kind": "port", "sample": f"{cpu['steps']} RK steps of the full "
+                               f"mesh, {cpu['sec']:.1f} s"}
     print(json.dumps(out), flush=True)
 
 

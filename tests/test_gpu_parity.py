@@ -294,6 +294,31 @@ def test_source_parity(form):
     g.close(); ref.close()
 
 
+def test_mixed_inverse_mass_pair_isolated():
+    """The mixed form's FP64-class pieces apart from its FP32 contractions:
+    from a zero state the first RK stage sees only the Gaussian/Ricker source
+    (the split pairs are exactly zero, so contractions and flux add nothing).
+    The stage multiplies the source's float pair by the dt-scaled inverse
+    mass, held as a float pair (hi = the top 24 mantissa bits, lo = the rest
+    rounded to 24 bits: ~48 bits), and applies the FP64 RK update.  Against
+    the oracle's FP64 stage: 1e-13 relative (an FP32 coefficient would give
+    ~6e-8)."""
+    ref = make_ref(5, (3, 3, 3), (0, 0, 0), (1, 1, 1), (PEC,) * 3, eps=eps_bumpy, mu=mu_bumpy)
+    src = dict(xc=(0.3, 0.45, 0.5), sigma=0.08, amp=2.0, f0=2.0, t0=0.1)
+    ref.set_source(**src)
+    g = gpu_from_box(ref, "mixed")
+    g.set_source(**src)
+    z = np.zeros((3, ref.npts))
+    ref.set_state(z, z); g.set_state(z, z)
+    dt = 0.2 * ref.dxmin()
+    ref.stage(1, 0.05, dt)
+    g.stage(1, 0.05, dt)
+    gH, gE = g.get_state()
+    assert np.abs(ref.en[2]).max() > 0
+    assert rel_err(gH, gE, ref.hn, ref.en) <= 1e-13
+    g.close(); ref.close()
+
+
 @pytest.mark.parametrize("form", ["plain", "fused64", "mixed"])
 def test_op_rk_host_equals_device_steps(form):
     ref = ref_for("mixed_bc", materials=True)
