@@ -310,6 +310,17 @@ __device__ __forceinline__ void add_jump(float2& J, double d) {
   J = make_float2(s, (J.y + d2f_lo(d)) + t);
 }
 
+// Field component of the k-th parked partner value of face f: all six with
+// the extension terms, else H and E along the two axes tangential to f
+// (k = 0, 1: H; k = 2, 3: E; lower axis first).
+template <bool EXT>
+__device__ __forceinline__ int partner_comp(int f, int k) {
+  if (EXT) return k;
+  const int ax = slot_axis(f);
+  const int tang = (k & 1) ? (ax == 2 ? 1 : 2) : (ax == 0 ? 1 : 0);
+  return (k < 2 ? 0 : 3) + tang;
+}
+
 // The jump p - (uh + ul) of a partner value p (FP64) against the own split
 // pair, as an unevaluated pair: the hi difference with its rounding error
 // (two-sum: a jump as large as the field needs 25 bits), the lo parts beside
@@ -563,7 +574,11 @@ __global__ void __launch_bounds__(MCfg<NX>::NT, mixed_min_blocks<NX, EXT>())
     const int* nbr = a.nbr + 6 * e;
     const float* eg = a.egm + 16 * e;
     // ---- early loads: partner face nodes (kept in registers until the flux)
-    double nbv[FPT][6];
+    // The flux of a face uses the components tangential to it: without the
+    // extension terms only those four are loaded (H and E along the two
+    // other axes); the graphene sheets need all six.
+    constexpr int NPC = EXT ? 6 : 4;
+    double nbv[FPT][NPC];
 #pragma unroll
     for (int q = 0; q < FPT; ++q) {
       const int t = tid + q * NT;
@@ -573,7 +588,7 @@ __global__ void __launch_bounds__(MCfg<NX>::NT, mixed_min_blocks<NX, EXT>())
         if (pe >= 0) {
           const long pv = (long)pe * N3 + face_vol<NX>(slot_opp(f), ab % NX, ab / NX);
 #pragma unroll
-          for (int c = 0; c < 6; ++c) nbv[q][c] = __ldg(a.u_in + c * P + pv);
+          for (int k = 0; k < NPC; ++k) nbv[q][k] = __ldg(a.u_in + partner_comp<EXT>(f, k) * P + pv);
         }
       }
     }
@@ -656,7 +671,7 @@ __global__ void __launch_bounds__(MCfg<NX>::NT, mixed_min_blocks<NX, EXT>())
       const int t = tid + q * NT;
       if (t < NF && nbr[t / N2] >= 0)
 #pragma unroll
-        for (int c = 0; c < 6; ++c) s_nbv[c * NF + t] = nbv[q][c];
+        for (int k = 0; k < NPC; ++k) s_nbv[k * NF + t] = nbv[q][k];
     }
 #pragma unroll
     for (int q = 0; q < FPT; ++q) {
@@ -667,12 +682,18 @@ __global__ void __launch_bounds__(MCfg<NX>::NT, mixed_min_blocks<NX, EXT>())
         const int pv = pnode<NX>(face_vol<NX>(f, fa, fb));
         const int pe = nbr[f];
         float2 JH[3], JE[3];  // jumps partner - own as unevaluated pairs
+        const int ax = slot_axis(f), ta = ax == 0 ? 1 : 0;  // the tangential axes ta < tb
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
+          if (!EXT && c == ax) {  // the normal component: not in the flux
+            JH[c] = JE[c] = make_float2(0.0f, 0.0f);
+            continue;
+          }
           const float2 h = s_u2[c * N3P + pv], ev = s_u2[(c + 3) * N3P + pv];
           if (pe >= 0) {
-            JH[c] = jump_pair(s_nbv[c * NF + t], h);
-            JE[c] = jump_pair(s_nbv[(c + 3) * NF + t], ev);
+            const int kh = EXT ? c : (c == ta ? 0 : 1), ke = EXT ? c + 3 : kh + 2;
+            JH[c] = jump_pair(s_nbv[kh * NF + t], h);
+            JE[c] = jump_pair(s_nbv[ke * NF + t], ev);
           } else {  // PEC mirror H+ = H-, E+ = -E-: [H] = 0, [E] = -2E exactly
             JH[c] = make_float2(0.0f, 0.0f);
             JE[c] = make_float2(-2.0f * ev.x, -2.0f * ev.y);
@@ -708,7 +729,7 @@ __global__ void __launch_bounds__(MCfg<NX>::NT, mixed_min_blocks<NX, EXT>())
               const float2 h = s_u2[c * N3P + pv], ev = s_u2[(c + 3) * N3P + pv];
               fhm[c] = f2d(h.x) + f2d(h.y);
               fem[c] = f2d(ev.x) + f2d(ev.y);
-              fhp[c] = pe >= 0 ? s_nbv[c * NF + t] : 0.0;
+              fhp[c] = pe >= 0 ? s_nbv[c * NF + t] : 0.0;  // EXT: all six parked
               fep[c] = pe >= 0 ? s_nbv[(c + 3) * NF + t] : 0.0;
               if (io >= 0) {
                 const double* iv = a.inc_val + (long)io * 12 * NF + t;
