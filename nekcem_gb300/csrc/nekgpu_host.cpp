@@ -7,6 +7,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -236,11 +237,14 @@ void free_all(Context* c) {
   for (cudaEvent_t& e : c->chunk_fence)
     if (e) cudaEventDestroy(e), e = nullptr;
   if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
+  if (c->copy_out_stream) cudaStreamDestroy(c->copy_out_stream);
+  for (cudaStream_t& q : c->stage_stream)
+    if (q) cudaStreamDestroy(q), q = nullptr;
   if (c->stream) cudaStreamDestroy(c->stream);
   c->chunk_in.clear();
   c->chunk_done.clear();
   c->ev0 = c->ev1 = nullptr;
-  c->copy_stream = c->stream = nullptr;
+  c->copy_stream = c->copy_out_stream = c->stream = nullptr;
 }
 
 // ---------------------------------------------------------------------------
@@ -1203,57 +1207,95 @@ int plain_stage(Context* c, int rkstep, double time, double dt) {
 }
 
 // ---------------------------------------------------------------------------
-// One RK step on host fields with the copies overlapped (mixed form).
-// The elements are cut into up to eight contiguous chunks of whole waves of
-// the stage kernel's blocks.  The state is copied in chunk by chunk on a copy
-// stream; stage 1 of a chunk waits only for the copies of the chunks holding
-// its elements' face partners (periodic wrap-around included), stage 5 runs
-// chunk by chunk and each chunk is copied back as soon as it is done.  The
-// kernels, their inputs and so the results are those of the plain sequence
-// copy in, five stages, copy out.
+// One RK step on host fields with the copies overlapped (mixed form), as a
+// wavefront over element chunks.
+// The elements are cut into up to sixteen contiguous chunks.  Stage s of a
+// chunk reads the stage-(s-1) state of its own elements and of its face
+// partners, and overwrites the buffer that stage s-1 read there, so it waits
+// (events) only for stage s-1 of the chunks holding those partners; stage 1
+// waits for their copies in.  The copies in follow a breadth-first order of
+// the chunk graph from chunk 0, so every stage can start on the first chunks
+// while later chunks are still arriving, and each chunk goes back as soon as
+// its stage 5 is done, while other chunks still compute.  Each stage has its
+// own stream and the two copy directions theirs, so copies in and out, and
+// stages on different chunks, run together.  The kernels and their inputs are
+// those of the plain sequence copy in, five stages, copy out: the results are
+// bit-identical to it.
 // ---------------------------------------------------------------------------
+#ifndef NEKGPU_WAVEFRONT_CHUNKS
+#define NEKGPU_WAVEFRONT_CHUNKS 16
+#endif
+constexpr int kWavefrontChunks = NEKGPU_WAVEFRONT_CHUNKS;  // at most, and at least 64 elements each
+
 bool chunked_step_applies(Context* c) {
   if (c->form != NEKGPU_MIXED || c->ndim != 3 || c->curved || c->host_nbr.empty()) return false;
   const MixedDev& m = c->margs;
   if (m.pml.slot || m.disp.slot || m.inc_elem || m.gr.elem) return false;
   if (c->chunk_begin.empty()) {
-    // chunks of whole waves of the stage kernel's persistent grid (known
-    // after a first launch), so that no chunk launch ends in a partial wave
-    // but the last
-    const int wave = c->fused_grid > 0 ? c->fused_grid : 0;
-    if (wave <= 0) return false;
-    const int waves = (c->nelt + wave - 1) / wave;
-    const int per = (waves + 7) / 8;  // waves per chunk: at most eight chunks
-    const int nch = (waves + per - 1) / per;
-    if (nch < 2) return false;
+    const int nch = std::min(kWavefrontChunks, c->nelt / 64);
+    if (nch < 4) return false;
     c->chunk_begin.resize(nch + 1);
-    for (int k = 0; k <= nch; ++k) c->chunk_begin[k] = (int)std::min<long>(c->nelt, (long)k * per * wave);
+    for (int k = 0; k <= nch; ++k) c->chunk_begin[k] = (int)((long)c->nelt * k / nch);
     std::vector<int> owner(c->nelt);
     for (int k = 0; k < nch; ++k)
       for (int e = c->chunk_begin[k]; e < c->chunk_begin[k + 1]; ++e) owner[e] = k;
-    c->chunk_wait.assign(nch, 0);
+    c->chunk_adj.assign(nch, {});
     for (int k = 0; k < nch; ++k) {
-      int w = k;
+      std::vector<char> mark(nch, 0);
+      mark[k] = 1;
       for (int e = c->chunk_begin[k]; e < c->chunk_begin[k + 1]; ++e)
         for (int f = 0; f < 6; ++f) {
           const int p = c->host_nbr[6 * (long)e + f];
-          if (p >= 0) w = std::max(w, owner[p]);
+          if (p >= 0) mark[owner[p]] = 1;
         }
-      c->chunk_wait[k] = w;
+      for (int j = 0; j < nch; ++j)
+        if (mark[j]) c->chunk_adj[k].push_back(j);
     }
-    c->chunk_order.resize(nch);
-    for (int k = 0; k < nch; ++k) c->chunk_order[k] = k;
-    std::stable_sort(c->chunk_order.begin(), c->chunk_order.end(),
-                     [&](int x, int y) { return c->chunk_wait[x] < c->chunk_wait[y]; });
+    // copies in: breadth-first from chunk 0 (an arc around a periodic ring)
+    std::vector<int> pos(nch, -1);
+    c->chunk_in_order.clear();
+    for (int root = 0; root < nch; ++root) {  // (a graph in pieces: each piece)
+      if (pos[root] >= 0) continue;
+      std::vector<int> queue{root};
+      pos[root] = (int)c->chunk_in_order.size();
+      c->chunk_in_order.push_back(root);
+      for (size_t q = 0; q < queue.size(); ++q)
+        for (int j : c->chunk_adj[queue[q]])
+          if (pos[j] < 0) {
+            pos[j] = (int)c->chunk_in_order.size();
+            c->chunk_in_order.push_back(j);
+            queue.push_back(j);
+          }
+    }
+    // launches in the order their inputs become ready: the level of stage s
+    // of chunk i is one more than the latest level among its dependencies
+    std::vector<int> lvl(pos), nl(nch);
+    std::vector<std::array<int, 3>> key;
+    for (int st = 1; st <= 5; ++st) {
+      for (int i = 0; i < nch; ++i) {
+        int l = 0;
+        for (int j : c->chunk_adj[i]) l = std::max(l, lvl[j] + 1);
+        nl[i] = l;
+        key.push_back({l, st, i});
+      }
+      lvl = nl;
+    }
+    std::sort(key.begin(), key.end());
+    c->chunk_launch.clear();
+    for (const auto& k : key) c->chunk_launch.push_back({k[1], k[2]});
     c->chunk_in.assign(nch, nullptr);
-    c->chunk_done.assign(nch, nullptr);
-    for (int k = 0; k < nch; ++k)
-      if (check_cuda(cudaEventCreateWithFlags(&c->chunk_in[k], cudaEventDisableTiming)) ||
-          check_cuda(cudaEventCreateWithFlags(&c->chunk_done[k], cudaEventDisableTiming)))
-        return false;
+    c->chunk_done.assign(5 * (size_t)nch, nullptr);
+    for (cudaEvent_t& e : c->chunk_in)
+      if (check_cuda(cudaEventCreateWithFlags(&e, cudaEventDisableTiming))) return false;
+    for (cudaEvent_t& e : c->chunk_done)
+      if (check_cuda(cudaEventCreateWithFlags(&e, cudaEventDisableTiming))) return false;
     for (cudaEvent_t& e : c->chunk_fence)
       if (check_cuda(cudaEventCreateWithFlags(&e, cudaEventDisableTiming))) return false;
-    if (check_cuda(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking))) return false;
+    if (check_cuda(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking)) ||
+        check_cuda(cudaStreamCreateWithFlags(&c->copy_out_stream, cudaStreamNonBlocking)))
+      return false;
+    for (cudaStream_t& q : c->stage_stream)
+      if (check_cuda(cudaStreamCreateWithFlags(&q, cudaStreamNonBlocking))) return false;
   }
   return c->copy_stream != nullptr;
 }
@@ -1262,12 +1304,16 @@ int chunked_step(Context* c, double* hn, double* en, long ld, double time, doubl
   const int nch = (int)c->chunk_begin.size() - 1;
   const long N3 = (long)c->nx * c->nx * c->nx;
   const size_t pitch = ld * sizeof(double), w = c->npts * sizeof(double);
-  // the copy stream must not overwrite the state before earlier work on it is done
-  if (check_cuda(cudaEventRecord(c->chunk_fence[0], c->stream)) ||
-      check_cuda(cudaStreamWaitEvent(c->copy_stream, c->chunk_fence[0], 0)))
-    return NEKGPU_ERR_CUDA;
-  double* u = state(c);
-  for (int k = 0; k < nch; ++k) {
+  int st;
+  if ((st = scale_coef_pairs(c, dt))) return st;  // (once per dt, on the context stream)
+  // every stream follows the earlier work on the context stream
+  if (check_cuda(cudaEventRecord(c->chunk_fence[0], c->stream))) return NEKGPU_ERR_CUDA;
+  for (cudaStream_t q : {c->copy_stream, c->copy_out_stream, c->stage_stream[0], c->stage_stream[1],
+                         c->stage_stream[2], c->stage_stream[3], c->stage_stream[4]})
+    if (check_cuda(cudaStreamWaitEvent(q, c->chunk_fence[0], 0))) return NEKGPU_ERR_CUDA;
+  const int cur0 = c->cur;
+  double* u = c->d_u[cur0];
+  for (int k : c->chunk_in_order) {
     const long off = c->chunk_begin[k] * N3;
     const size_t bytes = (c->chunk_begin[k + 1] - c->chunk_begin[k]) * N3 * sizeof(double);
     if (check_cuda(cudaMemcpy2DAsync(u + off, w, hn + off, pitch, bytes, 3, cudaMemcpyHostToDevice,
@@ -1277,31 +1323,43 @@ int chunked_step(Context* c, double* hn, double* en, long ld, double time, doubl
         check_cuda(cudaEventRecord(c->chunk_in[k], c->copy_stream)))
       return NEKGPU_ERR_CUDA;
   }
-  int st;
-  for (int k : c->chunk_order) {
-    if (check_cuda(cudaStreamWaitEvent(c->stream, c->chunk_in[c->chunk_wait[k]], 0))) return NEKGPU_ERR_CUDA;
-    if ((st = mixed_stage_range(c, 1, time, dt, c->chunk_begin[k], c->chunk_begin[k + 1]))) return st;
-  }
-  c->cur ^= 1;
-  for (int r = 2; r <= 4; ++r)
-    if ((st = mixed_stage(c, r, time, dt))) return st;
-  double* out = c->d_u[c->cur ^ 1];
-  for (int k = 0; k < nch; ++k) {
-    if ((st = mixed_stage_range(c, 5, time, dt, c->chunk_begin[k], c->chunk_begin[k + 1]))) return st;
-    if (check_cuda(cudaEventRecord(c->chunk_done[k], c->stream)) ||
-        check_cuda(cudaStreamWaitEvent(c->copy_stream, c->chunk_done[k], 0)))
+  double* out = c->d_u[cur0 ^ 1];  // stage 5's output buffer
+  cudaStream_t saved = c->stream;
+  for (const auto& sk : c->chunk_launch) {
+    const int rk = sk.first, k = sk.second;
+    cudaStream_t q = c->stage_stream[rk - 1];
+    for (int j : c->chunk_adj[k]) {
+      cudaEvent_t dep = rk == 1 ? c->chunk_in[j] : c->chunk_done[(size_t)(rk - 2) * nch + j];
+      if (check_cuda(cudaStreamWaitEvent(q, dep, 0))) {
+        c->stream = saved;
+        return NEKGPU_ERR_CUDA;
+      }
+    }
+    c->stream = q;
+    c->cur = cur0 ^ ((rk - 1) & 1);
+    st = mixed_stage_range(c, rk, time, dt, c->chunk_begin[k], c->chunk_begin[k + 1]);
+    c->stream = saved;
+    if (st) {
+      c->cur = cur0;
+      return st;
+    }
+    if (check_cuda(cudaEventRecord(c->chunk_done[(size_t)(rk - 1) * nch + k], q)))
       return NEKGPU_ERR_CUDA;
-    const long off = c->chunk_begin[k] * N3;
-    const size_t bytes = (c->chunk_begin[k + 1] - c->chunk_begin[k]) * N3 * sizeof(double);
-    if (check_cuda(cudaMemcpy2DAsync(hn + off, pitch, out + off, w, bytes, 3, cudaMemcpyDeviceToHost,
-                                     c->copy_stream)) ||
-        check_cuda(cudaMemcpy2DAsync(en + off, pitch, out + 3 * c->npts + off, w, bytes, 3,
-                                     cudaMemcpyDeviceToHost, c->copy_stream)))
-      return NEKGPU_ERR_CUDA;
+    if (rk == 5) {
+      const long off = c->chunk_begin[k] * N3;
+      const size_t bytes = (c->chunk_begin[k + 1] - c->chunk_begin[k]) * N3 * sizeof(double);
+      if (check_cuda(cudaStreamWaitEvent(c->copy_out_stream, c->chunk_done[4 * (size_t)nch + k], 0)) ||
+          check_cuda(cudaMemcpy2DAsync(hn + off, pitch, out + off, w, bytes, 3, cudaMemcpyDeviceToHost,
+                                       c->copy_out_stream)) ||
+          check_cuda(cudaMemcpy2DAsync(en + off, pitch, out + 3 * c->npts + off, w, bytes, 3,
+                                       cudaMemcpyDeviceToHost, c->copy_out_stream)))
+        return NEKGPU_ERR_CUDA;
+    }
   }
-  c->cur ^= 1;
-  // later work on the context stream follows the copies back
-  if (check_cuda(cudaEventRecord(c->chunk_fence[1], c->copy_stream)) ||
+  c->cur = cur0 ^ 1;
+  // later work on the context stream follows the copies back (which follow
+  // every stage: each stage-(s-1) launch is a dependency of some stage-s one)
+  if (check_cuda(cudaEventRecord(c->chunk_fence[1], c->copy_out_stream)) ||
       check_cuda(cudaStreamWaitEvent(c->stream, c->chunk_fence[1], 0)))
     return NEKGPU_ERR_CUDA;
   return NEKGPU_OK;

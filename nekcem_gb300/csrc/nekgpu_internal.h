@@ -349,14 +349,19 @@ struct Context {
   double volume = 0;
   cudaStream_t stream = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-  // host-field step in element chunks (nekgpu_op_rk_host, mixed form): copies
-  // on their own stream, one event per chunk copied in / finished
-  cudaStream_t copy_stream = nullptr;
-  std::vector<cudaEvent_t> chunk_in, chunk_done;
+  // host-field step as a wavefront over element chunks (nekgpu_op_rk_host,
+  // mixed form): copies in and out on their own streams, one stream per RK
+  // stage, one event per chunk copied in and per chunk and stage finished
+  cudaStream_t copy_stream = nullptr;      // host to device
+  cudaStream_t copy_out_stream = nullptr;  // device to host
+  cudaStream_t stage_stream[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+  std::vector<cudaEvent_t> chunk_in;       // nchunk
+  std::vector<cudaEvent_t> chunk_done;     // 5 * nchunk: stage s of chunk i at s*nchunk + i
   cudaEvent_t chunk_fence[2] = {nullptr, nullptr};  // stream hand-overs before / after
-  std::vector<int> chunk_begin;  // nchunk + 1 element offsets
-  std::vector<int> chunk_order;  // stage-1 launch order of the chunks
-  std::vector<int> chunk_wait;   // per chunk: the last copy its stage-1 launch needs
+  std::vector<int> chunk_begin;              // nchunk + 1 element offsets
+  std::vector<std::vector<int>> chunk_adj;   // per chunk: itself and the chunks of its face partners
+  std::vector<int> chunk_in_order;           // order of the copies in
+  std::vector<std::pair<int, int>> chunk_launch;  // (stage, chunk) launch order
 
   // device memory
   double* d_u[2] = {nullptr, nullptr};  // state (plain uses d_u[0] only)
