@@ -210,10 +210,11 @@ struct MCfg {
   // Where the components finish (inverse mass, RK update) without the
   // extension terms: true = the t-line tasks finish H1, H2, E1, E2 on their
   // lines and H3, E3 (no t-derivative) finish beside them, with no barrier and
-  // no residual round trip; false = node by node after the t-lines (NX = 8:
-  // at 64 registers the t-line tasks cannot cover the loads of eight finishes;
-  // measured 3 % slower there, 20 % faster at NX = 6).
-  static constexpr bool kFin = !kSwz;
+  // no residual round trip; false = node by node after the t-lines (NX = 8
+  // and 9: the t-line tasks cannot cover the loads of eight or nine finishes;
+  // the in-line finish measured 5 % slower at NX = 8 and 16 % slower at
+  // NX = 9, 20 % faster at NX = 6).
+  static constexpr bool kFin = !kSwz && NX != 9;
   // Two areas of SA bytes swap roles from one element to the next.  One holds,
   // in turn, the staged FP64 state (until the split), the partner face values
   // parked for the flux (FP64) and the residual pairs (hi, lo); the other the
@@ -262,10 +263,9 @@ __device__ __forceinline__ int pnode(int v) {  // stored index of node v = i + N
 // read again from global memory (an L2 hit: the element's block was copied in
 // at the start of its turn), the RK register and the coefficients were
 // prefetched into L2 with that copy.
-__device__ __forceinline__ void rk_finish(const MixedDev& a, int c, long g, float Rh, float Rl,
-                                          bool first_stage) {
+__device__ __forceinline__ void rk_finish_cf(const MixedDev& a, int c, long g, float Rh, float Rl,
+                                             float2 cf, bool first_stage) {
   const long P = a.npts;
-  const float2 cf = a.coef[(c < 3 ? 0 : P) + g];
   const float p = cf.x * Rh;
   float ee = fmaf(cf.x, Rh, -p);
   ee = fmaf(cf.x, Rl, ee);
@@ -274,6 +274,10 @@ __device__ __forceinline__ void rk_finish(const MixedDev& a, int c, long g, floa
   const double kn = first_stage ? r : fma(a.a, a.k[c * P + g], r);
   a.k[c * P + g] = kn;
   a.u_out[c * P + g] = fma(a.b, kn, __ldg(a.u_in + c * P + g));
+}
+__device__ __forceinline__ void rk_finish(const MixedDev& a, int c, long g, float Rh, float Rl,
+                                          bool first_stage) {
+  rk_finish_cf(a, c, g, Rh, Rl, a.coef[(c < 3 ? 0 : a.npts) + g], first_stage);
 }
 
 // c1*J1 + c2*J2 times the lift factor lf, all float pairs, as a float pair.
@@ -860,8 +864,11 @@ __global__ void __launch_bounds__(MCfg<NX>::NT, mixed_min_blocks<NX, EXT>())
         if (EXT && pml_l >= 0) pml_node<N3>(a, pml_l, v, (long)e * N3 + v, first_stage, Rh, Rl);
         if (EXT && disp_l >= 0) disp_node<N3>(a, disp_l, v, (long)e * N3 + v, first_stage, Rh, Rl);
         if (so >= 0) add_pair_product(Rh[5], Rl[5], a.src_w[(long)so * N3 + v], a.src_ft2);
+        // the node's two coefficient pairs, H and E, once for its six components
+        const long g = (long)e * N3 + v;
+        const float2 cfH = a.coef[g], cfE = a.coef[P + g];
 #pragma unroll
-        for (int c = 0; c < 6; ++c) rk_finish(a, c, (long)e * N3 + v, Rh[c], Rl[c], first_stage);
+        for (int c = 0; c < 6; ++c) rk_finish_cf(a, c, g, Rh[c], Rl[c], c < 3 ? cfH : cfE, first_stage);
       }
     }
   }
