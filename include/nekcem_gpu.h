@@ -219,15 +219,18 @@ int nekgpu_set_graphene(nekgpu_ctx* ctx, const double* params, const int* slots,
 int nekgpu_set_graphene_current(nekgpu_ctx* ctx, const double* fjn, long ld);
 int nekgpu_get_graphene_current(nekgpu_ctx* ctx, double* fjn, long ld);
 
-/* ---- dealiased curl (NEKGPU_PLAIN) ------------------------------------------ */
+/* ---- dealiased curl (NEKGPU_PLAIN; NEKGPU_FUSED64 on curvilinear meshes) ------ */
 /* param(18) = -1: maxwell_wght_dcurl (src/cem_maxwell.F:1541-1729) on lxd GLL
  * points per direction instead of maxwell_wght_curl.  The tables are the
  * reference's (built on its first dcurl call): jgl(lxd,nx1) interpolation
  * (gen_int), dxmd(lxd,lxd) derivative (gen_dgl), w3md(lxd^3) weights, and
  * metd the nine metric cofactors interpolated to the lxd^3 points, ordered
  * rx, ry, rz, sx, sy, sz, tx, ty, tz, each (lxd^3, nelt).  lxd = 0 switches
- * back; NEKGPU_ERR_UNSUPPORTED for the other forms, 2-D meshes or an lxd
- * whose element working set does not fit in shared memory (~220 KB). */
+ * back.  The fused FP64 form on a curvilinear mesh takes it too: each stage
+ * computes the dealiased volume term first, then adds flux, lift, source,
+ * inverse mass and RK update in its one stage kernel.  NEKGPU_ERR_UNSUPPORTED
+ * for the other forms and for fused forms on affine meshes, 2-D meshes or an
+ * lxd whose element working set does not fit in shared memory (~220 KB). */
 int nekgpu_set_dealias(nekgpu_ctx* ctx, int lxd, const double* jgl, const double* dxmd,
                        const double* w3md, const double* metd);
 

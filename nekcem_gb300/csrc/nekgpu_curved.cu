@@ -5,7 +5,10 @@
 // read directly (cem_maxwell_flux3d and gs_op_fields,
 // src/cem_maxwell.F:922-1002, 1368-1426), the lift (:725-735), the volume
 // source, the inverse mass and the low-storage RK update
-// (src/cem_common.F:18-75), one kernel per stage.
+// (src/cem_common.F:18-75), one kernel per stage.  With the dealiased curl
+// (param(18) = -1, maxwell_wght_dcurl) its volume term comes from k_dcurl,
+// launched before the stage kernel, which then adds flux, lift, source,
+// inverse mass and RK update in one pass.
 //
 // One block of N3 threads per element at a time (thread per node); the
 // element's six field components sit in shared memory for the derivative
@@ -60,8 +63,13 @@ __global__ void __launch_bounds__((NX * NX * NX + 31) / 32 * 32)
     __syncthreads();
 
     // ---- weighted curl with the general metrics ---------------------------
+    // (or, with the dealiased curl, its volume term computed before)
     double res[6];
-    if (node) {
+    if (node && a.vres) {
+      const long g = (long)e * N3 + tid;
+#pragma unroll
+      for (int c = 0; c < 6; ++c) res[c] = a.vres[c * P + g];
+    } else if (node) {
       double dr[6], ds[6], dt[6];
 #pragma unroll
       for (int c = 0; c < 6; ++c) {
@@ -199,6 +207,11 @@ int curved_stage(Context* c, int rkstep, double time, double dt) {
   a.src_elem = c->fargs.src_elem;
   a.src_w = reinterpret_cast<const double*>(c->fargs.src_w);
   if (c->src.enabled) a.src_ft = source_ft(c->src, time + dt * c->rk_c[rkstep - 1]);
+  a.vres = nullptr;
+  if (c->pargs.md > 0) {  // param(18) = -1: the dealiased curl of the stage's input
+    if ((st = dcurl_into(c, a.u_in, c->d_vres))) return st;
+    a.vres = c->d_vres;
+  }
   switch (c->nx) {
     case 3: st = launch_curved<3>(c, a); break;
     case 4: st = launch_curved<4>(c, a); break;

@@ -1995,12 +1995,14 @@ int nekgpu_set_array(nekgpu_ctx* c, const char* name, const double* in) {
   return check_cuda(cudaMemcpy(c->d_pml_aux, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice));
 }
 
-// Dealiased curl of the plain form: the driver's tables as the reference
-// builds them on the first maxwell_wght_dcurl call.
+// Dealiased curl (plain form, and the fused FP64 form on curvilinear
+// meshes): the driver's tables as the reference builds them on the first
+// maxwell_wght_dcurl call.
 int nekgpu_set_dealias(nekgpu_ctx* c, int lxd, const double* jgl, const double* dxmd,
                        const double* w3md, const double* metd) {
   if (!c) return NEKGPU_ERR_ARG;
-  if (c->form != NEKGPU_PLAIN || c->ndim == 2) return NEKGPU_ERR_UNSUPPORTED;
+  const bool fused_curved = c->form == NEKGPU_FUSED64 && c->curved;
+  if ((c->form != NEKGPU_PLAIN && !fused_curved) || c->ndim == 2) return NEKGPU_ERR_UNSUPPORTED;
   {
     PlainDev& pa = c->pargs;
     for (const void* q : {(const void*)pa.jgl, (const void*)pa.jgt, (const void*)pa.dxmd,
@@ -2028,6 +2030,7 @@ int nekgpu_set_dealias(nekgpu_ctx* c, int lxd, const double* jgl, const double* 
   if ((st = A.put(&d1, vjgl)) || (st = A.put(&d2, vjgt)) || (st = A.put(&d3, vD)) ||
       (st = A.put(&d4, vDt)) || (st = A.put(&d5, vw3)) || (st = A.put(&d6, vmet)))
     return st;
+  if (fused_curved && !c->d_vres && (st = A.get(&c->d_vres, 6 * (size_t)c->npts))) return st;
   PlainDev& a = c->pargs;
   a.jgl = d1; a.jgt = d2; a.dxmd = d3; a.dxtmd = d4; a.w3md = d5; a.metd = d6;
   a.md = md;

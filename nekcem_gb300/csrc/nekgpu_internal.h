@@ -309,6 +309,7 @@ struct CurvedDev {
   const double* src_w;    // nx^3 per source element
   double src_ft;
   double a, b;
+  const double* vres;     // 6*npts volume term from the dealiased curl, or null: the curl in-kernel
   double D[kMaxNx * kMaxNx];  // D(i,j) at [i + nx*j]
 };
 
@@ -344,6 +345,7 @@ struct Context {
   bool curved = false;      // fused FP64 form on a curvilinear mesh (nekgpu_curved.cu)
   CurvedDev cargs{};
   int device = 0;
+  double* d_vres = nullptr;  // fused FP64 form with the dealiased curl: its volume term
   int nx = 0, nelt = 0;
   long npts = 0, nxzfl = 0;
   double volume = 0;
@@ -464,6 +466,8 @@ int plain_pml_step(Context* c);                                   // pml_step
 int plain_pml_rk_update(Context* c, double ca, double cb, double dt);
 // shared memory of the dealiased curl kernel for nx1 = mx, lxd = md
 size_t dcurl_smem(int mx, int md);
+// the dealiased weighted curl (k_dcurl) of state u into res (6*npts, H then E)
+int dcurl_into(Context* c, const double* u, double* res);
 // cem_maxwell_drude / cem_maxwell_lorentz with the currents' rk4_upd
 int plain_dispersive(Context* c, double ca, double cb, double dt);
 // userinc: adds the stage's incident values to the restricted face fields

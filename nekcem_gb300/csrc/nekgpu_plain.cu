@@ -490,6 +490,24 @@ size_t dcurl_smem(int mx, int md) {
          sizeof(double);
 }
 
+int dcurl_into(Context* c, const double* u, double* res) {
+  static bool dattr = false;
+  if (!dattr) {
+    if (check_cuda(cudaFuncSetAttribute(k_dcurl, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024)))
+      return NEKGPU_ERR_CUDA;
+    dattr = true;
+  }
+  PlainDev p = c->pargs;
+  p.nx = c->nx;
+  p.nelt = c->nelt;
+  p.npts = c->npts;
+  p.u = const_cast<double*>(u);
+  p.res = res;
+  k_dcurl<<<c->nelt, kThreads, dcurl_smem(c->nx, p.md), c->stream>>>(p);
+  c->last_launches += 1;
+  return last_error();
+}
+
 int plain_cem_maxwell(Context* c) {
   if (c->pargs.md) {
     static bool dattr = false;
