@@ -134,10 +134,13 @@ int nekgpu_device_check(int device);
 /* ---- setup / teardown ----------------------------------------------------- */
 /* Replaces cem_maxwell_init's hand-off: uploads the static arrays once.
  * The face pairing comes from glo_face exactly as gs_setup groups it
- * (src/jl/gs.h:17-60); groups of more than two are rejected.  The fused forms
- * need affine elements (per-element-constant metrics) with axis-aligned faces
- * whose paired nodes share in-face order; otherwise NEKGPU_ERR_MESH and the
- * caller may use NEKGPU_PLAIN, which takes any conforming hex mesh. */
+ * (src/jl/gs.h:17-60); groups of more than two are rejected.  On affine
+ * elements (per-element-constant metrics) with axis-aligned faces whose paired
+ * nodes share in-face order the fused forms use their compact per-element
+ * geometry; on any other conforming hex mesh with the reference's face
+ * numbering and nx1 <= 8 they use their curvilinear kernels (per-node metrics,
+ * per-face-node normals and areas; no PML or dispersive media there).
+ * NEKGPU_PLAIN takes any conforming hex mesh. */
 int nekgpu_init(nekgpu_ctx** ctx, const nekgpu_mesh* mesh, int form);
 /* Builds the box case on the host (GLL points, geometry, face pairing,
  * materials) and uploads it. */

@@ -1058,14 +1058,30 @@ int upload_fused(Context* c, const Compact& cp) {
   return upload_pml_fused(c, A, cp, a.pml);
 }
 
-// Curvilinear mesh for the fused FP64 form: the reference's per-node metrics
-// and face arrays as given; face node partners from the gs ids.  The
-// reference's face numbering is required (the lift finds a node's face
-// slots from its position in the element).
+// Curvilinear mesh for the fused FP64 and the mixed forms: the reference's
+// per-node metrics and face arrays as given; face node partners from the gs
+// ids.  The reference's face numbering is required (the lift finds a node's
+// face slots from its position in the element).  The mixed form also takes
+// the library's GLL D of this order in its FP32 pieces (a caller's D must
+// agree with it).
 int upload_curved(Context* c, const nekgpu_mesh* m) {
   const int n = m->nx1;
   const long n2 = (long)n * n, n3 = n2 * n, npts = n3 * m->nelt, nxzfl = 6 * n2 * m->nelt;
   if (n < 3 || n > 8) return NEKGPU_ERR_UNSUPPORTED;
+  if (c->form == NEKGPU_MIXED) {
+    std::vector<double> z, w, D;
+    gll(n - 1, z, w, D);
+    double dmax = 0, diff = 0;
+    for (long k = 0; k < n2; ++k) {
+      dmax = std::max(dmax, std::fabs(D[k]));
+      diff = std::max(diff, std::fabs(D[k] - m->dxm1[k]));
+    }
+    if (diff > 1e-12 * dmax) return NEKGPU_ERR_MESH;
+    std::vector<float> tab;
+    split_D(D, n, tab);
+    const int st = mixed_upload_D(n, tab.data(), tab.size());
+    if (st) return st;
+  }
   if (m->npml > 0) return NEKGPU_ERR_UNSUPPORTED;  // no PML on curvilinear meshes
   for (long e = 0; e < m->nelt; ++e)
     for (int f = 0; f < 6; ++f)
@@ -1368,7 +1384,8 @@ int chunked_step(Context* c, double* hn, double* en, long ld, double time, doubl
 int do_stage(Context* c, int rkstep, double time, double dt) {
   if (rkstep < 1 || rkstep > 5) return NEKGPU_ERR_ARG;
   if (c->ndim == 2) return stage2d(c, rkstep, time, dt);
-  if (c->curved) return curved_stage(c, rkstep, time, dt);
+  if (c->curved)
+    return c->form == NEKGPU_MIXED ? mixed_curved_stage(c, rkstep, time, dt) : curved_stage(c, rkstep, time, dt);
   if (c->form == NEKGPU_PLAIN) return plain_stage(c, rkstep, time, dt);
   if (c->form == NEKGPU_MIXED) return mixed_stage(c, rkstep, time, dt);
   return fused_stage(c, rkstep, time, dt);
@@ -1448,8 +1465,8 @@ int nekgpu_init(nekgpu_ctx** ctx, const nekgpu_mesh* m, int form) {
   } else {
     Compact cp;
     st = build_compact(m, cp);
-    if (st == NEKGPU_ERR_MESH && form == NEKGPU_FUSED64) {
-      // not affine: the curvilinear variant of the fused FP64 form
+    if (st == NEKGPU_ERR_MESH && (form == NEKGPU_FUSED64 || form == NEKGPU_MIXED)) {
+      // not affine: the curvilinear variant of the fused FP64 or mixed form
       st = common_setup(c, form, m->nx1, m->nelt);
       if (!st) st = upload_curved(c, m);
     } else {
@@ -2212,7 +2229,7 @@ int nekgpu_set_source(nekgpu_ctx* c, int enabled, const double xc[3], double sig
     }
     int* d_off;
     if ((st = A.put(&d_off, off))) return st;
-    if (c->form == NEKGPU_MIXED) {
+    if (c->form == NEKGPU_MIXED && !c->curved) {
       // normalised like the residual: weight / (bm1 * 2/hx) = weight / (w3 * rx),
       // as a (hi, lo) float pair (~2^-48 of the weight)
       std::vector<float> wf(2 * wd.size());
@@ -2444,7 +2461,7 @@ int nekgpu_time_steps(nekgpu_ctx* c, int nsteps, double* time, double dt, double
   c->last_launches = 0;
   if (c->form != NEKGPU_PLAIN) {
     // keep the one-off rescale out of the timed region
-    int st = c->form == NEKGPU_MIXED ? scale_coef_pairs(c, dt) : scale_coef(c, dt);
+    int st = c->form == NEKGPU_MIXED && !c->curved ? scale_coef_pairs(c, dt) : scale_coef(c, dt);
     if (st) return st;
   }
   if (check_cuda(cudaEventRecord(c->ev0, c->stream))) return NEKGPU_ERR_CUDA;

@@ -500,6 +500,8 @@ int mixed_upload_D(int nx, const float* tab, size_t count);
 
 // nekgpu_curved.cu: one fused FP64 stage on a curvilinear mesh
 int curved_stage(Context* c, int rkstep, double time, double dt);
+// mixed stage on a curvilinear mesh (curved arrays, FP64 coefficients)
+int mixed_curved_stage(Context* c, int rkstep, double time, double dt);
 
 // nekgpu_2d.cu: one 2-D TE / TM stage in the reference's arithmetic
 int stage2d(Context* c, int rkstep, double time, double dt);

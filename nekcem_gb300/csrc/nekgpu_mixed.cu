@@ -910,6 +910,252 @@ int launch_mixed(Context* c, const MixedDev& a) {
   return check_cuda(cudaGetLastError());
 }
 
+// ===========================================================================
+// Mixed stage on curvilinear hexahedra (NEKGPU_MIXED on a mesh whose metrics
+// vary inside the elements): the general weighted curl with the nine
+// per-node metrics (maxwell_wght_curl, src/cem_maxwell.F:1428-1497), the
+// upwind flux with per-face-node normals and areas (cem_maxwell_flux3d,
+// src/cem_maxwell.F:922-1002) and the partner's values read directly, lift,
+// volume source, inverse mass and RK update -- the arrays of the curved FP64
+// form (CurvedDev), converted to float pairs on the fly by integer
+// operations.  The derivatives are exact-hi FP32 contractions as in the
+// affine kernel (the element's 10-bit grid per component, D in its Dh, Df,
+// Dm pieces); metrics, weights, normals, areas, face coefficients, source
+// weights and the inverse mass enter as float pairs in float-float
+// arithmetic; the RK update is FP64.  One block of NX^3 threads per element
+// (thread per node); the state of the thread's node stays in registers.
+// ===========================================================================
+struct PairF {
+  float h, l;
+};
+__device__ __forceinline__ PairF pr(double d) { return PairF{d2f_hi(d), d2f_lo(d)}; }
+__device__ __forceinline__ PairF pmul(PairF a, PairF b) {
+  const float p = a.h * b.h;
+  float e = fmaf(a.h, b.h, -p);
+  e = fmaf(a.h, b.l, e);
+  e = fmaf(a.l, b.h, e);
+  return PairF{p, e};
+}
+__device__ __forceinline__ PairF padd(PairF a, PairF b) {
+  float s, t;
+  two_sum(a.h, b.h, s, t);
+  return PairF{s, (a.l + b.l) + t};
+}
+__device__ __forceinline__ PairF pneg(PairF a) { return PairF{-a.h, -a.l}; }
+__device__ __forceinline__ PairF psub(PairF a, PairF b) { return padd(a, pneg(b)); }
+// a x b for pair 3-vectors
+__device__ __forceinline__ void pcross(const PairF* a, const PairF* b, PairF* o) {
+  o[0] = psub(pmul(a[1], b[2]), pmul(a[2], b[1]));
+  o[1] = psub(pmul(a[2], b[0]), pmul(a[0], b[2]));
+  o[2] = psub(pmul(a[0], b[1]), pmul(a[1], b[0]));
+}
+
+template <int NX>
+struct CMCfg {
+  static constexpr int N2 = NX * NX, N3 = N2 * NX, NF = 6 * N2;
+  static constexpr int NT = (N3 + 31) / 32 * 32, NW = NT / 32;
+  static constexpr size_t off_F = 6 * (size_t)N3 * 8;            // float2 split pairs [c][v]
+  static constexpr size_t off_D = off_F + 6 * (size_t)NF * 8;    // float2 flux pairs [c][face node]
+  static constexpr size_t off_Dm = off_D + (size_t)N2 * 8;       // (Dh, Df) [i + NX l]
+  static constexpr size_t off_wmax = off_Dm + (size_t)N2 * 4;    // Dm [i + NX l]
+  static constexpr size_t off_E = off_wmax + NW * 6 * 4;
+  static constexpr size_t smem = off_E + 8 * 4;
+};
+
+template <int NX>
+__global__ void __launch_bounds__(CMCfg<NX>::NT, 1) k_mixed_curved(const CurvedDev a) {
+  using C = CMCfg<NX>;
+  constexpr int N2 = C::N2, N3 = C::N3, NF = C::NF, NT = C::NT;
+  extern __shared__ __align__(16) unsigned char smem[];
+  float2* s_u2 = reinterpret_cast<float2*>(smem);
+  float2* s_F = reinterpret_cast<float2*>(smem + C::off_F);
+  float2* s_Dhf = reinterpret_cast<float2*>(smem + C::off_D);
+  float* s_Dm = reinterpret_cast<float*>(smem + C::off_Dm);
+  unsigned* s_wmax = reinterpret_cast<unsigned*>(smem + C::off_wmax);
+  unsigned* s_E = reinterpret_cast<unsigned*>(smem + C::off_E);
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const long P = a.npts;
+  const bool node = tid < N3;
+  const int vi = tid % NX, vj = (tid / NX) % NX, vk = tid / N2;
+  const bool first_stage = (a.a == 0.0);
+  constexpr int H = (NX + 1) / 2;
+  for (int t = tid; t < N2; t += NT) {
+    const int i = t % NX, l = t / NX;
+    s_Dhf[t] = c_mixD[NX][0][t];
+    const float2 m = c_mixD[NX][1][i / 2 + H * l];
+    s_Dm[t] = (i & 1) ? m.y : m.x;
+  }
+  for (int e = blockIdx.x; e < a.nelt; e += gridDim.x) {
+    __syncthreads();  // the previous element's shared data is consumed
+    const long g = (long)e * N3 + tid;
+    double u[6];
+    unsigned em[6];
+#pragma unroll
+    for (int c = 0; c < 6; ++c) {
+      u[c] = node ? a.u_in[c * P + g] : 0.0;
+      em[c] = ((unsigned)__double2hiint(u[c]) >> 20) & 0x7FFu;
+      em[c] = __reduce_max_sync(0xffffffffu, em[c]);
+    }
+    if (lane == 0)
+#pragma unroll
+      for (int c = 0; c < 6; ++c) s_wmax[warp * 6 + c] = em[c];
+    __syncthreads();
+    if (tid < 6) {
+      unsigned m = 0;
+      for (int w = 0; w < C::NW; ++w) m = max(m, s_wmax[w * 6 + tid]);
+      s_E[tid] = min(max(m, 906u), 1158u);
+    }
+    __syncthreads();
+    if (node) {  // split: uh on the element's 10-bit grid of the component, ul = u - uh
+      const float M = 12582912.0f;
+#pragma unroll
+      for (int c = 0; c < 6; ++c) {
+        const int E = (int)s_E[c];
+        const float qv = __int_as_float((E - 905) << 23);
+        const float qi = __int_as_float((1159 - E) << 23);
+        const float uf = d2f_hi(u[c]), ulo = d2f_lo(u[c]);
+        const float uh = (__fadd_rn(__fmaf_rn(uf, qi, M), -M)) * qv;
+        s_u2[c * N3 + tid] = make_float2(uh, __fadd_rn(__fsub_rn(uf, uh), ulo));
+      }
+    }
+    __syncthreads();
+    // ---- upwind flux per face node, float pairs ---------------------------
+    for (int t = tid; t < NF; t += NT) {
+      const int f = t / N2, ab = t - f * N2;
+      const int v = face_vol<NX>(f, ab % NX, ab / NX);
+      const long js = (long)e * NF + t, L = a.nxzfl;
+      const int pv = a.partner[js];
+      PairF JH[3], JE[3];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const float2 h = s_u2[c * N3 + v], ev = s_u2[(c + 3) * N3 + v];
+        if (pv >= 0) {
+          const float2 jh = jump_pair(a.u_in[c * P + pv], h), je = jump_pair(a.u_in[(c + 3) * P + pv], ev);
+          JH[c] = PairF{jh.x, jh.y};
+          JE[c] = PairF{je.x, je.y};
+        } else {  // PEC mirror: [H] = 0, [E] = -2E exactly
+          JH[c] = PairF{0.0f, 0.0f};
+          JE[c] = PairF{-2.0f * ev.x, -2.0f * ev.y};
+        }
+      }
+      const PairF n[3] = {pr(a.face[js]), pr(a.face[L + js]), pr(a.face[2 * L + js])};
+      const PairF area = pr(a.face[3 * L + js]);
+      PairF Y02{-0.5f, 0.0f}, C02Y{0.5f, 0.0f}, Z02{0.5f, 0.0f}, C02Z{0.5f, 0.0f};
+      if (a.fcoef) {
+        Y02 = pr(a.fcoef[js]); C02Y = pr(a.fcoef[L + js]);
+        Z02 = pr(a.fcoef[2 * L + js]); C02Z = pr(a.fcoef[3 * L + js]);
+      }
+      // n x [E], n x [H] (the gs sums of -n x E, -n x H), then the upwind terms
+      PairF nE[3], nH[3], fu[3], fw[3];
+      pcross(n, JE, nE);
+      pcross(n, JH, nH);
+      pcross(n, nH, fu);
+      pcross(n, nE, fw);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const PairF fh = pmul(area, psub(pmul(Y02, nE[c]), pmul(C02Y, fu[c])));
+        const PairF fe = pmul(area, psub(pmul(Z02, nH[c]), pmul(C02Z, fw[c])));
+        s_F[c * NF + t] = make_float2(fh.h, fh.l);
+        s_F[(3 + c) * NF + t] = make_float2(fe.h, fe.l);
+      }
+    }
+    __syncthreads();
+    if (!node) continue;
+    // ---- derivatives (exact-hi contractions) and the weighted curl -----------
+    // d_dir u_c at the node as a pair: hi = sum Dh uh (exact), lo = the rest
+    auto deriv = [&](int c, int dir) {
+      const float2* pu = s_u2 + c * N3;
+      const int row = dir == 0 ? vi : (dir == 1 ? vj : vk);
+      float2 x = make_float2(0.0f, 0.0f);
+      float m = 0.0f;
+#pragma unroll
+      for (int l = 0; l < NX; ++l) {
+        const int q = dir == 0 ? l + NX * vj + N2 * vk
+                               : (dir == 1 ? vi + NX * l + N2 * vk : vi + NX * vj + N2 * l);
+        const float2 uu = pu[q];
+        x = __ffma2_rn(s_Dhf[row + NX * l], uu, x);
+        m = fmaf(s_Dm[row + NX * l], uu.x, m);
+      }
+      return PairF{x.x, x.y + m};
+    };
+    // curl_k = eps(k, ax, q) d u_q / d x_ax with d/dx_ax = sum_dir metric(dir, ax) d/d_dir,
+    // accumulated direction by direction (one row of D live at a time): the
+    // two axes other than q give
+    //   w[(q+2)%3] -= metric(dir, (q+1)%3) du_q/d_dir,  w[(q+1)%3] += metric(dir, (q+2)%3) du_q/d_dir
+    PairF w[6] = {{0.0f, 0.0f}, {0.0f, 0.0f}, {0.0f, 0.0f},
+                  {0.0f, 0.0f}, {0.0f, 0.0f}, {0.0f, 0.0f}};  // curl H, curl E
+#pragma unroll
+    for (int dir = 0; dir < 3; ++dir) {
+      const PairF m3[3] = {pr(a.metrics[(3 * dir) * P + g]), pr(a.metrics[(3 * dir + 1) * P + g]),
+                           pr(a.metrics[(3 * dir + 2) * P + g])};  // r|s|t x, y, z
+#pragma unroll
+      for (int c = 0; c < 6; ++c) {
+        const int q = c % 3, o = c - q;
+        const PairF d = deriv(c, dir);
+        w[o + (q + 2) % 3] = psub(w[o + (q + 2) % 3], pmul(d, m3[(q + 1) % 3]));
+        w[o + (q + 1) % 3] = padd(w[o + (q + 1) % 3], pmul(d, m3[(q + 2) % 3]));
+      }
+    }
+    const PairF w3 = pr(a.w3[tid]);
+    PairF res[6];  // resH = -W curl E, resE = W curl H
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+      res[q] = pneg(pmul(w3, w[3 + q]));
+      res[3 + q] = pmul(w3, w[q]);
+    }
+    // ---- lift in face-slot order ---------------------------------------------
+    auto add = [&](int f, int ab) {
+#pragma unroll
+      for (int c = 0; c < 6; ++c) {
+        const float2 F = s_F[c * NF + f * N2 + ab];
+        res[c] = padd(res[c], PairF{F.x, F.y});
+      }
+    };
+    if (vj == 0) add(0, vi + NX * vk);
+    if (vi == NX - 1) add(1, vj + NX * vk);
+    if (vj == NX - 1) add(2, vi + NX * vk);
+    if (vi == 0) add(3, vj + NX * vk);
+    if (vk == 0) add(4, vi + NX * vj);
+    if (vk == NX - 1) add(5, vi + NX * vj);
+    // ---- volume source (usersrc), mass-weighted ----------------------------------
+    if (a.src_elem) {
+      const int so = a.src_elem[e];
+      if (so >= 0) res[5] = padd(res[5], pmul(pr(a.src_w[(long)so * N3 + tid]), pr(a.src_ft)));
+    }
+    // ---- inverse mass (pair product, one DADD) and the FP64 RK update ------------
+    const PairF ch = pr(a.coef[g]), ce = pr(a.coef[P + g]);
+#pragma unroll
+    for (int c = 0; c < 6; ++c) {
+      const PairF p = pmul(res[c], c < 3 ? ch : ce);
+      const double r = f2d(p.h) + f2d(p.l);
+      const double kn = first_stage ? r : fma(a.a, a.k[c * P + g], r);
+      a.k[c * P + g] = kn;
+      a.u_out[c * P + g] = fma(a.b, kn, a.u_in[c * P + g]);
+    }
+  }
+}
+
+template <int NX>
+int launch_mixed_curved(Context* c, const CurvedDev& a) {
+  using C = CMCfg<NX>;
+  static int grid = 0;
+  if (!grid) {
+    if (check_cuda(cudaFuncSetAttribute(k_mixed_curved<NX>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)C::smem)))
+      return NEKGPU_ERR_CUDA;
+    int per_sm = 0, sms = 0;
+    if (check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_mixed_curved<NX>, C::NT, C::smem)))
+      return NEKGPU_ERR_CUDA;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
+    if (per_sm < 1) return NEKGPU_ERR_UNSUPPORTED;
+    grid = per_sm * sms;
+  }
+  const int g = c->nelt < grid ? c->nelt : grid;
+  k_mixed_curved<NX><<<g, C::NT, C::smem, c->stream>>>(a);
+  c->last_launches += 1;
+  return check_cuda(cudaGetLastError());
+}
+
 // The bounded wait run out on purpose: an mbarrier that nothing arrives at,
 // polled `polls` times, then the status word is set as a stage kernel sets it
 // when its copy never lands.  No fault, no trap, no endless loop.
@@ -987,6 +1233,34 @@ int mixed_stage_range(Context* c, int rkstep, double time, double dt, int e0, in
     default: return NEKGPU_ERR_UNSUPPORTED;
   }
   return st;
+}
+
+// One mixed stage on a curvilinear mesh (the curved form's arrays, FP64
+// coefficients scaled once per dt).
+int mixed_curved_stage(Context* c, int rkstep, double time, double dt) {
+  int st = scale_coef(c, dt);
+  if (st) return st;
+  CurvedDev a = c->cargs;
+  a.u_in = c->d_u[c->cur];
+  a.u_out = c->d_u[c->cur ^ 1];
+  a.a = c->rk_a[rkstep - 1];
+  a.b = c->rk_b[rkstep - 1];
+  a.src_elem = c->fargs.src_elem;
+  a.src_w = reinterpret_cast<const double*>(c->fargs.src_w);
+  a.vres = nullptr;
+  if (c->src.enabled) a.src_ft = source_ft(c->src, time + dt * c->rk_c[rkstep - 1]);
+  switch (c->nx) {
+    case 3: st = launch_mixed_curved<3>(c, a); break;
+    case 4: st = launch_mixed_curved<4>(c, a); break;
+    case 5: st = launch_mixed_curved<5>(c, a); break;
+    case 6: st = launch_mixed_curved<6>(c, a); break;
+    case 7: st = launch_mixed_curved<7>(c, a); break;
+    case 8: st = launch_mixed_curved<8>(c, a); break;
+    default: return NEKGPU_ERR_UNSUPPORTED;
+  }
+  if (st) return st;
+  c->cur ^= 1;
+  return NEKGPU_OK;
 }
 
 int mixed_stage(Context* c, int rkstep, double time, double dt) {
