@@ -336,10 +336,13 @@ int nekgpu_selftest_wait(nekgpu_ctx* ctx, int polls);
  * value is non-finite or above 1e20 in magnitude */
 int nekgpu_check_blowup(nekgpu_ctx* ctx);
 
-/* ---- discrete adjoint (NEKGPU_FUSED64) --------------------------------------- */
+/* ---- discrete adjoint (NEKGPU_FUSED64, NEKGPU_MIXED; affine meshes) -------- */
 /* No routine of the reference computes gradients; this is the discrete
  * adjoint of nsteps RK45 steps of the FP64 fused stage (cem_maxwell_op_rk,
  * src/cem_maxwell.F:327-345) for J = sum_n jw[n] |E(n)|^2 at the final time.
+ * The forward steps (first pass and recomputations) run in the context's
+ * form: with NEKGPU_MIXED they are mixed stages, whose trajectory agrees with
+ * the FP64 one to ~1e-10, and the FP64 reverse stages read those states.
  * Starts from the context's current state and leaves it at the final state.
  * Schedules: stride > 0 checkpoints the state every `stride` steps and the
  * reverse sweep recomputes one segment at a time, keeping its stage states
@@ -348,7 +351,8 @@ int nekgpu_check_blowup(nekgpu_ctx* ctx);
  * the device memory left (under NEKGPU_MEM_BUDGET_MB: the budget less the
  * context's own memory), else falls back to the binomial schedule with the
  * snapshots that fit; stride < 0 uses the binomial schedule with -stride
- * snapshots (17 states + snapshots; forward steps recomputed more often).
+ * device snapshots (15 states + snapshots; forward steps recomputed more
+ * often), plus the host snapshots of nekgpu_adjoint_host_snapshots.
  * NEKGPU_ERR_NOMEM when the chosen schedule does not fit.  Returns J, dJ/deps
  * at every node (npts, host array) and the device times up to J (forward)
  * and of the rest (reverse sweep, recomputation included), in ms.
@@ -362,6 +366,12 @@ int nekgpu_adjoint_gradient(nekgpu_ctx* ctx, int nsteps, double t0, double dt, c
  * context (it allocates nothing on the device); nekgpu_adjoint_run runs
  * nekgpu_adjoint_gradient with them.  NEKGPU_ERR_STATE if run comes first. */
 int nekgpu_adjoint_init(nekgpu_ctx* ctx, const double* jw, int stride);
+/* Pinned host-memory snapshots (one state each, 48 bytes per node) that the
+ * binomial schedule may use beyond the device snapshots (default 0): a state
+ * too large for many device snapshots reverses with fewer recomputations.
+ * Each use of a host snapshot copies one state over the host link.  Gradients
+ * are bit-identical whatever memory the snapshots live in. */
+int nekgpu_adjoint_host_snapshots(nekgpu_ctx* ctx, int n);
 int nekgpu_adjoint_run(nekgpu_ctx* ctx, int nsteps, double t0, double dt, double* J,
                        double* dJdeps);
 

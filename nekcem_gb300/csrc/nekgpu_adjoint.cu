@@ -207,6 +207,15 @@ __global__ void k_adjoint_seed(double* w, const double* ub, const double* coef, 
   w[i] = b * coef[(i < 3 * P ? 0 : P) + g] * ub[i];
 }
 
+// dt hbm1 | dt ebm1: the same product the fused FP64 form's coefficient
+// scaling forms from its unnormalised base
+__global__ void k_adjoint_coef64(double* coef, const double* hbm1, const double* ebm1, long P,
+                                 double dt) {
+  const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (i >= 2 * P) return;
+  coef[i] = dt * (i < P ? hbm1[i] : ebm1[i - P]);
+}
+
 template <int NX>
 int launch_adjoint(Context* c, const AdjointDev& a) {
   using C = ACfg<NX>;
@@ -246,9 +255,17 @@ int adjoint_stage(Context* c, const AdjointDev& a) {
   }
 }
 
-int adjoint_seed(Context* c, double* w, const double* ub, double b) {
+int adjoint_seed(Context* c, double* w, const double* ub, const double* coef, double b) {
   const long n = 6 * c->npts;
-  k_adjoint_seed<<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(w, ub, c->d_coef, c->npts, b);
+  k_adjoint_seed<<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(w, ub, coef, c->npts, b);
+  c->last_launches += 1;
+  return check_cuda(cudaGetLastError());
+}
+
+int adjoint_coef64(Context* c, double* coef, double dt) {
+  const long n = c->npts;
+  k_adjoint_coef64<<<(unsigned)((2 * n + 255) / 256), 256, 0, c->stream>>>(coef, c->d_hbm1,
+                                                                           c->d_ebm1, n, dt);
   c->last_launches += 1;
   return check_cuda(cudaGetLastError());
 }

@@ -1,13 +1,17 @@
 // Driver of the discrete adjoint (nekgpu_adjoint_gradient).  J = sum jw |E|^2
-// at the final time; the reverse stages are in nekgpu_adjoint.cu.  Two
-// schedules, chosen by the device memory available:
+// at the final time; the reverse stages are in nekgpu_adjoint.cu.  The
+// forward steps (first pass and recomputations) run in the context's form:
+// the fused FP64 stage, or the mixed stage (whose trajectory agrees with the
+// FP64 one to ~1e-10); the reverse stages are FP64 in both.  Two schedules,
+// chosen by the device memory available:
 //  * sqrt(steps) checkpoints: the forward pass stores the state every S
 //    steps; the reverse sweep recomputes one segment at a time, keeping every
 //    stage's state and RK register of the segment, and runs its reverse
 //    stages (ceil(n/S) + 2 x 2 x (5S+1) + 4 states);
 //  * binomial snapshots when that does not fit: a revolve-type schedule over
-//    the snapshots that fit, with one step's stage storage (17 states +
-//    snapshots); more forward steps are recomputed.
+//    the snapshots that fit, plus any pinned host-memory snapshots the caller
+//    allows, with one step's stage storage (15 states + device snapshots);
+//    more forward steps are recomputed.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -81,7 +85,9 @@ int build_adjoint_data(Context* c) {
       check_cuda(cudaMemcpy(nbr.data(), c->d_nbr, nbr.size() * sizeof(int), cudaMemcpyDeviceToHost)))
     return NEKGPU_ERR_CUDA;
   const double C0 = c->fargs.C0;
-  if (c->d_fcoef) {
+  if (c->form == NEKGPU_MIXED) {
+    fc = c->host_fcoef64;  // the device holds float pairs
+  } else if (c->d_fcoef) {
     fc.resize(4 * (size_t)nxzfl);
     if (check_cuda(cudaMemcpy(fc.data(), c->d_fcoef, fc.size() * 8, cudaMemcpyDeviceToHost)))
       return NEKGPU_ERR_CUDA;
@@ -205,6 +211,48 @@ int copy_state(Context* c, double* dst, const double* src) {
                                     cudaMemcpyDeviceToDevice, c->stream));
 }
 
+// A snapshot slot of the binomial schedule: device memory, or pinned host
+// memory (reached over the host link; one copy each way per use).
+struct Slot {
+  double* p = nullptr;
+  bool host = false;
+};
+
+// state copy between a slot and a device buffer, on the context stream
+int copy_slot(Context* c, double* dst, bool dst_host, const double* src, bool src_host) {
+  const cudaMemcpyKind kind = src_host ? cudaMemcpyHostToDevice
+                                       : (dst_host ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice);
+  return check_cuda(cudaMemcpyAsync(dst, src, 6 * c->npts * sizeof(double), kind, c->stream));
+}
+
+// Pinned host snapshots of one call; freed on every exit path (cudaFreeHost
+// waits for the device).
+struct HostSlots {
+  std::vector<void*> ptrs;
+  ~HostSlots() {
+    for (void* p : ptrs) cudaFreeHost(p);
+  }
+  double* get(size_t count) {
+    void* p = nullptr;
+    if (cudaHostAlloc(&p, count * sizeof(double), cudaHostAllocDefault) != cudaSuccess) {
+      cudaGetLastError();
+      return nullptr;
+    }
+    ptrs.push_back(p);
+    return (double*)p;
+  }
+};
+
+// forward stages in the context's form
+int fwd_stage(Context* c, int r, double t, double dt) {
+  return c->form == NEKGPU_MIXED ? mixed_stage(c, r, t, dt) : fused_stage(c, r, t, dt);
+}
+int fwd_stage_buffers(Context* c, int r, double t, double dt, const double* u_in, double* u_out,
+                      double* k_in, double* k_out) {
+  return c->form == NEKGPU_MIXED ? mixed_stage_buffers(c, r, t, dt, u_in, u_out, k_in, k_out)
+                                 : fused_stage_buffers(c, r, t, dt, u_in, u_out, k_in, k_out);
+}
+
 }  // namespace
 
 namespace {
@@ -244,15 +292,19 @@ struct Sweep {
   double* ub[2];
   double* wb[2];
   double* deps;
+  const double* coef64 = nullptr;  // dt hbm1 | dt ebm1 in FP64
   int cu = 0;
   AdjointDev a{};
   double J = 0.0;
   bool seeded = false;
+  std::vector<double> final_host;  // u(T), read back by the seed
 
   // J and the adjoint seed from the final state: ub = (0, 2 jw E), w = b_5 dt M^-1 ub
   int seed(const double* u_final) {
     const long npts = c->npts, ns = 6 * npts;
-    std::vector<double> uf(ns), ubf(ns, 0.0);
+    std::vector<double>& uf = final_host;
+    std::vector<double> ubf(ns, 0.0);
+    uf.resize(ns);
     if (check_cuda(cudaMemcpyAsync(uf.data(), u_final, ns * 8, cudaMemcpyDeviceToHost, c->stream)) ||
         check_cuda(cudaStreamSynchronize(c->stream)))
       return NEKGPU_ERR_CUDA;
@@ -270,7 +322,7 @@ struct Sweep {
       return NEKGPU_ERR_CUDA;
     cu = 0;
     seeded = true;
-    return adjoint_seed(c, wb[0], ub[0], c->rk_b[4]);
+    return adjoint_seed(c, wb[0], ub[0], coef64, c->rk_b[4]);
   }
 
   // the five reverse stages of step j from its stage states (U[0..4]) and
@@ -296,7 +348,7 @@ struct Sweep {
   void init_args() {
     a.nelt = c->nelt;
     a.npts = c->npts;
-    a.coef = c->d_coef;
+    a.coef = coef64;
     a.bm1 = c->d_bm1;
     a.deps = deps;
     a.nbr = c->d_nbr;
@@ -316,44 +368,48 @@ struct Sweep {
 // stage storage, and the forward steps between snapshots recomputed.
 struct Binomial {
   Sweep& w;
-  std::vector<double*> free_slots;
+  std::vector<Slot> free_slots;  // device slots first: the deepest levels take them
   double* SU[6];  // stage states of one step: SU[0] is the step's start state, SU[5] its end
-  double* SK[6];  // RK registers: SK[0] is read (never used) by stage 1
-  double* scratch;      // a recomputed step start when no snapshot is free
-  double* final_state;  // u(T), put back in the context at the end
+  double* SK[6];  // RK registers; SK[0], read (never used) by stage 1, aliases SK[5]
+  double* scratch;  // device: a recomputed step start, or a host snapshot brought in
   cudaEvent_t ev_seed = nullptr;
 
-  int advance(const double* src, int j0, int k, double* dst) {
+  int advance(Slot src, int j0, int k, Slot dst) {
     Context* c = w.c;
-    int st = copy_state(c, c->d_u[c->cur], src);
+    int st = copy_slot(c, c->d_u[c->cur], false, src.p, src.host);
     for (int j = j0; j < j0 + k && !st; ++j)
-      for (int r = 1; r <= 5 && !st; ++r) st = fused_stage(c, r, w.tstep[j], w.dt);
-    if (!st) st = copy_state(c, dst, c->d_u[c->cur]);
+      for (int r = 1; r <= 5 && !st; ++r) st = fwd_stage(c, r, w.tstep[j], w.dt);
+    if (!st) st = copy_slot(c, dst.p, dst.host, c->d_u[c->cur], false);
     return st;
   }
 
-  int step(int j, double* src) {
+  int step(int j, Slot src) {
     Context* c = w.c;
-    SU[0] = src;
     int st = NEKGPU_OK;
+    SU[0] = src.p;
+    if (src.host) {
+      if ((st = copy_slot(c, scratch, false, src.p, true))) return st;
+      SU[0] = scratch;
+    }
     for (int r = 1; r <= 5 && !st; ++r)
-      st = fused_stage_buffers(c, r, w.tstep[j], w.dt, SU[r - 1], SU[r], SK[r - 1], SK[r]);
+      st = fwd_stage_buffers(c, r, w.tstep[j], w.dt, SU[r - 1], SU[r], SK[r - 1], SK[r]);
     if (st) return st;
     if (!w.seeded) {  // the first step reversed is the last one: its output is u(T)
-      if ((st = copy_state(c, final_state, SU[5])) || (st = w.seed(SU[5]))) return st;
+      if ((st = w.seed(SU[5]))) return st;
       if (check_cuda(cudaEventRecord(ev_seed, c->stream))) return NEKGPU_ERR_CUDA;
     }
     return w.reverse_step(SU, SK);
   }
 
   // reverse steps b-1 .. a; the state at step a is in `sa`; s free snapshots
-  int rev(int a, int b, double* sa, int s) {
+  int rev(int a, int b, Slot sa, int s) {
     const int n = b - a;
     if (n == 1) return step(a, sa);
     if (s == 0 || free_slots.empty()) {
+      const Slot sc{scratch, false};
       for (int j = b - 1; j >= a; --j) {
-        int st = j > a ? advance(sa, a, j - a, scratch) : NEKGPU_OK;
-        if (!st) st = step(j, j > a ? scratch : sa);
+        int st = j > a ? advance(sa, a, j - a, sc) : NEKGPU_OK;
+        if (!st) st = step(j, j > a ? sc : sa);
         if (st) return st;
       }
       return NEKGPU_OK;
@@ -362,7 +418,7 @@ struct Binomial {
     while (beta(s, t) < n) ++t;
     const int right = (int)std::min<double>(beta(s - 1, t), (double)(n - 1));
     const int m = b - right;
-    double* sm = free_slots.back();
+    const Slot sm = free_slots.back();
     free_slots.pop_back();
     int st = advance(sa, a, m - a, sm);
     if (!st) st = rev(m, b, sm, s - 1);
@@ -379,9 +435,10 @@ extern "C" int nekgpu_adjoint_gradient(nekgpu_ctx* c, int nsteps, double t0, dou
                                        double* fwd_ms, double* adj_ms) {
   if (!c || !jw || !J || !dJdeps || nsteps < 1) return NEKGPU_ERR_ARG;
   // no adjoint through PML or dispersive currents
-  if (c->form != NEKGPU_FUSED64 || c->npml || c->disp_n || c->ndim == 2 || c->curved ||
-      !c->inc_slots.empty() || c->grdev.ng)
+  if ((c->form != NEKGPU_FUSED64 && c->form != NEKGPU_MIXED) || c->npml || c->disp_n ||
+      c->ndim == 2 || c->curved || !c->inc_slots.empty() || c->grdev.ng)
     return NEKGPU_ERR_UNSUPPORTED;
+  const bool mixed = c->form == NEKGPU_MIXED;
   if (!c->have_state) return NEKGPU_ERR_STATE;
   int st = build_adjoint_data(c);
   if (st) return st;
@@ -390,12 +447,14 @@ extern "C" int nekgpu_adjoint_gradient(nekgpu_ctx* c, int nsteps, double t0, dou
 
   // ---- memory plan ----------------------------------------------------------------
   // sqrt scheme: ceil(n/S) checkpoints + sets x 2 x (5S+1) segment states +
-  // 4 adjoint states; binomial scheme: 4 adjoint + 11 stage + 2 states +
-  // snapshots.  Both also hold dJ/deps (npts doubles).
+  // 4 adjoint states; binomial scheme: 4 adjoint + 10 stage + 1 scratch
+  // states + device snapshots (+ the pinned host snapshots allowed by
+  // nekgpu_adjoint_host_snapshots).  Both also hold dJ/deps (npts doubles)
+  // and, for the mixed form, the FP64 inverse-mass scale (2 npts doubles).
   // stride > 0: segments of `stride` steps; 0: sqrt(steps) segments if they
   // fit, else the binomial schedule with the snapshots that fit; < 0: the
-  // binomial schedule with -stride snapshots.
-  const double avail = (double)adjoint_budget(c) - (double)npts * 8;
+  // binomial schedule with -stride device snapshots.
+  const double avail = (double)adjoint_budget(c) - (double)npts * 8 - (mixed ? 16.0 * npts : 0.0);
   const int S = stride > 0 ? stride : (int)std::ceil(std::sqrt((double)nsteps));
   const int nseg = (nsteps + S - 1) / S;
   auto sqrt_states = [&](int sets) { return (double)nseg + 4.0 + sets * 2.0 * (5.0 * S + 1.0); };
@@ -405,11 +464,14 @@ extern "C" int nekgpu_adjoint_gradient(nekgpu_ctx* c, int nsteps, double t0, dou
     else if (sqrt_states(1) * state_b <= avail) nsets = 1;
     else if (stride > 0) return NEKGPU_ERR_NOMEM;  // the caller fixed the stride
   }
-  int nslots = 0;
+  int ndev = 0, nhost = 0;
   if (nsets == 0) {
-    const double fit = std::floor(avail / state_b - 17.0);
-    nslots = (int)std::min<double>(stride < 0 ? -(double)stride : fit, (double)nsteps);
-    if (nslots < 1 || nslots > fit) return NEKGPU_ERR_NOMEM;
+    const double fit = std::floor(avail / state_b - 15.0);
+    if (fit < 0) return NEKGPU_ERR_NOMEM;  // not even the stage storage
+    ndev = (int)std::min<double>(stride < 0 ? -(double)stride : fit, (double)nsteps);
+    if (ndev > fit) return NEKGPU_ERR_NOMEM;
+    nhost = std::min(c->adj_host_snapshots, nsteps - ndev);
+    if (ndev + nhost < 1) return NEKGPU_ERR_NOMEM;
   }
 
   Scratch mem;
@@ -428,21 +490,32 @@ extern "C" int nekgpu_adjoint_gradient(nekgpu_ctx* c, int nsteps, double t0, dou
   w.wb[1] = mem.get(ns);
   w.deps = mem.get(npts);
   if (!w.ub[0] || !w.ub[1] || !w.wb[0] || !w.wb[1] || !w.deps) return NEKGPU_ERR_NOMEM;
+  if (mixed) {  // the context's coefficients are float pairs: an FP64 copy for the reverse
+    double* cf = mem.get(2 * npts);
+    if (!cf) return NEKGPU_ERR_NOMEM;
+    if ((st = scale_coef_pairs(c, dt)) || (st = adjoint_coef64(c, cf, dt))) return st;
+    w.coef64 = cf;
+  } else {
+    if ((st = scale_coef(c, dt))) return st;
+    w.coef64 = c->d_coef;
+  }
   w.init_args();
-  if ((st = scale_coef(c, dt))) return st;
   float f_ms = 0, a_ms = 0;
 
   if (nsets == 0) {
     // ---- binomial schedule -------------------------------------------------------
     Binomial bs{w};
     for (int r = 1; r <= 5; ++r)
-      if (!(bs.SU[r] = mem.get(ns))) return NEKGPU_ERR_NOMEM;
-    for (int r = 0; r <= 5; ++r)
-      if (!(bs.SK[r] = mem.get(ns))) return NEKGPU_ERR_NOMEM;
-    if (!(bs.scratch = mem.get(ns)) || !(bs.final_state = mem.get(ns))) return NEKGPU_ERR_NOMEM;
-    std::vector<double*> slots(nslots);
-    for (auto& p : slots)
-      if (!(p = mem.get(ns))) return NEKGPU_ERR_NOMEM;
+      if (!(bs.SU[r] = mem.get(ns)) || !(bs.SK[r] = mem.get(ns))) return NEKGPU_ERR_NOMEM;
+    bs.SK[0] = bs.SK[5];
+    if (!(bs.scratch = mem.get(ns))) return NEKGPU_ERR_NOMEM;
+    HostSlots hmem;
+    std::vector<Slot> slots(ndev + nhost);
+    for (int q = 0; q < ndev + nhost; ++q) {
+      slots[q].host = q >= ndev;
+      slots[q].p = slots[q].host ? hmem.get(ns) : mem.get(ns);
+      if (!slots[q].p) return NEKGPU_ERR_NOMEM;
+    }
     bs.free_slots.assign(slots.begin() + 1, slots.end());
     if (check_cuda(cudaEventCreate(&bs.ev_seed))) return NEKGPU_ERR_CUDA;
     struct EvGuard {
@@ -450,9 +523,12 @@ extern "C" int nekgpu_adjoint_gradient(nekgpu_ctx* c, int nsteps, double t0, dou
       ~EvGuard() { cudaEventDestroy(e); }
     } guard{bs.ev_seed};
     if (check_cuda(cudaEventRecord(c->ev0, c->stream))) return NEKGPU_ERR_CUDA;
-    if ((st = copy_state(c, slots[0], c->d_u[c->cur]))) return st;
-    if ((st = bs.rev(0, nsteps, slots[0], nslots - 1))) return st;
-    if ((st = copy_state(c, c->d_u[c->cur], bs.final_state))) return st;
+    if ((st = copy_slot(c, slots[0].p, slots[0].host, c->d_u[c->cur], false))) return st;
+    if ((st = bs.rev(0, nsteps, slots[0], ndev + nhost - 1))) return st;
+    // u(T) back into the context (the seed read it to the host)
+    if (check_cuda(cudaMemcpyAsync(c->d_u[c->cur], w.final_host.data(), ns * 8,
+                                   cudaMemcpyHostToDevice, c->stream)))
+      return NEKGPU_ERR_CUDA;
     if (check_cuda(cudaEventRecord(c->ev1, c->stream)) || check_cuda(cudaEventSynchronize(c->ev1)))
       return NEKGPU_ERR_CUDA;
     cudaEventElapsedTime(&f_ms, c->ev0, bs.ev_seed);
@@ -480,7 +556,7 @@ extern "C" int nekgpu_adjoint_gradient(nekgpu_ctx* c, int nsteps, double t0, dou
     for (int n = 0; n < nsteps; ++n) {
       if (n % S == 0 && (st = copy_state(c, ckpt[n / S], c->d_u[c->cur]))) return st;
       for (int r = 1; r <= 5; ++r)
-        if ((st = fused_stage(c, r, w.tstep[n], dt))) return st;
+        if ((st = fwd_stage(c, r, w.tstep[n], dt))) return st;
     }
     if (check_cuda(cudaEventRecord(c->ev1, c->stream)) || check_cuda(cudaEventSynchronize(c->ev1)))
       return NEKGPU_ERR_CUDA;
@@ -496,8 +572,8 @@ extern "C" int nekgpu_adjoint_gradient(nekgpu_ctx* c, int nsteps, double t0, dou
       for (int s2 = 0; s2 < nS && !r; ++s2)
         for (int q = 1; q <= 5 && !r; ++q) {
           const int i = 5 * s2 + q;
-          r = fused_stage_buffers(c, q, w.tstep[n0 + s2], dt, U[b][i - 1], U[b][i], K[b][i - 1],
-                                  K[b][i]);
+          r = fwd_stage_buffers(c, q, w.tstep[n0 + s2], dt, U[b][i - 1], U[b][i], K[b][i - 1],
+                                K[b][i]);
         }
       c->stream = main_stream;
       return r;
@@ -553,9 +629,15 @@ extern "C" int nekgpu_adjoint_gradient(nekgpu_ctx* c, int nsteps, double t0, dou
   return NEKGPU_OK;
 }
 
+extern "C" int nekgpu_adjoint_host_snapshots(nekgpu_ctx* c, int n) {
+  if (!c || n < 0 || n > (1 << 16)) return NEKGPU_ERR_ARG;
+  c->adj_host_snapshots = n;
+  return NEKGPU_OK;
+}
+
 extern "C" int nekgpu_adjoint_init(nekgpu_ctx* c, const double* jw, int stride) {
   if (!c || !jw) return NEKGPU_ERR_ARG;
-  if (c->form != NEKGPU_FUSED64) return NEKGPU_ERR_UNSUPPORTED;
+  if (c->form != NEKGPU_FUSED64 && c->form != NEKGPU_MIXED) return NEKGPU_ERR_UNSUPPORTED;
   c->adj_jw.assign(jw, jw + c->npts);
   c->adj_stride = stride;
   return NEKGPU_OK;

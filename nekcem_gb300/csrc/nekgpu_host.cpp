@@ -1008,6 +1008,7 @@ int upload_fused(Context* c, const Compact& cp) {
     m.nelt = c->nelt;
     m.npts = c->npts;
     m.k = c->d_k;
+    m.k_out = c->d_k;
     m.coef = reinterpret_cast<const float2*>(c->d_coef);
     m.nbr = c->d_nbr;
     m.egm = c->d_egm;
@@ -1028,6 +1029,17 @@ int upload_fused(Context* c, const Compact& cp) {
     std::vector<float> tab;
     split_D(D, c->nx, tab);
     if ((st = mixed_upload_D(c->nx, tab.data(), tab.size()))) return st;
+    // what the FP64 reverse stages of the adjoint read: the element geometry,
+    // D, the GLL weights, C0 and the FP64 face coefficients (host copy)
+    if ((st = A.put(&c->d_egeom, cp.egeom))) return st;
+    FusedDev& f = c->fargs;
+    f = FusedDev{};
+    f.nelt = c->nelt;
+    f.npts = c->npts;
+    f.C0 = cp.C0;
+    for (int i = 0; i < c->nx * c->nx; ++i) f.D[i] = cp.D[i];
+    for (int i = 0; i < c->nx; ++i) f.w[i] = cp.w[i];
+    if (!cp.uniform) c->host_fcoef64 = cp.fcoef;
     return upload_pml_fused(c, A, cp, m.pml);
   }
   if ((st = A.put(&c->d_egeom, cp.egeom))) return st;

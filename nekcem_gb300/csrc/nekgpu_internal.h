@@ -248,7 +248,8 @@ struct MixedDev {
   long npts;
   const double* u_in;
   double* u_out;
-  double* k;
+  double* k;            // RK register read by the stage
+  double* k_out;        // where the stage writes it (k itself, or a stage buffer)
   const float2* coef;   // 2*npts (hi, lo) pairs of dt*hbm1*w3*rx | dt*ebm1*w3*rx
   const int* nbr;       // 6*nelt
   const float* egm;     // 16*nelt: rho_y (hi,lo), rho_z (hi,lo), lift factor per slot (6 hi, 6 lo)
@@ -434,6 +435,10 @@ struct Context {
   double* d_adj_slot = nullptr;
   std::vector<double> adj_jw;  // objective weights set by nekgpu_adjoint_init
   int adj_stride = 0;
+  int adj_host_snapshots = 0;  // pinned host snapshot slots the binomial schedule may add
+  // mixed form: the FP64 face coefficients (4 per face node, as FusedDev::fcoef)
+  // for the adjoint's face-slot table; empty when uniform
+  std::vector<double> host_fcoef64;
 
   // plain form
   PlainDev pargs{};
@@ -486,6 +491,10 @@ int scale_coef(Context* c, double dt);
 
 // nekgpu_mixed.cu
 int mixed_stage(Context* c, int rkstep, double time, double dt);
+// one mixed stage between given buffers (u_in -> u_out, k_in -> k_out), as
+// fused_stage_buffers; the context's own state is untouched
+int mixed_stage_buffers(Context* c, int rkstep, double time, double dt, const double* u_in,
+                        double* u_out, double* k_in, double* k_out);
 // launches a kernel whose bounded mbarrier wait runs out (sets the status word)
 int wait_selftest(Context* c, int polls);
 // one mixed stage over elements [e0, e1) of the current state, writing the
@@ -509,7 +518,10 @@ int stage2d(Context* c, int rkstep, double time, double dt);
 // nekgpu_adjoint.cu
 int adjoint_stage(Context* c, const AdjointDev& a);
 // w = b * coef * ub (the stage weights of the last stage of the last step)
-int adjoint_seed(Context* c, double* w, const double* ub, double b);
+int adjoint_seed(Context* c, double* w, const double* ub, const double* coef, double b);
+// coef = dt hbm1 | dt ebm1 (2 npts), the FP64 inverse-mass scale of the
+// reverse stages, for a context whose own coefficients are float pairs
+int adjoint_coef64(Context* c, double* coef, double dt);
 
 // nekgpu_noalloc.cu: cem_error norms with a fixed device scratch array
 int norms_noalloc(Context* c, const double* exact_dev, double l2[6], double linf[6]);

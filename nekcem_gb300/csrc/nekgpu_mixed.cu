@@ -272,7 +272,7 @@ __device__ __forceinline__ void rk_finish_cf(const MixedDev& a, int c, long g, f
   ee = fmaf(cf.y, Rh, ee);
   const double r = f2d(p) + f2d(ee);
   const double kn = first_stage ? r : fma(a.a, a.k[c * P + g], r);
-  a.k[c * P + g] = kn;
+  a.k_out[c * P + g] = kn;
   a.u_out[c * P + g] = fma(a.b, kn, __ldg(a.u_in + c * P + g));
 }
 __device__ __forceinline__ void rk_finish(const MixedDev& a, int c, long g, float Rh, float Rl,
@@ -1261,6 +1261,38 @@ int mixed_curved_stage(Context* c, int rkstep, double time, double dt) {
   if (st) return st;
   c->cur ^= 1;
   return NEKGPU_OK;
+}
+
+int mixed_stage_buffers(Context* c, int rkstep, double time, double dt, const double* u_in,
+                        double* u_out, double* k_in, double* k_out) {
+  int st = scale_coef_pairs(c, dt);
+  if (st) return st;
+  MixedDev a = c->margs;
+  if (a.pml.slot || a.disp.slot || a.inc_elem || a.gr.elem) return NEKGPU_ERR_UNSUPPORTED;
+  a.e_begin = 0;
+  a.e_end = c->nelt;
+  a.u_in = u_in;
+  a.u_out = u_out;
+  a.k = k_in;
+  a.k_out = k_out;
+  a.a = c->rk_a[rkstep - 1];
+  a.b = c->rk_b[rkstep - 1];
+  a.dt = dt;
+  if (c->src.enabled) {
+    const double ft = source_ft(c->src, time + dt * c->rk_c[rkstep - 1]);
+    const float hi = (float)ft;
+    a.src_ft2 = make_float2(hi, (float)(ft - (double)hi));
+  }
+  switch (c->nx) {
+    case 3: return launch_mixed<3, false>(c, a);
+    case 4: return launch_mixed<4, false>(c, a);
+    case 5: return launch_mixed<5, false>(c, a);
+    case 6: return launch_mixed<6, false>(c, a);
+    case 7: return launch_mixed<7, false>(c, a);
+    case 8: return launch_mixed<8, false>(c, a);
+    case 9: return launch_mixed<9, false>(c, a);
+    default: return NEKGPU_ERR_UNSUPPORTED;
+  }
 }
 
 int mixed_stage(Context* c, int rkstep, double time, double dt) {

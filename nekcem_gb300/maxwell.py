@@ -349,14 +349,21 @@ class MaxwellGPU:
     def check_blowup(self):
         L.check(L.load().nekgpu_check_blowup(self._h), "nekgpu_check_blowup")
 
-    # ---- discrete adjoint (FP64 fused form) ------------------------------------
-    def adjoint_gradient(self, nsteps: int, t0: float, dt: float, jw: np.ndarray, stride: int = 0):
+    # ---- discrete adjoint (fused FP64 and mixed forms) ----------------------------
+    def adjoint_gradient(self, nsteps: int, t0: float, dt: float, jw: np.ndarray, stride: int = 0,
+                         host_snapshots: Optional[int] = None):
         """J = sum_g jw[g] |E(g)|^2 after nsteps steps from the current state and
-        dJ/deps at every node, by the discrete adjoint.  ``stride`` > 0:
-        checkpoints every stride steps; 0: every ceil(sqrt(nsteps)) steps when
-        that fits in device memory, else the binomial schedule; < 0: the
-        binomial schedule with -stride snapshots.  Leaves the final state in
-        the context.  Returns (J, dJdeps, forward_ms, adjoint_ms)."""
+        dJ/deps at every node, by the discrete adjoint (forward steps in the
+        context's form, reverse stages in FP64).  ``stride`` > 0: checkpoints
+        every stride steps; 0: every ceil(sqrt(nsteps)) steps when that fits
+        in device memory, else the binomial schedule; < 0: the binomial
+        schedule with -stride device snapshots.  ``host_snapshots``: pinned
+        host snapshots the binomial schedule may add (kept for later calls).
+        Leaves the final state in the context.  Returns (J, dJdeps,
+        forward_ms, adjoint_ms)."""
+        if host_snapshots is not None:
+            L.check(L.load().nekgpu_adjoint_host_snapshots(self._h, int(host_snapshots)),
+                    "nekgpu_adjoint_host_snapshots")
         jw = np.ascontiguousarray(jw, dtype=np.float64).reshape(self.npts)
         out = np.empty(self.npts)
         J = C.c_double(); fms = C.c_double(); ams = C.c_double()

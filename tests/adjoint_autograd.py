@@ -19,10 +19,12 @@ class BoxProblem:
         self.N, self.nel, self.lo, self.hi, self.bc = N, nel, lo, hi, bc
         self.H0, self.E0, self.jw = H0, E0, jw
         self.nsteps, self.dt, self.t0, self.source, self.stride = nsteps, dt, t0, source, stride
+        self.form = "fused64"       # form of the gradient's forward steps
+        self.host_snapshots = None  # pinned host snapshots for the binomial schedule
         self.last_ms = None
 
-    def context(self, eps: np.ndarray) -> MaxwellGPU:
-        g = MaxwellGPU.from_box(self.N, self.nel, self.lo, self.hi, self.bc, form="fused64",
+    def context(self, eps: np.ndarray, form: str = "fused64") -> MaxwellGPU:
+        g = MaxwellGPU.from_box(self.N, self.nel, self.lo, self.hi, self.bc, form=form,
                                 permittivity=np.ascontiguousarray(eps, dtype=np.float64))
         if self.source:
             g.set_source(**self.source)
@@ -38,8 +40,9 @@ class BoxProblem:
         return float(np.sum(self.jw * (E * E)))
 
     def gradient(self, eps: np.ndarray):
-        g = self.context(eps)
-        J, dJ, fms, ams = g.adjoint_gradient(self.nsteps, self.t0, self.dt, self.jw, self.stride)
+        g = self.context(eps, self.form)
+        J, dJ, fms, ams = g.adjoint_gradient(self.nsteps, self.t0, self.dt, self.jw, self.stride,
+                                             host_snapshots=self.host_snapshots)
         g.close()
         self.last_ms = (fms, ams)
         return J, dJ

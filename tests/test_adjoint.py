@@ -4,7 +4,10 @@ CPU: the torch tape restatement (tests/tape_maxwell.py) matches the oracle's
 time steps, and its tape gradient matches central differences of the oracle.
 GPU: nekgpu_adjoint_gradient matches central differences of the library's
 own FP64 forward (h = 1e-6, 20 seeded directions, 1e-6 relative), the tape
-gradient node by node, and does not depend on the checkpoint stride.
+gradient node by node, and does not depend on the checkpoint stride or on
+where its snapshots live (device or pinned host memory).  With the forward
+steps in the mixed form (reverse stages FP64) it stays within 1e-8 of the
+FP64 gradient and passes the same central-difference check.
 """
 from __future__ import annotations
 
@@ -137,8 +140,61 @@ def test_adjoint_matches_tape_node_by_node():
 
 
 @pytest.mark.gpu
-def test_adjoint_gradient_does_not_depend_on_the_checkpoint_stride():
+@pytest.mark.parametrize("N,nel,bc,nsteps", MESHES)
+def test_mixed_forward_adjoint_matches_fp64_and_central_differences(N, nel, bc, nsteps):
+    """Forward steps in the mixed form, reverse stages in FP64: J within
+    1e-8 and dJ/deps within 1e-8 (of its largest entry) of the all-FP64
+    gradient, and central differences of the FP64 forward (h = 1e-6, 20
+    directions) within 1e-6 relative."""
+    pb, eps, _, _ = gpu_problem(N, nel, bc, seed=21 + N, nsteps=nsteps)
+    J0, g0 = pb.gradient(eps)
+    pb.form = "mixed"
+    J1, g1 = pb.gradient(eps)
+    assert J1 == pytest.approx(J0, rel=1e-8)
+    assert np.abs(g1 - g0).max() <= 1e-8 * np.abs(g0).max()
+    rng = np.random.default_rng(200 + N)
+    h = 1e-6
+    worst = 0.0
+    for _ in range(20):
+        d = rng.standard_normal(eps.size)
+        fd = (pb.objective(eps + h * d) - pb.objective(eps - h * d)) / (2 * h)
+        ad = float(g1 @ d)
+        worst = max(worst, abs(fd - ad) / abs(ad))
+    assert worst <= 1e-6, worst
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("form", ["fused64", "mixed"])
+def test_host_snapshots_give_the_same_gradient(form):
+    """Four binomial snapshots split between device and pinned host memory
+    (4+0, 3+1, 2+2, 1+3): the same schedule, so bit-identical gradients, and
+    the final state left in the context equals a plain forward run's."""
+    pb, eps, _, _ = gpu_problem(4, (2, 2, 2), (PEC, PER, PEC), seed=73, nsteps=13)
+    pb.form = form
+    pb.stride = -4
+    J0, g0 = pb.gradient(eps)
+    for dev, host in ((3, 1), (2, 2), (1, 3)):
+        pb.stride, pb.host_snapshots = -dev, host
+        J1, g1 = pb.gradient(eps)
+        assert J1 == J0
+        np.testing.assert_array_equal(g1, g0, err_msg=f"{dev} device + {host} host")
+    g = pb.context(eps, form)
+    g.adjoint_gradient(pb.nsteps, 0.0, pb.dt, pb.jw, -1, host_snapshots=3)
+    H, E = g.get_state()
+    g.close()
+    g = pb.context(eps, form)
+    g.run(pb.nsteps, 0.0, pb.dt)
+    H2, E2 = g.get_state()
+    g.close()
+    np.testing.assert_array_equal(H, H2)
+    np.testing.assert_array_equal(E, E2)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("form", ["fused64", "mixed"])
+def test_adjoint_gradient_does_not_depend_on_the_checkpoint_stride(form):
     pb, eps, _, _ = gpu_problem(4, (2, 2, 2), (PEC, PEC, PEC), seed=41, nsteps=17)
+    pb.form = form
     grads = []
     for stride in (1, 4, 17, 0):
         pb.stride = stride
@@ -160,7 +216,7 @@ def test_autograd_function_backward_is_the_adjoint():
 
 @pytest.mark.gpu
 def test_adjoint_rejects_other_forms_and_missing_state():
-    g = MaxwellGPU.from_box(3, (2, 2, 2), (0, 0, 0), (1, 1, 1), (PEC,) * 3, form="mixed")
+    g = MaxwellGPU.from_box(3, (2, 2, 2), (0, 0, 0), (1, 1, 1), (PEC,) * 3, form="mixed_naive")
     g.set_state(np.zeros((3, g.npts)), np.zeros((3, g.npts)))
     with pytest.raises(L.NekgpuError) as e:
         g.adjoint_gradient(2, 0.0, 0.01, np.ones(g.npts))
