@@ -64,7 +64,23 @@ def parse():
                    help="steps of the adjoint ratio run (default: the workload's 2000)")
     p.add_argument("--accuracy-steps", type=int, default=0,
                    help="steps of the accuracy runs (default: the configuration's own)")
+    p.add_argument("--adjoint-only", action="store_true",
+                   help="only the adjoint run (large: mixed forward, FP64 reverse, 180 GB)")
     return p.parse_args()
+
+
+def host_snapshot_count(state_bytes, most=24):
+    """Pinned host snapshots for the large gradient: at most half of the
+    host's available memory, and at most `most`."""
+    avail = 0
+    try:
+        with open("/proc/meminfo") as f:
+            for ln in f:
+                if ln.startswith("MemAvailable:"):
+                    avail = int(ln.split()[1]) * 1024
+    except OSError:
+        pass
+    return max(0, min(most, int(0.5 * avail // state_bytes))), avail
 
 
 def measured_peaks():
@@ -301,15 +317,17 @@ def e2e(steps, warmup, dist=None, min_sec=1.0, min_windows=3):
                 d2h=bytes_io, link_h2d_gbs=bytes_io / t_in / 1e9, link_d2h_gbs=bytes_io / t_out / 1e9)
 
 
-def adjoint_ratio(nsteps=0, case="adjoint", budget_mb=None):
+def adjoint_ratio(nsteps=0, case="adjoint", budget_mb=None, form="fused64", host_snapshots=0):
     """Gradient time over forward time.  Default: the adjoint workload (unit
     PEC box, 8^3 elements, N=7, eps = 1 + 3 sigmoid(smooth random field, seed
     4), Gaussian E_z source, 2000 steps, J = sum bm1 |E|^2 over [0.7,0.9]^3).
     case="large": the 64^3-element N=7 box with its own eps, under a device
     memory budget (NEKGPU_MEM_BUDGET_MB) that bounds the context and the
-    gradient together.  Forward: nekgpu_time_steps of the FP64 fused form
-    (CUDA events); gradient: nekgpu_adjoint_gradient, its own CUDA-event
-    times (forward part + reverse sweep, recomputation included)."""
+    gradient together.  Forward: nekgpu_time_steps of the context's form
+    (CUDA events; over at most 50 steps, scaled to nsteps); gradient:
+    nekgpu_adjoint_gradient (forward steps in the context's form, FP64
+    reverse stages), its own CUDA-event times (forward part + reverse sweep,
+    recomputation included), and its wall time."""
     from nekcem_gb300 import MaxwellGPU, cases
     c = cases.make(case)
     old = os.environ.get("NEKGPU_MEM_BUDGET_MB")
@@ -317,7 +335,7 @@ def adjoint_ratio(nsteps=0, case="adjoint", budget_mb=None):
         os.environ["NEKGPU_MEM_BUDGET_MB"] = str(int(budget_mb))
     try:
         eps = case_eps(c)
-        g = MaxwellGPU.from_box(c.N, c.nel, c.lo, c.hi, c.bc, form="fused64", permittivity=eps)
+        g = MaxwellGPU.from_box(c.N, c.nel, c.lo, c.hi, c.bc, form=form, permittivity=eps)
         x, y, z = g.coords()
         bm1 = g.array("bmn")
         if c.source:
@@ -333,9 +351,14 @@ def adjoint_ratio(nsteps=0, case="adjoint", budget_mb=None):
         g.set_state(H0, E0)
         g.time_steps(3, 0.0, dt)  # warm-up
         g.set_state(H0, E0)
-        _, fwd_ms = g.time_steps(n, 0.0, dt)
+        nf = min(n, 50)
+        _, fwd_ms = g.time_steps(nf, 0.0, dt)
+        fwd_ms *= n / nf
         g.set_state(H0, E0)
-        J, dJ, fwd_part_ms, rev_ms = g.adjoint_gradient(n, 0.0, dt, jw)
+        t_wall = time.perf_counter()
+        J, dJ, fwd_part_ms, rev_ms = g.adjoint_gradient(n, 0.0, dt, jw,
+                                                        host_snapshots=host_snapshots)
+        t_wall = time.perf_counter() - t_wall
         g.close()
     finally:
         if budget_mb:
@@ -347,7 +370,9 @@ def adjoint_ratio(nsteps=0, case="adjoint", budget_mb=None):
            "steps": n, "forward_ms": fwd_ms, "gradient_ms": fwd_part_ms + rev_ms,
            "gradient_forward_part_ms": fwd_part_ms, "reverse_sweep_ms": rev_ms,
            "ratio": (fwd_part_ms + rev_ms) / fwd_ms, "J": J,
-           "grad_norm": float(np.linalg.norm(dJ))}
+           "grad_norm": float(np.linalg.norm(dJ)), "forward_form": form,
+           "forward_timing": f"{nf} steps, scaled to {n}", "gradient_wall_s": t_wall,
+           "host_snapshots": host_snapshots}
     if budget_mb:
         out["device_memory_budget_bytes"] = int(budget_mb) << 20
     return out
@@ -424,6 +449,19 @@ def main():
         return
     import nekcem_gb300
     nekcem_gb300.load()
+    if args.adjoint_only:
+        if CASE == "large":
+            # 180 GB (171,661 MiB) of device memory for the context and the
+            # gradient together; mixed forward steps, FP64 reverse stages,
+            # binomial snapshots on the device and in pinned host memory
+            nh, avail = host_snapshot_count(6 * 8 * 64 ** 3 * 8 ** 3)
+            out = adjoint_ratio(args.adjoint_steps or 1000, case="large", budget_mb=171661,
+                                form="mixed", host_snapshots=nh)
+            out["host_mem_available_bytes"] = avail
+        else:
+            out = adjoint_ratio(args.adjoint_steps)
+        print(json.dumps({"adjoint": out}), flush=True)
+        return
     dist, rank, world = dist_setup(args.gpus)
     device = int(os.environ.get("LOCAL_RANK", 0))
     peak, peak_kind = measured_peaks()
