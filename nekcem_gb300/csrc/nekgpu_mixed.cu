@@ -80,6 +80,25 @@ __device__ __forceinline__ double f2d(float f) {
   return __hiloint2double((int)(mag ? hi : b), (int)(b << 29));
 }
 
+// s + t as an FP64 value for a non-overlapping float pair (|t| <= ulp(s)/2, a
+// two-sum output), by integer operations: t, in units of the FP64 ulp of s,
+// is below 2^29 and lands in the 29 low mantissa bits that s leaves zero
+// (added, or subtracted with a borrow from s's last float bit; in units of
+// the lower binade when s is a power of two and t takes it below).  Exact
+// whenever s + t fits in 53 bits, else t's bits below them are truncated
+// (under one FP64 ulp).  Zero or subnormal t, or subnormal s: f2d(s).
+__device__ __forceinline__ double pair_to_double(float s, float t) {
+  const unsigned bs = __float_as_uint(s), bt = __float_as_uint(t);
+  const int es = (int)((bs >> 23) & 0xFFu), et = (int)((bt >> 23) & 0xFFu);
+  const unsigned opp = (bs ^ bt) >> 31;
+  const int sh = et - es + 29 + (int)(opp & ((bs & 0x7FFFFFu) == 0u ? 1u : 0u));
+  unsigned mt = (bt & 0x7FFFFFu) | 0x800000u;
+  mt = (et != 0 && es != 0) ? mt : 0u;
+  const unsigned x = sh >= 0 ? (mt << sh) : (mt >> min(-sh, 31));
+  const long long xs = opp ? -(long long)x : (long long)x;
+  return __longlong_as_double(__double_as_longlong(f2d(s)) + xs);
+}
+
 // Knuth two-sum: s + e == a + b exactly
 __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
   s = a + b;
@@ -215,6 +234,9 @@ struct MCfg {
   // the in-line finish measured 5 % slower at NX = 8 and 16 % slower at
   // NX = 9, 20 % faster at NX = 6).
   static constexpr bool kFin = !kSwz && NX != 9;
+  // r = p + ee without an FP64 add (rk_finish_cf) where that measured faster:
+  // N=7 -1.8 %, N=6 -1.9 %, N=4 -0.9 % per step; N=8 unchanged; N=5 +5.4 %
+  static constexpr bool kIntAdd = NX == 5 || NX == 7 || NX == 8;
   // Two areas of SA bytes swap roles from one element to the next.  One holds,
   // in turn, the staged FP64 state (until the split), the partner face values
   // parked for the flux (FP64) and the residual pairs (hi, lo); the other the
@@ -263,6 +285,10 @@ __device__ __forceinline__ int pnode(int v) {  // stored index of node v = i + N
 // read again from global memory (an L2 hit: the element's block was copied in
 // at the start of its turn), the RK register and the coefficients were
 // prefetched into L2 with that copy.
+// IA: r = p + ee formed by a two-sum and pair_to_double (integer and FP32
+// operations) instead of an FP64 add: two FP64 operations per component
+// instead of three, for the orders whose finish the FP64 pipe limits.
+template <bool IA>
 __device__ __forceinline__ void rk_finish_cf(const MixedDev& a, int c, long g, float Rh, float Rl,
                                              float2 cf, bool first_stage) {
   const long P = a.npts;
@@ -270,14 +296,22 @@ __device__ __forceinline__ void rk_finish_cf(const MixedDev& a, int c, long g, f
   float ee = fmaf(cf.x, Rh, -p);
   ee = fmaf(cf.x, Rl, ee);
   ee = fmaf(cf.y, Rh, ee);
-  const double r = f2d(p) + f2d(ee);
+  double r;
+  if constexpr (IA) {
+    float s, t;
+    two_sum(p, ee, s, t);
+    r = pair_to_double(s, t);
+  } else {
+    r = f2d(p) + f2d(ee);
+  }
   const double kn = first_stage ? r : fma(a.a, a.k[c * P + g], r);
   a.k_out[c * P + g] = kn;
   a.u_out[c * P + g] = fma(a.b, kn, __ldg(a.u_in + c * P + g));
 }
+template <bool IA>
 __device__ __forceinline__ void rk_finish(const MixedDev& a, int c, long g, float Rh, float Rl,
                                           bool first_stage) {
-  rk_finish_cf(a, c, g, Rh, Rl, a.coef[(c < 3 ? 0 : a.npts) + g], first_stage);
+  rk_finish_cf<IA>(a, c, g, Rh, Rl, a.coef[(c < 3 ? 0 : a.npts) + g], first_stage);
 }
 
 // c1*J1 + c2*J2 times the lift factor lf, all float pairs, as a float pair.
@@ -417,7 +451,7 @@ __device__ __forceinline__ void line_phase(const float2* s_u2, float2* s_R2, con
           two_sum(old.x, h, sum, err);
           const int vol = DIR == 0 ? i + NX * la + C::N2 * lb
                                    : (DIR == 1 ? la + NX * i + C::N2 * lb : la + NX * lb + C::N2 * i);
-          rk_finish(a, rt, (long)e * C::N3 + vol, sum, (old.y + r) + err, first_stage);
+          rk_finish<C::kIntAdd>(a, rt, (long)e * C::N3 + vol, sum, (old.y + r) + err, first_stage);
         } else if (init) {
           *Rp = make_float2(h, r);
         } else {
@@ -825,7 +859,7 @@ __global__ void __launch_bounds__(MCfg<NX>::NT, mixed_min_blocks<NX, EXT>())
           const float2 rr = s_R2[c * N3P + pnode<NX>(v)];
           float Rh = rr.x, Rl = rr.y;
           if (c == 5 && so >= 0) add_pair_product(Rh, Rl, a.src_w[(long)so * N3 + v], a.src_ft2);
-          rk_finish(a, c, (long)e * N3 + v, Rh, Rl, first_stage);
+          rk_finish<C::kIntAdd>(a, c, (long)e * N3 + v, Rh, Rl, first_stage);
         }
       }
       __syncthreads();  // the split pairs are consumed: the next element may land
@@ -868,7 +902,8 @@ __global__ void __launch_bounds__(MCfg<NX>::NT, mixed_min_blocks<NX, EXT>())
         const long g = (long)e * N3 + v;
         const float2 cfH = a.coef[g], cfE = a.coef[P + g];
 #pragma unroll
-        for (int c = 0; c < 6; ++c) rk_finish_cf(a, c, g, Rh[c], Rl[c], c < 3 ? cfH : cfE, first_stage);
+        for (int c = 0; c < 6; ++c)
+          rk_finish_cf<C::kIntAdd>(a, c, g, Rh[c], Rl[c], c < 3 ? cfH : cfE, first_stage);
       }
     }
   }
