@@ -224,7 +224,15 @@ struct DevAlloc {
   }
 };
 
+void drop_step_graphs(Context* c) {
+  for (auto& g : c->step_graphs)
+    if (g.exec) cudaGraphExecDestroy(g.exec);
+  c->step_graphs.clear();
+}
+
 void free_all(Context* c) {
+  drop_step_graphs(c);
+  if (c->h_status) cudaFreeHost(c->h_status), c->h_status = nullptr;
   for (void* p : c->allocs) cudaFree(p);
   c->allocs.clear();
   c->alloc_bytes.clear();
@@ -790,6 +798,8 @@ int upload_common(Context* c, DevAlloc& A, const std::vector<double>& bm1,
   if ((st = A.put(&c->d_hbm1, hbm1))) return st;
   if ((st = A.get(&c->d_red, 512 * 12))) return st;
   if ((st = A.get(&c->d_status, 4))) return st;
+  if (check_cuda(cudaHostAlloc(&c->h_status, sizeof(int), cudaHostAllocDefault)))
+    return NEKGPU_ERR_CUDA;
   if (check_cuda(cudaMemset(c->d_k, 0, 6 * c->npts * sizeof(double)))) return NEKGPU_ERR_CUDA;
   if (check_cuda(cudaMemset(c->d_status, 0, 4 * sizeof(int)))) return NEKGPU_ERR_CUDA;
   double vol = 0;
@@ -1188,10 +1198,20 @@ bool valid_form(int form) {
 }
 
 int sync_status(Context* c) {
-  if (check_cuda(cudaStreamSynchronize(c->stream))) return NEKGPU_ERR_CUDA;
-  int h = 0;
-  if (check_cuda(cudaMemcpy(&h, c->d_status, sizeof(int), cudaMemcpyDeviceToHost))) return NEKGPU_ERR_CUDA;
-  return h ? NEKGPU_ERR_TIMEOUT : NEKGPU_OK;
+  if (!c->h_status) {  // (a context without the page-locked word)
+    if (check_cuda(cudaStreamSynchronize(c->stream))) return NEKGPU_ERR_CUDA;
+    int h = 0;
+    if (check_cuda(cudaMemcpy(&h, c->d_status, sizeof(int), cudaMemcpyDeviceToHost)))
+      return NEKGPU_ERR_CUDA;
+    return h ? NEKGPU_ERR_TIMEOUT : NEKGPU_OK;
+  }
+  // the status word follows the stream's work into page-locked memory: one
+  // synchronisation, no separate copy call
+  if (check_cuda(cudaMemcpyAsync(c->h_status, c->d_status, sizeof(int), cudaMemcpyDeviceToHost,
+                                 c->stream)) ||
+      check_cuda(cudaStreamSynchronize(c->stream)))
+    return NEKGPU_ERR_CUDA;
+  return *c->h_status ? NEKGPU_ERR_TIMEOUT : NEKGPU_OK;
 }
 
 double* state(Context* c) { return c->d_u[c->cur]; }
@@ -1390,6 +1410,72 @@ int chunked_step(Context* c, double* hn, double* en, long ld, double time, doubl
   if (check_cuda(cudaEventRecord(c->chunk_fence[1], c->copy_out_stream)) ||
       check_cuda(cudaStreamWaitEvent(c->stream, c->chunk_fence[1], 0)))
     return NEKGPU_ERR_CUDA;
+  return NEKGPU_OK;
+}
+
+bool pinned_host(const void* p) {
+  cudaPointerAttributes a{};
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeHost;
+}
+
+// The wavefront step through a CUDA graph: captured on the first call with a
+// given key (host arrays, state parity, dt, stage arguments) and replayed
+// with one launch afterwards, so the ~80 kernels, 64 copies and their
+// event dependencies cost one enqueue instead of several hundred.  Only for
+// page-locked host arrays (a capture cannot hold pageable copies) and steps
+// whose kernels take no time-dependent argument (no volume source); else,
+// or when the capture fails, the step is enqueued directly.
+int chunked_step_graph(Context* c, double* hn, double* en, long ld, double time, double dt) {
+  if (c->src.enabled || !pinned_host(hn) || !pinned_host(en))
+    return chunked_step(c, hn, en, ld, time, dt);
+  int st = scale_coef_pairs(c, dt);  // outside the capture: the graph reads the scaled pairs
+  if (st) return st;
+  const int cur0 = c->cur;
+  Context::StepGraph* hit = nullptr;
+  for (auto& g : c->step_graphs)
+    if (g.hn == hn && g.en == en && g.ld == ld && g.cur == cur0 && g.dt == dt &&
+        std::memcmp(g.margs, &c->margs, sizeof(MixedDev)) == 0)
+      hit = &g;
+  if (!hit) {
+    Context::StepGraph g{};
+    g.hn = hn;
+    g.en = en;
+    g.ld = ld;
+    g.cur = cur0;
+    g.dt = dt;
+    std::memcpy(g.margs, &c->margs, sizeof(MixedDev));
+    const long l0 = c->last_launches;
+    if (cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeRelaxed) != cudaSuccess) {
+      cudaGetLastError();
+      return chunked_step(c, hn, en, ld, time, dt);
+    }
+    st = chunked_step(c, hn, en, ld, time, dt);
+    cudaGraph_t graph = nullptr;
+    const cudaError_t ec = cudaStreamEndCapture(c->stream, &graph);
+    c->cur = cur0;  // nothing ran
+    g.launches = c->last_launches - l0;
+    c->last_launches = l0;
+    cudaError_t ei = cudaErrorUnknown;
+    if (!st && ec == cudaSuccess && graph) ei = cudaGraphInstantiate(&g.exec, graph, 0);
+    if (graph) cudaGraphDestroy(graph);
+    if (st || ec != cudaSuccess || ei != cudaSuccess) {
+      cudaGetLastError();
+      return chunked_step(c, hn, en, ld, time, dt);
+    }
+    if (c->step_graphs.size() >= 4) {  // (two parities x two array sets)
+      cudaGraphExecDestroy(c->step_graphs.front().exec);
+      c->step_graphs.erase(c->step_graphs.begin());
+    }
+    c->step_graphs.push_back(g);
+    hit = &c->step_graphs.back();
+  }
+  if (check_cuda(cudaGraphLaunch(hit->exec, c->stream))) return NEKGPU_ERR_CUDA;
+  c->last_launches += hit->launches;
+  c->cur = cur0 ^ 1;
   return NEKGPU_OK;
 }
 
@@ -2319,6 +2405,7 @@ int nekgpu_register_host(nekgpu_ctx* c, void* ptr, long bytes) {
 
 int nekgpu_unregister_host(nekgpu_ctx* c, void* ptr) {
   if (!c || !ptr) return NEKGPU_ERR_ARG;
+  drop_step_graphs(c);  // their copies may read this memory
   return check_cuda(cudaHostUnregister(ptr));
 }
 
@@ -2341,7 +2428,7 @@ int nekgpu_op_rk_host(nekgpu_ctx* c, double* hn, double* en, long ld, double tim
   c->last_launches = 0;
   int st = NEKGPU_OK;
   if (chunked_step_applies(c)) {
-    if ((st = chunked_step(c, hn, en, ld, time, dt))) return st;
+    if ((st = chunked_step_graph(c, hn, en, ld, time, dt))) return st;
     c->have_state = true;
     return sync_status(c);
   }

@@ -365,6 +365,21 @@ struct Context {
   std::vector<std::vector<int>> chunk_adj;   // per chunk: itself and the chunks of its face partners
   std::vector<int> chunk_in_order;           // order of the copies in
   std::vector<std::pair<int, int>> chunk_launch;  // (stage, chunk) launch order
+  // the wavefront step captured as a CUDA graph (pinned host arrays, no
+  // time-dependent source), replayed with one launch; keyed by what the
+  // captured copies and kernels read: the host arrays, the state parity, dt
+  // and the stage arguments (byte copy of margs)
+  struct StepGraph {
+    double* hn;
+    double* en;
+    long ld;
+    int cur;
+    double dt;
+    unsigned char margs[sizeof(MixedDev)];
+    cudaGraphExec_t exec;
+    long launches;  // kernels in the graph
+  };
+  std::vector<StepGraph> step_graphs;
 
   // device memory
   double* d_u[2] = {nullptr, nullptr};  // state (plain uses d_u[0] only)
@@ -374,6 +389,7 @@ struct Context {
   double* d_eps_mu = nullptr;  // 2*npts: eps (=1/(ebm1*bm1)), mu
   double* d_red = nullptr;     // reduction scratch
   int* d_status = nullptr;
+  int* h_status = nullptr;  // page-locked copy of d_status[0], read after each sync
   std::vector<void*> allocs;
   std::vector<size_t> alloc_bytes;  // size of each entry of allocs
   size_t dev_bytes = 0;  // device bytes held in allocs

@@ -373,6 +373,46 @@ def test_op_rk_host_chunked_equals_device_steps(bc):
     g1.close(); g2.close()
 
 
+@pytest.mark.parametrize("bc", [(1, 1, 1), (1, 0, 1)], ids=["periodic", "mixed_bc"])
+def test_op_rk_host_graph_equals_device_steps(bc):
+    """Page-locked host arrays and no time-dependent source: the wavefront
+    step is captured once per state parity as a CUDA graph and replayed.
+    Six steps (two captures, four replays) are bit-identical to device
+    steps and report the graph's kernels; after the arrays are unregistered
+    the step is enqueued directly and still agrees."""
+    from nekcem_gb300 import MaxwellGPU
+    nel, lo, hi = (16, 12, 12), (0.0, 0.0, 0.0), (1.0, 1.0, 1.0)
+    g1 = MaxwellGPU.from_box(7, nel, lo, hi, bc, form="mixed")
+    g2 = MaxwellGPU.from_box(7, nel, lo, hi, bc, form="mixed")
+    x, y, z = g1.coords()
+    k = 2 * np.pi
+    H = np.stack([np.sin(k * y) * np.cos(k * z), np.cos(k * x) * np.sin(k * z), 0.3 * np.sin(k * x)])
+    E = np.stack([np.cos(k * y), np.sin(k * z) * np.cos(k * x), np.sin(k * x) * np.sin(k * y)])
+    dt = 0.002
+    g1.set_state(H, E)
+    Hh, Eh = np.ascontiguousarray(H.copy()), np.ascontiguousarray(E.copy())
+    g2.register_host(Hh); g2.register_host(Eh)
+    t, launches = 0.0, []
+    for _ in range(6):
+        g2.op_rk_host(Hh, Eh, t, dt)
+        launches.append(g2.last_launches())
+        t += dt
+    g1.run(6, 0.0, dt)
+    a_H, a_E = g1.get_state()
+    np.testing.assert_array_equal(a_H, Hh)
+    np.testing.assert_array_equal(a_E, Eh)
+    # the first call also scales the inverse-mass pairs for dt (one kernel)
+    assert launches[0] - launches[1] in (0, 1), launches
+    assert all(n == launches[1] and n >= 20 for n in launches[1:]), launches
+    g2.unregister_host(Hh); g2.unregister_host(Eh)
+    g2.op_rk_host(Hh, Eh, t, dt)
+    g1.run(1, t, dt)
+    a_H, a_E = g1.get_state()
+    np.testing.assert_array_equal(a_H, Hh)
+    np.testing.assert_array_equal(a_E, Eh)
+    g1.close(); g2.close()
+
+
 @pytest.mark.parametrize("form", ["fused64", "mixed"])
 def test_deterministic(form):
     ref = ref_for("periodic_n8", materials=True)
@@ -409,16 +449,25 @@ def test_state_leading_dimension():
     g.close(); ref.close()
 
 
-def test_fused_rejects_non_affine_mesh():
-    """A curvilinear (non-affine) mesh is refused by the fused forms with
+def test_fused_forms_take_curvilinear_meshes_and_refuse_other_face_numbering():
+    """A non-affine mesh runs in the fused forms through their curvilinear
+    kernels; a face numbering other than the reference's (two cemface
+    entries of one face swapped) is refused by the fused forms with
     NEKGPU_ERR_MESH and accepted by the plain form."""
     from tests.helpers import oracle_arrays
     ref = ref_for("pec_n5")
     arr = oracle_arrays(ref)
     arr["rxmn"] = arr["rxmn"] * (1.0 + 0.01 * np.sin(np.arange(ref.npts)))
-    with pytest.raises(NekgpuError) as ei:
-        MaxwellGPU.from_arrays(arr, ref.n, ref.nelt, form="mixed")
-    assert ei.value.status == -2
+    for form in ("mixed", "fused64"):
+        MaxwellGPU.from_arrays(arr, ref.n, ref.nelt, form=form).close()
+    arr = oracle_arrays(ref)
+    cf = arr["cemface"].copy()
+    cf[[0, 1]] = cf[[1, 0]]
+    arr["cemface"] = cf
+    for form in ("mixed", "fused64"):
+        with pytest.raises(NekgpuError) as ei:
+            MaxwellGPU.from_arrays(arr, ref.n, ref.nelt, form=form)
+        assert ei.value.status == -2
     g = MaxwellGPU.from_arrays(arr, ref.n, ref.nelt, form="plain")
     g.close(); ref.close()
 
