@@ -153,6 +153,13 @@ __device__ __forceinline__ void tma_load_1d(void* dst, const void* src, unsigned
 }
 // bulk prefetch of a global range into L2 (a hint: no completion to wait for);
 // address and size multiples of 16 bytes
+// 8-byte asynchronous global -> shared copies (element blocks whose size is
+// not a multiple of 16 bytes, where a bulk copy cannot start on every element)
+__device__ __forceinline__ void cp_async8(void* dst, const void* src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(smem_addr(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 __device__ __forceinline__ void prefetch_l2(const void* src, unsigned bytes) {
   asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(src), "r"(bytes) : "memory");
 }
@@ -226,6 +233,10 @@ struct MCfg {
   static constexpr int FPT = (NF + NT - 1) / NT;
   static constexpr int TPT = (NTASK + NT - 1) / NT;
   static constexpr bool kTma = (N3 % 2) == 0;
+  // odd node counts: the next element staged by per-thread 8-byte async
+  // copies where that measured faster (N=8 +3 %, N=6 +0.9 %; N=4, N=2 load
+  // synchronously: -0.5 %, -1.8 % with the async copies)
+  static constexpr bool kAsync = !kTma && NX >= 7;
   // Where the components finish (inverse mass, RK update) without the
   // extension terms: true = the t-line tasks finish H1, H2, E1, E2 on their
   // lines and H3, E3 (no t-derivative) finish beside them, with no barrier and
@@ -599,9 +610,22 @@ __global__ void __launch_bounds__(MCfg<NX>::NT, mixed_min_blocks<NX, EXT>())
     // and the face impedance coefficients the flux reads (float4 per face node)
     if (a.fcoef) prefetch_l2(reinterpret_cast<const float4*>(a.fcoef) + 2L * e * NF, NF * 32u);
   };
+  // the same with every thread copying its own nodes (odd node counts)
+  auto issue_async = [&](int e, int into, int t) {
+    double* dst = reinterpret_cast<double*>(smem + into * C::SA);
+#pragma unroll
+    for (int q = 0; q < NPT; ++q) {
+      const int v = t + q * NT;
+      if (v < N3)
+#pragma unroll
+        for (int c = 0; c < 6; ++c) cp_async8(dst + c * N3 + v, a.u_in + c * P + (long)e * N3 + v);
+    }
+    cp_async_commit();
+  };
   unsigned parity = 0;
   int buf = 0;  // area of the element's staged state and residual pairs
   if (C::kTma && tid == 0 && a.e_begin + (int)blockIdx.x < a.e_end) issue_tma(a.e_begin + blockIdx.x, 0);
+  if (C::kAsync && a.e_begin + (int)blockIdx.x < a.e_end) issue_async(a.e_begin + blockIdx.x, 0, tid);
 
   for (int e = a.e_begin + blockIdx.x; e < a.e_end; e += gridDim.x, buf ^= 1) {
     int tid = opaque_tid();
@@ -634,6 +658,8 @@ __global__ void __launch_bounds__(MCfg<NX>::NT, mixed_min_blocks<NX, EXT>())
     if (C::kTma) {
       if (!mbar_wait_bounded(bar, parity, a.status)) s_abort = 1;
       parity ^= 1u;
+    } else if (C::kAsync) {
+      cp_async_wait_all();  // this thread's copies; the barrier below: everyone's
     } else {
 #pragma unroll
       for (int q = 0; q < NPT; ++q) {
@@ -867,6 +893,7 @@ __global__ void __launch_bounds__(MCfg<NX>::NT, mixed_min_blocks<NX, EXT>())
         fence_proxy_async_smem();
         issue_tma(en, buf ^ 1);
       }
+      if (C::kAsync && en < a.e_end) issue_async(en, buf ^ 1, tid);
     } else {
       tid = opaque_tid();
       __syncthreads();
@@ -877,6 +904,7 @@ __global__ void __launch_bounds__(MCfg<NX>::NT, mixed_min_blocks<NX, EXT>())
         fence_proxy_async_smem();
         issue_tma(en, buf ^ 1);
       }
+      if (C::kAsync && en < a.e_end) issue_async(en, buf ^ 1, tid);
       // ---- source, inverse mass, RK update ----------------------------------------
       // All six components of a node at once (the PML and dispersive terms
       // couple them to the node's auxiliary fields).
