@@ -21,9 +21,15 @@
 // projected out).  Every element gathers what lands on its own nodes, reading
 // the partner elements' face nodes, so all writes are element-local: no
 // atomics, and the adjoint state ping-pongs like the forward state.
+// The D^T contractions run in double-float FP32 arithmetic (D w and the
+// stage weights as (hi, lo) float pairs, products with their FMA error
+// terms, two-sum accumulation: ~2^-47 of the sum of the magnitudes, near
+// FP64's 2^-53) and join the FP64 arithmetic as one FP64 value each; the rest
+// is FP64.  The contractions were 96 of the ~166 FP64 operations per node.
 #include <cuda_runtime.h>
 
 #include "nekgpu_internal.h"
+#include "nekgpu_pair.cuh"
 
 namespace nekgpu {
 
@@ -49,8 +55,10 @@ struct ACfg {
   static constexpr int N2 = NX * NX, N3 = N2 * NX, NF = 6 * N2;
   static constexpr int NT = ((N3 + 31) / 32) * 32;
   static constexpr int FPT = (NF + NT - 1) / NT;
-  // shared: w (6*N3), D w (NX*NX), face results (5*NF)
-  static constexpr size_t smem = (6 * N3 + NX * NX + 5 * NF) * sizeof(double);
+  // shared: w (6*N3), D w (NX*NX), face results (5*NF) in FP64; w and D w
+  // as float pairs (6*N3 + NX*NX)
+  static constexpr size_t smem = (6 * N3 + NX * NX + 5 * NF) * sizeof(double) +
+                                 (6 * N3 + NX * NX) * sizeof(float2);
 };
 
 template <int NX>
@@ -62,11 +70,16 @@ __global__ void __launch_bounds__(ACfg<NX>::NT) k_adjoint_stage(const AdjointDev
   double* s_D = s_w + 6 * N3;       // D(m,i) w_m at [m + NX*i]
   double* s_fu = s_D + NX * NX;     // [4][NF]  tangential face contributions to ub
   double* s_fe = s_fu + 4 * NF;     // [NF]     face contributions to deps
+  float2* s_wp = reinterpret_cast<float2*>(s_fe + NF);  // [6][N3] w as (hi, lo)
+  float2* s_Dp = s_wp + 6 * N3;                          // D w as (hi, lo)
   const int tid = threadIdx.x;
   const long P = a.npts, PF = (long)a.nelt * NF;
   const bool node = tid < N3;
   const int vi = tid % NX, vj = (tid / NX) % NX, vk = tid / N2;
-  for (int t = tid; t < NX * NX; t += NT) s_D[t] = a.Dw[t];
+  for (int t = tid; t < NX * NX; t += NT) {
+    s_D[t] = a.Dw[t];
+    s_Dp[t] = make_float2(d2f_hi(a.Dw[t]), d2f_lo(a.Dw[t]));
+  }
   const double wi = a.w[vi], wj = a.w[vj], wk = a.w[vk];
 
   for (int e = blockIdx.x; e < a.nelt; e += gridDim.x) {
@@ -79,6 +92,7 @@ __global__ void __launch_bounds__(ACfg<NX>::NT) k_adjoint_stage(const AdjointDev
         ub[c] = a.ub_in[c * P + g];
         wn[c] = a.w_in[c * P + g];
         s_w[c * N3 + tid] = wn[c];
+        s_wp[c * N3 + tid] = make_float2(d2f_hi(wn[c]), d2f_lo(wn[c]));
       }
 #pragma unroll
       for (int c = 3; c < 6; ++c) {
@@ -146,27 +160,29 @@ __global__ void __launch_bounds__(ACfg<NX>::NT) k_adjoint_stage(const AdjointDev
     // ---- transposed weighted curl: D^T contractions of w3 w ------------------
     const double* eg = a.egeom + 9 * e;
     const double Rr = eg[0] * wj * wk, Ss = eg[1] * wi * wk, Tt = eg[2] * wi * wj;
-    auto dtr = [&](int c) {  // sum_m D(m,i) w_m w(m,j,k)
-      const double* z = s_w + c * N3 + NX * vj + N2 * vk;
-      double s = s_D[NX * vi] * z[0];
+    // sum_m D(m,row) w_m z_m over one line of the stage weights, double-float
+    auto dot = [&](const float2* z, int zs, int row) -> double {
+      float S = 0.0f, E = 0.0f;
 #pragma unroll
-      for (int m = 1; m < NX; ++m) s = fma(s_D[m + NX * vi], z[m], s);
-      return s;
+      for (int m = 0; m < NX; ++m) {
+        const float2 d = s_Dp[m + NX * row];
+        const float2 x = z[zs * m];
+        const float p = d.x * x.x;
+        float e = fmaf(d.x, x.x, -p);
+        e = fmaf(d.x, x.y, e);
+        e = fmaf(d.y, x.x, e);
+        float s, t;
+        two_sum(S, p, s, t);
+        S = s;
+        E += e + t;
+      }
+      float s, t;
+      two_sum(S, E, s, t);
+      return pair_to_double(s, t);
     };
-    auto dts = [&](int c) {
-      const double* z = s_w + c * N3 + vi + N2 * vk;
-      double s = s_D[NX * vj] * z[0];
-#pragma unroll
-      for (int m = 1; m < NX; ++m) s = fma(s_D[m + NX * vj], z[NX * m], s);
-      return s;
-    };
-    auto dtt = [&](int c) {
-      const double* z = s_w + c * N3 + vi + NX * vj;
-      double s = s_D[NX * vk] * z[0];
-#pragma unroll
-      for (int m = 1; m < NX; ++m) s = fma(s_D[m + NX * vk], z[N2 * m], s);
-      return s;
-    };
+    auto dtr = [&](int c) { return dot(s_wp + c * N3 + NX * vj + N2 * vk, 1, vi); };
+    auto dts = [&](int c) { return dot(s_wp + c * N3 + vi + N2 * vk, NX, vj); };
+    auto dtt = [&](int c) { return dot(s_wp + c * N3 + vi + NX * vj, N2, vk); };
     double out[6];
     out[0] = fma(Tt, dtt(4), fma(-Ss, dts(5), ub[0]));
     out[1] = fma(Rr, dtr(5), fma(-Tt, dtt(3), ub[1]));
