@@ -373,13 +373,17 @@ struct Binomial {
   double* SK[6];  // RK registers; SK[0], read (never used) by stage 1, aliases SK[5]
   double* scratch;  // device: a recomputed step start, or a host snapshot brought in
   cudaEvent_t ev_seed = nullptr;
+  // the slot whose state the working buffer d_u[cur] holds (the snapshot an
+  // advance just wrote): a later read of that slot skips its copy back
+  const double* resident = nullptr;
 
   int advance(Slot src, int j0, int k, Slot dst) {
     Context* c = w.c;
-    int st = copy_slot(c, c->d_u[c->cur], false, src.p, src.host);
+    int st = resident == src.p ? NEKGPU_OK : copy_slot(c, c->d_u[c->cur], false, src.p, src.host);
     for (int j = j0; j < j0 + k && !st; ++j)
       for (int r = 1; r <= 5 && !st; ++r) st = fwd_stage(c, r, w.tstep[j], w.dt);
     if (!st) st = copy_slot(c, dst.p, dst.host, c->d_u[c->cur], false);
+    resident = st ? nullptr : dst.p;
     return st;
   }
 
@@ -388,8 +392,12 @@ struct Binomial {
     int st = NEKGPU_OK;
     SU[0] = src.p;
     if (src.host) {
-      if ((st = copy_slot(c, scratch, false, src.p, true))) return st;
-      SU[0] = scratch;
+      if (resident == src.p) {  // the stages read the working buffer; it stays as it is
+        SU[0] = c->d_u[c->cur];
+      } else {
+        if ((st = copy_slot(c, scratch, false, src.p, true))) return st;
+        SU[0] = scratch;
+      }
     }
     for (int r = 1; r <= 5 && !st; ++r)
       st = fwd_stage_buffers(c, r, w.tstep[j], w.dt, SU[r - 1], SU[r], SK[r - 1], SK[r]);
@@ -524,6 +532,7 @@ extern "C" int nekgpu_adjoint_gradient(nekgpu_ctx* c, int nsteps, double t0, dou
     } guard{bs.ev_seed};
     if (check_cuda(cudaEventRecord(c->ev0, c->stream))) return NEKGPU_ERR_CUDA;
     if ((st = copy_slot(c, slots[0].p, slots[0].host, c->d_u[c->cur], false))) return st;
+    bs.resident = slots[0].p;
     if ((st = bs.rev(0, nsteps, slots[0], ndev + nhost - 1))) return st;
     // u(T) back into the context (the seed read it to the host)
     if (check_cuda(cudaMemcpyAsync(c->d_u[c->cur], w.final_host.data(), ns * 8,
