@@ -261,6 +261,41 @@ __device__ __forceinline__ void rk_finish_cf(const MixedDev& a, int c, long g, f
   a.k_out[c * P + g] = kn;
   a.u_out[c * P + g] = fma(a.b, kn, __ldg(a.u_in + c * P + g));
 }
+// All six components of node g: the node's RK register and state loaded
+// first (twelve loads in flight; the stores of one component would otherwise
+// keep the next component's loads behind them, k_out possibly being k), then
+// the six updates as in rk_finish_cf.
+template <bool IA>
+__device__ __forceinline__ void rk_finish_node(const MixedDev& a, long g, const float* Rh,
+                                               const float* Rl, float2 cfH, float2 cfE,
+                                               bool first_stage) {
+  const long P = a.npts;
+  double kk[6], uu[6];
+#pragma unroll
+  for (int c = 0; c < 6; ++c) {
+    kk[c] = first_stage ? 0.0 : a.k[c * P + g];
+    uu[c] = __ldg(a.u_in + c * P + g);
+  }
+#pragma unroll
+  for (int c = 0; c < 6; ++c) {
+    const float2 cf = c < 3 ? cfH : cfE;
+    const float p = cf.x * Rh[c];
+    float ee = fmaf(cf.x, Rh[c], -p);
+    ee = fmaf(cf.x, Rl[c], ee);
+    ee = fmaf(cf.y, Rh[c], ee);
+    double r;
+    if constexpr (IA) {
+      float s, t;
+      two_sum(p, ee, s, t);
+      r = pair_to_double(s, t);
+    } else {
+      r = f2d(p) + f2d(ee);
+    }
+    const double kn = first_stage ? r : fma(a.a, kk[c], r);
+    a.k_out[c * P + g] = kn;
+    a.u_out[c * P + g] = fma(a.b, kn, uu[c]);
+  }
+}
 template <bool IA>
 __device__ __forceinline__ void rk_finish(const MixedDev& a, int c, long g, float Rh, float Rl,
                                           bool first_stage) {
@@ -871,9 +906,7 @@ __global__ void __launch_bounds__(MCfg<NX>::NT, mixed_min_blocks<NX, EXT>())
         // the node's two coefficient pairs, H and E, once for its six components
         const long g = (long)e * N3 + v;
         const float2 cfH = a.coef[g], cfE = a.coef[P + g];
-#pragma unroll
-        for (int c = 0; c < 6; ++c)
-          rk_finish_cf<C::kIntAdd>(a, c, g, Rh[c], Rl[c], c < 3 ? cfH : cfE, first_stage);
+        rk_finish_node<C::kIntAdd>(a, g, Rh, Rl, cfH, cfE, first_stage);
       }
     }
   }
