@@ -102,6 +102,10 @@ __device__ __forceinline__ void cp_async8(void* dst, const void* src) {
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+// one line into L1 ahead of a load
+__device__ __forceinline__ void prefetch_l1(const void* p) {
+  asm volatile("prefetch.global.L1 [%0];\n" ::"l"(p));
+}
 __device__ __forceinline__ void prefetch_l2(const void* src, unsigned bytes) {
   asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(src), "r"(bytes) : "memory");
 }
@@ -179,6 +183,11 @@ struct MCfg {
   // copies where that measured faster (N=8 +3 %, N=6 +0.9 %; N=4, N=2 load
   // synchronously: -0.5 %, -1.8 % with the async copies)
   static constexpr bool kAsync = !kTma && NX >= 7;
+  // L1 prefetch of the finish's loads where it measured faster: in the t-line
+  // tasks that finish (N=6 +2.5 %, N=4 +0.4 %; N=5 -1.9 %: it spills there)
+  // and for the next node of the node-by-node finish (N=8 +1.4 %; N=7 -2.2 %)
+  static constexpr bool kPfLine = NX == 5 || NX == 7;
+  static constexpr bool kPfNode = NX == 9;
   // Where the components finish (inverse mass, RK update) without the
   // extension terms: true = the t-line tasks finish H1, H2, E1, E2 on their
   // lines and H3, E3 (no t-derivative) finish beside them, with no barrier and
@@ -380,6 +389,17 @@ __device__ __forceinline__ void line_phase(const float2* s_u2, float2* s_R2, con
       const float sg = kLineSign[DIR][slot];
       const bool init = kLineInit[DIR][slot] != 0;
       const float2* pu = s_u2 + comp * C::N3P;
+      if (FIN && C::kPfLine) {  // the line's RK register and state, read by its finish: into L1 now
+        const long P = a.npts;
+#pragma unroll
+        for (int i = 0; i < NX; ++i) {
+          const int vol = DIR == 0 ? i + NX * la + C::N2 * lb
+                                   : (DIR == 1 ? la + NX * i + C::N2 * lb : la + NX * lb + C::N2 * i);
+          const long g = (long)e * C::N3 + vol;
+          if (!first_stage) prefetch_l1(a.k + rt * P + g);
+          prefetch_l1(a.u_in + rt * P + g);
+        }
+      }
       // lifted flux at the line's ends: faces 3|1 (r), 0|2 (s), 4|5 (t)
       constexpr int FM = DIR == 0 ? 3 : (DIR == 1 ? 0 : 4);
       constexpr int FP = DIR == 0 ? 1 : (DIR == 1 ? 2 : 5);
@@ -892,6 +912,14 @@ __global__ void __launch_bounds__(MCfg<NX>::NT, mixed_min_blocks<NX, EXT>())
       for (int q = 0; q < NPT; ++q) {
         const int v = tid + q * NT;
         if (v >= N3) continue;
+        if (C::kPfNode && q + 1 < NPT && v + NT < N3) {  // the next node's loads into L1 meanwhile
+          const long g2 = (long)e * N3 + v + NT;
+#pragma unroll
+          for (int c = 0; c < 6; ++c) {
+            if (!first_stage) prefetch_l1(a.k + c * P + g2);
+            prefetch_l1(a.u_in + c * P + g2);
+          }
+        }
         const int pv = pnode<NX>(v);
         float Rh[6], Rl[6];
 #pragma unroll
