@@ -515,7 +515,8 @@ int mixed_stage_buffers(Context* c, int rkstep, double time, double dt, const do
 int wait_selftest(Context* c, int polls);
 // one mixed stage over elements [e0, e1) of the current state, writing the
 // other state buffer without switching to it
-int mixed_stage_range(Context* c, int rkstep, double time, double dt, int e0, int e1);
+int mixed_stage_range(Context* c, int rkstep, double time, double dt, int e0, int e1,
+                      bool pdl = false);
 // the mixed form keeps dt-scaled coefficients as (hi, lo) float pairs in d_coef
 int scale_coef_pairs(Context* c, double dt);
 // D(i,j) in three FP32 pieces: Dh on a 10-bit grid per row (exact products

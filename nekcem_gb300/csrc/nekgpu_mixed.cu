@@ -579,6 +579,13 @@ __global__ void __launch_bounds__(MCfg<NX>::NT, mixed_min_blocks<NX, EXT>())
   unsigned* s_E = reinterpret_cast<unsigned*>(smem + C::off_E);
   uint64_t* bar = reinterpret_cast<uint64_t*>(smem + C::off_bar);
   __shared__ int s_abort;
+  // launched as a programmatic dependent of the previous stage (device-
+  // resident steps): read nothing the previous stage wrote before it has
+  // completed and its writes are visible (a no-op for an ordinary launch).
+  // Each block lets the next stage launch when it starts its last element,
+  // so the next stage's blocks take the SMs this grid leaves (triggering at
+  // entry let several stages' grids pile up waiting: C1 1.5x slower)
+  asm volatile("griddepcontrol.wait;\n" ::: "memory");
 
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   int tid = threadIdx.x;
@@ -626,6 +633,7 @@ __global__ void __launch_bounds__(MCfg<NX>::NT, mixed_min_blocks<NX, EXT>())
 
   for (int e = a.e_begin + blockIdx.x; e < a.e_end; e += gridDim.x, buf ^= 1) {
     int tid = opaque_tid();
+    if (e + (int)gridDim.x >= a.e_end) asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory");
     double* s_u64 = reinterpret_cast<double*>(smem + buf * C::SA);
     float2* s_R2 = reinterpret_cast<float2*>(smem + buf * C::SA);
     float2* s_u2 = reinterpret_cast<float2*>(smem + (buf ^ 1) * C::SA);
@@ -950,7 +958,7 @@ __global__ void k_scale_coef_pairs(float2* coef, const double* base, long n2, do
 }
 
 template <int NX, bool EXT>
-int launch_mixed(Context* c, const MixedDev& a) {
+int launch_mixed(Context* c, const MixedDev& a, bool pdl) {
   using C = MCfg<NX>;
   auto kern = k_mixed_stage<NX, EXT>;
   static bool ready = false;
@@ -971,7 +979,21 @@ int launch_mixed(Context* c, const MixedDev& a) {
   if (n <= 0) return NEKGPU_OK;
   const int g = n < grid ? n : grid;
   c->fused_grid = g;
-  kern<<<g, C::NT, C::smem, c->stream>>>(a);
+  if (pdl) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(g);
+    cfg.blockDim = dim3(C::NT);
+    cfg.dynamicSmemBytes = C::smem;
+    cfg.stream = c->stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    if (check_cuda(cudaLaunchKernelEx(&cfg, kern, a))) return NEKGPU_ERR_CUDA;
+  } else {
+    kern<<<g, C::NT, C::smem, c->stream>>>(a);
+  }
   c->last_launches += 1;
   return check_cuda(cudaGetLastError());
 }
@@ -1266,7 +1288,7 @@ int scale_coef_pairs(Context* c, double dt) {
   return check_cuda(cudaGetLastError());
 }
 
-int mixed_stage_range(Context* c, int rkstep, double time, double dt, int e0, int e1) {
+int mixed_stage_range(Context* c, int rkstep, double time, double dt, int e0, int e1, bool pdl) {
   int st = scale_coef_pairs(c, dt);
   if (st) return st;
   MixedDev a = c->margs;
@@ -1289,13 +1311,13 @@ int mixed_stage_range(Context* c, int rkstep, double time, double dt, int e0, in
     a.gr.f_out = c->d_gr_f[c->gr_cur ^ 1];
   }
   switch (c->nx) {
-    case 3: st = ext ? launch_mixed<3, true>(c, a) : launch_mixed<3, false>(c, a); break;
-    case 4: st = ext ? launch_mixed<4, true>(c, a) : launch_mixed<4, false>(c, a); break;
-    case 5: st = ext ? launch_mixed<5, true>(c, a) : launch_mixed<5, false>(c, a); break;
-    case 6: st = ext ? launch_mixed<6, true>(c, a) : launch_mixed<6, false>(c, a); break;
-    case 7: st = ext ? launch_mixed<7, true>(c, a) : launch_mixed<7, false>(c, a); break;
-    case 8: st = ext ? launch_mixed<8, true>(c, a) : launch_mixed<8, false>(c, a); break;
-    case 9: st = ext ? launch_mixed<9, true>(c, a) : launch_mixed<9, false>(c, a); break;
+    case 3: st = ext ? launch_mixed<3, true>(c, a, pdl) : launch_mixed<3, false>(c, a, pdl); break;
+    case 4: st = ext ? launch_mixed<4, true>(c, a, pdl) : launch_mixed<4, false>(c, a, pdl); break;
+    case 5: st = ext ? launch_mixed<5, true>(c, a, pdl) : launch_mixed<5, false>(c, a, pdl); break;
+    case 6: st = ext ? launch_mixed<6, true>(c, a, pdl) : launch_mixed<6, false>(c, a, pdl); break;
+    case 7: st = ext ? launch_mixed<7, true>(c, a, pdl) : launch_mixed<7, false>(c, a, pdl); break;
+    case 8: st = ext ? launch_mixed<8, true>(c, a, pdl) : launch_mixed<8, false>(c, a, pdl); break;
+    case 9: st = ext ? launch_mixed<9, true>(c, a, pdl) : launch_mixed<9, false>(c, a, pdl); break;
     default: return NEKGPU_ERR_UNSUPPORTED;
   }
   return st;
@@ -1350,19 +1372,19 @@ int mixed_stage_buffers(Context* c, int rkstep, double time, double dt, const do
     a.src_ft2 = make_float2(hi, (float)(ft - (double)hi));
   }
   switch (c->nx) {
-    case 3: return launch_mixed<3, false>(c, a);
-    case 4: return launch_mixed<4, false>(c, a);
-    case 5: return launch_mixed<5, false>(c, a);
-    case 6: return launch_mixed<6, false>(c, a);
-    case 7: return launch_mixed<7, false>(c, a);
-    case 8: return launch_mixed<8, false>(c, a);
-    case 9: return launch_mixed<9, false>(c, a);
+    case 3: return launch_mixed<3, false>(c, a, false);
+    case 4: return launch_mixed<4, false>(c, a, false);
+    case 5: return launch_mixed<5, false>(c, a, false);
+    case 6: return launch_mixed<6, false>(c, a, false);
+    case 7: return launch_mixed<7, false>(c, a, false);
+    case 8: return launch_mixed<8, false>(c, a, false);
+    case 9: return launch_mixed<9, false>(c, a, false);
     default: return NEKGPU_ERR_UNSUPPORTED;
   }
 }
 
 int mixed_stage(Context* c, int rkstep, double time, double dt) {
-  const int st = mixed_stage_range(c, rkstep, time, dt, 0, c->nelt);
+  const int st = mixed_stage_range(c, rkstep, time, dt, 0, c->nelt, true);
   if (st) return st;
   c->cur ^= 1;
   if (c->margs.gr.elem) c->gr_cur ^= 1;
