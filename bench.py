@@ -378,12 +378,31 @@ def adjoint_ratio(nsteps=0, case="adjoint", budget_mb=None, form="fused64", host
     return out
 
 
-def cpu_sample(min_sec=10.0):
+def cpu_model():
+    """The host CPU as /proc/cpuinfo names it (model name, or implementer and
+    part on Arm)."""
+    try:
+        with open("/proc/cpuinfo") as f:
+            info = f.read().splitlines()
+    except OSError:
+        return "unknown"
+    fields = {}
+    for ln in info:
+        if ":" in ln:
+            k, v = (p.strip() for p in ln.split(":", 1))
+            fields.setdefault(k, v)
+    if "model name" in fields:
+        return fields["model name"]
+    return f"implementer {fields.get('CPU implementer', '?')} part {fields.get('CPU part', '?')}"
+
+
+def cpu_sample(min_sec=10.0, threads=None):
     """The CPU oracle (FP64 restatement of the reference's routines, all host
-    threads) on the same mesh: RK steps until `min_sec` of wall time."""
+    threads unless `threads` is given) on the same mesh: RK steps until
+    `min_sec` of wall time."""
     from nekcem_gb300 import cases
     from oracle import refcpu as R
-    threads = os.cpu_count() or 1
+    threads = threads or os.cpu_count() or 1
     R.set_threads(threads)
     c = cases.make(CASE)
     ref = R.RefBox(c.N, c.nel, c.lo, c.hi, c.bc)
@@ -538,9 +557,13 @@ def main():
         out["adjoint"] = adjoint_ratio(args.adjoint_steps or 10, case="large", budget_mb=171661)
     if not args.no_cpu and world == 1 and npts <= 10_000_000:
         cpu = cpu_sample()
+        one = cpu_sample(threads=1)
         out["cpu_baseline"] = {"value": cpu["value"], "unit": UNIT, "cores": cpu["threads"],
                                "kind": "port", "sample": f"{cpu['steps']} RK steps of the full "
-                               f"mesh, {cpu['sec']:.1f} s"}
+                               f"mesh, {cpu['sec']:.1f} s", "cpu": cpu_model(),
+                               "single_thread": {"value": one["value"], "cores": 1,
+                                                 "sample": f"{one['steps']} RK steps of the full "
+                                                 f"mesh, {one['sec']:.1f} s"}}
     print(json.dumps(out), flush=True)
 
 
