@@ -359,6 +359,14 @@ def adjoint_ratio(nsteps=0, case="adjoint", budget_mb=None, form="fused64", host
         J, dJ, fwd_part_ms, rev_ms = g.adjoint_gradient(n, 0.0, dt, jw,
                                                         host_snapshots=host_snapshots)
         t_wall = time.perf_counter() - t_wall
+        hyb = None
+        if form == "fused64" and case == "adjoint":
+            # the same gradient with the segments recomputed in mixed stages
+            g.set_state(H0, E0)
+            Jh, dJh, fh, rh = g.adjoint_gradient(n, 0.0, dt, jw, recompute_mixed=True)
+            hyb = {"gradient_ms": fh + rh, "reverse_sweep_ms": rh, "ratio": (fh + rh) / fwd_ms,
+                   "J_equal": Jh == J,
+                   "grad_max_rel_diff": float(np.abs(dJh - dJ).max() / np.abs(dJ).max())}
         g.close()
     finally:
         if budget_mb:
@@ -373,6 +381,8 @@ def adjoint_ratio(nsteps=0, case="adjoint", budget_mb=None, form="fused64", host
            "grad_norm": float(np.linalg.norm(dJ)), "forward_form": form,
            "forward_timing": f"{nf} steps, scaled to {n}", "gradient_wall_s": t_wall,
            "host_snapshots": host_snapshots}
+    if hyb:
+        out["mixed_recompute"] = hyb
     if budget_mb:
         out["device_memory_budget_bytes"] = int(budget_mb) << 20
     return out

@@ -372,6 +372,14 @@ int nekgpu_adjoint_init(nekgpu_ctx* ctx, const double* jw, int stride);
  * Each use of a host snapshot copies one state over the host link.  Gradients
  * are bit-identical whatever memory the snapshots live in. */
 int nekgpu_adjoint_host_snapshots(nekgpu_ctx* ctx, int n);
+/* NEKGPU_FUSED64 on affine meshes: on != 0 recomputes the segments of the
+ * sqrt(steps) schedule with mixed stages (started at the FP64 checkpoints)
+ * instead of FP64 ones; the first pass, J and the checkpoints stay FP64, and
+ * the reverse stages read stage states within ~1e-10 per step of the FP64
+ * ones (gradients within ~1e-8 of the exact discrete adjoint's).  The
+ * binomial schedule is not affected.  NEKGPU_ERR_UNSUPPORTED for other forms
+ * or meshes. */
+int nekgpu_adjoint_recompute_mixed(nekgpu_ctx* ctx, int on);
 int nekgpu_adjoint_run(nekgpu_ctx* ctx, int nsteps, double t0, double dt, double* J,
                        double* dJdeps);
 

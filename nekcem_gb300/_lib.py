@@ -109,6 +109,7 @@ SIGNATURES = [
                                          C.c_int, dp, dp]),
     ("nekgpu_adjoint_init", C.c_int, [C.c_void_p, dp, C.c_int]),
     ("nekgpu_adjoint_host_snapshots", C.c_int, [C.c_void_p, C.c_int]),
+    ("nekgpu_adjoint_recompute_mixed", C.c_int, [C.c_void_p, C.c_int]),
     ("nekgpu_adjoint_run", C.c_int, [C.c_void_p, C.c_int, C.c_double, C.c_double, dp, dp]),
     ("nekgpu_write_vtk", C.c_int, [C.c_void_p, C.c_char_p, dp, dp, C.c_long]),
     ("nekgpu_checkpoint_save", C.c_int, [C.c_void_p, C.c_char_p, C.c_double, C.c_long]),

@@ -462,7 +462,12 @@ extern "C" int nekgpu_adjoint_gradient(nekgpu_ctx* c, int nsteps, double t0, dou
   // stride > 0: segments of `stride` steps; 0: sqrt(steps) segments if they
   // fit, else the binomial schedule with the snapshots that fit; < 0: the
   // binomial schedule with -stride device snapshots.
-  const double avail = (double)adjoint_budget(c) - (double)npts * 8 - (mixed ? 16.0 * npts : 0.0);
+  // fused FP64 with mixed recomputation: the mixed stage arguments of the
+  // context (coefficient pairs and their FP64 base, 32 B per face node of
+  // face coefficient pairs) -- about 32 + 4.5 * 6/nx bytes per node
+  const bool hybrid = !mixed && c->adj_mixed_recompute;
+  const double hybrid_b = hybrid ? (32.0 + 32.0 * 6.0 / c->nx) * npts : 0.0;
+  const double avail = (double)adjoint_budget(c) - (double)npts * 8 - (mixed ? 16.0 * npts : 0.0) - hybrid_b;
   const int S = stride > 0 ? stride : (int)std::ceil(std::sqrt((double)nsteps));
   const int nseg = (nsteps + S - 1) / S;
   auto sqrt_states = [&](int sets) { return (double)nseg + 4.0 + sets * 2.0 * (5.0 * S + 1.0); };
@@ -559,6 +564,12 @@ extern "C" int nekgpu_adjoint_gradient(nekgpu_ctx* c, int nsteps, double t0, dou
     }
     StreamPair sp;
     if (nsets == 2 && !sp.create()) nsets = 1;
+    // the recomputed segments in mixed stages (fused FP64 contexts that ask
+    // for it): the first pass, J and the checkpoints stay FP64; the stage
+    // states the reverse stages read come from mixed steps started at the
+    // FP64 checkpoints (within ~1e-10 per step of the FP64 ones)
+    MixedDev comp{};
+    if (hybrid && (st = mixed_companion(c, dt, mem.ptrs, comp))) return st;
 
     // forward pass with checkpoints
     if (check_cuda(cudaEventRecord(c->ev0, c->stream))) return NEKGPU_ERR_CUDA;
@@ -581,8 +592,10 @@ extern "C" int nekgpu_adjoint_gradient(nekgpu_ctx* c, int nsteps, double t0, dou
       for (int s2 = 0; s2 < nS && !r; ++s2)
         for (int q = 1; q <= 5 && !r; ++q) {
           const int i = 5 * s2 + q;
-          r = fwd_stage_buffers(c, q, w.tstep[n0 + s2], dt, U[b][i - 1], U[b][i], K[b][i - 1],
-                                K[b][i]);
+          r = hybrid ? mixed_stage_dev(c, comp, q, w.tstep[n0 + s2], dt, U[b][i - 1], U[b][i],
+                                       K[b][i - 1], K[b][i])
+                     : fwd_stage_buffers(c, q, w.tstep[n0 + s2], dt, U[b][i - 1], U[b][i],
+                                         K[b][i - 1], K[b][i]);
         }
       c->stream = main_stream;
       return r;
@@ -635,6 +648,13 @@ extern "C" int nekgpu_adjoint_gradient(nekgpu_ctx* c, int nsteps, double t0, dou
   *J = w.J;
   if (fwd_ms) *fwd_ms = f_ms;
   if (adj_ms) *adj_ms = a_ms;
+  return NEKGPU_OK;
+}
+
+extern "C" int nekgpu_adjoint_recompute_mixed(nekgpu_ctx* c, int on) {
+  if (!c) return NEKGPU_ERR_ARG;
+  if (on && (c->form != NEKGPU_FUSED64 || c->curved || c->ndim != 3)) return NEKGPU_ERR_UNSUPPORTED;
+  c->adj_mixed_recompute = on != 0;
   return NEKGPU_OK;
 }
 

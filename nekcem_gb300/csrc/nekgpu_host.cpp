@@ -1502,6 +1502,133 @@ int do_steps(Context* c, int nsteps, double* time, double dt) {
 
 }  // namespace
 
+namespace nekgpu {
+
+int mixed_companion(Context* c, double dt, std::vector<void*>& owned, MixedDev& m) {
+  if (c->form != NEKGPU_FUSED64 || c->curved || c->ndim != 3 || c->nx < 3 || c->nx > kMaxMixed)
+    return NEKGPU_ERR_UNSUPPORTED;
+  if (c->npml || c->disp_n || !c->inc_slots.empty() || c->grdev.ng) return NEKGPU_ERR_UNSUPPORTED;
+  const int n = c->nx;
+  const long n3 = (long)n * n * n, npts = c->npts, nxzfl = c->nxzfl, nelt = c->nelt;
+  auto dev = [&](size_t bytes) -> void* {
+    void* p = nullptr;
+    if (cudaMalloc(&p, bytes) != cudaSuccess) {
+      cudaGetLastError();
+      return nullptr;
+    }
+    owned.push_back(p);
+    return p;
+  };
+  // D in its FP32 pieces (the library's GLL D; the context's must agree)
+  std::vector<double> z, w, D;
+  gll(n - 1, z, w, D);
+  double dmax = 0, diff = 0;
+  for (size_t k = 0; k < D.size(); ++k) {
+    dmax = std::max(dmax, std::fabs(D[k]));
+    diff = std::max(diff, std::fabs(D[k] - c->fargs.D[k]));
+  }
+  if (diff > 1e-12 * dmax) return NEKGPU_ERR_MESH;
+  std::vector<float> tab;
+  split_D(D, n, tab);
+  int st = mixed_upload_D(n, tab.data(), tab.size());
+  if (st) return st;
+  std::vector<double> eg(9 * (size_t)nelt), hb(npts), eb(npts);
+  if (check_cuda(cudaMemcpy(eg.data(), c->d_egeom, eg.size() * 8, cudaMemcpyDeviceToHost)) ||
+      check_cuda(cudaMemcpy(hb.data(), c->d_hbm1, npts * 8, cudaMemcpyDeviceToHost)) ||
+      check_cuda(cudaMemcpy(eb.data(), c->d_ebm1, npts * 8, cudaMemcpyDeviceToHost)))
+    return NEKGPU_ERR_CUDA;
+  m = MixedDev{};
+  m.nelt = c->nelt;
+  m.npts = npts;
+  m.k = m.k_out = c->d_k;
+  m.nbr = c->d_nbr;
+  m.C0f = (float)c->fargs.C0;
+  m.status = c->d_status;
+  // per element: rho_y, rho_z pairs and the lift factors (as upload_fused)
+  {
+    const double wend = c->fargs.w[0];
+    std::vector<float> egm(16 * (size_t)nelt, 0.0f);
+    for (long e = 0; e < nelt; ++e) {
+      const double* g = &eg[9 * (size_t)e];
+      const double ry = g[1] / g[0], rz = g[2] / g[0];
+      float* o = &egm[16 * (size_t)e];
+      o[0] = (float)ry; o[1] = (float)(ry - (double)o[0]);
+      o[2] = (float)rz; o[3] = (float)(rz - (double)o[2]);
+      for (int f = 0; f < 6; ++f) {
+        const double lf = g[3 + f] / (wend * g[0]);
+        o[4 + f] = (float)lf;
+        o[10 + f] = (float)(lf - (double)o[4 + f]);
+      }
+    }
+    float* d = (float*)dev(egm.size() * sizeof(float));
+    if (!d || check_cuda(cudaMemcpy(d, egm.data(), egm.size() * sizeof(float), cudaMemcpyHostToDevice)))
+      return d ? NEKGPU_ERR_CUDA : NEKGPU_ERR_NOMEM;
+    m.egm = d;
+  }
+  // normalised inverse mass hbm1*w3*rx | ebm1*w3*rx, scaled by dt into pairs
+  {
+    std::vector<double> base(2 * (size_t)npts);
+    for (long g = 0; g < npts; ++g) {
+      const double f = c->host_w3[g % n3] * eg[9 * (g / n3)];
+      base[g] = hb[g] * f;
+      base[npts + g] = eb[g] * f;
+    }
+    double* db = (double*)dev(base.size() * 8);
+    float2* cf = (float2*)dev(base.size() * sizeof(float2));
+    if (!db || !cf) return NEKGPU_ERR_NOMEM;
+    if (check_cuda(cudaMemcpy(db, base.data(), base.size() * 8, cudaMemcpyHostToDevice))) return NEKGPU_ERR_CUDA;
+    if ((st = mixed_scale_pairs(c, cf, db, 2 * npts, dt))) return st;
+    m.coef = cf;
+  }
+  // face coefficients as pairs (hi float4, lo float4 per face node)
+  if (c->d_fcoef) {
+    std::vector<double> fc(4 * (size_t)nxzfl);
+    if (check_cuda(cudaMemcpy(fc.data(), c->d_fcoef, fc.size() * 8, cudaMemcpyDeviceToHost)))
+      return NEKGPU_ERR_CUDA;
+    std::vector<float> f(8 * (size_t)nxzfl);
+    for (long j = 0; j < nxzfl; ++j)
+      for (int q = 0; q < 4; ++q) {
+        const double v = fc[4 * j + q];
+        f[8 * j + q] = (float)v;
+        f[8 * j + 4 + q] = (float)(v - (double)f[8 * j + q]);
+      }
+    float* d = (float*)dev(f.size() * sizeof(float));
+    if (!d || check_cuda(cudaMemcpy(d, f.data(), f.size() * sizeof(float), cudaMemcpyHostToDevice)))
+      return d ? NEKGPU_ERR_CUDA : NEKGPU_ERR_NOMEM;
+    m.fcoef = d;
+  }
+  // volume source: the FP64 weights normalised by w3*rx, as pairs
+  if (c->src.enabled && c->fargs.src_elem) {
+    std::vector<int> off(nelt);
+    if (check_cuda(cudaMemcpy(off.data(), c->fargs.src_elem, nelt * sizeof(int), cudaMemcpyDeviceToHost)))
+      return NEKGPU_ERR_CUDA;
+    int cnt = 0;
+    for (int o : off) cnt = std::max(cnt, o + 1);
+    std::vector<double> wd((size_t)cnt * n3);
+    if (cnt && check_cuda(cudaMemcpy(wd.data(), c->fargs.src_w, wd.size() * 8, cudaMemcpyDeviceToHost)))
+      return NEKGPU_ERR_CUDA;
+    std::vector<float> wf(2 * wd.size());
+    for (long e = 0; e < nelt; ++e) {
+      if (off[e] < 0) continue;
+      for (long v = 0; v < n3; ++v) {
+        const size_t i = (size_t)off[e] * n3 + v;
+        const double x = wd[i] / (c->host_w3[v] * eg[9 * (size_t)e]);
+        wf[2 * i] = (float)x;
+        wf[2 * i + 1] = (float)(x - (double)wf[2 * i]);
+      }
+    }
+    float* d = (float*)dev(std::max<size_t>(wf.size(), 2) * sizeof(float));
+    if (!d) return NEKGPU_ERR_NOMEM;
+    if (cnt && check_cuda(cudaMemcpy(d, wf.data(), wf.size() * sizeof(float), cudaMemcpyHostToDevice)))
+      return NEKGPU_ERR_CUDA;
+    m.src_elem = c->fargs.src_elem;
+    m.src_w = reinterpret_cast<const float2*>(d);
+  }
+  return NEKGPU_OK;
+}
+
+}  // namespace nekgpu
+
 // ===========================================================================
 // C ABI
 // ===========================================================================

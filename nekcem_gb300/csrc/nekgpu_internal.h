@@ -452,6 +452,7 @@ struct Context {
   std::vector<double> adj_jw;  // objective weights set by nekgpu_adjoint_init
   int adj_stride = 0;
   int adj_host_snapshots = 0;  // pinned host snapshot slots the binomial schedule may add
+  bool adj_mixed_recompute = false;  // fused FP64: the sqrt schedule's segments recomputed in mixed stages
   // mixed form: the FP64 face coefficients (4 per face node, as FusedDev::fcoef)
   // for the adjoint's face-slot table; empty when uniform
   std::vector<double> host_fcoef64;
@@ -511,6 +512,17 @@ int mixed_stage(Context* c, int rkstep, double time, double dt);
 // fused_stage_buffers; the context's own state is untouched
 int mixed_stage_buffers(Context* c, int rkstep, double time, double dt, const double* u_in,
                         double* u_out, double* k_in, double* k_out);
+// the same with explicit stage arguments (coefficient pairs already scaled),
+// e.g. those of mixed_companion
+int mixed_stage_dev(Context* c, MixedDev a, int rkstep, double time, double dt, const double* u_in,
+                    double* u_out, double* k_in, double* k_out);
+// coef = (hi, lo) pairs of dt * base (n2 values)
+int mixed_scale_pairs(Context* c, float2* coef, const double* base, long n2, double dt);
+// The mixed-form stage arguments for an affine fused FP64 context (normalised
+// inverse-mass pairs scaled by dt, per-element factors, face coefficient
+// pairs, normalised source weight pairs; D's FP32 pieces uploaded): device
+// buffers are appended to `owned` for the caller to free.
+int mixed_companion(Context* c, double dt, std::vector<void*>& owned, MixedDev& m);
 // launches a kernel whose bounded mbarrier wait runs out (sets the status word)
 int wait_selftest(Context* c, int polls);
 // one mixed stage over elements [e0, e1) of the current state, writing the

@@ -1351,11 +1351,21 @@ int mixed_curved_stage(Context* c, int rkstep, double time, double dt) {
   return NEKGPU_OK;
 }
 
+int mixed_scale_pairs(Context* c, float2* coef, const double* base, long n2, double dt) {
+  k_scale_coef_pairs<<<(unsigned)((n2 + 255) / 256), 256, 0, c->stream>>>(coef, base, n2, dt);
+  c->last_launches += 1;
+  return check_cuda(cudaGetLastError());
+}
+
 int mixed_stage_buffers(Context* c, int rkstep, double time, double dt, const double* u_in,
                         double* u_out, double* k_in, double* k_out) {
-  int st = scale_coef_pairs(c, dt);
+  const int st = scale_coef_pairs(c, dt);
   if (st) return st;
-  MixedDev a = c->margs;
+  return mixed_stage_dev(c, c->margs, rkstep, time, dt, u_in, u_out, k_in, k_out);
+}
+
+int mixed_stage_dev(Context* c, MixedDev a, int rkstep, double time, double dt, const double* u_in,
+                    double* u_out, double* k_in, double* k_out) {
   if (a.pml.slot || a.disp.slot || a.inc_elem || a.gr.elem) return NEKGPU_ERR_UNSUPPORTED;
   a.e_begin = 0;
   a.e_end = c->nelt;

@@ -351,7 +351,8 @@ class MaxwellGPU:
 
     # ---- discrete adjoint (fused FP64 and mixed forms) ----------------------------
     def adjoint_gradient(self, nsteps: int, t0: float, dt: float, jw: np.ndarray, stride: int = 0,
-                         host_snapshots: Optional[int] = None):
+                         host_snapshots: Optional[int] = None,
+                         recompute_mixed: Optional[bool] = None):
         """J = sum_g jw[g] |E(g)|^2 after nsteps steps from the current state and
         dJ/deps at every node, by the discrete adjoint (forward steps in the
         context's form, reverse stages in FP64).  ``stride`` > 0: checkpoints
@@ -359,8 +360,12 @@ class MaxwellGPU:
         in device memory, else the binomial schedule; < 0: the binomial
         schedule with -stride device snapshots.  ``host_snapshots``: pinned
         host snapshots the binomial schedule may add (kept for later calls).
-        Leaves the final state in the context.  Returns (J, dJdeps,
-        forward_ms, adjoint_ms)."""
+        ``recompute_mixed`` (fused FP64 form): the sqrt schedule's segments
+        recomputed in mixed stages (kept for later calls).  Leaves the final
+        state in the context.  Returns (J, dJdeps, forward_ms, adjoint_ms)."""
+        if recompute_mixed is not None:
+            L.check(L.load().nekgpu_adjoint_recompute_mixed(self._h, int(bool(recompute_mixed))),
+                    "nekgpu_adjoint_recompute_mixed")
         if host_snapshots is not None:
             L.check(L.load().nekgpu_adjoint_host_snapshots(self._h, int(host_snapshots)),
                     "nekgpu_adjoint_host_snapshots")

@@ -21,6 +21,7 @@ class BoxProblem:
         self.nsteps, self.dt, self.t0, self.source, self.stride = nsteps, dt, t0, source, stride
         self.form = "fused64"       # form of the gradient's forward steps
         self.host_snapshots = None  # pinned host snapshots for the binomial schedule
+        self.recompute_mixed = None  # fused FP64: segments recomputed in mixed stages
         self.last_ms = None
 
     def context(self, eps: np.ndarray, form: str = "fused64") -> MaxwellGPU:
@@ -42,7 +43,8 @@ class BoxProblem:
     def gradient(self, eps: np.ndarray):
         g = self.context(eps, self.form)
         J, dJ, fms, ams = g.adjoint_gradient(self.nsteps, self.t0, self.dt, self.jw, self.stride,
-                                             host_snapshots=self.host_snapshots)
+                                             host_snapshots=self.host_snapshots,
+                                             recompute_mixed=self.recompute_mixed)
         g.close()
         self.last_ms = (fms, ams)
         return J, dJ

@@ -164,6 +164,30 @@ def test_mixed_forward_adjoint_matches_fp64_and_central_differences(N, nel, bc, 
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("N,nel,bc,nsteps", [MESHES[1], MESHES[2]])
+def test_mixed_recompute_matches_exact_and_central_differences(N, nel, bc, nsteps):
+    """Fused FP64 context, sqrt(steps) segments recomputed in mixed stages
+    from the FP64 checkpoints: J is the FP64 forward's (bit for bit), dJ/deps
+    within 1e-8 (of its largest entry) of the exact gradient, and central
+    differences of the FP64 forward (h = 1e-6, 10 directions) within 1e-6."""
+    pb, eps, _, _ = gpu_problem(N, nel, bc, seed=21 + N, nsteps=nsteps, stride=4)
+    J0, g0 = pb.gradient(eps)
+    pb.recompute_mixed = True
+    J1, g1 = pb.gradient(eps)
+    assert J1 == J0
+    assert np.abs(g1 - g0).max() <= 1e-8 * np.abs(g0).max()
+    rng = np.random.default_rng(300 + N)
+    h = 1e-6
+    worst = 0.0
+    for _ in range(10):
+        d = rng.standard_normal(eps.size)
+        fd = (pb.objective(eps + h * d) - pb.objective(eps - h * d)) / (2 * h)
+        ad = float(g1 @ d)
+        worst = max(worst, abs(fd - ad) / abs(ad))
+    assert worst <= 1e-6, worst
+
+
+@pytest.mark.gpu
 @pytest.mark.parametrize("form", ["fused64", "mixed"])
 def test_host_snapshots_give_the_same_gradient(form):
     """Four binomial snapshots split between device and pinned host memory
@@ -299,13 +323,18 @@ def test_adjoint_workload_matches_central_differences_at_full_length():
     dt = c.timestep(x, y, z)
     pb = BoxProblem(c.N, c.nel, c.lo, c.hi, c.bc, H0, E0, jw, c.nsteps, dt, source=c.source)
     J, grad = pb.gradient(eps)
+    pb.recompute_mixed = True  # the same with the segments recomputed in mixed stages
+    Jm, gradm = pb.gradient(eps)
     assert c.nsteps == 2000
     assert J == pytest.approx(pb.objective(eps), rel=1e-14)
+    assert Jm == J
     h = 1e-6
-    worst = 0.0
+    worst = worst_m = 0.0
     for seed in range(1000, 1020):
         d = np.random.default_rng(seed).standard_normal(eps.size)
         fd = (pb.objective(eps + h * d) - pb.objective(eps - h * d)) / (2 * h)
-        ad = float(grad @ d)
+        ad, adm = float(grad @ d), float(gradm @ d)
         worst = max(worst, abs(fd - ad) / abs(ad))
+        worst_m = max(worst_m, abs(fd - adm) / abs(adm))
     assert worst <= 1e-6, worst
+    assert worst_m <= 1e-6, worst_m
