@@ -21,11 +21,13 @@
 // projected out).  Every element gathers what lands on its own nodes, reading
 // the partner elements' face nodes, so all writes are element-local: no
 // atomics, and the adjoint state ping-pongs like the forward state.
-// The D^T contractions run in double-float FP32 arithmetic (D w and the
-// stage weights as (hi, lo) float pairs, products with their FMA error
-// terms, two-sum accumulation: ~2^-47 of the sum of the magnitudes, near
-// FP64's 2^-53) and join the FP64 arithmetic as one FP64 value each; the rest
-// is FP64.  The contractions were 96 of the ~166 FP64 operations per node.
+// The D^T contractions and the face terms run in double-float FP32
+// arithmetic (D w, the stage weights, the face-slot coefficients and the
+// jumps as (hi, lo) float pairs, products with their FMA error terms,
+// two-sum accumulation: ~2^-47 of the sum of the magnitudes, near FP64's
+// 2^-53) and join the FP64 arithmetic as one FP64 value each; the updates of
+// ub, w and deps are FP64.  The contractions and face terms were ~130 of the
+// ~166 FP64 operations per node.
 #include <cuda_runtime.h>
 
 #include "nekgpu_internal.h"
@@ -42,6 +44,31 @@ __host__ __device__ constexpr int slot_opp(int f) { return f < 4 ? (f + 2) & 3 :
 __host__ __device__ constexpr int tan1(int a) { return a == 0 ? 1 : (a == 1 ? 2 : 0); }
 __host__ __device__ constexpr int tan2(int a) { return a == 0 ? 2 : (a == 1 ? 0 : 1); }
 
+// double-float values: (h, l) with h + l the value to ~2^-48
+struct P2 {
+  float h, l;
+};
+__device__ __forceinline__ P2 p2(double d) { return P2{d2f_hi(d), d2f_lo(d)}; }
+__device__ __forceinline__ P2 p2(float2 v) { return P2{v.x, v.y}; }
+__device__ __forceinline__ P2 pmul(P2 a, P2 b) {
+  const float p = a.h * b.h;
+  float e = fmaf(a.h, b.h, -p);
+  e = fmaf(a.h, b.l, e);
+  e = fmaf(a.l, b.h, e);
+  return P2{p, e};
+}
+__device__ __forceinline__ P2 padd(P2 a, P2 b) {
+  float s, t;
+  two_sum(a.h, b.h, s, t);
+  return P2{s, (a.l + b.l) + t};
+}
+__device__ __forceinline__ P2 pneg(P2 a) { return P2{-a.h, -a.l}; }
+__device__ __forceinline__ double pdbl(P2 a) {
+  float s, t;
+  two_sum(a.h, a.l, s, t);
+  return pair_to_double(s, t);
+}
+
 template <int NX>
 __device__ __forceinline__ int face_vol(int f, int a, int b) {
   const int fixed = slot_side(f) < 0 ? 0 : NX - 1;
@@ -55,10 +82,9 @@ struct ACfg {
   static constexpr int N2 = NX * NX, N3 = N2 * NX, NF = 6 * N2;
   static constexpr int NT = ((N3 + 31) / 32) * 32;
   static constexpr int FPT = (NF + NT - 1) / NT;
-  // shared: w (6*N3), D w (NX*NX), face results (5*NF) in FP64; w and D w
-  // as float pairs (6*N3 + NX*NX)
-  static constexpr size_t smem = (6 * N3 + NX * NX + 5 * NF) * sizeof(double) +
-                                 (6 * N3 + NX * NX) * sizeof(float2);
+  // shared: face results (5*NF) in FP64; the stage weights w and D w as
+  // float pairs (6*N3 + NX*NX)
+  static constexpr size_t smem = 5 * NF * sizeof(double) + (6 * N3 + NX * NX) * sizeof(float2);
 };
 
 template <int NX>
@@ -66,9 +92,7 @@ __global__ void __launch_bounds__(ACfg<NX>::NT) k_adjoint_stage(const AdjointDev
   using C = ACfg<NX>;
   constexpr int N2 = C::N2, N3 = C::N3, NT = C::NT, NF = C::NF, FPT = C::FPT;
   extern __shared__ double sm[];
-  double* s_w = sm;                 // [6][N3]  stage weights w of the element
-  double* s_D = s_w + 6 * N3;       // D(m,i) w_m at [m + NX*i]
-  double* s_fu = s_D + NX * NX;     // [4][NF]  tangential face contributions to ub
+  double* s_fu = sm;                // [4][NF]  tangential face contributions to ub
   double* s_fe = s_fu + 4 * NF;     // [NF]     face contributions to deps
   float2* s_wp = reinterpret_cast<float2*>(s_fe + NF);  // [6][N3] w as (hi, lo)
   float2* s_Dp = s_wp + 6 * N3;                          // D w as (hi, lo)
@@ -77,7 +101,6 @@ __global__ void __launch_bounds__(ACfg<NX>::NT) k_adjoint_stage(const AdjointDev
   const bool node = tid < N3;
   const int vi = tid % NX, vj = (tid / NX) % NX, vk = tid / N2;
   for (int t = tid; t < NX * NX; t += NT) {
-    s_D[t] = a.Dw[t];
     s_Dp[t] = make_float2(d2f_hi(a.Dw[t]), d2f_lo(a.Dw[t]));
   }
   const double wi = a.w[vi], wj = a.w[vj], wk = a.w[vk];
@@ -85,13 +108,12 @@ __global__ void __launch_bounds__(ACfg<NX>::NT) k_adjoint_stage(const AdjointDev
   for (int e = blockIdx.x; e < a.nelt; e += gridDim.x) {
     const long g = (long)e * N3 + tid;
     double ub[6], wn[6], mass = 0.0;
-    __syncthreads();  // s_w / s_fu of the previous element are consumed
+    __syncthreads();  // s_wp / s_fu of the previous element are consumed
     if (node) {
 #pragma unroll
       for (int c = 0; c < 6; ++c) {
         ub[c] = a.ub_in[c * P + g];
         wn[c] = a.w_in[c * P + g];
-        s_w[c * N3 + tid] = wn[c];
         s_wp[c * N3 + tid] = make_float2(d2f_hi(wn[c]), d2f_lo(wn[c]));
       }
 #pragma unroll
@@ -113,47 +135,59 @@ __global__ void __launch_bounds__(ACfg<NX>::NT) k_adjoint_stage(const AdjointDev
       const int vl = face_vol<NX>(f, fa, fb);
       const long gn = (long)e * N3 + vl;
       const long j = (long)e * NF + t;
-      double k[16];
+      // the slot's coefficients, the stage weights and the jumps as float
+      // pairs; sums of products in double-float arithmetic (as the D^T
+      // contractions), each result joined into one FP64 value
+      const float2* kslot = reinterpret_cast<const float2*>(a.slot);
+      P2 k[16];
 #pragma unroll
-      for (int m = 0; m < 16; ++m) k[m] = a.slot[m * PF + j];
+      for (int m = 0; m < 16; ++m) {
+        const float2 kv = kslot[m * PF + j];
+        k[m] = P2{kv.x, kv.y};
+      }
       // own stage weights (tangential) from shared memory
-      const double nH1 = s_w[t1 * N3 + vl], nH2 = s_w[t2 * N3 + vl];
-      const double nE1 = s_w[(3 + t1) * N3 + vl], nE2 = s_w[(3 + t2) * N3 + vl];
-      double pH1 = 0.0, pH2 = 0.0, pE1 = 0.0, pE2 = 0.0;
+      const P2 nH1 = p2(s_wp[t1 * N3 + vl]), nH2 = p2(s_wp[t2 * N3 + vl]);
+      const P2 nE1 = p2(s_wp[(3 + t1) * N3 + vl]), nE2 = p2(s_wp[(3 + t2) * N3 + vl]);
+      P2 pH1{0.0f, 0.0f}, pH2{0.0f, 0.0f}, pE1{0.0f, 0.0f}, pE2{0.0f, 0.0f};
       // jump u+ - u- of u_{i-1} (PEC: u-, the -2 of the mirror is in the coefficients)
-      double dH1 = a.u_prev[t1 * P + gn], dH2 = a.u_prev[t2 * P + gn];
-      double dE1 = a.u_prev[(3 + t1) * P + gn], dE2 = a.u_prev[(3 + t2) * P + gn];
+      const double oH1 = a.u_prev[t1 * P + gn], oH2 = a.u_prev[t2 * P + gn];
+      const double oE1 = a.u_prev[(3 + t1) * P + gn], oE2 = a.u_prev[(3 + t2) * P + gn];
+      P2 dH1 = p2(oH1), dH2 = p2(oH2), dE1 = p2(oE1), dE2 = p2(oE2);
       const int pe = a.nbr[6 * e + f];
       if (pe >= 0) {
         const long gp = (long)pe * N3 + face_vol<NX>(slot_opp(f), fa, fb);
-        pH1 = a.w_in[t1 * P + gp];
-        pH2 = a.w_in[t2 * P + gp];
-        pE1 = a.w_in[(3 + t1) * P + gp];
-        pE2 = a.w_in[(3 + t2) * P + gp];
-        dH1 = a.u_prev[t1 * P + gp] - dH1;
-        dH2 = a.u_prev[t2 * P + gp] - dH2;
-        dE1 = a.u_prev[(3 + t1) * P + gp] - dE1;
-        dE2 = a.u_prev[(3 + t2) * P + gp] - dE2;
+        pH1 = p2(a.w_in[t1 * P + gp]);
+        pH2 = p2(a.w_in[t2 * P + gp]);
+        pE1 = p2(a.w_in[(3 + t1) * P + gp]);
+        pE2 = p2(a.w_in[(3 + t2) * P + gp]);
+        dH1 = padd(p2(a.u_prev[t1 * P + gp]), pneg(dH1));
+        dH2 = padd(p2(a.u_prev[t2 * P + gp]), pneg(dH2));
+        dE1 = padd(p2(a.u_prev[(3 + t1) * P + gp]), pneg(dE1));
+        dE2 = padd(p2(a.u_prev[(3 + t2) * P + gp]), pneg(dE2));
       }
       // k: 0 kH 1 kHx 2 kE 3 kEx | 4 pH 5 pHx 6 pE 7 pEx | 8..11 gA..gD | 12..15 hA..hD
-      s_fu[0 * NF + t] = fma(k[0], nH1, fma(-k[1], nE2, fma(k[4], pH1, -k[5] * pE2)));
-      s_fu[1 * NF + t] = fma(k[0], nH2, fma(k[1], nE1, fma(k[4], pH2, k[5] * pE1)));
-      s_fu[2 * NF + t] = fma(-k[3], nH2, fma(k[2], nE1, fma(-k[7], pH2, k[6] * pE1)));
-      s_fu[3 * NF + t] = fma(k[3], nH1, fma(k[2], nE2, fma(k[7], pH1, k[6] * pE2)));
+      s_fu[0 * NF + t] = pdbl(padd(padd(pmul(k[0], nH1), pneg(pmul(k[1], nE2))),
+                                   padd(pmul(k[4], pH1), pneg(pmul(k[5], pE2)))));
+      s_fu[1 * NF + t] = pdbl(padd(padd(pmul(k[0], nH2), pmul(k[1], nE1)),
+                                   padd(pmul(k[4], pH2), pmul(k[5], pE1))));
+      s_fu[2 * NF + t] = pdbl(padd(padd(pneg(pmul(k[3], nH2)), pmul(k[2], nE1)),
+                                   padd(pneg(pmul(k[7], pH2)), pmul(k[6], pE1))));
+      s_fu[3 * NF + t] = pdbl(padd(padd(pmul(k[3], nH1), pmul(k[2], nE2)),
+                                   padd(pmul(k[7], pH1), pmul(k[6], pE2))));
       // fe = A.PdH + B.(e_a x dE) + C.(e_a x dH) + D.PdE with A = gA wH(n) + hA wH(p) ...
-      const double A1 = fma(k[8], nH1, k[12] * pH1), A2 = fma(k[8], nH2, k[12] * pH2);
-      const double B1 = fma(k[9], nH1, k[13] * pH1), B2 = fma(k[9], nH2, k[13] * pH2);
-      const double C1 = fma(k[10], nE1, k[14] * pE1), C2 = fma(k[10], nE2, k[14] * pE2);
-      const double D1 = fma(k[11], nE1, k[15] * pE1), D2 = fma(k[11], nE2, k[15] * pE2);
-      double fe = A1 * dH1;
-      fe = fma(A2, dH2, fe);
-      fe = fma(-B1, dE2, fe);
-      fe = fma(B2, dE1, fe);
-      fe = fma(-C1, dH2, fe);
-      fe = fma(C2, dH1, fe);
-      fe = fma(D1, dE1, fe);
-      fe = fma(D2, dE2, fe);
-      s_fe[t] = fe;
+      const P2 A1 = padd(pmul(k[8], nH1), pmul(k[12], pH1)), A2 = padd(pmul(k[8], nH2), pmul(k[12], pH2));
+      const P2 B1 = padd(pmul(k[9], nH1), pmul(k[13], pH1)), B2 = padd(pmul(k[9], nH2), pmul(k[13], pH2));
+      const P2 C1 = padd(pmul(k[10], nE1), pmul(k[14], pE1)), C2 = padd(pmul(k[10], nE2), pmul(k[14], pE2));
+      const P2 D1 = padd(pmul(k[11], nE1), pmul(k[15], pE1)), D2 = padd(pmul(k[11], nE2), pmul(k[15], pE2));
+      P2 fe = pmul(A1, dH1);
+      fe = padd(fe, pmul(A2, dH2));
+      fe = padd(fe, pneg(pmul(B1, dE2)));
+      fe = padd(fe, pmul(B2, dE1));
+      fe = padd(fe, pneg(pmul(C1, dH2)));
+      fe = padd(fe, pmul(C2, dH1));
+      fe = padd(fe, pmul(D1, dE1));
+      fe = padd(fe, pmul(D2, dE2));
+      s_fe[t] = pdbl(fe);
     }
     __syncthreads();
     if (!node) continue;

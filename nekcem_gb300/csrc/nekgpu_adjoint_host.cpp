@@ -176,7 +176,15 @@ int build_adjoint_data(Context* c) {
   c->alloc_bytes.push_back(k.size() * 8);
   c->dev_bytes += k.size() * 8;
   c->d_adj_slot = (double*)pd;
-  if (check_cuda(cudaMemcpy(pd, k.data(), k.size() * 8, cudaMemcpyHostToDevice))) return NEKGPU_ERR_CUDA;
+  // stored as (hi, lo) float pairs (the same 8 bytes per coefficient): the
+  // reverse stage works them in double-float arithmetic
+  std::vector<float> kp(2 * k.size());
+  for (size_t i = 0; i < k.size(); ++i) {
+    kp[2 * i] = (float)k[i];
+    kp[2 * i + 1] = (float)(k[i] - (double)kp[2 * i]);
+  }
+  if (check_cuda(cudaMemcpy(pd, kp.data(), kp.size() * sizeof(float), cudaMemcpyHostToDevice)))
+    return NEKGPU_ERR_CUDA;
   return NEKGPU_OK;
 }
 

@@ -285,7 +285,7 @@ struct AdjointDev {
   double* deps;          // accumulated dJ/deps per node
   const int* nbr;
   const double* egeom;
-  const double* slot;    // [16][nxzfl] static face-slot coefficients
+  const double* slot;    // [16][nxzfl] static face-slot coefficients as (hi, lo) float pairs
   double a, b_next, inv_dt;
   double Dw[kMaxNx * kMaxNx];  // D(m,i) w_m at [m + NX*i]
   double w[kMaxNx];
