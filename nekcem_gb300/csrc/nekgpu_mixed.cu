@@ -1212,13 +1212,19 @@ __global__ void __launch_bounds__(CMCfg<NX>::NT, 1) k_mixed_curved(const CurvedD
     }
     // ---- inverse mass (pair product, one DADD) and the FP64 RK update ------------
     const PairF ch = pr(a.coef[g]), ce = pr(a.coef[P + g]);
+    double kk[6], uu[6];  // all twelve loads before the stores (k may be read and written)
+#pragma unroll
+    for (int c = 0; c < 6; ++c) {
+      kk[c] = first_stage ? 0.0 : a.k[c * P + g];
+      uu[c] = a.u_in[c * P + g];
+    }
 #pragma unroll
     for (int c = 0; c < 6; ++c) {
       const PairF p = pmul(res[c], c < 3 ? ch : ce);
       const double r = f2d(p.h) + f2d(p.l);
-      const double kn = first_stage ? r : fma(a.a, a.k[c * P + g], r);
+      const double kn = first_stage ? r : fma(a.a, kk[c], r);
       a.k[c * P + g] = kn;
-      a.u_out[c * P + g] = fma(a.b, kn, a.u_in[c * P + g]);
+      a.u_out[c * P + g] = fma(a.b, kn, uu[c]);
     }
   }
 }
