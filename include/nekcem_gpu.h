@@ -332,6 +332,11 @@ int nekgpu_energy(nekgpu_ctx* ctx, double* energy);
  * copies, and gives up; returns NEKGPU_ERR_TIMEOUT (the status word the stage
  * kernels set when a wait runs out) and leaves the context usable. */
 int nekgpu_selftest_wait(nekgpu_ctx* ctx, int polls);
+/* The mixed stage's join of a float pair (s, t), |t| <= ulp(s)/2, into one
+ * FP64 value by integer operations, applied to n host pairs on device 0
+ * (test hook): out[i] = s[i] + t[i], exact whenever the sum fits in 53 bits,
+ * else truncated below one FP64 ulp. */
+int nekgpu_selftest_pair_join(const float* s, const float* t, double* out, long n);
 /* chk_blowup (src/cem_common.F:1150-1165): NEKGPU_ERR_BLOWUP if any state
  * value is non-finite or above 1e20 in magnitude */
 int nekgpu_check_blowup(nekgpu_ctx* ctx);

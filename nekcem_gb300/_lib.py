@@ -105,6 +105,7 @@ SIGNATURES = [
     ("nekgpu_energy", C.c_int, [C.c_void_p, dp]),
     ("nekgpu_check_blowup", C.c_int, [C.c_void_p]),
     ("nekgpu_selftest_wait", C.c_int, [C.c_void_p, C.c_int]),
+    ("nekgpu_selftest_pair_join", C.c_int, [C.c_void_p, C.c_void_p, dp, C.c_long]),
     ("nekgpu_adjoint_gradient", C.c_int, [C.c_void_p, C.c_int, C.c_double, C.c_double, dp, dp, dp,
                                          C.c_int, dp, dp]),
     ("nekgpu_adjoint_init", C.c_int, [C.c_void_p, dp, C.c_int]),

@@ -2661,6 +2661,31 @@ int nekgpu_energy(nekgpu_ctx* c, double* energy) {
   return util_energy(c, energy);
 }
 
+int nekgpu_selftest_pair_join(const float* s, const float* t, double* out, long n) {
+  if (!s || !t || !out || n < 1 || n > (1L << 26)) return NEKGPU_ERR_ARG;
+  int st = nekgpu_device_check(0);
+  if (st) return st;
+  float *ds = nullptr, *dt = nullptr;
+  double* dout = nullptr;
+  if (cudaMalloc(&ds, n * sizeof(float)) != cudaSuccess || cudaMalloc(&dt, n * sizeof(float)) != cudaSuccess ||
+      cudaMalloc(&dout, n * sizeof(double)) != cudaSuccess) {
+    cudaGetLastError();
+    cudaFree(ds), cudaFree(dt), cudaFree(dout);
+    return NEKGPU_ERR_NOMEM;
+  }
+  st = NEKGPU_OK;
+  if (check_cuda(cudaMemcpy(ds, s, n * sizeof(float), cudaMemcpyHostToDevice)) ||
+      check_cuda(cudaMemcpy(dt, t, n * sizeof(float), cudaMemcpyHostToDevice)))
+    st = NEKGPU_ERR_CUDA;
+  if (!st) st = pair_join_selftest(ds, dt, dout, n);
+  if (!st && check_cuda(cudaMemcpy(out, dout, n * sizeof(double), cudaMemcpyDeviceToHost)))
+    st = NEKGPU_ERR_CUDA;
+  cudaFree(ds);
+  cudaFree(dt);
+  cudaFree(dout);
+  return st;
+}
+
 int nekgpu_selftest_wait(nekgpu_ctx* c, int polls) {
   if (!c || polls < 1 || polls > (1 << 22)) return NEKGPU_ERR_ARG;
   c->last_launches = 0;

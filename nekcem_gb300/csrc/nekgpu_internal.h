@@ -508,6 +508,8 @@ int scale_coef(Context* c, double dt);
 
 // nekgpu_mixed.cu
 int mixed_stage(Context* c, int rkstep, double time, double dt);
+// pair_to_double on n device pairs (default stream)
+int pair_join_selftest(const float* s, const float* t, double* out, long n);
 // one mixed stage between given buffers (u_in -> u_out, k_in -> k_out), as
 // fused_stage_buffers; the context's own state is untouched
 int mixed_stage_buffers(Context* c, int rkstep, double time, double dt, const double* u_in,

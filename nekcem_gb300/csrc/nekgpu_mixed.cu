@@ -1265,7 +1265,18 @@ __global__ void k_wait_selftest(int polls, int* status) {
   if (!done && threadIdx.x == 0) atomicExch(status, 1);
 }
 
+// pair_to_double over arrays (self-test of the finish's integer join)
+__global__ void k_pair_join(const float* s, const float* t, double* out, long n) {
+  const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (i < n) out[i] = pair_to_double(s[i], t[i]);
+}
+
 }  // namespace
+
+int pair_join_selftest(const float* s, const float* t, double* out, long n) {
+  k_pair_join<<<(unsigned)((n + 255) / 256), 256>>>(s, t, out, n);
+  return check_cuda(cudaGetLastError());
+}
 
 int wait_selftest(Context* c, int polls) {
   k_wait_selftest<<<1, 32, 0, c->stream>>>(polls, c->d_status);
