@@ -18,10 +18,13 @@ def declared():
     return sorted(set(re.findall(r"\b(nekgpu_\w+)\s*\(", src)))
 
 
-def test_header_declares_the_survey_entry_points():
+def test_header_declares_the_boundary_entry_points():
+    """The calls a Fortran driver makes in place of cem_maxwell_init,
+    cem_maxwell_op_rk and cem_error, and the adjoint pair."""
     names = declared()
     for must in ("nekgpu_init", "nekgpu_set_state", "nekgpu_get_state", "nekgpu_stage",
-                 "nekgpu_step", "nekgpu_norms", "nekgpu_finalize", "nekgpu_op_rk_host"):
+                 "nekgpu_step", "nekgpu_norms", "nekgpu_finalize", "nekgpu_op_rk_host",
+                 "nekgpu_adjoint_init", "nekgpu_adjoint_run"):
         assert must in names
 
 
