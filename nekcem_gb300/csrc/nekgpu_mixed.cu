@@ -159,7 +159,10 @@ __device__ __forceinline__ int opaque_tid() {
 constexpr int cmax(int a, int b) { return a > b ? a : b; }
 constexpr int round32(int a) { return (a + 31) / 32 * 32; }
 
-template <int NX>
+// TPL: threads per line task (2: each computes half of a line's outputs, for
+// meshes with fewer elements than SMs, where the time per stage is one
+// element's latency)
+template <int NX, int TPL = 1>
 struct MCfg {
   static constexpr int N2 = NX * NX, N3 = N2 * NX;
   // Node layout of the FP32 pair arrays.  NX = 8: unpadded, node
@@ -173,11 +176,11 @@ struct MCfg {
   static constexpr int N3P = NX * SZ;
   static constexpr int NF = 6 * N2;
   static constexpr int NTASK = 4 * N2;  // line tasks per direction
-  static constexpr int NT = round32(cmax(NTASK, (N3 + 1) / 2));
+  static constexpr int NT = round32(cmax(NTASK * TPL, (N3 + 1) / 2));
   static constexpr int NW = NT / 32;
   static constexpr int NPT = (N3 + NT - 1) / NT;
   static constexpr int FPT = (NF + NT - 1) / NT;
-  static constexpr int TPT = (NTASK + NT - 1) / NT;
+  static constexpr int TPT = (NTASK * TPL + NT - 1) / NT;
   static constexpr bool kTma = (N3 % 2) == 0;
   // odd node counts: the next element staged by per-thread 8-byte async
   // copies where that measured faster (N=8 +3 %, N=6 +0.9 %; N=4, N=2 load
@@ -366,24 +369,97 @@ __device__ __forceinline__ float2 jump_pair(double p, float2 own) {
   return make_float2(s, (d2f_lo(p) - own.y) + t);
 }
 
+// Outputs I0 .. I0+NXP-1 of one line task (all NX of them, or one half when
+// two threads share the line): the contraction, the rho factor, the lifted
+// flux at the line's ends and the accumulation into the residual pairs (or,
+// FIN, the finish).
+template <int NX, int DIR, bool FIN, int TPL, int I0, int NXP>
+__device__ __forceinline__ void line_outputs(const float2* u, float2* R0, float2 flux_m,
+                                             float2 flux_p, bool cubic, float rh, float rl,
+                                             float sg, bool init, int la, int lb, int rt,
+                                             const MixedDev& a, int e, bool first_stage) {
+  using C = MCfg<NX, TPL>;
+  // packed in float pairs:
+  //   (hi_i, lo_i)   += (Dh, Df)(i,l) * (uh, ul)_l      hi exact
+  //   (m_i, m_i+1)   += (Dm(i,l), Dm(i+1,l)) * (uh, uh)_l
+  constexpr int H = (NX + 1) / 2, HP = (NXP + 1) / 2, J0 = I0 / 2;
+  static_assert(I0 % 2 == 0, "output pairs start on an even output");
+  float2 x[NXP], y[HP];
+#pragma unroll
+  for (int j = 0; j < NXP; ++j) x[j] = __fmul2_rn(c_mixD[NX][0][I0 + j], u[0]);
+#pragma unroll
+  for (int j = 0; j < HP; ++j) y[j] = __fmul2_rn(c_mixD[NX][1][J0 + j], make_float2(u[0].x, u[0].x));
+#pragma unroll
+  for (int l = 1; l < NX; ++l) {
+    const float2 uu = make_float2(u[l].x, u[l].x);
+#pragma unroll
+    for (int j = 0; j < NXP; ++j) x[j] = __ffma2_rn(c_mixD[NX][0][I0 + j + NX * l], u[l], x[j]);
+#pragma unroll
+    for (int j = 0; j < HP; ++j) y[j] = __ffma2_rn(c_mixD[NX][1][J0 + j + H * l], uu, y[j]);
+  }
+#pragma unroll
+  for (int j = 0; j < NXP; ++j) {
+    const int i = I0 + j;
+    float h = x[j].x, r = x[j].y + ((j & 1) ? y[j / 2].y : y[j / 2].x);
+    if (DIR != 0 && !cubic) {  // times rho = g_dir/g_x as a float pair
+      const float p = rh * h;
+      float ee = fmaf(rh, h, -p);
+      ee = fmaf(rh, r, ee);
+      ee = fmaf(rl, h, ee);
+      h = p;
+      r = ee;
+    }
+    h *= sg;
+    r *= sg;
+    if (i == 0 || i == NX - 1) {  // the lifted flux pair of the end's face
+      const float2 F = i == 0 ? flux_m : flux_p;
+      float s, t;
+      two_sum(h, F.x, s, t);
+      h = s;
+      r = (r + F.y) + t;
+    }
+    float2* Rp = R0 + line_node<NX, DIR>(la, lb, i);
+    if (FIN) {
+      const float2 old = *Rp;
+      float sum, err;
+      two_sum(old.x, h, sum, err);
+      const int vol = DIR == 0 ? i + NX * la + C::N2 * lb
+                               : (DIR == 1 ? la + NX * i + C::N2 * lb : la + NX * lb + C::N2 * i);
+      rk_finish<C::kIntAdd>(a, rt, (long)e * C::N3 + vol, sum, (old.y + r) + err, first_stage);
+    } else if (init) {
+      *Rp = make_float2(h, r);
+    } else {
+      const float2 old = *Rp;
+      float sum, err;
+      two_sum(old.x, h, sum, err);
+      *Rp = make_float2(sum, (old.y + r) + err);
+    }
+  }
+}
+
 // One direction of the contraction: tasks (component, line) accumulate the
 // signed derivative pair into the residual pair arrays.  The line's two end
 // nodes lie on the faces normal to DIR; the lifted flux of those faces in the
 // task's residual component (s_F, stored in this direction's slot order) is
 // added to their low parts.  FIN (last direction): the residual of the
 // task's component is complete at the line's nodes, so the task finishes
-// them (inverse mass, RK update) instead of storing the pairs.
-template <int NX, int DIR, bool FIN>
+// them (inverse mass, RK update) instead of storing the pairs.  TPL = 2: two
+// threads per line, each with half of its outputs (the halves in separate
+// warps, so the branch on the half is warp-uniform).
+template <int NX, int DIR, bool FIN, int TPL = 1>
 __device__ __forceinline__ void line_phase(const float2* s_u2, float2* s_R2, const float2* s_F,
                                            bool cubic, float rh, float rl, const MixedDev& a,
                                            int e, bool first_stage) {
-  using C = MCfg<NX>;
+  using C = MCfg<NX, TPL>;
+  static_assert(TPL == 1 || (TPL == 2 && !FIN && NX % 4 == 0), "two threads per line: NX = 4k, no FIN");
   const int tid = opaque_tid();
 #pragma unroll
   for (int q = 0; q < C::TPT; ++q) {
     const int task = tid + q * C::NT;
-    if (task < C::NTASK) {
-      const int slot = task / C::N2, lam = task - slot * C::N2;
+    if (task < C::NTASK * TPL) {
+      const int part = TPL == 1 ? 0 : task / C::NTASK;
+      const int lt = task - part * C::NTASK;
+      const int slot = lt / C::N2, lam = lt - slot * C::N2;
       const int la = lam % NX, lb = lam / NX;
       const int comp = kLineComp[DIR][slot], rt = kLineRes[DIR][slot];
       const float sg = kLineSign[DIR][slot];
@@ -408,66 +484,16 @@ __device__ __forceinline__ void line_phase(const float2* s_u2, float2* s_R2, con
       float2 u[NX];
 #pragma unroll
       for (int l = 0; l < NX; ++l) u[l] = pu[line_node<NX, DIR>(la, lb, l)];
-      // all NX outputs of the line at once, packed in float pairs:
-      //   (hi_i, lo_i)   += (Dh, Df)(i,l) * (uh, ul)_l      hi exact
-      //   (m_i, m_i+1)   += (Dm(i,l), Dm(i+1,l)) * (uh, uh)_l
-      constexpr int H = (NX + 1) / 2;
-      float2 x[NX], y[H];
-#pragma unroll
-      for (int i = 0; i < NX; ++i) x[i] = __fmul2_rn(c_mixD[NX][0][i], u[0]);
-#pragma unroll
-      for (int i = 0; i < H; ++i) y[i] = __fmul2_rn(c_mixD[NX][1][i], make_float2(u[0].x, u[0].x));
-#pragma unroll
-      for (int l = 1; l < NX; ++l) {
-        const float2 uu = make_float2(u[l].x, u[l].x);
-#pragma unroll
-        for (int i = 0; i < NX; ++i) x[i] = __ffma2_rn(c_mixD[NX][0][i + NX * l], u[l], x[i]);
-#pragma unroll
-        for (int i = 0; i < H; ++i) y[i] = __ffma2_rn(c_mixD[NX][1][i + H * l], uu, y[i]);
-      }
-      float hi[NX], lo[NX];
-#pragma unroll
-      for (int i = 0; i < NX; ++i) {
-        hi[i] = x[i].x;
-        lo[i] = x[i].y + ((i & 1) ? y[i / 2].y : y[i / 2].x);
-      }
       float2* R0 = s_R2 + rt * C::N3P;
-#pragma unroll
-      for (int i = 0; i < NX; ++i) {
-        float h = hi[i], r = lo[i];
-        if (DIR != 0 && !cubic) {  // times rho = g_dir/g_x as a float pair
-          const float p = rh * h;
-          float e = fmaf(rh, h, -p);
-          e = fmaf(rh, r, e);
-          e = fmaf(rl, h, e);
-          h = p;
-          r = e;
-        }
-        h *= sg;
-        r *= sg;
-        if (i == 0 || i == NX - 1) {  // the lifted flux pair of the end's face
-          const float2 F = i == 0 ? flux_m : flux_p;
-          float s, t;
-          two_sum(h, F.x, s, t);
-          h = s;
-          r = (r + F.y) + t;
-        }
-        float2* Rp = R0 + line_node<NX, DIR>(la, lb, i);
-        if (FIN) {
-          const float2 old = *Rp;
-          float sum, err;
-          two_sum(old.x, h, sum, err);
-          const int vol = DIR == 0 ? i + NX * la + C::N2 * lb
-                                   : (DIR == 1 ? la + NX * i + C::N2 * lb : la + NX * lb + C::N2 * i);
-          rk_finish<C::kIntAdd>(a, rt, (long)e * C::N3 + vol, sum, (old.y + r) + err, first_stage);
-        } else if (init) {
-          *Rp = make_float2(h, r);
-        } else {
-          const float2 old = *Rp;
-          float sum, err;
-          two_sum(old.x, h, sum, err);
-          *Rp = make_float2(sum, (old.y + r) + err);
-        }
+      if constexpr (TPL == 1) {
+        line_outputs<NX, DIR, FIN, TPL, 0, NX>(u, R0, flux_m, flux_p, cubic, rh, rl, sg, init, la, lb,
+                                               rt, a, e, first_stage);
+      } else if (part == 0) {
+        line_outputs<NX, DIR, FIN, TPL, 0, NX / 2>(u, R0, flux_m, flux_p, cubic, rh, rl, sg, init, la,
+                                                   lb, rt, a, e, first_stage);
+      } else {
+        line_outputs<NX, DIR, FIN, TPL, NX / 2, NX / 2>(u, R0, flux_m, flux_p, cubic, rh, rl, sg, init,
+                                                        la, lb, rt, a, e, first_stage);
       }
     }
   }
@@ -559,17 +585,17 @@ __device__ __forceinline__ void disp_node(const MixedDev& a, int l, int v, long 
 // memory with the face flux as float pairs: a fourth does not fit; up to 80
 // registers), six at NX = 6 (160 threads, 32 KB, 64 registers), two at NX = 9
 // (384 threads, 94 KB), three otherwise and with the extension branches.
-template <int NX, bool EXT>
+template <int NX, bool EXT, int TPL = 1>
 constexpr int mixed_min_blocks() {
-  return NX == 9 ? 2 : (EXT ? 3 : (NX == 6 ? 6 : 3));
+  return TPL == 2 ? 1 : (NX == 9 ? 2 : (EXT ? 3 : (NX == 6 ? 6 : 3)));
 }
 
 // EXT: the variant with the PML, dispersive-current, incident-field and
 // graphene branches
-template <int NX, bool EXT>
-__global__ void __launch_bounds__(MCfg<NX>::NT, mixed_min_blocks<NX, EXT>())
+template <int NX, bool EXT, int TPL = 1>
+__global__ void __launch_bounds__(MCfg<NX, TPL>::NT, mixed_min_blocks<NX, EXT, TPL>())
     k_mixed_stage(const MixedDev a) {
-  using C = MCfg<NX>;
+  using C = MCfg<NX, TPL>;
   constexpr int N2 = C::N2, N3 = C::N3, NT = C::NT, NF = C::NF, N3P = C::N3P;
   constexpr int NPT = C::NPT, FPT = C::FPT;
   constexpr bool FIN = !EXT && C::kFin;  // the extension terms need all six at a node
@@ -869,13 +895,13 @@ __global__ void __launch_bounds__(MCfg<NX>::NT, mixed_min_blocks<NX, EXT>())
     {
       const bool cubic = eg[0] == 1.0f && eg[1] == 0.0f && eg[2] == 1.0f && eg[3] == 0.0f;
       const float r1h = eg[0], r1l = eg[1], r2h = eg[2], r2l = eg[3];
-      line_phase<NX, 0, false>(s_u2, s_R2, s_F, cubic, 0.0f, 0.0f, a, e, first_stage);
+      line_phase<NX, 0, false, TPL>(s_u2, s_R2, s_F, cubic, 0.0f, 0.0f, a, e, first_stage);
       __syncthreads();
-      line_phase<NX, 1, false>(s_u2, s_R2, s_F, cubic, r1h, r1l, a, e, first_stage);
+      line_phase<NX, 1, false, TPL>(s_u2, s_R2, s_F, cubic, r1h, r1l, a, e, first_stage);
       __syncthreads();
       // without the extension terms each component can finish on its own
       // (MCfg::kFin): H3, E3 (no t-derivative) are complete since the s-lines
-      line_phase<NX, 2, FIN>(s_u2, s_R2, s_F, cubic, r2h, r2l, a, e, first_stage);
+      line_phase<NX, 2, FIN, TPL>(s_u2, s_R2, s_F, cubic, r2h, r2l, a, e, first_stage);
     }
     if constexpr (FIN) {
       tid = opaque_tid();
@@ -957,10 +983,10 @@ __global__ void k_scale_coef_pairs(float2* coef, const double* base, long n2, do
   coef[i] = make_float2(d2f_hi(v), d2f_lo(v));
 }
 
-template <int NX, bool EXT>
+template <int NX, bool EXT, int TPL = 1>
 int launch_mixed(Context* c, const MixedDev& a, bool pdl) {
-  using C = MCfg<NX>;
-  auto kern = k_mixed_stage<NX, EXT>;
+  using C = MCfg<NX, TPL>;
+  auto kern = k_mixed_stage<NX, EXT, TPL>;
   static bool ready = false;
   static int grid = 0;
   if (!ready) {
@@ -1305,6 +1331,17 @@ int scale_coef_pairs(Context* c, double dt) {
   return check_cuda(cudaGetLastError());
 }
 
+int num_sms(Context* c) {
+  static int n = 0;
+  if (!n) {
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, c->device) != cudaSuccess) {
+      cudaGetLastError();
+      n = 1;
+    }
+  }
+  return n;
+}
+
 int mixed_stage_range(Context* c, int rkstep, double time, double dt, int e0, int e1, bool pdl) {
   int st = scale_coef_pairs(c, dt);
   if (st) return st;
@@ -1333,7 +1370,13 @@ int mixed_stage_range(Context* c, int rkstep, double time, double dt, int e0, in
     case 5: st = ext ? launch_mixed<5, true>(c, a, pdl) : launch_mixed<5, false>(c, a, pdl); break;
     case 6: st = ext ? launch_mixed<6, true>(c, a, pdl) : launch_mixed<6, false>(c, a, pdl); break;
     case 7: st = ext ? launch_mixed<7, true>(c, a, pdl) : launch_mixed<7, false>(c, a, pdl); break;
-    case 8: st = ext ? launch_mixed<8, true>(c, a, pdl) : launch_mixed<8, false>(c, a, pdl); break;
+    case 8:
+      // fewer elements than SMs: two threads per line (one element per SM
+      // either way; the element's latency is the stage's time)
+      st = ext ? launch_mixed<8, true>(c, a, pdl)
+               : (e1 - e0 <= num_sms(c) ? launch_mixed<8, false, 2>(c, a, pdl)
+                                         : launch_mixed<8, false>(c, a, pdl));
+      break;
     case 9: st = ext ? launch_mixed<9, true>(c, a, pdl) : launch_mixed<9, false>(c, a, pdl); break;
     default: return NEKGPU_ERR_UNSUPPORTED;
   }

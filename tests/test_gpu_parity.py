@@ -42,6 +42,9 @@ MESHES = {
     "n3": dict(N=2, nel=(2, 3, 2), lo=(0, 0, 0), hi=(1, 1, 1), bc=(PEC, PEC, PER)),
     "single_periodic": dict(N=5, nel=(1, 1, 1), lo=(0, 0, 0), hi=(2, 2, 2), bc=(PER, PER, PER)),
     "single_pec": dict(N=6, nel=(1, 1, 1), lo=(0, 0, 0), hi=(1, 1, 1), bc=(PEC, PEC, PEC)),
+    # N=7 with non-cubic elements and fewer elements than SMs (the mixed
+    # form's two-threads-per-line kernel)
+    "rect_n7": dict(N=7, nel=(2, 3, 1), lo=(0, 0, 0), hi=(1, 2, 0.5), bc=(PEC, PER, PEC)),
 }
 
 
